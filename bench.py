@@ -1,0 +1,306 @@
+#!/usr/bin/env python
+"""Benchmark: tets/s of the per-tet implicit-arrangement path (stages a-d) on one GB300.
+
+Default workload (the large degenerate implicit arrangement): tet5 grid with 129^3 vertices
+(10,485,760 tets) over [-1,1]^3 and 32 FP64 functions: 8 planes (4 exact duplicates, 4 through grid
+vertices), 8 spheres, 8 cylinders, 8 tori; seeded synthetic data.  --config mi runs the material
+interface workload (65^3 vertices, 8 materials).
+
+One step = sampling -> sign filter -> per-tet cut -> mesh extraction with vertex coordinates,
+through the C ABI (ria_grid_implicit_arrangement); `value` is tets/s with the function
+descriptors as the only input (the grid and its sampled values are produced on the device), timed
+with CUDA events on the library's stream.  `e2e` goes through the reference-shaped host-buffer
+entry points: ria_sample_functions (host points in, host values out, as the reference's
+load_functions) and ria_compute_implicit_arrangement (host pts / tets / values in), then copies the
+mesh (points, vertex records, faces) back; host<->device copies are inside its timed region.
+
+--impl reference times the CPU restatement of the reference path (oracle/) on this host's cores on a
+bounded slab of the same workload (the reference itself depends on absent third-party libraries and
+cannot be built).  Under torchrun only rank 0 runs it.
+"""
+from __future__ import annotations
+
+import argparse
+import importlib
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+PKG = "robust-implicit-surface-networks_gb300"
+
+METRIC = "tets/s (arrangement+extract) on 1 GB300"
+
+
+def _peaks():
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clocks and throttle reasons while the timed region runs."""
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def workload(name):
+    fns = importlib.import_module(PKG + ".functions")
+    if name == "ia-degenerate":
+        return fns.workload_ia_degenerate()
+    if name == "mi":
+        return fns.workload_mi()
+    if name == "ia-small":
+        return fns.workload_ia_small()
+    raise SystemExit(f"unknown config {name}")
+
+
+def algorithmic_bytes(wl, st):
+    """Bytes each stage must move at least (per-unit figures in the design doc)."""
+    V, T, F = wl.n_verts, wl.n_tets, len(wl.funcs)
+    A = st["num_intersecting_tet"]
+    nv, nf = st["num_verts"], st["num_faces"]
+    return {
+        "sample": 8 * V * F + 16 * V,           # values written + per-vertex masks written
+        "filter": 16 * V + 28 * A,              # masks read once + active-tet lists written
+        "cut": None,                            # compute-bound (FP64 predicates, per-thread state)
+        "extract": 20 * A + 24 * nv + 88 * nv + 8 * 4 * nf,  # lists read + points, vertex records, faces
+    }
+
+
+def cpu_slab(wl, seconds_target=12.0):
+    """A contiguous slab of cube layers of the workload grid (re-indexed): the bounded CPU sample."""
+    fns = importlib.import_module(PKG + ".functions")
+    res = wl.res
+    n = res + 1
+    layers = max(1, min(res, int(round(res * seconds_target / 60.0))))
+    i0 = (res - layers) // 2
+    xs, ys, zs = fns.grid_coords(res, wl.bbox_min, wl.bbox_max)
+    import numpy as np
+
+    pts_all, tets_all = fns.generate_tet_mesh(res, wl.bbox_min, wl.bbox_max)
+    per_layer = 5 * res * res
+    tets = tets_all[i0 * per_layer:(i0 + layers) * per_layer] - i0 * n * n
+    pts = pts_all[i0 * n * n:(i0 + layers + 1) * n * n]
+    return pts, tets, f"{layers} of {res} cube layers ({len(tets)} tets), x-slab starting at layer {i0}"
+
+
+def run_reference(args, wl, world):
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import pyoracle
+
+    pyoracle.build()
+    cores = os.cpu_count() or 1
+    pts, tets, desc = cpu_slab(wl)
+    times = []
+    for it in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        fv = pyoracle.sample(wl.funcs, pts, threads=cores)
+        pyoracle.run(wl.mode, pts, tets, fv, threads=cores)
+        dt = time.perf_counter() - t0
+        if it >= args.warmup:
+            times.append(dt)
+    per = statistics.median(times)
+    value = len(tets) / per
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "tets/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": per * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+        "config": {"workload": wl.name, "tets": wl.n_tets, "functions": len(wl.funcs), "sample": desc},
+        "cpu_baseline": {"value": value, "unit": "tets/s", "cores": cores, "kind": "port",
+                         "sample": desc + "; stages a-d of the CPU restatement (oracle/), stages a-c threaded, "
+                                          "extraction single-threaded as in the reference"},
+        "e2e": {"value": value, "unit": "tets/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="ia-degenerate", choices=["ia-degenerate", "mi", "ia-small"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    wl = workload(args.config)
+
+    if args.impl == "reference":
+        if rank == 0:
+            run_reference(args, wl, world)
+        return
+
+    import numpy as np
+    import torch
+
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    pkg = importlib.import_module(PKG)
+    pkg.build()
+    L = pkg.load()
+    grid = pkg.grid_implicit_arrangement if wl.mode == "ia" else pkg.grid_material_interface
+    host = pkg.implicit_arrangement if wl.mode == "ia" else pkg.material_interface
+
+    for _ in range(args.warmup):
+        m = grid(wl.res, wl.funcs)
+        st = m.stats
+        m.close()
+
+    # ---- device-resident throughput
+    launches0 = int(L.ria_kernel_launches())
+    dev_ms, stage = [], {"sample": [], "filter": [], "cut": [], "extract": []}
+    with ClockSampler(local) as clk:
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            m = grid(wl.res, wl.funcs)
+            tm = m.timings
+            dev_ms.append(tm["total"] * 1e3)
+            for k in stage:
+                stage[k].append(tm[k] * 1e3)
+            m.close()
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+    launches = int(L.ria_kernel_launches()) - launches0
+    ms = statistics.mean(dev_ms)
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * wl.n_tets / (ms * 1e-3)
+
+    # ---- end to end through the host-buffer entry points
+    fns = importlib.import_module(PKG + ".functions")
+    pts, tets = fns.generate_tet_mesh(wl.res, wl.bbox_min, wl.bbox_max)
+    pts = np.ascontiguousarray(pts)
+    tets = np.ascontiguousarray(tets)
+    e2e_times = []
+    h2d = d2h = 0
+    for it in range(1 + args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        fv = pkg.sample_functions(wl.funcs, pts)
+        m = host(pts, tets, fv)
+        outs = [m["xyz"], m["verts"], m["face_offsets"], m["face_verts"], m["face_tets"], m["face_func"]]
+        m.close()
+        dt = time.perf_counter() - t0
+        if it > 0:
+            e2e_times.append(dt)
+        h2d = pts.nbytes + wl.funcs.nbytes + pts.nbytes + tets.nbytes + fv.nbytes
+        d2h = fv.nbytes + sum(o.nbytes for o in outs)
+    e2e = world * wl.n_tets / statistics.median(e2e_times)
+
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return
+
+    peak, peak_kind = _peaks()
+    ab = algorithmic_bytes(wl, st)
+    stage_ms = {k: statistics.mean(v) for k, v in stage.items()}
+    cand = {k: v for k, v in stage_ms.items() if ab[k] is not None}
+    dom = max(cand, key=cand.get)
+    achieved = ab[dom] / (stage_ms[dom] * 1e-3) / 1e9
+    line = {
+        "metric": METRIC, "value": value, "unit": "tets/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+        "config": {"workload": wl.name, "tets": wl.n_tets, "verts": wl.n_verts, "functions": len(wl.funcs),
+                   "mode": wl.mode, "l2": "inputs larger than L2 (V x F FP64 values %.0f MB)" %
+                   (8 * wl.n_verts * len(wl.funcs) / 1e6), "parallelism": "replicas" if world > 1 else "single"},
+        "stage_ms": stage_ms,
+        "stats": st,
+        "wall_ms_per_step": wall / args.steps * 1e3,
+        "e2e": {"value": e2e, "unit": "tets/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+        "gpu_launches": launches,
+        "roofline": {"bound": "hbm", "kernel_stage": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_kind": peak_kind, "traffic": None},
+        "clocks": clk.summary(),
+    }
+    if not args.no_cpu_baseline:
+        sys.path.insert(0, os.path.join(REPO, "oracle"))
+        import pyoracle
+
+        pyoracle.build()
+        cpts, ctets, desc = cpu_slab(wl)
+        t0 = time.perf_counter()
+        cfv = pyoracle.sample(wl.funcs, cpts, threads=1)
+        pyoracle.run(wl.mode, cpts, ctets, cfv, threads=1)
+        dt = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": len(ctets) / dt, "unit": "tets/s", "cores": 1, "kind": "port",
+                                "sample": desc + "; stages a-d of the CPU restatement (oracle/), one thread"}
+    print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

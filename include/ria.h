@@ -1,0 +1,219 @@
+/*
+ * ria.h - C ABI of the GB300 implementation of the per-tet implicit-arrangement path of
+ * Robust-Implicit-Surface-Networks (duxingyi-charles).
+ *
+ * Plain pointers and sizes only.  Every call runs on the current CUDA device; there is no CPU
+ * fallback: without a usable CUDA device the calls return RIA_ENODEVICE.
+ *
+ * Reference interfaces replaced (paths inside the reference project):
+ *   implicit_arrangement(...)        src/implicit_arrangement.h:39-62 (stages signs, filter,
+ *                                    per-tet cut, extract_iso_mesh, compute_iso_vert_xyz:
+ *                                    src/implicit_arrangement.cpp:53-403)
+ *   material_interface(...)          src/material_interface.h:38-61 (src/material_interface.cpp:53-448)
+ *   load_functions(...)              the external implicit_functions library, called at
+ *                                    app/implicit_arrangement.cpp:59 and app/material_interface.cpp:62
+ *   compute_arrangement(planes)      simplicial_arrangement (external), called at
+ *                                    src/implicit_arrangement.cpp:279,283
+ *   compute_material_interface(m)    simplicial_arrangement (external), called at
+ *                                    src/material_interface.cpp:323,327
+ *   generate_tet_mesh(...)           src/io.cpp:95-152 (the *_grid_* entry points build the grid
+ *                                    on the device)
+ * The downstream stages (edges, patches, chains, face pairing, shells, cells) stay on the host and
+ * consume the mesh returned here.
+ */
+#ifndef RIA_H
+#define RIA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define RIA_API __attribute__((visibility("default")))
+#else
+#define RIA_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum ria_status {
+    RIA_OK = 0,
+    RIA_EINVAL = 1,       /* bad argument (null pointer, n_func > 64, index out of range, ...) */
+    RIA_ENOMEM = 2,       /* device or host allocation failed */
+    RIA_ECAPACITY = 3,    /* a tet's arrangement exceeds the per-tet capacity (about 10 active functions in general position) */
+    RIA_EDEGENERATE = 4,  /* an exact predicate exceeded its expansion capacity (extreme dynamic range) */
+    RIA_ETIMEOUT = 5,     /* reserved for bounded device waits */
+    RIA_ECUDA = 6,        /* a CUDA runtime call failed */
+    RIA_EINTERNAL = 7,    /* an internal consistency check failed */
+    RIA_ENODEVICE = 8     /* no CUDA device (the library never computes on the CPU) */
+} ria_status;
+
+/* Implicit function descriptor (one JSON object of a reference function file).
+ *   RIA_FUNC_PLANE           p[0..2] point, p[3..5] normal:        n . (x - p)
+ *   RIA_FUNC_SPHERE          p[0..2] centre, p[3] radius:          r - |x - c|
+ *   RIA_FUNC_SPHERE_SQUARED  p[0..2] centre, p[3] radius:          r*r - |x - c|^2
+ *   RIA_FUNC_CYLINDER        p[0..2] axis point, p[3..5] unit axis, p[6] radius:
+ *                            v = x - a; t = v . u; r - |v - t u|
+ *   RIA_FUNC_TORUS           p[0..2] centre, p[3..5] unit axis, p[6] major R, p[7] minor r:
+ *                            v = x - c; h = v . u; rho = |v - h u|; r - sqrt((rho - R)^2 + h^2)
+ *   RIA_FUNC_ZERO            0
+ * flipped != 0 negates the value.  Every value is FP64, evaluated left to right as written with
+ * each operation rounded on its own (no fused multiply-add) and a correctly rounded sqrt. */
+enum {
+    RIA_FUNC_ZERO = 0,
+    RIA_FUNC_PLANE = 1,
+    RIA_FUNC_SPHERE = 2,
+    RIA_FUNC_SPHERE_SQUARED = 3,
+    RIA_FUNC_CYLINDER = 4,
+    RIA_FUNC_TORUS = 5
+};
+
+typedef struct ria_function {
+    int32_t type;
+    int32_t flipped;
+    double p[12];
+} ria_function;
+
+/* Switches of the reference JSON config (src/io.h:12-28).  use_lookup = 0 forces
+ * use_secondary_lookup = 0 (src/implicit_arrangement.cpp:38-40).  The lookup tables only choose
+ * the code path; the result is the same either way. */
+typedef struct ria_config {
+    int32_t use_lookup;
+    int32_t use_secondary_lookup;
+    int32_t use_topo_ray_shooting; /* accepted for the downstream stages; unused here */
+    int32_t robust_test;           /* -R: cut every tet in both plane orders and compare the
+                                      vertex/face/cell counts (src/implicit_arrangement.cpp:137-243);
+                                      the call then returns without a mesh */
+    int32_t keep_records;          /* keep the per-tet records (RIA_MESH_REC_*) */
+} ria_config;
+
+typedef struct ria_mesh ria_mesh;
+
+/* Mesh fields.  Index values use int64 with -1 for "none" (the reference's size_t Mesh_None).
+ *
+ * Per-tet record layout (little endian, RIA_MESH_REC_BYTES; one record per tet with at least one
+ * active function, in tet order).  Labels 0..3 are the tet faces (label b is the face opposite
+ * corner b); label 4+j is the j-th active function (or material) of the tet.
+ *   implicit arrangement:
+ *     u8 type=1, u8 k, u16 nv, u16 nf, u16 nc, u16 nloop
+ *     u8 rep[k]        representative label of the group of coincident planes (0xFF: zero plane)
+ *     u8 vlab[nv][3]   sorted labels of the planes that define each vertex
+ *     face[nf]         u8 supporting plane, u8 flags (bit 0: on the tet boundary),
+ *                      u16 positive cell, u16 negative cell (0xFFFF: none), u16 loop length
+ *     u16 loops[nloop] vertex ids, each loop starting at its smallest id, counter-clockwise seen
+ *                      from the positive side
+ *     u64 cells[nc]    sign vector of each cell (bit 4+j set on the positive side of plane 4+j)
+ *   material interface:
+ *     u8 type=2, u8 k, u16 nv, u16 nf, u16 nc, u16 nloop
+ *     u8 rep[k]        representative label of the group of identical materials
+ *     u8 vlab[nv][4]   sorted labels
+ *     face[nf]         u8 positive label, u8 negative label, u16 loop length
+ *     u16 loops[nloop]
+ *     u8 cells[nc]     material label of each cell
+ * Vertices are sorted by label, faces by (supporting plane, sorted vertex ids) or by
+ * (positive, negative) label, cells by sign vector or label. */
+typedef enum ria_mesh_field {
+    RIA_MESH_POINTS = 0,          /* double [n_verts][3] */
+    RIA_MESH_VERTS = 1,           /* int64 [n_verts][11]: tet_index, tet_vert_index, simplex_size,
+                                     simplex_vert_indices[4], func_indices[4] (IA: 3 used;
+                                     MI: material_indices) */
+    RIA_MESH_FACE_OFFSETS = 2,    /* int64 [n_faces + 1] */
+    RIA_MESH_FACE_VERTS = 3,      /* int64 [...] */
+    RIA_MESH_FACE_TET_OFFSETS = 4,/* int64 [n_faces + 1] */
+    RIA_MESH_FACE_TETS = 5,       /* int64 [...][2]: (tet, local face) */
+    RIA_MESH_FACE_FUNC = 6,       /* int64 [n_faces][2]: func_index (first, second) */
+    RIA_MESH_FUNC_IN_TET = 7,     /* int64 [...]: active functions per tet, ascending (CRS) */
+    RIA_MESH_START_INDEX = 8,     /* int64 [n_tets + 1] */
+    RIA_MESH_REC_OFFSETS = 9,     /* int64 [n_tets + 1] byte offsets into RIA_MESH_REC_BYTES */
+    RIA_MESH_REC_BYTES = 10,      /* uint8 [...] */
+    RIA_MESH_STATS = 11,          /* int64 [RIA_NUM_STATS] */
+    RIA_MESH_TIMINGS = 12,        /* double [RIA_NUM_TIMINGS]: seconds of each device stage */
+    RIA_MESH_FUNC_VALS = 13       /* double [n_pts][n_func]: the sampled values (grid entry points) */
+} ria_mesh_field;
+
+/* RIA_MESH_STATS entries, named as in the reference's stats.json
+ * (src/implicit_arrangement.cpp:46-49,80,119,322-327,390-393; src/material_interface.cpp) */
+enum {
+    RIA_STAT_NUM_PTS = 0,
+    RIA_STAT_NUM_TETS = 1,
+    RIA_STAT_NUM_DEGENERATE_VERTEX = 2,
+    RIA_STAT_NUM_INTERSECTING_TET = 3,
+    RIA_STAT_NUM_A_FUNC = 4,     /* IA: num_1_func; MI: num_2_func */
+    RIA_STAT_NUM_B_FUNC = 5,     /* IA: num_2_func; MI: num_3_func */
+    RIA_STAT_NUM_MORE_FUNC = 6,
+    RIA_STAT_NUM_VERTS = 7,      /* num_iso_verts / num_MI_verts */
+    RIA_STAT_NUM_FACES = 8,      /* num_iso_faces / num_MI_faces */
+    RIA_STAT_NUM_DEFERRED = 9,   /* tets cut by the exact (slow) variant */
+    RIA_STAT_ROBUST_FAILURES = 10,/* robust_test: tets whose two plane orders disagree */
+    RIA_NUM_STATS = 11
+};
+enum {
+    RIA_TIME_SAMPLE = 0,   /* stage a (grid entry points) or upload */
+    RIA_TIME_FILTER = 1,   /* stage b */
+    RIA_TIME_CUT = 2,      /* stage c */
+    RIA_TIME_EXTRACT = 3,  /* stage d: dedup, faces, vertex xyz */
+    RIA_TIME_TOTAL = 4,
+    RIA_NUM_TIMINGS = 5
+};
+
+/* ---- whole-grid entry points (host buffers) --------------------------------------------------
+ * pts: n_pts x 3 doubles; tets: n_tets x 4 vertex ids; func_vals: n_pts x n_func, row major
+ * (the reference's Eigen RowMajor funcVals).  n_func <= 64. */
+RIA_API ria_status ria_compute_implicit_arrangement(const ria_config* cfg, const double* pts, uint64_t n_pts,
+                                            const int64_t* tets, uint64_t n_tets, const double* func_vals,
+                                            uint32_t n_func, ria_mesh** out);
+RIA_API ria_status ria_compute_material_interface(const ria_config* cfg, const double* pts, uint64_t n_pts,
+                                          const int64_t* tets, uint64_t n_tets, const double* func_vals,
+                                          uint32_t n_func, ria_mesh** out);
+
+/* Same inputs already resident on the current device; work is queued on `stream`
+ * (a cudaStream_t, NULL for the default stream) and the call returns when the mesh is ready. */
+RIA_API ria_status ria_compute_implicit_arrangement_device(const ria_config* cfg, const double* d_pts, uint64_t n_pts,
+                                                   const int64_t* d_tets, uint64_t n_tets,
+                                                   const double* d_func_vals, uint32_t n_func, void* stream,
+                                                   ria_mesh** out);
+RIA_API ria_status ria_compute_material_interface_device(const ria_config* cfg, const double* d_pts, uint64_t n_pts,
+                                                 const int64_t* d_tets, uint64_t n_tets,
+                                                 const double* d_func_vals, uint32_t n_func, void* stream,
+                                                 ria_mesh** out);
+
+/* tet5 grid of `resolution` cubes per axis over [bbox_min, bbox_max] (src/io.cpp:95-152), with the
+ * functions sampled on the device (stage a).  The mesh keeps the sampled values
+ * (RIA_MESH_FUNC_VALS). */
+RIA_API ria_status ria_grid_implicit_arrangement(const ria_config* cfg, uint32_t resolution, const double* bbox_min,
+                                         const double* bbox_max, const ria_function* funcs, uint32_t n_func,
+                                         ria_mesh** out);
+RIA_API ria_status ria_grid_material_interface(const ria_config* cfg, uint32_t resolution, const double* bbox_min,
+                                       const double* bbox_max, const ria_function* funcs, uint32_t n_func,
+                                       ria_mesh** out);
+
+/* Stage a alone: func_vals[n_pts][n_func] = funcs evaluated at pts (host buffers). */
+RIA_API ria_status ria_sample_functions(const ria_function* funcs, uint32_t n_func, const double* pts, uint64_t n_pts,
+                                double* func_vals);
+
+/* ---- per-tet entry points (the simplicial_arrangement calls) ---------------------------------
+ * values: for tet t, rows value_offsets[t] .. value_offsets[t+1]-1 of 4 corner values each
+ * (a plane or a material).  records receives the canonical records back to back; record_offsets
+ * (n_tets + 1 entries) their byte offsets.  Returns RIA_ECAPACITY if `capacity` is too small. */
+RIA_API ria_status ria_compute_arrangement_batch(const double* values, const uint32_t* value_offsets, uint64_t n_tets,
+                                         uint8_t* records, uint64_t capacity, uint64_t* record_offsets);
+RIA_API ria_status ria_compute_material_interface_batch(const double* values, const uint32_t* value_offsets,
+                                                uint64_t n_tets, uint8_t* records, uint64_t capacity,
+                                                uint64_t* record_offsets);
+
+/* ---- results ---------------------------------------------------------------------------------- */
+RIA_API uint64_t ria_mesh_count(const ria_mesh* mesh, ria_mesh_field field); /* elements of the field */
+RIA_API ria_status ria_mesh_copy(const ria_mesh* mesh, ria_mesh_field field, void* host_dst);
+RIA_API void ria_mesh_free(ria_mesh* mesh);
+
+/* Message of the last failing call on this thread. */
+RIA_API const char* ria_last_error(void);
+/* Diagnostics: number of kernels this library has launched in this process. */
+RIA_API uint64_t ria_kernel_launches(void);
+RIA_API int ria_device_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* RIA_H */

@@ -1,0 +1,94 @@
+"""ctypes binding of the C ABI (include/ria.h) for the Python test and benchmark harnesses.
+
+The library is built in-tree by build.py.  Loading fails loudly if it is missing: there is no
+Python or CPU fallback for any entry point.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import re
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libria.so")
+HEADER = os.path.join(os.path.dirname(HERE), "include", "ria.h")
+
+RIA_OK, RIA_EINVAL, RIA_ENOMEM, RIA_ECAPACITY, RIA_EDEGENERATE, RIA_ETIMEOUT, RIA_ECUDA, RIA_EINTERNAL, RIA_ENODEVICE = range(9)
+
+(FIELD_POINTS, FIELD_VERTS, FIELD_FACE_OFFSETS, FIELD_FACE_VERTS, FIELD_FACE_TET_OFFSETS, FIELD_FACE_TETS,
+ FIELD_FACE_FUNC, FIELD_FUNC_IN_TET, FIELD_START_INDEX, FIELD_REC_OFFSETS, FIELD_REC_BYTES, FIELD_STATS,
+ FIELD_TIMINGS, FIELD_FUNC_VALS) = range(14)
+
+STAT_NAMES = ["num_pts", "num_tets", "num_degenerate_vertex", "num_intersecting_tet", "num_a_func", "num_b_func",
+              "num_more_func", "num_verts", "num_faces", "num_deferred", "robust_failures"]
+TIMING_NAMES = ["sample", "filter", "cut", "extract", "total"]
+
+
+class RiaError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"ria status {status}: {msg}")
+        self.status = status
+
+
+class Config(ctypes.Structure):
+    _fields_ = [("use_lookup", ctypes.c_int32), ("use_secondary_lookup", ctypes.c_int32),
+                ("use_topo_ray_shooting", ctypes.c_int32), ("robust_test", ctypes.c_int32),
+                ("keep_records", ctypes.c_int32)]
+
+
+def declared_functions() -> list[str]:
+    """Names of every function declared in include/ria.h."""
+    with open(HEADER) as f:
+        src = f.read()
+    return re.findall(r"RIA_API\s+[\w\s\*]+?\b(ria_\w+)\s*\(", src)
+
+
+_lib = None
+
+
+def load():
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f"{LIB_PATH} is missing: build it with build.py (there is no fallback path)")
+    L = ctypes.CDLL(LIB_PATH)
+    vp, u64, u32, i32 = ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_int32
+    cfgp = ctypes.POINTER(Config)
+    for name in ("ria_compute_implicit_arrangement", "ria_compute_material_interface"):
+        fn = getattr(L, name)
+        fn.restype = i32
+        fn.argtypes = [cfgp, vp, u64, vp, u64, vp, u32, ctypes.POINTER(vp)]
+    for name in ("ria_compute_implicit_arrangement_device", "ria_compute_material_interface_device"):
+        fn = getattr(L, name)
+        fn.restype = i32
+        fn.argtypes = [cfgp, vp, u64, vp, u64, vp, u32, vp, ctypes.POINTER(vp)]
+    for name in ("ria_grid_implicit_arrangement", "ria_grid_material_interface"):
+        fn = getattr(L, name)
+        fn.restype = i32
+        fn.argtypes = [cfgp, u32, vp, vp, vp, u32, ctypes.POINTER(vp)]
+    L.ria_sample_functions.restype = i32
+    L.ria_sample_functions.argtypes = [vp, u32, vp, u64, vp]
+    for name in ("ria_compute_arrangement_batch", "ria_compute_material_interface_batch"):
+        fn = getattr(L, name)
+        fn.restype = i32
+        fn.argtypes = [vp, vp, u64, vp, u64, vp]
+    L.ria_mesh_count.restype = u64
+    L.ria_mesh_count.argtypes = [vp, i32]
+    L.ria_mesh_copy.restype = i32
+    L.ria_mesh_copy.argtypes = [vp, i32, vp]
+    L.ria_mesh_free.restype = None
+    L.ria_mesh_free.argtypes = [vp]
+    L.ria_last_error.restype = ctypes.c_char_p
+    L.ria_last_error.argtypes = []
+    L.ria_device_count.restype = ctypes.c_int
+    L.ria_device_count.argtypes = []
+    L.ria_kernel_launches.restype = u64
+    L.ria_kernel_launches.argtypes = []
+    _lib = L
+    return L
+
+
+def check(status: int):
+    if status != RIA_OK:
+        raise RiaError(status, load().ria_last_error().decode())

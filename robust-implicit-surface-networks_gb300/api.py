@@ -1,0 +1,167 @@
+"""Python mirror of the reference's pipeline entry points over the C ABI (tests and benchmark).
+
+  implicit_arrangement(pts, tets, func_vals, ...)   src/implicit_arrangement.h:39-62
+  material_interface(pts, tets, func_vals, ...)     src/material_interface.h:38-61
+  grid_implicit_arrangement / grid_material_interface: tet5 grid + sampling on the device
+  compute_arrangement_batch / compute_material_interface_batch: the per-tet
+      simplicial_arrangement calls for many tets at once
+Results come back as numpy arrays; every computation runs on the GPU.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from .functions import FUNC_DTYPE
+
+
+class Mesh:
+    """Owner of a ria_mesh handle (device buffers); fields are copied to the host on demand."""
+
+    _FIELDS = {
+        "xyz": (_lib.FIELD_POINTS, np.float64, (-1, 3)),
+        "verts": (_lib.FIELD_VERTS, np.int64, (-1, 11)),
+        "face_offsets": (_lib.FIELD_FACE_OFFSETS, np.int64, None),
+        "face_verts": (_lib.FIELD_FACE_VERTS, np.int64, None),
+        "face_tet_offsets": (_lib.FIELD_FACE_TET_OFFSETS, np.int64, None),
+        "face_tets": (_lib.FIELD_FACE_TETS, np.int64, (-1, 2)),
+        "face_func": (_lib.FIELD_FACE_FUNC, np.int64, (-1, 2)),
+        "func_in_tet": (_lib.FIELD_FUNC_IN_TET, np.int64, None),
+        "start_index": (_lib.FIELD_START_INDEX, np.int64, None),
+        "rec_offsets": (_lib.FIELD_REC_OFFSETS, np.int64, None),
+        "rec_bytes": (_lib.FIELD_REC_BYTES, np.uint8, None),
+        "func_vals": (_lib.FIELD_FUNC_VALS, np.float64, None),
+    }
+
+    def __init__(self, handle):
+        self._h = handle
+        self._cache = {}
+
+    def __del__(self):
+        self.close()
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _lib.load().ria_mesh_free(self._h)
+            self._h = None
+
+    def _copy(self, field, dtype):
+        L = _lib.load()
+        n = int(L.ria_mesh_count(self._h, field))
+        out = np.zeros(n, dtype=dtype)
+        if n:
+            _lib.check(L.ria_mesh_copy(self._h, field, out.ctypes.data))
+        return out
+
+    def __getitem__(self, name):
+        if name not in self._cache:
+            if name == "stats":
+                a = np.zeros(len(_lib.STAT_NAMES), dtype=np.int64)
+                _lib.check(_lib.load().ria_mesh_copy(self._h, _lib.FIELD_STATS, a.ctypes.data))
+                self._cache[name] = a
+            elif name == "timings":
+                a = np.zeros(len(_lib.TIMING_NAMES), dtype=np.float64)
+                _lib.check(_lib.load().ria_mesh_copy(self._h, _lib.FIELD_TIMINGS, a.ctypes.data))
+                self._cache[name] = a
+            else:
+                field, dt, shape = self._FIELDS[name]
+                a = self._copy(field, dt)
+                self._cache[name] = a.reshape(shape) if shape else a
+        return self._cache[name]
+
+    @property
+    def stats(self) -> dict:
+        return dict(zip(_lib.STAT_NAMES, self["stats"].tolist()))
+
+    @property
+    def timings(self) -> dict:
+        return dict(zip(_lib.TIMING_NAMES, self["timings"].tolist()))
+
+
+def _config(use_lookup=True, use_secondary_lookup=True, use_topo_ray_shooting=True, robust_test=False):
+    if not use_lookup:
+        use_secondary_lookup = False
+    return _lib.Config(int(use_lookup), int(use_secondary_lookup), int(use_topo_ray_shooting), int(robust_test), 1)
+
+
+def _run_host(name, pts, tets, func_vals, **kw):
+    L = _lib.load()
+    pts = np.ascontiguousarray(pts, dtype=np.float64).reshape(-1, 3)
+    tets = np.ascontiguousarray(tets, dtype=np.int64).reshape(-1, 4)
+    fv = np.ascontiguousarray(func_vals, dtype=np.float64)
+    if fv.ndim != 2 or fv.shape[0] != pts.shape[0]:
+        raise ValueError("func_vals must be n_pts x n_func")
+    cfg = _config(**kw)
+    h = ctypes.c_void_p()
+    st = getattr(L, name)(ctypes.byref(cfg), pts.ctypes.data, pts.shape[0], tets.ctypes.data, tets.shape[0],
+                          fv.ctypes.data, fv.shape[1], ctypes.byref(h))
+    _lib.check(st)
+    return Mesh(h)
+
+
+def implicit_arrangement(pts, tets, func_vals, **kw) -> Mesh:
+    return _run_host("ria_compute_implicit_arrangement", pts, tets, func_vals, **kw)
+
+
+def material_interface(pts, tets, func_vals, **kw) -> Mesh:
+    return _run_host("ria_compute_material_interface", pts, tets, func_vals, **kw)
+
+
+def _run_grid(name, res, funcs, bbox_min=(-1.0, -1.0, -1.0), bbox_max=(1.0, 1.0, 1.0), **kw):
+    L = _lib.load()
+    funcs = np.ascontiguousarray(funcs, dtype=FUNC_DTYPE)
+    bmin = np.asarray(bbox_min, dtype=np.float64)
+    bmax = np.asarray(bbox_max, dtype=np.float64)
+    cfg = _config(**kw)
+    h = ctypes.c_void_p()
+    st = getattr(L, name)(ctypes.byref(cfg), int(res), bmin.ctypes.data, bmax.ctypes.data, funcs.ctypes.data,
+                          len(funcs), ctypes.byref(h))
+    _lib.check(st)
+    return Mesh(h)
+
+
+def grid_implicit_arrangement(res, funcs, **kw) -> Mesh:
+    return _run_grid("ria_grid_implicit_arrangement", res, funcs, **kw)
+
+
+def grid_material_interface(res, funcs, **kw) -> Mesh:
+    return _run_grid("ria_grid_material_interface", res, funcs, **kw)
+
+
+def sample_functions(funcs, pts) -> np.ndarray:
+    L = _lib.load()
+    funcs = np.ascontiguousarray(funcs, dtype=FUNC_DTYPE)
+    pts = np.ascontiguousarray(pts, dtype=np.float64).reshape(-1, 3)
+    out = np.zeros((pts.shape[0], len(funcs)))
+    _lib.check(L.ria_sample_functions(funcs.ctypes.data, len(funcs), pts.ctypes.data, pts.shape[0], out.ctypes.data))
+    return out
+
+
+def _batch(name, rows_per_tet):
+    L = _lib.load()
+    offs = np.zeros(len(rows_per_tet) + 1, dtype=np.uint32)
+    for i, r in enumerate(rows_per_tet):
+        offs[i + 1] = offs[i] + len(r)
+    vals = np.ascontiguousarray(np.concatenate([np.asarray(r, dtype=np.float64).reshape(-1, 4) for r in rows_per_tet])
+                                if len(rows_per_tet) else np.zeros((0, 4)))
+    cap = 6144 * max(1, len(rows_per_tet))
+    buf = np.zeros(cap, dtype=np.uint8)
+    roff = np.zeros(len(rows_per_tet) + 1, dtype=np.uint64)
+    _lib.check(getattr(L, name)(vals.ctypes.data, offs.ctypes.data, len(rows_per_tet), buf.ctypes.data, cap,
+                                roff.ctypes.data))
+    return [bytes(buf[int(roff[i]):int(roff[i + 1])]) for i in range(len(rows_per_tet))]
+
+
+def compute_arrangement_batch(planes_per_tet) -> list[bytes]:
+    """Canonical arrangement record of each tet (rows: 4 corner values per plane)."""
+    return _batch("ria_compute_arrangement_batch", planes_per_tet)
+
+
+def compute_material_interface_batch(materials_per_tet) -> list[bytes]:
+    return _batch("ria_compute_material_interface_batch", materials_per_tet)
+
+
+def device_count() -> int:
+    return int(_lib.load().ria_device_count())

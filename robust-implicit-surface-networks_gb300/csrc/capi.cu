@@ -1,0 +1,770 @@
+// C ABI (include/ria.h): host orchestration of stages (a)-(d) on the current CUDA device.
+//
+// One call runs: sampling or upload -> vertex masks -> ordered compaction of the active tets
+// (tets whose single active plane / two active materials are resolved from the per-device lookup
+// table) -> fast per-tet cut -> exact cut of the deferred tets -> extraction.  Device memory comes
+// from the stream-ordered allocator and is returned to its pool when the mesh is freed.
+#include <cuda_runtime.h>
+
+#include <cub/cub.cuh>
+#include <atomic>
+#include <chrono>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "device_common.cuh"
+#include "launch.hpp"
+
+using namespace ria;
+
+namespace {
+std::atomic<uint64_t> g_launches{0};
+}
+
+void ria::note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+
+namespace {
+
+thread_local std::string g_err;
+
+ria_status fail(ria_status s, const std::string& msg) {
+    g_err = msg;
+    return s;
+}
+
+#define RIA_CUDA(call)                                                                        \
+    do {                                                                                      \
+        cudaError_t e_ = (call);                                                              \
+        if (e_ != cudaSuccess) return fail(RIA_ECUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+struct DeviceCtx {
+    bool ready[2] = {false, false};
+    uint8_t* table[2] = {nullptr, nullptr};
+    uint32_t* table_off[2] = {nullptr, nullptr};
+    IASum4* table_sum[2] = {nullptr, nullptr};
+};
+
+std::mutex g_mu;
+std::vector<DeviceCtx> g_ctx;
+
+constexpr int64_t kFastRecordBytes = 1024;  // bound of a record of the fast variants
+constexpr int64_t kBigRecordBytes = 5120;   // bound of a record of the exact variants
+constexpr int64_t kBigSlots = 152 * 64;     // concurrent exact-variant threads
+
+ria_status current_device(int* dev) {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+        cudaGetLastError();
+        return fail(RIA_ENODEVICE, "no CUDA device: this library only computes on the GPU");
+    }
+    RIA_CUDA(cudaGetDevice(dev));
+    return RIA_OK;
+}
+
+// Build (once per device) the lookup table of one mode with the exact per-tet cut.
+ria_status ensure_table(bool mi, cudaStream_t s, DeviceCtx** out) {
+    int dev = 0;
+    ria_status st = current_device(&dev);
+    if (st != RIA_OK) return st;
+    std::lock_guard<std::mutex> lk(g_mu);
+    if ((int)g_ctx.size() <= dev) g_ctx.resize(dev + 1);
+    DeviceCtx& c = g_ctx[dev];
+    const int m = mi ? 1 : 0;
+    if (!c.ready[0] && !c.ready[1]) {
+        // keep freed blocks in the stream-ordered pool so that repeated calls do not re-allocate
+        cudaMemPool_t pool;
+        if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+            uint64_t thr = ~0ull;
+            cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+        }
+    }
+    if (!c.ready[m]) {
+        RIA_CUDA(cudaMalloc(&c.table[m], (size_t)kTablePatterns * kTableStride));
+        RIA_CUDA(cudaMalloc(&c.table_off[m], sizeof(uint32_t) * kTablePatterns));
+        RIA_CUDA(cudaMalloc(&c.table_sum[m], sizeof(IASum4) * kTablePatterns));
+        void* scratch = nullptr;
+        uint32_t* status = nullptr;
+        RIA_CUDA(cudaMalloc(&scratch, cut_big_slot_bytes(mi) * kTablePatterns));
+        RIA_CUDA(cudaMalloc(&status, sizeof(uint32_t)));
+        RIA_CUDA(cudaMemsetAsync(status, 0, sizeof(uint32_t), s));
+        launch_build_table(mi, c.table[m], c.table_off[m], c.table_sum[m], scratch, status, s);
+        RIA_CUDA(cudaGetLastError());
+        uint32_t h = 0;
+        RIA_CUDA(cudaMemcpyAsync(&h, status, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+        RIA_CUDA(cudaStreamSynchronize(s));
+        cudaFree(scratch);
+        cudaFree(status);
+        if (h) return fail(RIA_EINTERNAL, "lookup table construction failed");
+        c.ready[m] = true;
+    }
+    *out = &c;
+    return RIA_OK;
+}
+
+ria_status map_status(uint32_t st) {
+    if (st & ST_INTERNAL) return fail(RIA_EINTERNAL, "per-tet cut: internal consistency check failed");
+    if (st & ST_EXACT) return fail(RIA_EDEGENERATE, "exact predicate exceeded its expansion capacity");
+    if (st & ST_CAPACITY) return fail(RIA_ECAPACITY, "a tet's arrangement exceeds the per-tet capacity");
+    if (st & ST_HASH_FULL) return fail(RIA_EINTERNAL, "deduplication hash table full");
+    if (st & ST_NONMANIFOLD) return fail(RIA_EINVAL, "a tet face is shared by more than two tets");
+    return RIA_OK;
+}
+
+struct Inputs {
+    bool mi = false;
+    int64_t V = 0, T = 0;
+    int F = 0;
+    GridDesc g{0, {0, 0, 0}, {0, 0, 0}};
+    const double* d_pts = nullptr;
+    const int64_t* d_tets = nullptr;
+    const double* d_fv = nullptr;       // explicit values, or
+    const ria_function* funcs = nullptr;  // functions sampled on the grid (host array)
+};
+
+// device allocations of one call
+struct Allocs {
+    cudaStream_t s;
+    std::vector<void*> v;
+    template <class T>
+    T* get(int64_t n, cudaError_t* err) {
+        void* p = nullptr;
+        cudaError_t e = cudaMallocAsync(&p, sizeof(T) * (size_t)(n > 0 ? n : 1), s);
+        if (e != cudaSuccess) {
+            *err = e;
+            return nullptr;
+        }
+        v.push_back(p);
+        return (T*)p;
+    }
+    void release() {
+        for (void* p : v) cudaFreeAsync(p, s);
+        v.clear();
+    }
+};
+
+}  // namespace
+
+struct ria_mesh {
+    bool mi = false;
+    int64_t V = 0, T = 0;
+    int F = 0;
+    cudaStream_t s = nullptr;
+    bool own_stream = false;
+    ExtractOut ex;
+    Allocs keep;  // retained device state (active lists, record heaps, sampled values, ...)
+    int64_t A = 0;
+    uint32_t* act_tet = nullptr;
+    uint64_t* act_mask = nullptr;
+    uint64_t* act_desc = nullptr;
+    uint8_t* heap = nullptr;
+    uint8_t* heap_big = nullptr;
+    const uint8_t* table = nullptr;
+    const uint32_t* table_off = nullptr;
+    double* fv = nullptr;
+    bool have_rec = false, have_fit = false;
+    int64_t* rec_offsets = nullptr;
+    uint8_t* rec_bytes = nullptr;
+    int64_t n_rec_bytes = 0;
+    int64_t* start_index = nullptr;
+    int64_t* func_in_tet = nullptr;
+    int64_t n_fit = 0;
+    int64_t stats[RIA_NUM_STATS] = {0};
+    double timings[RIA_NUM_TIMINGS] = {0};
+};
+
+namespace {
+
+ria_status run_pipeline(const ria_config* cfg, const Inputs& in, cudaStream_t s, bool own_stream, ria_mesh** out) {
+    if (!cfg || !out) return fail(RIA_EINVAL, "null argument");
+    if (in.F < 1 || in.F > 64) return fail(RIA_EINVAL, "n_func must be in 1..64");
+    if (in.V <= 0 || in.V >= (1ll << 31)) return fail(RIA_EINVAL, "n_pts must be in 1..2^31-1");
+    if (in.T < 0 || in.T >= (1ll << 32)) return fail(RIA_EINVAL, "n_tets must be below 2^32");
+    const bool mi = in.mi;
+    const bool use_table = cfg->use_lookup != 0;
+    DeviceCtx* ctx = nullptr;
+    ria_status st = ensure_table(mi, s, &ctx);
+    if (st != RIA_OK) return st;
+
+    ria_mesh* M = new ria_mesh();
+    M->mi = mi;
+    M->V = in.V;
+    M->T = in.T;
+    M->F = in.F;
+    M->s = s;
+    M->own_stream = own_stream;
+    M->keep.s = s;
+    M->table = ctx->table[mi];
+    M->table_off = ctx->table_off[mi];
+    Allocs tmp{s, {}};
+    cudaError_t err = cudaSuccess;
+    cudaEvent_t ev[5];
+    for (auto& e : ev) cudaEventCreate(&e);
+    auto destroy_events = [&]() {
+        for (auto& e : ev) cudaEventDestroy(e);
+    };
+    auto bail = [&](ria_status r) {
+        tmp.release();
+        cudaStreamSynchronize(s);
+        destroy_events();
+        M->own_stream = false;  // the caller owns the stream until the call succeeds
+        ria_mesh_free(M);
+        return r;
+    };
+    cudaEventRecord(ev[0], s);
+
+    // counters: 0 status, 1 n_zero, 2..4 k histogram, 5 heap used, 6 big heap used, 7 deferred, 8 robust failures
+    unsigned long long* cnt = tmp.get<unsigned long long>(16, &err);
+    uint32_t* status = (uint32_t*)cnt;
+    if (err != cudaSuccess) return bail(fail(RIA_ENOMEM, "device allocation failed"));
+    cudaMemsetAsync(cnt, 0, sizeof(unsigned long long) * 16, s);
+    if (in.d_tets) {
+        // every kernel below indexes through the tets: check them before any of them runs
+        launch_check_tets(in.d_tets, in.T, in.V, status, s);
+        uint32_t hst = 0;
+        cudaMemcpyAsync(&hst, status, 4, cudaMemcpyDeviceToHost, s);
+        if (cudaStreamSynchronize(s) != cudaSuccess) return bail(fail(RIA_ECUDA, cudaGetErrorString(cudaGetLastError())));
+        if (hst & ST_BADINPUT) return bail(fail(RIA_EINVAL, "a tet refers to a vertex outside 0..n_pts-1"));
+    }
+
+    // ---- stage a
+    ulonglong2* vmask = tmp.get<ulonglong2>(in.V, &err);
+    const double* fv = in.d_fv;
+    if (in.funcs) {
+        double* d_fv = M->keep.get<double>(in.V * in.F, &err);
+        ria_function* d_funcs = tmp.get<ria_function>(in.F, &err);
+        if (err != cudaSuccess) return bail(fail(RIA_ENOMEM, "device allocation failed"));
+        cudaMemcpyAsync(d_funcs, in.funcs, sizeof(ria_function) * in.F, cudaMemcpyHostToDevice, s);
+        launch_sample_grid(mi, d_funcs, in.F, in.g, d_fv, vmask, cnt + 1, s);
+        fv = d_fv;
+        M->fv = d_fv;
+    } else {
+        if (err != cudaSuccess) return bail(fail(RIA_ENOMEM, "device allocation failed"));
+        launch_vertex_masks(mi, fv, in.V, in.F, vmask, cnt + 1, s);
+    }
+    cudaEventRecord(ev[1], s);
+
+    // ---- stage b
+    const int64_t nb = filter_num_blocks(in.T);
+    uint32_t* blk = tmp.get<uint32_t>(2 * nb, &err);
+    uint32_t* blk_off = tmp.get<uint32_t>(2 * nb, &err);
+    if (err != cudaSuccess) return bail(fail(RIA_ENOMEM, "device allocation failed"));
+    int64_t A = 0, G = 0;
+    if (nb > 0) {
+        launch_filter_count(mi, vmask, fv, in.F, in.d_tets, in.g, in.T, use_table, blk, cnt + 2, s);
+        size_t bytes = 0;
+        cub::DeviceScan::ExclusiveSum(nullptr, bytes, blk, blk_off, 2 * nb, s);
+        uint8_t* scan_tmp = tmp.get<uint8_t>((int64_t)bytes, &err);
+        if (err != cudaSuccess) return bail(fail(RIA_ENOMEM, "device allocation failed"));
+        cub::DeviceScan::ExclusiveSum(scan_tmp, bytes, blk, blk_off, 2 * nb, s);
+        uint32_t h[3];
+        cudaMemcpyAsync(&h[0], blk_off + nb, 4, cudaMemcpyDeviceToHost, s);
+        cudaMemcpyAsync(&h[1], blk_off + 2 * nb - 1, 4, cudaMemcpyDeviceToHost, s);
+        cudaMemcpyAsync(&h[2], blk + 2 * nb - 1, 4, cudaMemcpyDeviceToHost, s);
+        if (cudaStreamSynchronize(s) != cudaSuccess) return bail(fail(RIA_ECUDA, cudaGetErrorString(cudaGetLastError())));
+        A = h[0];
+        G = (int64_t)h[1] + h[2] - A;
+    }
+    M->A = A;
+    M->act_tet = M->keep.get<uint32_t>(A, &err);
+    M->act_mask = M->keep.get<uint64_t>(A, &err);
+    M->act_desc = M->keep.get<uint64_t>(A, &err);
+    IASum4* act_sum = tmp.get<IASum4>(A, &err);
+    uint32_t* gen = tmp.get<uint32_t>(G, &err);
+    if (err != cudaSuccess) return bail(fail(RIA_ENOMEM, "device allocation failed"));
+    if (nb > 0) {
+        FilterOut fo{M->act_tet, M->act_mask, M->act_desc, act_sum, gen};
+        launch_filter_scatter(mi, vmask, fv, in.F, in.d_tets, in.g, in.T, use_table, blk_off, ctx->table_sum[mi], fo, s);
+    }
+    cudaEventRecord(ev[2], s);
+
+    // ---- stage c
+    CutArgs ca{};
+    ca.mi = mi;
+    ca.act_tet = M->act_tet;
+    ca.act_mask = M->act_mask;
+    ca.act_desc = M->act_desc;
+    ca.act_sum = act_sum;
+    ca.fv = fv;
+    ca.F = in.F;
+    ca.d_tets = in.d_tets;
+    ca.g = in.g;
+    ca.status = status;
+    int64_t n_def = 0;
+    if (cfg->robust_test) {
+        // every active tet, exact variant, both plane orders; no mesh is extracted
+        uint32_t* ident = tmp.get<uint32_t>(A, &err);
+        void* scratch = tmp.get<uint8_t>((int64_t)cut_big_slot_bytes(mi) * kBigSlots, &err);
+        if (err != cudaSuccess) return bail(fail(RIA_ENOMEM, "device allocation failed"));
+        std::vector<uint32_t> h(A);
+        for (int64_t i = 0; i < A; ++i) h[i] = (uint32_t)i;
+        cudaMemcpyAsync(ident, h.data(), 4 * A, cudaMemcpyHostToDevice, s);
+        ca.list = ident;
+        ca.n = A;
+        launch_robust(ca, scratch, kBigSlots, cnt + 8, s);
+        cudaStreamSynchronize(s);
+    } else if (G > 0) {
+        M->heap = M->keep.get<uint8_t>(G * kFastRecordBytes, &err);
+        uint32_t* deferred = tmp.get<uint32_t>(G, &err);
+        if (err != cudaSuccess) return bail(fail(RIA_ENOMEM, "device allocation failed"));
+        ca.list = gen;
+        ca.n = G;
+        ca.heap = M->heap;
+        ca.heap_used = cnt + 5;
+        ca.heap_cap = (uint64_t)G * kFastRecordBytes;
+        ca.desc_bit = 0;
+        ca.deferred = deferred;
+        ca.n_deferred = (unsigned int*)(cnt + 7);
+        launch_cut_fast(ca, s);
+        unsigned long long h = 0;
+        cudaMemcpyAsync(&h, cnt + 7, 8, cudaMemcpyDeviceToHost, s);
+        if (cudaStreamSynchronize(s) != cudaSuccess) return bail(fail(RIA_ECUDA, cudaGetErrorString(cudaGetLastError())));
+        n_def = (int64_t)(h & 0xFFFFFFFFull);
+        if (n_def > 0) {
+            M->heap_big = M->keep.get<uint8_t>(n_def * kBigRecordBytes, &err);
+            const int64_t slots = n_def < kBigSlots ? n_def : kBigSlots;
+            void* scratch = tmp.get<uint8_t>((int64_t)cut_big_slot_bytes(mi) * slots, &err);
+            if (err != cudaSuccess) return bail(fail(RIA_ENOMEM, "device allocation failed"));
+            CutArgs cb = ca;
+            cb.list = deferred;
+            cb.n = n_def;
+            cb.heap = M->heap_big;
+            cb.heap_used = cnt + 6;
+            cb.heap_cap = (uint64_t)n_def * kBigRecordBytes;
+            cb.desc_bit = kBigHeapBit;
+            launch_cut_big(cb, scratch, slots, s);
+        }
+    }
+    cudaEventRecord(ev[3], s);
+
+    // ---- stage d
+    if (!cfg->robust_test) {
+        ExtractArgs xa{};
+        xa.mi = mi;
+        xa.A = A;
+        xa.act_tet = M->act_tet;
+        xa.act_mask = M->act_mask;
+        xa.act_desc = M->act_desc;
+        xa.heap = M->heap;
+        xa.heap_big = M->heap_big;
+        xa.table = M->table;
+        xa.table_off = M->table_off;
+        xa.fv = fv;
+        xa.F = in.F;
+        xa.d_tets = in.d_tets;
+        xa.d_pts = in.d_pts;
+        xa.g = in.g;
+        xa.V = in.V;
+        xa.status = status;
+        // the extraction reads the status only through its own checks; stop early on cut errors
+        uint32_t hst = 0;
+        cudaMemcpyAsync(&hst, status, 4, cudaMemcpyDeviceToHost, s);
+        cudaStreamSynchronize(s);
+        if (hst) return bail(map_status(hst));
+        cudaError_t e = run_extract(xa, act_sum, M->ex, s);
+        if (e == cudaErrorNotSupported) return bail(fail(RIA_EINVAL, "material-interface extraction is not available"));
+        if (e != cudaSuccess) return bail(fail(RIA_ECUDA, std::string("extract: ") + cudaGetErrorString(e)));
+    }
+    cudaEventRecord(ev[4], s);
+
+    unsigned long long h[16];
+    cudaMemcpyAsync(h, cnt, sizeof(h), cudaMemcpyDeviceToHost, s);
+    cudaError_t se = cudaStreamSynchronize(s);
+    if (se != cudaSuccess) return bail(fail(RIA_ECUDA, cudaGetErrorString(se)));
+    ria_status ms = map_status((uint32_t)h[0]);
+    if (ms != RIA_OK) return bail(ms);
+    M->stats[RIA_STAT_NUM_PTS] = in.V;
+    M->stats[RIA_STAT_NUM_TETS] = in.T;
+    M->stats[RIA_STAT_NUM_DEGENERATE_VERTEX] = (int64_t)h[1];
+    M->stats[RIA_STAT_NUM_INTERSECTING_TET] = A;
+    M->stats[RIA_STAT_NUM_A_FUNC] = (int64_t)h[2];
+    M->stats[RIA_STAT_NUM_B_FUNC] = (int64_t)h[3];
+    M->stats[RIA_STAT_NUM_MORE_FUNC] = (int64_t)h[4];
+    M->stats[RIA_STAT_NUM_VERTS] = M->ex.n_verts;
+    M->stats[RIA_STAT_NUM_FACES] = M->ex.n_faces;
+    M->stats[RIA_STAT_NUM_DEFERRED] = n_def;
+    M->stats[RIA_STAT_ROBUST_FAILURES] = (int64_t)h[8];
+    float ms_[4];
+    for (int i = 0; i < 4; ++i) cudaEventElapsedTime(&ms_[i], ev[i], ev[i + 1]);
+    for (int i = 0; i < 4; ++i) M->timings[i] = ms_[i] * 1e-3;
+    float tot = 0;
+    cudaEventElapsedTime(&tot, ev[0], ev[4]);
+    M->timings[RIA_TIME_TOTAL] = tot * 1e-3;
+    destroy_events();
+    tmp.release();
+    *out = M;
+    if (cfg->robust_test && h[8] > 0) {
+        g_err = "robust test: results differ between the two plane orders";
+        return RIA_EINTERNAL;
+    }
+    return RIA_OK;
+}
+
+ria_status upload_and_run(bool mi, const ria_config* cfg, const double* pts, uint64_t n_pts, const int64_t* tets,
+                          uint64_t n_tets, const double* func_vals, uint32_t n_func, ria_mesh** out) {
+    if (!pts || !tets || !func_vals || !out) return fail(RIA_EINVAL, "null argument");
+    int dev = 0;
+    ria_status st = current_device(&dev);
+    if (st != RIA_OK) return st;
+    cudaStream_t s;
+    RIA_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    double* d_pts = nullptr;
+    int64_t* d_tets = nullptr;
+    double* d_fv = nullptr;
+    RIA_CUDA(cudaMallocAsync(&d_pts, sizeof(double) * 3 * n_pts, s));
+    RIA_CUDA(cudaMallocAsync(&d_tets, sizeof(int64_t) * 4 * (n_tets > 0 ? n_tets : 1), s));
+    RIA_CUDA(cudaMallocAsync(&d_fv, sizeof(double) * n_pts * n_func, s));
+    RIA_CUDA(cudaMemcpyAsync(d_pts, pts, sizeof(double) * 3 * n_pts, cudaMemcpyHostToDevice, s));
+    if (n_tets) RIA_CUDA(cudaMemcpyAsync(d_tets, tets, sizeof(int64_t) * 4 * n_tets, cudaMemcpyHostToDevice, s));
+    RIA_CUDA(cudaMemcpyAsync(d_fv, func_vals, sizeof(double) * n_pts * n_func, cudaMemcpyHostToDevice, s));
+    Inputs in;
+    in.mi = mi;
+    in.V = (int64_t)n_pts;
+    in.T = (int64_t)n_tets;
+    in.F = (int)n_func;
+    in.d_pts = d_pts;
+    in.d_tets = d_tets;
+    in.d_fv = d_fv;
+    st = run_pipeline(cfg, in, s, true, out);
+    if (st == RIA_OK) {
+        // the mesh keeps the uploaded inputs alive with its other buffers
+        (*out)->keep.v.push_back(d_pts);
+        (*out)->keep.v.push_back(d_tets);
+        (*out)->keep.v.push_back(d_fv);
+        (*out)->fv = d_fv;
+    } else {
+        cudaFreeAsync(d_pts, s);
+        cudaFreeAsync(d_tets, s);
+        cudaFreeAsync(d_fv, s);
+        cudaStreamSynchronize(s);
+        cudaStreamDestroy(s);
+    }
+    return st;
+}
+
+ria_status grid_run(bool mi, const ria_config* cfg, uint32_t res, const double* bmin, const double* bmax,
+                    const ria_function* funcs, uint32_t n_func, ria_mesh** out) {
+    if (!bmin || !bmax || !funcs || !out) return fail(RIA_EINVAL, "null argument");
+    if (res == 0 || res > 1200) return fail(RIA_EINVAL, "resolution must be in 1..1200");
+    int dev = 0;
+    ria_status st = current_device(&dev);
+    if (st != RIA_OK) return st;
+    cudaStream_t s;
+    RIA_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    Inputs in;
+    in.mi = mi;
+    const int64_t N = (int64_t)res + 1;
+    in.V = N * N * N;
+    in.T = 5 * (int64_t)res * res * res;
+    in.F = (int)n_func;
+    in.g.res = res;
+    for (int a = 0; a < 3; ++a) {
+        in.g.bmin[a] = bmin[a];
+        in.g.bmax[a] = bmax[a];
+    }
+    in.funcs = funcs;
+    st = run_pipeline(cfg, in, s, true, out);
+    if (st != RIA_OK) cudaStreamDestroy(s);
+    return st;
+}
+
+ria_status batch_run(bool mi, const double* values, const uint32_t* value_offsets, uint64_t n_tets,
+                     uint8_t* records, uint64_t capacity, uint64_t* record_offsets) {
+    if (!values || !value_offsets || !records || !record_offsets) return fail(RIA_EINVAL, "null argument");
+    DeviceCtx* ctx = nullptr;
+    int dev = 0;
+    ria_status st = current_device(&dev);
+    if (st != RIA_OK) return st;
+    for (uint64_t i = 0; i < n_tets; ++i)
+        if (value_offsets[i + 1] < value_offsets[i] || value_offsets[i + 1] - value_offsets[i] > 60)
+            return fail(RIA_EINVAL, "each tet needs 0..60 rows");
+    cudaStream_t s;
+    RIA_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    st = ensure_table(mi, s, &ctx);
+    if (st != RIA_OK) {
+        cudaStreamDestroy(s);
+        return st;
+    }
+    const int64_t n = (int64_t)n_tets;
+    const uint64_t rows = value_offsets[n_tets];
+    Allocs tmp{s, {}};
+    cudaError_t err = cudaSuccess;
+    double* d_vals = tmp.get<double>(4 * (int64_t)rows, &err);
+    uint32_t* d_off = tmp.get<uint32_t>(n + 1, &err);
+    uint32_t* ident = tmp.get<uint32_t>(n, &err);
+    uint64_t* desc = tmp.get<uint64_t>(n, &err);
+    IASum4* sum = tmp.get<IASum4>(n, &err);
+    uint8_t* heap = tmp.get<uint8_t>(n * kFastRecordBytes, &err);
+    uint32_t* deferred = tmp.get<uint32_t>(n, &err);
+    unsigned long long* cnt = tmp.get<unsigned long long>(8, &err);
+    int64_t* d_rec_off = tmp.get<int64_t>(n + 1, &err);
+    auto done = [&](ria_status r) {
+        tmp.release();
+        cudaStreamSynchronize(s);
+        cudaStreamDestroy(s);
+        return r;
+    };
+    if (err != cudaSuccess) return done(fail(RIA_ENOMEM, "device allocation failed"));
+    std::vector<uint32_t> h_ident(n);
+    for (int64_t i = 0; i < n; ++i) h_ident[i] = (uint32_t)i;
+    cudaMemcpyAsync(d_vals, values, sizeof(double) * 4 * rows, cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(d_off, value_offsets, sizeof(uint32_t) * (n + 1), cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(ident, h_ident.data(), sizeof(uint32_t) * n, cudaMemcpyHostToDevice, s);
+    cudaMemsetAsync(cnt, 0, 64, s);
+    cudaMemsetAsync(desc, 0, 8 * n, s);
+    CutArgs ca{};
+    ca.mi = mi;
+    ca.list = ident;
+    ca.n = n;
+    ca.act_desc = desc;
+    ca.act_sum = sum;
+    ca.heap = heap;
+    ca.heap_used = cnt + 1;
+    ca.heap_cap = (uint64_t)n * kFastRecordBytes;
+    ca.deferred = deferred;
+    ca.n_deferred = (unsigned int*)(cnt + 2);
+    ca.status = (uint32_t*)cnt;
+    ca.values = d_vals;
+    ca.value_off = d_off;
+    launch_cut_fast(ca, s);
+    unsigned long long h[4];
+    cudaMemcpyAsync(h, cnt, 32, cudaMemcpyDeviceToHost, s);
+    if (cudaStreamSynchronize(s) != cudaSuccess) return done(fail(RIA_ECUDA, cudaGetErrorString(cudaGetLastError())));
+    const int64_t n_def = (int64_t)(h[2] & 0xFFFFFFFFull);
+    uint8_t* heap_big = nullptr;
+    if (n_def > 0) {
+        heap_big = tmp.get<uint8_t>(n_def * kBigRecordBytes, &err);
+        const int64_t slots = n_def < kBigSlots ? n_def : kBigSlots;
+        void* scratch = tmp.get<uint8_t>((int64_t)cut_big_slot_bytes(mi) * slots, &err);
+        if (err != cudaSuccess) return done(fail(RIA_ENOMEM, "device allocation failed"));
+        CutArgs cb = ca;
+        cb.list = deferred;
+        cb.n = n_def;
+        cb.heap = heap_big;
+        cb.heap_used = cnt + 3;
+        cb.heap_cap = (uint64_t)n_def * kBigRecordBytes;
+        cb.desc_bit = kBigHeapBit;
+        launch_cut_big(cb, scratch, slots, s);
+    }
+    cudaMemcpyAsync(h, cnt, 8, cudaMemcpyDeviceToHost, s);
+    if (cudaStreamSynchronize(s) != cudaSuccess) return done(fail(RIA_ECUDA, cudaGetErrorString(cudaGetLastError())));
+    ria_status ms = map_status((uint32_t)h[0]);
+    if (ms != RIA_OK) return done(ms);
+    uint8_t* d_bytes = nullptr;
+    int64_t nbytes = 0;
+    cudaError_t e = gather_records(mi, n, n, ident, desc, heap, heap_big, ctx->table[mi], ctx->table_off[mi], d_rec_off,
+                                   &d_bytes, &nbytes, s);
+    if (e != cudaSuccess) return done(fail(RIA_ECUDA, cudaGetErrorString(e)));
+    tmp.v.push_back(d_bytes);
+    if ((uint64_t)nbytes > capacity) return done(fail(RIA_ECAPACITY, "record buffer too small"));
+    std::vector<int64_t> off(n + 1);
+    cudaMemcpyAsync(off.data(), d_rec_off, 8 * (n + 1), cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(records, d_bytes, (size_t)nbytes, cudaMemcpyDeviceToHost, s);
+    if (cudaStreamSynchronize(s) != cudaSuccess) return done(fail(RIA_ECUDA, cudaGetErrorString(cudaGetLastError())));
+    for (int64_t i = 0; i <= n; ++i) record_offsets[i] = (uint64_t)off[i];
+    return done(RIA_OK);
+}
+
+}  // namespace
+
+extern "C" {
+
+ria_status ria_compute_implicit_arrangement(const ria_config* cfg, const double* pts, uint64_t n_pts,
+                                            const int64_t* tets, uint64_t n_tets, const double* func_vals,
+                                            uint32_t n_func, ria_mesh** out) {
+    return upload_and_run(false, cfg, pts, n_pts, tets, n_tets, func_vals, n_func, out);
+}
+
+ria_status ria_compute_material_interface(const ria_config* cfg, const double* pts, uint64_t n_pts,
+                                          const int64_t* tets, uint64_t n_tets, const double* func_vals,
+                                          uint32_t n_func, ria_mesh** out) {
+    return upload_and_run(true, cfg, pts, n_pts, tets, n_tets, func_vals, n_func, out);
+}
+
+static ria_status device_run(bool mi, const ria_config* cfg, const double* d_pts, uint64_t n_pts,
+                             const int64_t* d_tets, uint64_t n_tets, const double* d_fv, uint32_t n_func, void* stream,
+                             ria_mesh** out) {
+    if (!d_pts || !d_tets || !d_fv) return fail(RIA_EINVAL, "null argument");
+    int dev = 0;
+    ria_status st = current_device(&dev);
+    if (st != RIA_OK) return st;
+    Inputs in;
+    in.mi = mi;
+    in.V = (int64_t)n_pts;
+    in.T = (int64_t)n_tets;
+    in.F = (int)n_func;
+    in.d_pts = d_pts;
+    in.d_tets = d_tets;
+    in.d_fv = d_fv;
+    return run_pipeline(cfg, in, (cudaStream_t)stream, false, out);
+}
+
+ria_status ria_compute_implicit_arrangement_device(const ria_config* cfg, const double* d_pts, uint64_t n_pts,
+                                                   const int64_t* d_tets, uint64_t n_tets, const double* d_func_vals,
+                                                   uint32_t n_func, void* stream, ria_mesh** out) {
+    return device_run(false, cfg, d_pts, n_pts, d_tets, n_tets, d_func_vals, n_func, stream, out);
+}
+
+ria_status ria_compute_material_interface_device(const ria_config* cfg, const double* d_pts, uint64_t n_pts,
+                                                 const int64_t* d_tets, uint64_t n_tets, const double* d_func_vals,
+                                                 uint32_t n_func, void* stream, ria_mesh** out) {
+    return device_run(true, cfg, d_pts, n_pts, d_tets, n_tets, d_func_vals, n_func, stream, out);
+}
+
+ria_status ria_grid_implicit_arrangement(const ria_config* cfg, uint32_t resolution, const double* bbox_min,
+                                         const double* bbox_max, const ria_function* funcs, uint32_t n_func,
+                                         ria_mesh** out) {
+    return grid_run(false, cfg, resolution, bbox_min, bbox_max, funcs, n_func, out);
+}
+
+ria_status ria_grid_material_interface(const ria_config* cfg, uint32_t resolution, const double* bbox_min,
+                                       const double* bbox_max, const ria_function* funcs, uint32_t n_func,
+                                       ria_mesh** out) {
+    return grid_run(true, cfg, resolution, bbox_min, bbox_max, funcs, n_func, out);
+}
+
+ria_status ria_sample_functions(const ria_function* funcs, uint32_t n_func, const double* pts, uint64_t n_pts,
+                                double* func_vals) {
+    if (!funcs || !pts || !func_vals) return fail(RIA_EINVAL, "null argument");
+    int dev = 0;
+    ria_status st = current_device(&dev);
+    if (st != RIA_OK) return st;
+    cudaStream_t s;
+    RIA_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    ria_function* d_funcs = nullptr;
+    double *d_pts = nullptr, *d_fv = nullptr;
+    RIA_CUDA(cudaMallocAsync(&d_funcs, sizeof(ria_function) * (n_func ? n_func : 1), s));
+    RIA_CUDA(cudaMallocAsync(&d_pts, sizeof(double) * 3 * (n_pts ? n_pts : 1), s));
+    RIA_CUDA(cudaMallocAsync(&d_fv, sizeof(double) * (n_pts * n_func ? n_pts * n_func : 1), s));
+    RIA_CUDA(cudaMemcpyAsync(d_funcs, funcs, sizeof(ria_function) * n_func, cudaMemcpyHostToDevice, s));
+    RIA_CUDA(cudaMemcpyAsync(d_pts, pts, sizeof(double) * 3 * n_pts, cudaMemcpyHostToDevice, s));
+    launch_sample_points(d_funcs, (int)n_func, d_pts, (int64_t)n_pts, d_fv, s);
+    RIA_CUDA(cudaMemcpyAsync(func_vals, d_fv, sizeof(double) * n_pts * n_func, cudaMemcpyDeviceToHost, s));
+    cudaFreeAsync(d_funcs, s);
+    cudaFreeAsync(d_pts, s);
+    cudaFreeAsync(d_fv, s);
+    cudaError_t e = cudaStreamSynchronize(s);
+    cudaStreamDestroy(s);
+    if (e != cudaSuccess) return fail(RIA_ECUDA, cudaGetErrorString(e));
+    return RIA_OK;
+}
+
+ria_status ria_compute_arrangement_batch(const double* values, const uint32_t* value_offsets, uint64_t n_tets,
+                                         uint8_t* records, uint64_t capacity, uint64_t* record_offsets) {
+    return batch_run(false, values, value_offsets, n_tets, records, capacity, record_offsets);
+}
+
+ria_status ria_compute_material_interface_batch(const double* values, const uint32_t* value_offsets,
+                                                uint64_t n_tets, uint8_t* records, uint64_t capacity,
+                                                uint64_t* record_offsets) {
+    return batch_run(true, values, value_offsets, n_tets, records, capacity, record_offsets);
+}
+
+static ria_status ensure_gathered(ria_mesh* m, ria_mesh_field f) {
+    if ((f == RIA_MESH_REC_OFFSETS || f == RIA_MESH_REC_BYTES) && !m->have_rec) {
+        cudaError_t err = cudaSuccess;
+        m->rec_offsets = m->keep.get<int64_t>(m->T + 1, &err);
+        if (err != cudaSuccess) return fail(RIA_ENOMEM, "device allocation failed");
+        cudaError_t e = gather_records(m->mi, m->A, m->T, m->act_tet, m->act_desc, m->heap, m->heap_big, m->table,
+                                       m->table_off, m->rec_offsets, &m->rec_bytes, &m->n_rec_bytes, m->s);
+        if (e != cudaSuccess) return fail(RIA_ECUDA, cudaGetErrorString(e));
+        m->keep.v.push_back(m->rec_bytes);
+        m->have_rec = true;
+    }
+    if ((f == RIA_MESH_FUNC_IN_TET || f == RIA_MESH_START_INDEX) && !m->have_fit) {
+        cudaError_t err = cudaSuccess;
+        m->start_index = m->keep.get<int64_t>(m->T + 1, &err);
+        if (err != cudaSuccess) return fail(RIA_ENOMEM, "device allocation failed");
+        cudaError_t e = gather_func_in_tet(m->A, m->T, m->act_tet, m->act_mask, m->start_index, &m->func_in_tet,
+                                           &m->n_fit, m->s);
+        if (e != cudaSuccess) return fail(RIA_ECUDA, cudaGetErrorString(e));
+        m->keep.v.push_back(m->func_in_tet);
+        m->have_fit = true;
+    }
+    return RIA_OK;
+}
+
+uint64_t ria_mesh_count(const ria_mesh* mc, ria_mesh_field f) {
+    ria_mesh* m = const_cast<ria_mesh*>(mc);
+    if (!m) return 0;
+    switch (f) {
+        case RIA_MESH_POINTS: return (uint64_t)m->ex.n_verts * 3;
+        case RIA_MESH_VERTS: return (uint64_t)m->ex.n_verts * 11;
+        case RIA_MESH_FACE_OFFSETS: return (uint64_t)m->ex.n_faces + 1;
+        case RIA_MESH_FACE_VERTS: return (uint64_t)m->ex.n_face_verts;
+        case RIA_MESH_FACE_TET_OFFSETS: return (uint64_t)m->ex.n_faces + 1;
+        case RIA_MESH_FACE_TETS: return (uint64_t)m->ex.n_face_tets * 2;
+        case RIA_MESH_FACE_FUNC: return (uint64_t)m->ex.n_faces * 2;
+        case RIA_MESH_FUNC_IN_TET:
+            if (ensure_gathered(m, f) != RIA_OK) return 0;
+            return (uint64_t)m->n_fit;
+        case RIA_MESH_START_INDEX: return (uint64_t)m->T + 1;
+        case RIA_MESH_REC_OFFSETS: return (uint64_t)m->T + 1;
+        case RIA_MESH_REC_BYTES:
+            if (ensure_gathered(m, f) != RIA_OK) return 0;
+            return (uint64_t)m->n_rec_bytes;
+        case RIA_MESH_STATS: return RIA_NUM_STATS;
+        case RIA_MESH_TIMINGS: return RIA_NUM_TIMINGS;
+        case RIA_MESH_FUNC_VALS: return m->fv ? (uint64_t)m->V * m->F : 0;
+    }
+    return 0;
+}
+
+ria_status ria_mesh_copy(const ria_mesh* mc, ria_mesh_field f, void* dst) {
+    ria_mesh* m = const_cast<ria_mesh*>(mc);
+    if (!m || !dst) return fail(RIA_EINVAL, "null argument");
+    ria_status st = ensure_gathered(m, f);
+    if (st != RIA_OK) return st;
+    const void* src = nullptr;
+    size_t bytes = 0;
+    switch (f) {
+        case RIA_MESH_POINTS: src = m->ex.xyz; bytes = 8 * 3 * (size_t)m->ex.n_verts; break;
+        case RIA_MESH_VERTS: src = m->ex.verts; bytes = 8 * 11 * (size_t)m->ex.n_verts; break;
+        case RIA_MESH_FACE_OFFSETS: src = m->ex.face_offsets; bytes = 8 * (size_t)(m->ex.n_faces + 1); break;
+        case RIA_MESH_FACE_VERTS: src = m->ex.face_verts; bytes = 8 * (size_t)m->ex.n_face_verts; break;
+        case RIA_MESH_FACE_TET_OFFSETS: src = m->ex.face_tet_offsets; bytes = 8 * (size_t)(m->ex.n_faces + 1); break;
+        case RIA_MESH_FACE_TETS: src = m->ex.face_tets; bytes = 16 * (size_t)m->ex.n_face_tets; break;
+        case RIA_MESH_FACE_FUNC: src = m->ex.face_func; bytes = 16 * (size_t)m->ex.n_faces; break;
+        case RIA_MESH_FUNC_IN_TET: src = m->func_in_tet; bytes = 8 * (size_t)m->n_fit; break;
+        case RIA_MESH_START_INDEX: src = m->start_index; bytes = 8 * (size_t)(m->T + 1); break;
+        case RIA_MESH_REC_OFFSETS: src = m->rec_offsets; bytes = 8 * (size_t)(m->T + 1); break;
+        case RIA_MESH_REC_BYTES: src = m->rec_bytes; bytes = (size_t)m->n_rec_bytes; break;
+        case RIA_MESH_STATS: std::memcpy(dst, m->stats, sizeof(m->stats)); return RIA_OK;
+        case RIA_MESH_TIMINGS: std::memcpy(dst, m->timings, sizeof(m->timings)); return RIA_OK;
+        case RIA_MESH_FUNC_VALS: src = m->fv; bytes = m->fv ? 8 * (size_t)m->V * m->F : 0; break;
+        default: return fail(RIA_EINVAL, "unknown field");
+    }
+    if (bytes == 0) return RIA_OK;
+    if (!src) return fail(RIA_EINVAL, "field not available on this mesh");
+    RIA_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, m->s));
+    RIA_CUDA(cudaStreamSynchronize(m->s));
+    return RIA_OK;
+}
+
+void ria_mesh_free(ria_mesh* m) {
+    if (!m) return;
+    for (void* p : {(void*)m->ex.xyz, (void*)m->ex.verts, (void*)m->ex.face_offsets, (void*)m->ex.face_verts,
+                    (void*)m->ex.face_tet_offsets, (void*)m->ex.face_tets, (void*)m->ex.face_func})
+        if (p) cudaFreeAsync(p, m->s);
+    m->keep.release();
+    cudaStreamSynchronize(m->s);
+    if (m->own_stream) cudaStreamDestroy(m->s);
+    delete m;
+}
+
+const char* ria_last_error(void) { return g_err.c_str(); }
+
+uint64_t ria_kernel_launches(void) { return g_launches.load(); }
+
+int ria_device_count(void) {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return n;
+}
+
+}  // extern "C"

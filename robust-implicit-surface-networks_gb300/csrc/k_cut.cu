@@ -1,0 +1,288 @@
+// Stage (c): the per-tet cut (src/implicit_arrangement.cpp:244-306, src/material_interface.cpp:288-351).
+//
+//   k_cut_fast   one thread per tet, state in local memory, FP64-filtered predicates only.  A tet
+//                whose predicate the filter cannot decide, or that outgrows the small capacities,
+//                is appended to a deferred list.
+//   k_cut_big    a fixed pool of threads, each with a state slot in global scratch memory, exact
+//                predicates and large capacities, walks the deferred list.
+//   k_build_table  the 81-pattern lookup tables (IA: one active plane; MI: two active
+//                materials), computed on the device by the exact variant from one representative
+//                tet per sign pattern (corner values in {-1, 0, 1}).
+// Records are appended to a byte heap with an atomic bump pointer; their placement does not affect
+// the result, which only depends on the per-tet record contents.
+#include "device_common.cuh"
+#include "launch.hpp"
+
+namespace ria {
+
+namespace {
+
+constexpr int kFastMaxK = 8;
+
+template <class Sum>
+__device__ __forceinline__ IASum4 pack_sum(const Sum& s);
+template <>
+__device__ __forceinline__ IASum4 pack_sum<IASummary>(const IASummary& s) {
+    return IASum4{s.n_iso_v, s.n_iso_f, s.n_iso_loop, s.n_bnd_f};
+}
+template <>
+__device__ __forceinline__ IASum4 pack_sum<MISummary>(const MISummary& s) {
+    return IASum4{s.n_mi_v, s.n_mi_f, s.n_mi_loop, s.n_bnd_f};
+}
+
+template <bool MI>
+struct Traits;
+template <>
+struct Traits<false> {
+    using Fast = IACutFast;
+    using Big = IACutBig;
+    using Sum = IASummary;
+};
+template <>
+struct Traits<true> {
+    using Fast = MICutFast;
+    using Big = MICutBig;
+    using Sum = MISummary;
+};
+
+template <bool MI>
+struct BigSlot {
+    typename Traits<MI>::Big cut;
+    double planes[4 * 64];
+};
+
+__device__ __forceinline__ int gather_planes(const CutArgs& a, uint32_t ai, double* planes, int kmax) {
+    if (a.values) {
+        const uint32_t r0 = a.value_off[ai], r1 = a.value_off[ai + 1];
+        const int k = (int)(r1 - r0);
+        if (k > kmax) return k;
+        for (int i = 0; i < 4 * k; ++i) planes[i] = a.values[4 * (size_t)r0 + i];
+        return k;
+    }
+    const uint32_t t = a.act_tet[ai];
+    uint64_t m = a.act_mask[ai];
+    const int k = __popcll(m);
+    if (k > kmax) return k;
+    int64_t v[4];
+    TetSrc ts{a.d_tets, a.g.res};
+    ts.get(t, v);
+    int i = 0;
+    while (m) {
+        int j = __ffsll((long long)m) - 1;
+        m &= m - 1;
+        for (int c = 0; c < 4; ++c) planes[4 * i + c] = a.fv[v[c] * a.F + j];
+        ++i;
+    }
+    return k;
+}
+
+template <class Cut, class Sum>
+__device__ __forceinline__ void finish_cut(const CutArgs& a, uint32_t ai, Cut& c) {
+    c.canonicalize();
+    const int size = c.record_size();
+    unsigned long long off = atomicAdd(a.heap_used, (unsigned long long)size);
+    if (off + size > a.heap_cap) {
+        raise_status(a.status, ST_CAPACITY);
+        return;
+    }
+    Sum s;
+    c.emit(a.heap + off, s);
+    a.act_desc[ai] = off | a.desc_bit;
+    a.act_sum[ai] = pack_sum<Sum>(s);
+}
+
+template <bool MI>
+__global__ void __launch_bounds__(128) k_cut_fast(CutArgs a) {
+    using Fast = typename Traits<MI>::Fast;
+    using Sum = typename Traits<MI>::Sum;
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n) return;
+    const uint32_t ai = a.list[i];
+    double planes[4 * kFastMaxK];
+    const int k = gather_planes(a, ai, planes, kFastMaxK);
+    int st = CUT_DEFER;
+    Fast c;
+    if (k <= kFastMaxK) st = c.run(planes, k);
+    if (st == CUT_OK) {
+        finish_cut<Fast, Sum>(a, ai, c);
+    } else if (st == CUT_DEFER) {
+        unsigned int d = atomicAdd(a.n_deferred, 1u);
+        a.deferred[d] = ai;
+    } else {
+        raise_status(a.status, ST_INTERNAL);
+    }
+}
+
+template <bool MI>
+__global__ void __launch_bounds__(64) k_cut_big(CutArgs a, BigSlot<MI>* scratch, int64_t slots) {
+    using Sum = typename Traits<MI>::Sum;
+    const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (tid >= slots) return;
+    BigSlot<MI>& S = scratch[tid];
+    for (int64_t i = tid; i < a.n; i += slots) {
+        const uint32_t ai = a.list[i];
+        const int k = gather_planes(a, ai, S.planes, 60);
+        if (k > 60) {
+            raise_status(a.status, ST_CAPACITY);
+            continue;
+        }
+        int st = S.cut.run(S.planes, k);
+        if (st != CUT_OK) {
+            raise_status(a.status, ST_CAPACITY);
+            continue;
+        }
+        finish_cut<typename Traits<MI>::Big, Sum>(a, ai, S.cut);
+    }
+}
+
+template <bool MI>
+__global__ void k_build_table(uint8_t* table, uint32_t* table_off, IASum4* table_sum, BigSlot<MI>* scratch,
+                              uint32_t* status) {
+    using Sum = typename Traits<MI>::Sum;
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= kTablePatterns) return;
+    BigSlot<MI>& S = scratch[p];
+    int q = p;
+    for (int c = 0; c < 4; ++c) {
+        double sgn = (double)(q % 3) - 1.0;
+        q /= 3;
+        if (MI) {
+            S.planes[c] = 0.0;      // material a
+            S.planes[4 + c] = sgn;  // material b: b - a has the pattern's signs
+        } else {
+            S.planes[c] = sgn;
+        }
+    }
+    int st = S.cut.run(S.planes, MI ? 2 : 1);
+    if (st != CUT_OK) {
+        raise_status(status, ST_INTERNAL);
+        return;
+    }
+    S.cut.canonicalize();
+    if (S.cut.record_size() > kTableStride) {
+        raise_status(status, ST_INTERNAL);
+        return;
+    }
+    Sum s;
+    S.cut.emit(table + p * kTableStride, s);
+    table_off[p] = (uint32_t)(p * kTableStride);
+    table_sum[p] = pack_sum<Sum>(s);
+}
+
+// The reference's robustness mode (src/implicit_arrangement.cpp:137-243,
+// src/material_interface.cpp:174-287): cut each tet with its rows in the given order and in the
+// reversed order, and count the tets whose vertex, face or cell counts differ.
+template <bool MI>
+__global__ void __launch_bounds__(64) k_robust(CutArgs a, BigSlot<MI>* scratch, int64_t slots,
+                                               unsigned long long* n_fail) {
+    const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (tid >= slots) return;
+    BigSlot<MI>& S = scratch[tid];
+    for (int64_t i = tid; i < a.n; i += slots) {
+        const uint32_t ai = a.list[i];
+        const int k = gather_planes(a, ai, S.planes, 30);
+        if (k > 30) {
+            raise_status(a.status, ST_CAPACITY);
+            continue;
+        }
+        for (int r = 0; r < k; ++r)
+            for (int c = 0; c < 4; ++c) S.planes[4 * (2 * k - 1 - r) + c] = S.planes[4 * r + c];
+        int counts[2][3];
+        bool ok = true;
+        for (int pass = 0; pass < 2 && ok; ++pass) {
+            int st = S.cut.run(S.planes + (pass ? 4 * k : 0), k);
+            if (st != CUT_OK) {
+                ok = false;
+                break;
+            }
+            S.cut.canonicalize();
+            if constexpr (MI) {
+                counts[pass][0] = S.cut.onv;
+                counts[pass][1] = S.cut.onf;
+                counts[pass][2] = S.cut.onc;
+            } else {
+                counts[pass][0] = S.cut.nv_live;
+                counts[pass][1] = S.cut.nf;
+                counts[pass][2] = S.cut.nc;
+            }
+        }
+        if (!ok) {
+            raise_status(a.status, ST_CAPACITY);
+            continue;
+        }
+        if (counts[0][0] != counts[1][0] || counts[0][1] != counts[1][1] || counts[0][2] != counts[1][2])
+            atomicAdd(n_fail, 1ull);
+    }
+}
+
+}  // namespace
+
+void launch_robust(const CutArgs& a, void* scratch, int64_t slots, unsigned long long* n_fail, cudaStream_t s) {
+    if (a.n == 0) return;
+    const int bs = 64;
+    const int64_t use = a.n < slots ? a.n : slots;
+    const unsigned nb = (unsigned)((use + bs - 1) / bs);
+    if (a.mi)
+        {
+            k_robust<true><<<nb, bs, 0, s>>>(a, (BigSlot<true>*)scratch, use, n_fail);
+            note_launch();
+        }
+    else
+        {
+            k_robust<false><<<nb, bs, 0, s>>>(a, (BigSlot<false>*)scratch, use, n_fail);
+            note_launch();
+        }
+}
+
+size_t cut_big_slot_bytes(bool mi) { return mi ? sizeof(BigSlot<true>) : sizeof(BigSlot<false>); }
+
+void launch_cut_fast(const CutArgs& a, cudaStream_t s) {
+    if (a.n == 0) return;
+    const int bs = 128;
+    const unsigned nb = (unsigned)((a.n + bs - 1) / bs);
+    if (a.mi)
+        {
+            k_cut_fast<true><<<nb, bs, 0, s>>>(a);
+            note_launch();
+        }
+    else
+        {
+            k_cut_fast<false><<<nb, bs, 0, s>>>(a);
+            note_launch();
+        }
+}
+
+void launch_cut_big(const CutArgs& a, void* scratch, int64_t slots, cudaStream_t s) {
+    if (a.n == 0) return;
+    const int bs = 64;
+    const int64_t use = a.n < slots ? a.n : slots;
+    const unsigned nb = (unsigned)((use + bs - 1) / bs);
+    if (a.mi)
+        {
+            k_cut_big<true><<<nb, bs, 0, s>>>(a, (BigSlot<true>*)scratch, use);
+            note_launch();
+        }
+    else
+        {
+            k_cut_big<false><<<nb, bs, 0, s>>>(a, (BigSlot<false>*)scratch, use);
+            note_launch();
+        }
+}
+
+void launch_build_table(bool mi, uint8_t* table, uint32_t* table_off, IASum4* table_sum, void* scratch,
+                        uint32_t* status, cudaStream_t s) {
+    const int bs = 32;
+    const unsigned nb = (kTablePatterns + bs - 1) / bs;
+    if (mi)
+        {
+            k_build_table<true><<<nb, bs, 0, s>>>(table, table_off, table_sum, (BigSlot<true>*)scratch, status);
+            note_launch();
+        }
+    else
+        {
+            k_build_table<false><<<nb, bs, 0, s>>>(table, table_off, table_sum, (BigSlot<false>*)scratch, status);
+            note_launch();
+        }
+}
+
+}  // namespace ria

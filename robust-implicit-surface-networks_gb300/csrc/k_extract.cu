@@ -1,0 +1,705 @@
+// Stage (d): mesh extraction (src/extract_mesh.cpp:10-265 extract_iso_mesh) and vertex coordinates
+// (src/extract_mesh.cpp:1446-1538 compute_iso_vert_xyz, src/extract_mesh.h:111-159).
+//
+// The reference walks the tets in order and numbers a vertex or face at its first occurrence,
+// deduplicating through hash maps keyed by
+//   tet vertex v | tet edge (v1, v2, f) | tet face (v1, v2, v3, f1, f2)   (vertices)
+//   (smallest, second smallest, largest vertex id)                        (faces on the tet boundary)
+// Here every occurrence gets its position in that serial order from exclusive scans of the
+// per-tet counts; keyed occurrences lower their key's owner to their position with atomicMin
+// (a direct-mapped array for tet vertices, a 128-bit open-addressing hash otherwise); an occurrence
+// is new iff it owns its key, and the new occurrences are numbered by one more scan.  The result is
+// the reference's numbering exactly.
+#include <cub/cub.cuh>
+
+#include <vector>
+
+#include "device_common.cuh"
+#include "launch.hpp"
+
+namespace ria {
+
+namespace {
+
+constexpr int kBs = 256;
+
+enum : uint64_t { OCC_SELF = 0, OCC_CORNER = 1, OCC_EDGE = 2, OCC_FACE = 3 };
+
+struct U4 {
+    uint32_t a, b, c, d;
+};
+struct U4Sum {
+    __host__ __device__ U4 operator()(const U4& x, const U4& y) const { return U4{x.a + y.a, x.b + y.b, x.c + y.c, x.d + y.d}; }
+};
+
+struct ExtractCtx {
+    ExtractArgs a;
+    RecSrc rs;
+    const U4* base;        // per active tet: occurrence bases (vert, face, loop, boundary face)
+    uint32_t* corner_owner;
+    HashTab he, hf, hb;
+    uint64_t* vocc;        // per vertex occurrence: type << 62 | payload
+    uint64_t* vsrc;        // per vertex occurrence: active index << 8 | local vertex
+    uint32_t* vowner;      // per vertex occurrence: owner position
+    uint32_t* vflag;       // 1 if new
+    uint32_t* vgid_new;    // exclusive scan of vflag
+    uint32_t* occ_gid;     // per vertex occurrence: global vertex id
+    uint64_t* focc;        // per face occurrence: OCC_SELF or slot in hb
+    uint32_t* fowner;
+    uint32_t* fflag;
+    uint32_t* fgid;
+    uint32_t* flen;
+    uint32_t* fdup;
+    uint32_t* fnewlen;
+    uint32_t* fntet;
+    uint32_t* foff;
+    uint32_t* ftoff;
+};
+
+__device__ __forceinline__ int local_func(uint64_t mask, int j) {  // j-th set bit of mask
+    for (int i = 0; i < j; ++i) mask &= mask - 1;
+    return __ffsll((long long)mask) - 1;
+}
+
+// iso flags of the local vertices of an IA record (up to 128 vertices)
+__device__ __forceinline__ void iso_vertex_flags(const IAView& r, uint64_t iso[2]) {
+    iso[0] = iso[1] = 0;
+    int off = 0;
+    for (int f = 0; f < r.nf; ++f) {
+        int L = r.len(f);
+        if (r.plane_is_iso(r.supp(f)))
+            for (int t = 0; t < L; ++t) {
+                int v = r.loopv(off + t);
+                iso[v >> 6] |= 1ull << (v & 63);
+            }
+        off += L;
+    }
+}
+
+__device__ __forceinline__ int iso_rank(const uint64_t iso[2], int v) {
+    if (v < 64) return __popcll(iso[0] & ((1ull << v) - 1));
+    return __popcll(iso[0]) + __popcll(iso[1] & ((1ull << (v - 64)) - 1));
+}
+
+struct VertKey {
+    int type;       // 1 corner, 2 edge, 3 face, 4 interior (simplex size)
+    int64_t sv[4];  // simplex vertex ids
+    int fn[3];      // global function ids
+};
+
+__device__ __forceinline__ VertKey ia_vertex_key(const IAView& r, int j, const int64_t tv[4], uint64_t mask) {
+    VertKey k;
+    const uint8_t* lab = r.vlab + 3 * j;
+    int nb = 0, bnd[3];
+    int ni = 0;
+    k.fn[0] = k.fn[1] = k.fn[2] = -1;
+    for (int t = 0; t < 3; ++t) {
+        if (lab[t] > 3)
+            k.fn[ni++] = local_func(mask, lab[t] - 4);
+        else
+            bnd[nb++] = lab[t];
+    }
+    for (int c = 0; c < 4; ++c) k.sv[c] = -1;
+    switch (nb) {
+        case 3: {
+            int c0 = 0;
+            for (int c = 0; c < 4; ++c)
+                if (c != bnd[0] && c != bnd[1] && c != bnd[2]) c0 = c;
+            k.type = 1;
+            k.sv[0] = tv[c0];
+            break;
+        }
+        case 2: {
+            int n = 0;
+            for (int c = 0; c < 4; ++c)
+                if (c != bnd[0] && c != bnd[1]) k.sv[n++] = tv[c];
+            if (k.sv[0] > k.sv[1]) {
+                int64_t x = k.sv[0];
+                k.sv[0] = k.sv[1];
+                k.sv[1] = x;
+            }
+            k.type = 2;
+            break;
+        }
+        case 1: {
+            int n = 0;
+            for (int c = 0; c < 4; ++c)
+                if (c != bnd[0]) k.sv[n++] = tv[c];
+            for (int x = 1; x < 3; ++x)
+                for (int y = x; y > 0 && k.sv[y - 1] > k.sv[y]; --y) {
+                    int64_t s = k.sv[y];
+                    k.sv[y] = k.sv[y - 1];
+                    k.sv[y - 1] = s;
+                }
+            k.type = 3;
+            break;
+        }
+        default:
+            for (int c = 0; c < 4; ++c) k.sv[c] = tv[c];
+            k.type = 4;
+    }
+    return k;
+}
+
+__global__ void k_base_in(int64_t A, const IASum4* __restrict__ sum, U4* __restrict__ out) {
+    int64_t a = (int64_t)blockIdx.x * kBs + threadIdx.x;
+    if (a >= A) return;
+    IASum4 s = sum[a];
+    out[a] = U4{s.a, s.b, s.c, s.d};
+}
+
+// D2: keys of the iso vertices
+__global__ void __launch_bounds__(kBs) k_ia_vert_keys(ExtractCtx C) {
+    const int64_t a = (int64_t)blockIdx.x * kBs + threadIdx.x;
+    if (a >= C.a.A) return;
+    IAView r;
+    r.init(C.rs.get(C.a.act_desc[a]));
+    int64_t tv[4];
+    TetSrc ts{C.a.d_tets, C.a.g.res};
+    ts.get(C.a.act_tet[a], tv);
+    const uint64_t mask = C.a.act_mask[a];
+    uint64_t iso[2];
+    iso_vertex_flags(r, iso);
+    uint32_t pos = C.base[a].a;
+    for (int j = 0; j < r.nv; ++j) {
+        if (!((iso[j >> 6] >> (j & 63)) & 1)) continue;
+        VertKey k = ia_vertex_key(r, j, tv, mask);
+        uint64_t occ;
+        if (k.type == 1) {
+            atomicMin(&C.corner_owner[k.sv[0]], pos);
+            occ = (OCC_CORNER << 62) | (uint64_t)k.sv[0];
+        } else if (k.type == 2) {
+            int64_t s = ht_insert_min(C.he, ((uint64_t)k.sv[0] << 32) | (uint64_t)k.sv[1], (uint64_t)k.fn[0] + 1, pos);
+            if (s < 0) raise_status(C.a.status, ST_HASH_FULL);
+            occ = (OCC_EDGE << 62) | (uint64_t)(s < 0 ? 0 : s);
+        } else if (k.type == 3) {
+            int64_t s = ht_insert_min(C.hf, ((uint64_t)k.sv[0] << 32) | (uint64_t)k.sv[1],
+                                      ((uint64_t)k.sv[2] << 32) | ((uint64_t)k.fn[0] << 16) | (uint64_t)k.fn[1], pos);
+            if (s < 0) raise_status(C.a.status, ST_HASH_FULL);
+            occ = (OCC_FACE << 62) | (uint64_t)(s < 0 ? 0 : s);
+        } else {
+            occ = OCC_SELF << 62;
+        }
+        C.vocc[pos] = occ;
+        C.vsrc[pos] = ((uint64_t)a << 8) | (uint64_t)j;
+        ++pos;
+    }
+}
+
+// D3: owner and new flag of each vertex occurrence
+__global__ void k_vert_owner(ExtractCtx C, int64_t n) {
+    const int64_t p = (int64_t)blockIdx.x * kBs + threadIdx.x;
+    if (p >= n) return;
+    const uint64_t occ = C.vocc[p];
+    const uint64_t ty = occ >> 62, pay = occ & ((1ull << 62) - 1);
+    uint32_t own;
+    if (ty == OCC_SELF) own = (uint32_t)p;
+    else if (ty == OCC_CORNER) own = C.corner_owner[pay];
+    else if (ty == OCC_EDGE) own = C.he.owner[pay];
+    else own = C.hf.owner[pay];
+    C.vowner[p] = own;
+    C.vflag[p] = own == (uint32_t)p ? 1u : 0u;
+}
+
+// D4: global vertex ids, vertex records and coordinates of the new vertices
+__global__ void k_vert_emit(ExtractCtx C, int64_t n, int64_t* __restrict__ verts, double* __restrict__ xyz) {
+    const int64_t p = (int64_t)blockIdx.x * kBs + threadIdx.x;
+    if (p >= n) return;
+    const uint32_t own = C.vowner[p];
+    C.occ_gid[p] = C.vgid_new[own];
+    if (own != (uint32_t)p) return;
+    const uint32_t gid = C.vgid_new[p];
+    const uint64_t src = C.vsrc[p];
+    const int64_t a = (int64_t)(src >> 8);
+    const int j = (int)(src & 0xFF);
+    IAView r;
+    r.init(C.rs.get(C.a.act_desc[a]));
+    int64_t tv[4];
+    TetSrc ts{C.a.d_tets, C.a.g.res};
+    const uint32_t tet = C.a.act_tet[a];
+    ts.get(tet, tv);
+    VertKey k = ia_vertex_key(r, j, tv, C.a.act_mask[a]);
+    int64_t* rec = verts + 11 * (int64_t)gid;
+    rec[0] = tet;
+    rec[1] = j;
+    rec[2] = k.type;
+    for (int c = 0; c < 4; ++c) rec[3 + c] = k.sv[c];
+    for (int c = 0; c < 3; ++c) rec[7 + c] = k.fn[c];
+    rec[10] = -1;
+    // coordinates, with the reference's formulas and operation order
+    PtSrc ps;
+    ps.pts = C.a.d_pts;
+    ps.res = C.a.g.res;
+    for (int c = 0; c < 3; ++c) {
+        ps.bmin[c] = C.a.g.bmin[c];
+        ps.bmax[c] = C.a.g.bmax[c];
+    }
+    const double* fv = C.a.fv;
+    const int F = C.a.F;
+    double out[3];
+    switch (k.type) {
+        case 2: {
+            double p1[3], p2[3];
+            ps.get(k.sv[0], p1);
+            ps.get(k.sv[1], p2);
+            double f1 = fv[k.sv[0] * F + k.fn[0]], f2 = fv[k.sv[1] * F + k.fn[0]];
+            double b0 = f2 / (f2 - f1);
+            double b1 = 1 - b0;
+            for (int c = 0; c < 3; ++c) out[c] = b0 * p1[c] + b1 * p2[c];
+            break;
+        }
+        case 3: {
+            double P[3][3];
+            for (int t = 0; t < 3; ++t) ps.get(k.sv[t], P[t]);
+            double a1[3], a2[3];
+            for (int t = 0; t < 3; ++t) {
+                a1[t] = fv[k.sv[t] * F + k.fn[0]];
+                a2[t] = fv[k.sv[t] * F + k.fn[1]];
+            }
+            double n1 = a1[2] * a2[1] - a1[1] * a2[2];
+            double n2 = a1[0] * a2[2] - a1[2] * a2[0];
+            double n3 = a1[1] * a2[0] - a1[0] * a2[1];
+            double d = n1 + n2 + n3;
+            double w0 = n1 / d, w1 = n2 / d, w2 = n3 / d;
+            for (int c = 0; c < 3; ++c) out[c] = w0 * P[0][c] + w1 * P[1][c] + w2 * P[2][c];
+            break;
+        }
+        case 4: {
+            double P[4][3];
+            for (int t = 0; t < 4; ++t) ps.get(k.sv[t], P[t]);
+            double p1[4], p2[4], p3[4];
+            for (int t = 0; t < 4; ++t) {
+                p1[t] = fv[k.sv[t] * F + k.fn[0]];
+                p2[t] = fv[k.sv[t] * F + k.fn[1]];
+                p3[t] = fv[k.sv[t] * F + k.fn[2]];
+            }
+            double n1 = p1[3] * (p2[2] * p3[1] - p2[1] * p3[2]) + p1[2] * (p2[1] * p3[3] - p2[3] * p3[1]) +
+                        p1[1] * (p2[3] * p3[2] - p2[2] * p3[3]);
+            double n2 = p1[3] * (p2[0] * p3[2] - p2[2] * p3[0]) + p1[2] * (p2[3] * p3[0] - p2[0] * p3[3]) +
+                        p1[0] * (p2[2] * p3[3] - p2[3] * p3[2]);
+            double n3 = p1[3] * (p2[1] * p3[0] - p2[0] * p3[1]) + p1[1] * (p2[0] * p3[3] - p2[3] * p3[0]) +
+                        p1[0] * (p2[3] * p3[1] - p2[1] * p3[3]);
+            double n4 = p1[2] * (p2[0] * p3[1] - p2[1] * p3[0]) + p1[1] * (p2[2] * p3[0] - p2[0] * p3[2]) +
+                        p1[0] * (p2[1] * p3[2] - p2[2] * p3[1]);
+            double d = n1 + n2 + n3 + n4;
+            double w0 = n1 / d, w1 = n2 / d, w2 = n3 / d, w3 = n4 / d;
+            for (int c = 0; c < 3; ++c) out[c] = w0 * P[0][c] + w1 * P[1][c] + w2 * P[2][c] + w3 * P[3][c];
+            break;
+        }
+        default:
+            ps.get(k.sv[0], out);
+    }
+    for (int c = 0; c < 3; ++c) xyz[3 * (int64_t)gid + c] = out[c];
+}
+
+// D5: keys of the iso faces on the tet boundary
+__global__ void __launch_bounds__(kBs) k_ia_face_keys(ExtractCtx C) {
+    const int64_t a = (int64_t)blockIdx.x * kBs + threadIdx.x;
+    if (a >= C.a.A) return;
+    IAView r;
+    r.init(C.rs.get(C.a.act_desc[a]));
+    uint64_t iso[2];
+    iso_vertex_flags(r, iso);
+    const uint32_t vb = C.base[a].a;
+    uint32_t fpos = C.base[a].b;
+    int off = 0;
+    for (int f = 0; f < r.nf; ++f) {
+        const int L = r.len(f);
+        if (r.plane_is_iso(r.supp(f))) {
+            uint64_t occ = OCC_SELF << 62;
+            if (r.bnd(f)) {
+                // (smallest, second smallest, largest) global vertex id (src/extract_mesh.h:68-92)
+                int64_t mn = -1, mx = -1;
+                int mpos = 0;
+                for (int t = 0; t < L; ++t) {
+                    int64_t g = C.occ_gid[vb + iso_rank(iso, r.loopv(off + t))];
+                    if (t == 0 || g < mn) {
+                        mn = g;
+                        mpos = t;
+                    }
+                    if (t == 0 || g > mx) mx = g;
+                }
+                int64_t second = mx + 1;
+                for (int t = 0; t < L; ++t) {
+                    int64_t g = C.occ_gid[vb + iso_rank(iso, r.loopv(off + t))];
+                    if (t != mpos && g < second) second = g;
+                }
+                int64_t s = ht_insert_min(C.hb, ((uint64_t)mn << 32) | (uint64_t)second, (uint64_t)mx + 1, fpos);
+                if (s < 0) raise_status(C.a.status, ST_HASH_FULL);
+                occ = (OCC_EDGE << 62) | (uint64_t)(s < 0 ? 0 : s);
+            }
+            C.focc[fpos] = occ;
+            C.flen[fpos] = (uint32_t)L;
+            ++fpos;
+        }
+        off += L;
+    }
+}
+
+// D6: owners of the face occurrences, duplicate counts
+__global__ void k_face_owner(ExtractCtx C, int64_t n) {
+    const int64_t p = (int64_t)blockIdx.x * kBs + threadIdx.x;
+    if (p >= n) return;
+    const uint64_t occ = C.focc[p];
+    uint32_t own = (occ >> 62) == OCC_SELF ? (uint32_t)p : C.hb.owner[occ & ((1ull << 62) - 1)];
+    C.fowner[p] = own;
+    C.fflag[p] = own == (uint32_t)p;
+    if (own != (uint32_t)p) atomicAdd(&C.fdup[own], 1u);
+}
+
+__global__ void k_face_sizes(ExtractCtx C, int64_t n) {
+    const int64_t p = (int64_t)blockIdx.x * kBs + threadIdx.x;
+    if (p >= n) return;
+    const bool isnew = C.fflag[p];
+    C.fnewlen[p] = isnew ? C.flen[p] : 0;
+    C.fntet[p] = isnew ? 1 + C.fdup[p] : 0;
+    if (isnew && C.fdup[p] > 1) raise_status(C.a.status, ST_NONMANIFOLD);
+}
+
+// D7: face vertex lists, function ids and tet-face lists
+__global__ void __launch_bounds__(kBs) k_ia_face_emit(ExtractCtx C, int64_t* __restrict__ face_offsets,
+                                                      int64_t* __restrict__ face_verts,
+                                                      int64_t* __restrict__ face_tet_offsets,
+                                                      int64_t* __restrict__ face_tets, int64_t* __restrict__ face_func) {
+    const int64_t a = (int64_t)blockIdx.x * kBs + threadIdx.x;
+    if (a >= C.a.A) return;
+    IAView r;
+    r.init(C.rs.get(C.a.act_desc[a]));
+    uint64_t iso[2];
+    iso_vertex_flags(r, iso);
+    const uint32_t vb = C.base[a].a;
+    uint32_t fpos = C.base[a].b;
+    const uint64_t mask = C.a.act_mask[a];
+    const int64_t tet = C.a.act_tet[a];
+    int off = 0;
+    for (int f = 0; f < r.nf; ++f) {
+        const int L = r.len(f);
+        if (r.plane_is_iso(r.supp(f))) {
+            const uint32_t own = C.fowner[fpos];
+            if (own == fpos) {
+                const uint32_t gid = C.fgid[fpos];
+                const uint32_t vo = C.foff[fpos];
+                face_offsets[gid] = vo;
+                for (int t = 0; t < L; ++t) face_verts[vo + t] = C.occ_gid[vb + iso_rank(iso, r.loopv(off + t))];
+                const uint32_t to = C.ftoff[fpos];
+                face_tet_offsets[gid] = to;
+                face_tets[2 * (int64_t)to] = tet;
+                face_tets[2 * (int64_t)to + 1] = f;
+                int lf = r.plane_func_local(r.supp(f));
+                face_func[2 * (int64_t)gid] = lf < 0 ? -1 : local_func(mask, lf);
+                face_func[2 * (int64_t)gid + 1] = -1;
+            } else {
+                const uint32_t to = C.ftoff[own] + 1;
+                face_tets[2 * (int64_t)to] = tet;
+                face_tets[2 * (int64_t)to + 1] = f;
+            }
+            ++fpos;
+        }
+        off += L;
+    }
+}
+
+__global__ void k_set_last(int64_t* p, int64_t idx, const uint32_t* a, const uint32_t* b, int64_t n) {
+    // p[idx] = a[n-1] + b[n-1] (exclusive-scan total), or 0 when n == 0
+    p[idx] = n ? (int64_t)a[n - 1] + (int64_t)b[n - 1] : 0;
+}
+
+inline unsigned nblk(int64_t n) { return (unsigned)((n + kBs - 1) / kBs); }
+
+uint64_t pow2_at_least(uint64_t x) {
+    uint64_t p = 1024;
+    while (p < x) p <<= 1;
+    return p;
+}
+
+struct Pool {
+    cudaStream_t s;
+    std::vector<void*> ptrs;
+    cudaError_t err = cudaSuccess;
+    template <class T>
+    T* get(int64_t n) {
+        void* p = nullptr;
+        if (n <= 0) n = 1;
+        cudaError_t e = cudaMallocAsync(&p, sizeof(T) * (size_t)n, s);
+        if (e != cudaSuccess) {
+            err = e;
+            return nullptr;
+        }
+        ptrs.push_back(p);
+        return (T*)p;
+    }
+    ~Pool() {
+        for (void* p : ptrs) cudaFreeAsync(p, s);
+    }
+};
+
+cudaError_t exscan_u32(const uint32_t* in, uint32_t* out, int64_t n, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    size_t bytes = 0;
+    cub::DeviceScan::ExclusiveSum(nullptr, bytes, in, out, n, s);
+    void* tmp = nullptr;
+    cudaError_t e = cudaMallocAsync(&tmp, bytes, s);
+    if (e != cudaSuccess) return e;
+    cub::DeviceScan::ExclusiveSum(tmp, bytes, in, out, n, s);
+    return cudaFreeAsync(tmp, s);
+}
+
+// total of an exclusive scan: out[n-1] + in[n-1]
+cudaError_t scan_total(const uint32_t* in, const uint32_t* out, int64_t n, int64_t* total, cudaStream_t s) {
+    if (n == 0) {
+        *total = 0;
+        return cudaSuccess;
+    }
+    uint32_t h[2];
+    cudaError_t e = cudaMemcpyAsync(&h[0], in + n - 1, 4, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&h[1], out + n - 1, 4, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    *total = (int64_t)h[0] + (int64_t)h[1];
+    return e;
+}
+
+}  // namespace
+
+cudaError_t run_extract(const ExtractArgs& a, const IASum4* act_sum, ExtractOut& out, cudaStream_t s) {
+    if (a.mi) return cudaErrorNotSupported;
+    Pool pool{s};
+    ExtractCtx C;
+    C.a = a;
+    C.rs = RecSrc{a.heap, a.heap_big, a.table, a.table_off};
+    const int64_t A = a.A;
+    out = ExtractOut();
+    // bases
+    U4* bin = pool.get<U4>(A);
+    U4* base = pool.get<U4>(A);
+    if (pool.err) return pool.err;
+    U4 tot{0, 0, 0, 0};
+    if (A > 0) {
+        {
+            k_base_in<<<nblk(A), kBs, 0, s>>>(A, act_sum, bin);
+            note_launch();
+        }
+        size_t bytes = 0;
+        cub::DeviceScan::ExclusiveScan(nullptr, bytes, bin, base, U4Sum(), U4{0, 0, 0, 0}, A, s);
+        void* tmp = pool.get<uint8_t>((int64_t)bytes);
+        if (pool.err) return pool.err;
+        cub::DeviceScan::ExclusiveScan(tmp, bytes, bin, base, U4Sum(), U4{0, 0, 0, 0}, A, s);
+        U4 h[2];
+        cudaMemcpyAsync(&h[0], bin + A - 1, sizeof(U4), cudaMemcpyDeviceToHost, s);
+        cudaMemcpyAsync(&h[1], base + A - 1, sizeof(U4), cudaMemcpyDeviceToHost, s);
+        cudaError_t e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) return e;
+        tot = U4Sum()(h[0], h[1]);
+    }
+    C.base = base;
+    const int64_t NV = tot.a, NF = tot.b, NB = tot.d;
+    // tables
+    C.corner_owner = pool.get<uint32_t>(a.V);
+    const uint64_t cap_e = pow2_at_least((uint64_t)NV), cap_f = pow2_at_least((uint64_t)NV / 2 + 1);
+    const uint64_t cap_b = pow2_at_least(2 * (uint64_t)NB + 1);
+    C.he = HashTab{pool.get<ulonglong2>((int64_t)cap_e), pool.get<uint32_t>((int64_t)cap_e), cap_e - 1};
+    C.hf = HashTab{pool.get<ulonglong2>((int64_t)cap_f), pool.get<uint32_t>((int64_t)cap_f), cap_f - 1};
+    C.hb = HashTab{pool.get<ulonglong2>((int64_t)cap_b), pool.get<uint32_t>((int64_t)cap_b), cap_b - 1};
+    C.vocc = pool.get<uint64_t>(NV);
+    C.vsrc = pool.get<uint64_t>(NV);
+    C.vowner = pool.get<uint32_t>(NV);
+    C.vflag = pool.get<uint32_t>(NV);
+    C.vgid_new = pool.get<uint32_t>(NV);
+    C.occ_gid = pool.get<uint32_t>(NV);
+    C.focc = pool.get<uint64_t>(NF);
+    C.fowner = pool.get<uint32_t>(NF);
+    C.fflag = pool.get<uint32_t>(NF);
+    C.fgid = pool.get<uint32_t>(NF);
+    C.flen = pool.get<uint32_t>(NF);
+    C.fdup = pool.get<uint32_t>(NF);
+    C.fnewlen = pool.get<uint32_t>(NF);
+    C.fntet = pool.get<uint32_t>(NF);
+    C.foff = pool.get<uint32_t>(NF);
+    C.ftoff = pool.get<uint32_t>(NF);
+    if (pool.err) return pool.err;
+    cudaMemsetAsync(C.corner_owner, 0xFF, sizeof(uint32_t) * (size_t)(a.V > 0 ? a.V : 1), s);
+    for (HashTab* h : {&C.he, &C.hf, &C.hb}) {
+        cudaMemsetAsync(h->keys, 0xFF, sizeof(ulonglong2) * (h->cap_mask + 1), s);
+        cudaMemsetAsync(h->owner, 0xFF, sizeof(uint32_t) * (h->cap_mask + 1), s);
+    }
+    cudaMemsetAsync(C.fdup, 0, sizeof(uint32_t) * (size_t)(NF > 0 ? NF : 1), s);
+    // vertices
+    if (A > 0) {
+        k_ia_vert_keys<<<nblk(A), kBs, 0, s>>>(C);
+        note_launch();
+    }
+    if (NV > 0) {
+        k_vert_owner<<<nblk(NV), kBs, 0, s>>>(C, NV);
+        note_launch();
+    }
+    cudaError_t e = exscan_u32(C.vflag, C.vgid_new, NV, s);
+    if (e != cudaSuccess) return e;
+    int64_t n_verts = 0;
+    e = scan_total(C.vflag, C.vgid_new, NV, &n_verts, s);
+    if (e != cudaSuccess) return e;
+    out.n_verts = n_verts;
+    cudaMallocAsync((void**)&out.xyz, sizeof(double) * 3 * (size_t)(n_verts > 0 ? n_verts : 1), s);
+    cudaMallocAsync((void**)&out.verts, sizeof(int64_t) * 11 * (size_t)(n_verts > 0 ? n_verts : 1), s);
+    if (NV > 0) {
+        k_vert_emit<<<nblk(NV), kBs, 0, s>>>(C, NV, out.verts, out.xyz);
+        note_launch();
+    }
+    // faces
+    if (A > 0) {
+        k_ia_face_keys<<<nblk(A), kBs, 0, s>>>(C);
+        note_launch();
+    }
+    if (NF > 0) {
+        k_face_owner<<<nblk(NF), kBs, 0, s>>>(C, NF);
+        note_launch();
+    }
+    if (NF > 0) {
+        k_face_sizes<<<nblk(NF), kBs, 0, s>>>(C, NF);
+        note_launch();
+    }
+    if ((e = exscan_u32(C.fflag, C.fgid, NF, s)) != cudaSuccess) return e;
+    if ((e = exscan_u32(C.fnewlen, C.foff, NF, s)) != cudaSuccess) return e;
+    if ((e = exscan_u32(C.fntet, C.ftoff, NF, s)) != cudaSuccess) return e;
+    int64_t n_faces = 0, n_fv = 0, n_ft = 0;
+    if ((e = scan_total(C.fflag, C.fgid, NF, &n_faces, s)) != cudaSuccess) return e;
+    if ((e = scan_total(C.fnewlen, C.foff, NF, &n_fv, s)) != cudaSuccess) return e;
+    if ((e = scan_total(C.fntet, C.ftoff, NF, &n_ft, s)) != cudaSuccess) return e;
+    out.n_faces = n_faces;
+    out.n_face_verts = n_fv;
+    out.n_face_tets = n_ft;
+    cudaMallocAsync((void**)&out.face_offsets, sizeof(int64_t) * (size_t)(n_faces + 1), s);
+    cudaMallocAsync((void**)&out.face_verts, sizeof(int64_t) * (size_t)(n_fv > 0 ? n_fv : 1), s);
+    cudaMallocAsync((void**)&out.face_tet_offsets, sizeof(int64_t) * (size_t)(n_faces + 1), s);
+    cudaMallocAsync((void**)&out.face_tets, sizeof(int64_t) * 2 * (size_t)(n_ft > 0 ? n_ft : 1), s);
+    cudaMallocAsync((void**)&out.face_func, sizeof(int64_t) * 2 * (size_t)(n_faces > 0 ? n_faces : 1), s);
+    if (A > 0)
+        {
+            k_ia_face_emit<<<nblk(A), kBs, 0, s>>>(C, out.face_offsets, out.face_verts, out.face_tet_offsets, out.face_tets,
+                                             out.face_func);
+            note_launch();
+        }
+    {
+        k_set_last<<<1, 1, 0, s>>>(out.face_offsets, n_faces, C.fnewlen, C.foff, NF);
+        note_launch();
+    }
+    {
+        k_set_last<<<1, 1, 0, s>>>(out.face_tet_offsets, n_faces, C.fntet, C.ftoff, NF);
+        note_launch();
+    }
+    return cudaGetLastError();
+}
+
+// ---- per-tet records and the active-function CRS, in tet order
+
+namespace {
+
+__global__ void k_rec_sizes(bool mi, int64_t A, const uint64_t* __restrict__ desc, RecSrc rs,
+                            uint32_t* __restrict__ sz) {
+    const int64_t a = (int64_t)blockIdx.x * kBs + threadIdx.x;
+    if (a >= A) return;
+    const uint8_t* b = rs.get(desc[a]);
+    sz[a] = mi ? mi_record_size(b) : ia_record_size(b);
+}
+
+__global__ void k_rec_copy(bool mi, int64_t A, const uint64_t* __restrict__ desc, RecSrc rs,
+                           const uint32_t* __restrict__ off, uint8_t* __restrict__ dst) {
+    const int64_t a = (int64_t)blockIdx.x * kBs + threadIdx.x;
+    if (a >= A) return;
+    const uint8_t* b = rs.get(desc[a]);
+    const int n = mi ? mi_record_size(b) : ia_record_size(b);
+    for (int i = 0; i < n; ++i) dst[off[a] + i] = b[i];
+}
+
+// per-tet offsets from per-active-tet offsets: off[t] = exclusive total before tet t
+__global__ void k_expand_offsets(int64_t T, int64_t A, const uint32_t* __restrict__ act_tet,
+                                 const uint32_t* __restrict__ aoff, const uint32_t* __restrict__ asz,
+                                 int64_t* __restrict__ toff) {
+    const int64_t t = (int64_t)blockIdx.x * kBs + threadIdx.x;
+    if (t > T) return;
+    // number of active tets before t (binary search in the sorted act_tet)
+    int64_t lo = 0, hi = A;
+    while (lo < hi) {
+        int64_t mid = (lo + hi) >> 1;
+        if ((int64_t)act_tet[mid] < t) lo = mid + 1;
+        else hi = mid;
+    }
+    toff[t] = lo == 0 ? 0 : (int64_t)aoff[lo - 1] + (int64_t)asz[lo - 1];
+}
+
+__global__ void k_popc(int64_t A, const uint64_t* __restrict__ mask, uint32_t* __restrict__ k) {
+    const int64_t a = (int64_t)blockIdx.x * kBs + threadIdx.x;
+    if (a < A) k[a] = __popcll(mask[a]);
+}
+
+__global__ void k_crs_fill(int64_t A, const uint64_t* __restrict__ mask, const uint32_t* __restrict__ off,
+                           int64_t* __restrict__ vals) {
+    const int64_t a = (int64_t)blockIdx.x * kBs + threadIdx.x;
+    if (a >= A) return;
+    uint64_t m = mask[a];
+    int64_t o = off[a];
+    while (m) {
+        vals[o++] = __ffsll((long long)m) - 1;
+        m &= m - 1;
+    }
+}
+
+}  // namespace
+
+cudaError_t gather_records(bool mi, int64_t A, int64_t T, const uint32_t* act_tet, const uint64_t* act_desc,
+                           const uint8_t* heap, const uint8_t* heap_big, const uint8_t* table,
+                           const uint32_t* table_off, int64_t* d_rec_offsets, uint8_t** d_rec_bytes, int64_t* n_bytes,
+                           cudaStream_t s) {
+    Pool pool{s};
+    RecSrc rs{heap, heap_big, table, table_off};
+    uint32_t* sz = pool.get<uint32_t>(A);
+    uint32_t* off = pool.get<uint32_t>(A);
+    if (pool.err) return pool.err;
+    if (A > 0) {
+        k_rec_sizes<<<nblk(A), kBs, 0, s>>>(mi, A, act_desc, rs, sz);
+        note_launch();
+    }
+    cudaError_t e = exscan_u32(sz, off, A, s);
+    if (e != cudaSuccess) return e;
+    int64_t total = 0;
+    if ((e = scan_total(sz, off, A, &total, s)) != cudaSuccess) return e;
+    *n_bytes = total;
+    if ((e = cudaMallocAsync((void**)d_rec_bytes, (size_t)(total > 0 ? total : 1), s)) != cudaSuccess) return e;
+    if (A > 0) {
+        k_rec_copy<<<nblk(A), kBs, 0, s>>>(mi, A, act_desc, rs, off, *d_rec_bytes);
+        note_launch();
+    }
+    {
+        k_expand_offsets<<<nblk(T + 1), kBs, 0, s>>>(T, A, act_tet, off, sz, d_rec_offsets);
+        note_launch();
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t gather_func_in_tet(int64_t A, int64_t T, const uint32_t* act_tet, const uint64_t* act_mask,
+                               int64_t* d_start, int64_t** d_vals, int64_t* n_vals, cudaStream_t s) {
+    Pool pool{s};
+    uint32_t* k = pool.get<uint32_t>(A);
+    uint32_t* off = pool.get<uint32_t>(A);
+    if (pool.err) return pool.err;
+    if (A > 0) {
+        k_popc<<<nblk(A), kBs, 0, s>>>(A, act_mask, k);
+        note_launch();
+    }
+    cudaError_t e = exscan_u32(k, off, A, s);
+    if (e != cudaSuccess) return e;
+    int64_t total = 0;
+    if ((e = scan_total(k, off, A, &total, s)) != cudaSuccess) return e;
+    *n_vals = total;
+    if ((e = cudaMallocAsync((void**)d_vals, sizeof(int64_t) * (size_t)(total > 0 ? total : 1), s)) != cudaSuccess)
+        return e;
+    if (A > 0) {
+        k_crs_fill<<<nblk(A), kBs, 0, s>>>(A, act_mask, off, *d_vals);
+        note_launch();
+    }
+    {
+        k_expand_offsets<<<nblk(T + 1), kBs, 0, s>>>(T, A, act_tet, off, k, d_start);
+        note_launch();
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace ria

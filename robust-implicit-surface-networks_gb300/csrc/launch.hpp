@@ -1,0 +1,129 @@
+// Host-side launchers of the device kernels (one declaration per kernel family).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "../../include/ria.h"
+
+namespace ria {
+
+// counts every kernel of this library as it is launched (ria_kernel_launches)
+void note_launch();
+
+struct IASum4 {  // IASummary / MISummary packed as 4 x u16 (MI: n_mi_v, n_mi_f, n_mi_loop, n_bnd_f)
+    uint16_t a, b, c, d;
+};
+
+struct GridDesc {
+    int64_t res;  // 0: explicit pts / tets
+    double bmin[3], bmax[3];
+};
+
+// ---- stage a / b (k_ab.cu)
+// grid sampling fused with the per-vertex masks: IA -> (pos, neg) masks; MI -> (argmax mask, 0)
+void launch_sample_grid(bool mi, const ria_function* d_funcs, int F, const GridDesc& g, double* fv,
+                        ulonglong2* vmask, unsigned long long* n_zero, cudaStream_t s);
+void launch_sample_points(const ria_function* d_funcs, int F, const double* pts, int64_t V, double* fv, cudaStream_t s);
+void launch_vertex_masks(bool mi, const double* fv, int64_t V, int F, ulonglong2* vmask, unsigned long long* n_zero,
+                         cudaStream_t s);
+
+// Ordered compaction of the active tets.  Pass 1 counts per block (active, generic) and the k
+// histogram; pass 2 writes, in tet order, the active tets and the tets that need the generic cut.
+struct FilterOut {
+    uint32_t* act_tet;    // [A]
+    uint64_t* act_mask;   // [A] active functions (bit j = function j)
+    uint64_t* act_desc;   // [A] record descriptor (lookup entries are filled here)
+    IASum4* act_sum;      // [A]
+    uint32_t* gen;        // [G] indices into the active arrays
+};
+// raises ST_BADINPUT if an explicit tet refers to a vertex outside 0..V-1
+void launch_check_tets(const int64_t* d_tets, int64_t T, int64_t V, uint32_t* status, cudaStream_t s);
+int64_t filter_num_blocks(int64_t T);
+void launch_filter_count(bool mi, const ulonglong2* vmask, const double* fv, int F, const int64_t* d_tets,
+                         const GridDesc& g, int64_t T, bool use_table, uint32_t* blk_counts /* [2][nblk] */,
+                         unsigned long long* khist /* [3] */, cudaStream_t s);
+void launch_filter_scatter(bool mi, const ulonglong2* vmask, const double* fv, int F, const int64_t* d_tets,
+                           const GridDesc& g, int64_t T, bool use_table, const uint32_t* blk_offsets /* [2][nblk] */,
+                           const IASum4* table_sum, FilterOut out, cudaStream_t s);
+
+// ---- stage c (k_cut.cu)
+struct CutArgs {
+    bool mi;
+    const uint32_t* list;  // indices into the active arrays
+    int64_t n;
+    const uint32_t* act_tet;
+    const uint64_t* act_mask;
+    uint64_t* act_desc;
+    IASum4* act_sum;
+    const double* fv;
+    int F;
+    const int64_t* d_tets;
+    GridDesc g;
+    uint8_t* heap;
+    unsigned long long* heap_used;
+    uint64_t heap_cap;
+    uint64_t desc_bit;           // or-ed into the descriptors written (0 or kBigHeapBit)
+    uint32_t* deferred;          // fast variant: tets handed to the exact variant
+    unsigned int* n_deferred;
+    uint32_t* status;
+    // explicit per-tet rows (the per-tet batch API): rows of tet i are value_off[i]..value_off[i+1]-1
+    const double* values = nullptr;
+    const uint32_t* value_off = nullptr;
+};
+void launch_cut_fast(const CutArgs& a, cudaStream_t s);
+void launch_cut_big(const CutArgs& a, void* scratch, int64_t scratch_slots, cudaStream_t s);
+size_t cut_big_slot_bytes(bool mi);
+// per-device lookup tables: IA one active plane, MI two active materials; 81 sign patterns each
+constexpr int kTablePatterns = 81;
+constexpr int kTableStride = 256;
+void launch_build_table(bool mi, uint8_t* table, uint32_t* table_off, IASum4* table_sum, void* scratch,
+                        uint32_t* status, cudaStream_t s);
+// robust test: cut every listed tet with its rows in the given and in the reversed order with the
+// exact variant; counts the tets whose vertex/face/cell counts differ
+void launch_robust(const CutArgs& a, void* scratch, int64_t scratch_slots, unsigned long long* n_fail,
+                   cudaStream_t s);
+
+// ---- stage d (k_extract.cu)
+struct ExtractArgs {
+    bool mi;
+    int64_t A;
+    const uint32_t* act_tet;
+    const uint64_t* act_mask;
+    const uint64_t* act_desc;
+    const uint8_t* heap;
+    const uint8_t* table;
+    const uint32_t* table_off;
+    const uint8_t* heap_big;
+    const double* fv;
+    int F;
+    const int64_t* d_tets;
+    const double* d_pts;
+    GridDesc g;
+    int64_t V;
+    uint32_t* status;
+};
+struct ExtractOut {
+    int64_t n_verts = 0, n_faces = 0, n_face_verts = 0, n_face_tets = 0;
+    double* xyz = nullptr;
+    int64_t* verts = nullptr;
+    int64_t* face_offsets = nullptr;
+    int64_t* face_verts = nullptr;
+    int64_t* face_tet_offsets = nullptr;
+    int64_t* face_tets = nullptr;
+    int64_t* face_func = nullptr;
+};
+// Runs the whole extraction; allocates the outputs with cudaMallocAsync on `s`.
+cudaError_t run_extract(const ExtractArgs& a, const IASum4* act_sum, ExtractOut& out, cudaStream_t s);
+
+// records in tet order (for RIA_MESH_REC_*)
+cudaError_t gather_records(bool mi, int64_t A, int64_t T, const uint32_t* act_tet, const uint64_t* act_desc,
+                           const uint8_t* heap, const uint8_t* heap_big, const uint8_t* table, const uint32_t* table_off,
+                           int64_t* d_rec_offsets /* [T+1] */, uint8_t** d_rec_bytes, int64_t* n_bytes,
+                           cudaStream_t s);
+// CRS of the active functions (RIA_MESH_FUNC_IN_TET / START_INDEX)
+cudaError_t gather_func_in_tet(int64_t A, int64_t T, const uint32_t* act_tet, const uint64_t* act_mask,
+                               int64_t* d_start /* [T+1] */, int64_t** d_func_in_tet, int64_t* n_vals,
+                               cudaStream_t s);
+
+}  // namespace ria

@@ -1,0 +1,38 @@
+"""ctypes binding of the test-only host build of the device cut headers."""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "_build", "libhostcheck.so")
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        subprocess.run(["make", "-C", HERE, "-s"], check=True)
+        L = ctypes.CDLL(LIB)
+        for f in (L.hc_ia_cut, L.hc_mi_cut):
+            f.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
+        L.hc_det_sign.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        _lib = L
+    return _lib
+
+
+def cut(mode, rows, big):
+    rows = np.ascontiguousarray(rows, dtype=np.float64).reshape(-1, 4)
+    buf = np.zeros(1 << 16, dtype=np.uint8)
+    summ = np.zeros(8, dtype=np.uint16)
+    f = lib().hc_ia_cut if mode == "ia" else lib().hc_mi_cut
+    n = f(rows.shape[0], rows.ctypes.data, 1 if big else 0, buf.ctypes.data, buf.size, summ.ctypes.data)
+    if n < 0:
+        return n, None
+    return bytes(buf[:n]), summ.copy()
+
+
+def det_sign(M):
+    M = np.ascontiguousarray(M, dtype=np.float64)
+    return lib().hc_det_sign(M.ctypes.data, M.shape[0])

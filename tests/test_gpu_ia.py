@@ -1,0 +1,126 @@
+"""GPU parity of the implicit-arrangement path against the CPU oracle (through the C ABI).
+
+Combinatorics (active-function CRS, per-tet records, vertex records, face lists, tet-face lists,
+function labels) must be bit-exact; vertex coordinates within 1e-12 relative (they are computed with
+the same operation order and in practice match exactly).
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+
+pytestmark = pytest.mark.gpu
+
+XYZ_RTOL = 1e-12
+
+
+def assert_mesh_equal(mesh, ref, records=True):
+    for k in ("verts", "face_offsets", "face_verts", "face_tet_offsets", "face_tets", "face_func"):
+        a, b = mesh[k], ref[k]
+        assert a.shape == b.shape and np.array_equal(a, b), k
+    x, y = mesh["xyz"], ref["xyz"]
+    assert x.shape == y.shape
+    assert np.all(np.abs(x - y) <= XYZ_RTOL * np.maximum(1.0, np.abs(y)))
+    assert np.array_equal(mesh["start_index"], ref["start_index"])
+    assert np.array_equal(mesh["func_in_tet"], ref["func_in_tet"])
+    if records:
+        assert np.array_equal(mesh["rec_offsets"], ref["rec_offsets"])
+        assert np.array_equal(mesh["rec_bytes"], ref["rec_bytes"])
+    st = mesh.stats
+    rs = ref["stats_named"]
+    for k in ("num_pts", "num_tets", "num_degenerate_vertex", "num_intersecting_tet", "num_a_func", "num_b_func",
+              "num_more_func", "num_verts", "num_faces"):
+        assert st[k] == rs[k], k
+
+
+@pytest.fixture(scope="module")
+def lib(pkg):
+    pkg.build()
+    return pkg.load()
+
+
+def test_sampling_bit_exact(pkg, fns, oracle, lib):
+    rng = np.random.default_rng(1)
+    specs = [
+        {"type": "plane", "point": [0.1, -0.2, 0.3], "normal": [0.3, 0.5, -0.8]},
+        {"type": "sphere", "center": [0.1, 0.2, -0.1], "radius": 0.4},
+        {"type": "sphere", "center": [0.1, 0.2, -0.1], "radius": 0.4, "squared": True, "is_flipped": True},
+        {"type": "cylinder", "axis_point": [0.0, 0.1, 0.2], "axis_vector": [1.0, 2.0, 3.0], "radius": 0.3},
+        {"type": "torus", "center": [0.0, 0.1, 0.2], "axis_vector": [0.2, -1.0, 0.4], "major_radius": 0.5,
+         "minor_radius": 0.1},
+        {"type": "zero"},
+    ]
+    funcs = fns.make_functions(specs)
+    pts = rng.uniform(-1, 1, size=(50000, 3))
+    assert np.array_equal(pkg.sample_functions(funcs, pts), oracle.sample(funcs, pts))
+
+
+@pytest.mark.parametrize("use_lookup", [True, False])
+def test_grid_small_workload(pkg, fns, oracle, lib, use_lookup):
+    wl = fns.workload_ia_small()
+    mesh = pkg.grid_implicit_arrangement(wl.res, wl.funcs, use_lookup=use_lookup)
+    pts, tets = fns.generate_tet_mesh(wl.res)
+    fv = oracle.sample(wl.funcs, pts)
+    assert np.array_equal(mesh["func_vals"].reshape(fv.shape), fv)
+    assert_mesh_equal(mesh, oracle.run("ia", pts, tets, fv))
+
+
+def test_host_buffers_custom_mesh(pkg, fns, oracle, lib):
+    m = np.load(os.path.join(GOLDEN, "mesh_8sphere.npz"))
+    funcs = fns.load_functions(os.path.join(GOLDEN, "functions", "8-sphere.json"))
+    fv = oracle.sample(funcs, m["pts"])
+    mesh = pkg.implicit_arrangement(m["pts"], m["tets"], fv)
+    assert_mesh_equal(mesh, oracle.run("ia", m["pts"], m["tets"], fv))
+
+
+@pytest.mark.parametrize("name", ["2-planesphere", "3-sphere-3", "1-plane"])
+def test_known_answer_fixtures(pkg, fns, oracle, lib, name):
+    """The reference's known-answer grids (101^3 cubes); the oracle's output there is pinned to the
+    reference's patch/chain counts by test_oracle_kat.py."""
+    funcs = fns.load_functions(os.path.join(GOLDEN, "functions", name + ".json"))
+    mesh = pkg.grid_implicit_arrangement(101, funcs)
+    pts, tets = fns.generate_tet_mesh(101)
+    fv = oracle.sample(funcs, pts, threads=os.cpu_count() or 1)
+    assert_mesh_equal(mesh, oracle.run("ia", pts, tets, fv, threads=os.cpu_count() or 1), records=False)
+
+
+@pytest.mark.parametrize("res", [24, 128])
+def test_degenerate_workload(pkg, fns, oracle, lib, res):
+    """32 functions with duplicated planes and planes through grid vertices (exact zeros)."""
+    wl = fns.workload_ia_degenerate(res=res)
+    mesh = pkg.grid_implicit_arrangement(wl.res, wl.funcs)
+    pts, tets = fns.generate_tet_mesh(wl.res)
+    fv = oracle.sample(wl.funcs, pts, threads=os.cpu_count() or 1)
+    assert np.array_equal(mesh["func_vals"].reshape(fv.shape), fv)
+    assert_mesh_equal(mesh, oracle.run("ia", pts, tets, fv, threads=os.cpu_count() or 1), records=res < 100)
+
+
+def test_batch_api_records(pkg, oracle, lib):
+    rng = np.random.default_rng(3)
+    rows = []
+    for _ in range(300):
+        k = int(rng.integers(1, 6))
+        rows.append(rng.normal(size=(k, 4)))
+    for _ in range(300):
+        k = int(rng.integers(1, 5))
+        rows.append(rng.integers(-2, 3, size=(k, 4)).astype(np.float64))
+    got = pkg.compute_arrangement_batch(rows)
+    for r, g in zip(rows, got):
+        assert g == oracle.ia_cut(r)
+
+
+def test_robust_mode(pkg, fns, lib):
+    wl = fns.workload_ia_small(res=16)
+    mesh = pkg.grid_implicit_arrangement(wl.res, wl.funcs, robust_test=True)
+    assert mesh.stats["robust_failures"] == 0
+
+
+def test_repeatable(pkg, fns, lib):
+    wl = fns.workload_ia_degenerate(res=32)
+    a = pkg.grid_implicit_arrangement(wl.res, wl.funcs)
+    b = pkg.grid_implicit_arrangement(wl.res, wl.funcs)
+    for k in ("verts", "face_verts", "face_tets", "xyz", "rec_bytes"):
+        assert np.array_equal(a[k], b[k]), k
