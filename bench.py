@@ -178,6 +178,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="ia-degenerate", choices=["ia-degenerate", "mi", "ia-small"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer end-to-end leg (profiling runs)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -244,7 +245,7 @@ def main():
     tets = np.ascontiguousarray(tets)
     e2e_times = []
     h2d = d2h = 0
-    for it in range(1 + args.steps):
+    for it in range(0 if args.no_e2e else 1 + args.steps):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         fv = pkg.sample_functions(wl.funcs, pts)
@@ -256,7 +257,7 @@ def main():
             e2e_times.append(dt)
         h2d = pts.nbytes + wl.funcs.nbytes + pts.nbytes + tets.nbytes + fv.nbytes
         d2h = fv.nbytes + sum(o.nbytes for o in outs)
-    e2e = world * wl.n_tets / statistics.median(e2e_times)
+    e2e = world * wl.n_tets / statistics.median(e2e_times) if e2e_times else None
 
     if rank != 0:
         if dist:

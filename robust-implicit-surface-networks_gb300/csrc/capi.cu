@@ -232,12 +232,17 @@ ria_status run_pipeline(const ria_config* cfg, const Inputs& in, cudaStream_t s,
     // ---- stage a
     ulonglong2* vmask = tmp.get<ulonglong2>(in.V, &err);
     const double* fv = in.d_fv;
+    double* coords = nullptr;
     if (in.funcs) {
+        const int64_t N = in.g.res + 1;
         double* d_fv = M->keep.get<double>(in.V * in.F, &err);
         ria_function* d_funcs = tmp.get<ria_function>(in.F, &err);
+        coords = tmp.get<double>(3 * N, &err);
+        double* tab = tmp.get<double>(6 * N * in.F, &err);
         if (err != cudaSuccess) return bail(fail(RIA_ENOMEM, "device allocation failed"));
         cudaMemcpyAsync(d_funcs, in.funcs, sizeof(ria_function) * in.F, cudaMemcpyHostToDevice, s);
-        launch_sample_grid(mi, d_funcs, in.F, in.g, d_fv, vmask, cnt + 1, s);
+        launch_grid_coords(in.g, coords, s);
+        launch_sample_grid(mi, d_funcs, in.F, in.g, coords, tab, d_fv, vmask, cnt + 1, s);
         fv = d_fv;
         M->fv = d_fv;
     } else {
@@ -317,6 +322,10 @@ ria_status run_pipeline(const ria_config* cfg, const Inputs& in, cudaStream_t s,
         ca.desc_bit = 0;
         ca.deferred = deferred;
         ca.n_deferred = (unsigned int*)(cnt + 7);
+        if (!mi && cfg->use_lookup) {
+            ca.table = ctx->table[0];
+            ca.table_off = ctx->table_off[0];
+        }
         launch_cut_fast(ca, s);
         unsigned long long h = 0;
         cudaMemcpyAsync(&h, cnt + 7, 8, cudaMemcpyDeviceToHost, s);
@@ -324,8 +333,6 @@ ria_status run_pipeline(const ria_config* cfg, const Inputs& in, cudaStream_t s,
         n_def = (int64_t)(h & 0xFFFFFFFFull);
         if (n_def > 0) {
             M->heap_big = M->keep.get<uint8_t>(n_def * kBigRecordBytes, &err);
-            const int64_t slots = n_def < kBigSlots ? n_def : kBigSlots;
-            void* scratch = tmp.get<uint8_t>((int64_t)cut_big_slot_bytes(mi) * slots, &err);
             if (err != cudaSuccess) return bail(fail(RIA_ENOMEM, "device allocation failed"));
             CutArgs cb = ca;
             cb.list = deferred;
@@ -334,7 +341,7 @@ ria_status run_pipeline(const ria_config* cfg, const Inputs& in, cudaStream_t s,
             cb.heap_used = cnt + 6;
             cb.heap_cap = (uint64_t)n_def * kBigRecordBytes;
             cb.desc_bit = kBigHeapBit;
-            launch_cut_big(cb, scratch, slots, s);
+            launch_cut_big(cb, s);
         }
     }
     cudaEventRecord(ev[3], s);
@@ -356,6 +363,7 @@ ria_status run_pipeline(const ria_config* cfg, const Inputs& in, cudaStream_t s,
         xa.d_tets = in.d_tets;
         xa.d_pts = in.d_pts;
         xa.g = in.g;
+        xa.coords = coords;
         xa.V = in.V;
         xa.status = status;
         // the extraction reads the status only through its own checks; stop early on cut errors
@@ -528,6 +536,10 @@ ria_status batch_run(bool mi, const double* values, const uint32_t* value_offset
     ca.status = (uint32_t*)cnt;
     ca.values = d_vals;
     ca.value_off = d_off;
+    if (!mi) {
+        ca.table = ctx->table[0];
+        ca.table_off = ctx->table_off[0];
+    }
     launch_cut_fast(ca, s);
     unsigned long long h[4];
     cudaMemcpyAsync(h, cnt, 32, cudaMemcpyDeviceToHost, s);
@@ -536,8 +548,6 @@ ria_status batch_run(bool mi, const double* values, const uint32_t* value_offset
     uint8_t* heap_big = nullptr;
     if (n_def > 0) {
         heap_big = tmp.get<uint8_t>(n_def * kBigRecordBytes, &err);
-        const int64_t slots = n_def < kBigSlots ? n_def : kBigSlots;
-        void* scratch = tmp.get<uint8_t>((int64_t)cut_big_slot_bytes(mi) * slots, &err);
         if (err != cudaSuccess) return done(fail(RIA_ENOMEM, "device allocation failed"));
         CutArgs cb = ca;
         cb.list = deferred;
@@ -546,7 +556,7 @@ ria_status batch_run(bool mi, const double* values, const uint32_t* value_offset
         cb.heap_used = cnt + 3;
         cb.heap_cap = (uint64_t)n_def * kBigRecordBytes;
         cb.desc_bit = kBigHeapBit;
-        launch_cut_big(cb, scratch, slots, s);
+        launch_cut_big(cb, s);
     }
     cudaMemcpyAsync(h, cnt, 8, cudaMemcpyDeviceToHost, s);
     if (cudaStreamSynchronize(s) != cudaSuccess) return done(fail(RIA_ECUDA, cudaGetErrorString(cudaGetLastError())));
@@ -640,7 +650,7 @@ ria_status ria_sample_functions(const ria_function* funcs, uint32_t n_func, cons
     RIA_CUDA(cudaMallocAsync(&d_fv, sizeof(double) * (n_pts * n_func ? n_pts * n_func : 1), s));
     RIA_CUDA(cudaMemcpyAsync(d_funcs, funcs, sizeof(ria_function) * n_func, cudaMemcpyHostToDevice, s));
     RIA_CUDA(cudaMemcpyAsync(d_pts, pts, sizeof(double) * 3 * n_pts, cudaMemcpyHostToDevice, s));
-    launch_sample_points(d_funcs, (int)n_func, d_pts, (int64_t)n_pts, d_fv, s);
+    launch_sample_points(d_funcs, (int)n_func, d_pts, (int64_t)n_pts, d_fv, nullptr, nullptr, s);
     RIA_CUDA(cudaMemcpyAsync(func_vals, d_fv, sizeof(double) * n_pts * n_func, cudaMemcpyDeviceToHost, s));
     cudaFreeAsync(d_funcs, s);
     cudaFreeAsync(d_pts, s);

@@ -46,6 +46,132 @@ struct IASummary {
     uint16_t n_bnd_f;     // iso faces on the tet boundary
 };
 
+// Group coincident planes: rep[i] is 0xFF for the zero plane, the tet face b for a plane with a
+// single nonzero corner value (a multiple of face b), the first earlier plane it is an exact multiple
+// of, or 4+i.  Returns the number of planes that remain (rep[i] == 4+i); `first` is the first one.
+RIA_HD int ia_group_planes(const double* pl, int k, uint8_t* rep, int& first) {
+    int eff = 0;
+    first = -1;
+    for (int i = 0; i < k; ++i) {
+        const double* a = pl + 4 * i;
+        int nz = 0, last = -1;
+        for (int c = 0; c < 4; ++c)
+            if (a[c] != 0.0) {
+                ++nz;
+                last = c;
+            }
+        if (nz == 0) {
+            rep[i] = 0xFF;
+            continue;
+        }
+        if (nz == 1) {
+            rep[i] = (uint8_t)last;
+            continue;
+        }
+        rep[i] = (uint8_t)(4 + i);
+        for (int j = 0; j < i; ++j) {
+            if (rep[j] != 4 + j) continue;
+            const double* b = pl + 4 * j;
+            bool prop = true;
+            for (int x = 0; x < 4 && prop; ++x)
+                for (int y = x + 1; y < 4 && prop; ++y)
+                    if (!prod_eq(a[x], b[y], a[y], b[x])) prop = false;
+            if (prop) {
+                rep[i] = (uint8_t)(4 + j);
+                break;
+            }
+        }
+        if (rep[i] == 4 + i) {
+            if (first < 0) first = i;
+            ++eff;
+        }
+    }
+    return eff;
+}
+
+// Sign pattern of one plane: sum over corners of (s_c + 1) 3^c.
+RIA_HD int ia_sign_pattern(const double* p) {
+    int q = 0, w = 1;
+    for (int c = 0; c < 4; ++c) {
+        q += ((p[c] > 0.0) ? 2 : (p[c] < 0.0 ? 0 : 1)) * w;
+        w *= 3;
+    }
+    return q;
+}
+
+RIA_HD int rd16h(const uint8_t* p) { return p[0] | (p[1] << 8); }
+
+// Size of the record built by ia_record_from_template for a tet with k planes.
+RIA_HD int ia_template_record_size(const uint8_t* tmpl, int k) {
+    int nv = rd16h(tmpl + 2), nf = rd16h(tmpl + 4), nc = rd16h(tmpl + 6), nl = rd16h(tmpl + 8);
+    return 10 + k + 3 * nv + 8 * nf + 2 * nl + 8 * nc;
+}
+
+// Extraction counts of an implicit-arrangement record (records have at most 128 vertices).
+RIA_HD void ia_record_summary(const uint8_t* b, IASummary& sum) {
+    const int k = b[1], nv = rd16h(b + 2), nf = rd16h(b + 4);
+    const uint8_t* rep = b + 10;
+    const uint8_t* faces = rep + k + 3 * nv;
+    const uint8_t* loops = faces + 8 * nf;
+    uint64_t iso[2] = {0, 0};
+    int nisof = 0, nloop = 0, nbnd = 0, off = 0;
+    for (int f = 0; f < nf; ++f) {
+        const int p = faces[8 * f];
+        const int L = rd16h(faces + 8 * f + 6);
+        bool is = p > 3;
+        for (int j = 0; j < k && !is; ++j) is = rep[j] == p;
+        if (is) {
+            ++nisof;
+            nloop += L;
+            if (faces[8 * f + 1] & 1) ++nbnd;
+            for (int t = 0; t < L; ++t) {
+                int v = rd16h(loops + 2 * (off + t));
+                iso[v >> 6] |= 1ull << (v & 63);
+            }
+        }
+        off += L;
+    }
+#if defined(__CUDA_ARCH__)
+    sum.n_iso_v = (uint16_t)(__popcll(iso[0]) + __popcll(iso[1]));
+#else
+    sum.n_iso_v = (uint16_t)(__builtin_popcountll(iso[0]) + __builtin_popcountll(iso[1]));
+#endif
+    sum.n_iso_f = (uint16_t)nisof;
+    sum.n_iso_loop = (uint16_t)nloop;
+    sum.n_bnd_f = (uint16_t)nbnd;
+}
+
+// The record of a tet whose planes all coincide with one plane i (or with tet faces / zero when
+// eff == 0): the one-plane table entry `tmpl` of plane i's sign pattern with plane label 4 renamed
+// 4+i, the cell sign bit moved accordingly, and the tet's own groups.  Equal to what the generic cut
+// produces, since that cut skips every plane grouped with an earlier one.
+RIA_HD void ia_record_from_template(const uint8_t* tmpl, int k, const uint8_t* rep, int eff, int i,
+                                    uint8_t* dst) {
+    const int nv = rd16h(tmpl + 2), nf = rd16h(tmpl + 4), nc = rd16h(tmpl + 6), nl = rd16h(tmpl + 8);
+    const uint8_t lab = (uint8_t)(4 + (eff ? i : 0));
+    for (int t = 0; t < 10; ++t) dst[t] = tmpl[t];
+    dst[1] = (uint8_t)k;
+    for (int j = 0; j < k; ++j) dst[10 + j] = rep[j];
+    const uint8_t* s = tmpl + 11;
+    uint8_t* d = dst + 10 + k;
+    for (int t = 0; t < 3 * nv; ++t) d[t] = s[t] == 4 ? lab : s[t];
+    s += 3 * nv;
+    d += 3 * nv;
+    for (int f = 0; f < nf; ++f)
+        for (int t = 0; t < 8; ++t) d[8 * f + t] = (t == 0 && s[8 * f] == 4) ? lab : s[8 * f + t];
+    s += 8 * nf;
+    d += 8 * nf;
+    for (int t = 0; t < 2 * nl; ++t) d[t] = s[t];
+    s += 2 * nl;
+    d += 2 * nl;
+    for (int c = 0; c < nc; ++c) {
+        uint64_t sig = 0;
+        for (int t = 0; t < 8; ++t) sig |= (uint64_t)s[8 * c + t] << (8 * t);
+        sig = eff ? ((sig & 16ull) ? (1ull << lab) : 0ull) : 0ull;
+        for (int t = 0; t < 8; ++t) d[8 * c + t] = (uint8_t)((sig >> (8 * t)) & 0xFF);
+    }
+}
+
 template <int MV, int MF, int MC, int ML, bool EXACT>
 struct IACut {
     const double* pl;  // k x 4 corner values
@@ -96,36 +222,8 @@ struct IACut {
     }
 
     RIA_HD void group_planes() {
-        for (int i = 0; i < k; ++i) {
-            const double* a = pl + 4 * i;
-            int nz = 0, last = -1;
-            for (int c = 0; c < 4; ++c)
-                if (a[c] != 0.0) {
-                    ++nz;
-                    last = c;
-                }
-            if (nz == 0) {
-                rep[i] = 0xFF;
-                continue;
-            }
-            if (nz == 1) {
-                rep[i] = (uint8_t)last;
-                continue;
-            }
-            rep[i] = (uint8_t)(4 + i);
-            for (int j = 0; j < i; ++j) {
-                if (rep[j] != 4 + j) continue;
-                const double* b = pl + 4 * j;
-                bool prop = true;
-                for (int x = 0; x < 4 && prop; ++x)
-                    for (int y = x + 1; y < 4 && prop; ++y)
-                        if (!prod_eq(a[x], b[y], a[y], b[x])) prop = false;
-                if (prop) {
-                    rep[i] = (uint8_t)(4 + j);
-                    break;
-                }
-            }
-        }
+        int first;
+        ia_group_planes(pl, k, rep, first);
     }
 
     // Returns CUT_OK, CUT_DEFER (fast variant: filter undecided or out of capacity) or CUT_FAIL.
@@ -366,30 +464,25 @@ struct IACut {
 
     RIA_HD uint32_t vkey(int v) const { return ((uint32_t)lab[v][0] << 16) | ((uint32_t)lab[v][1] << 8) | lab[v][2]; }
 
-    // lexicographic comparison of the sorted (renumbered) vertex sets of faces a and b
-    RIA_HD int face_cmp(int a, int b, uint8_t* tmp) const {
-        if (fsupp[a] != fsupp[b]) return fsupp[a] < fsupp[b] ? -1 : 1;
-        int la = flen[a], lb = flen[b];
-        uint8_t* sa = tmp;
-        uint8_t* sb = tmp + la;
-        for (int j = 0; j < la; ++j) sa[j] = vnew[loops[cur][foff[a] + j]];
-        for (int j = 0; j < lb; ++j) sb[j] = vnew[loops[cur][foff[b] + j]];
-        for (int x = 1; x < la; ++x)
-            for (int y = x; y > 0 && sa[y - 1] > sa[y]; --y) {
-                uint8_t t = sa[y];
-                sa[y] = sa[y - 1];
-                sa[y - 1] = t;
+    // Sort key of a face: supporting plane, then its three smallest (renumbered) vertex ids.  Two
+    // distinct faces on one plane share at most an edge, so the three smallest ids already order
+    // them as the full sorted vertex lists would.
+    RIA_HD uint32_t face_key(int f) const {
+        uint32_t s0 = 0xFF, s1 = 0xFF, s2 = 0xFF;
+        for (int j = 0; j < flen[f]; ++j) {
+            uint32_t v = vnew[loops[cur][foff[f] + j]];
+            if (v < s0) {
+                s2 = s1;
+                s1 = s0;
+                s0 = v;
+            } else if (v < s1) {
+                s2 = s1;
+                s1 = v;
+            } else if (v < s2) {
+                s2 = v;
             }
-        for (int x = 1; x < lb; ++x)
-            for (int y = x; y > 0 && sb[y - 1] > sb[y]; --y) {
-                uint8_t t = sb[y];
-                sb[y] = sb[y - 1];
-                sb[y - 1] = t;
-            }
-        int n = la < lb ? la : lb;
-        for (int j = 0; j < n; ++j)
-            if (sa[j] != sb[j]) return sa[j] < sb[j] ? -1 : 1;
-        return la == lb ? 0 : (la < lb ? -1 : 1);
+        }
+        return ((uint32_t)fsupp[f] << 24) | (s0 << 16) | (s1 << 8) | s2;
     }
 
     RIA_HDI void canonicalize() {
@@ -417,10 +510,13 @@ struct IACut {
                 corder[y - 1] = t;
             }
         for (int i = 0; i < nc; ++i) cnew[corder[i]] = (uint8_t)i;
-        for (int f = 0; f < nf; ++f) forder[f] = (uint8_t)f;
-        uint8_t tmp[2 * (MV + 8)];
+        uint32_t fkey[MF];
+        for (int f = 0; f < nf; ++f) {
+            forder[f] = (uint8_t)f;
+            fkey[f] = face_key(f);
+        }
         for (int x = 1; x < nf; ++x)
-            for (int y = x; y > 0 && face_cmp(forder[y - 1], forder[y], tmp) > 0; --y) {
+            for (int y = x; y > 0 && fkey[forder[y - 1]] > fkey[forder[y]]; --y) {
                 uint8_t t = forder[y];
                 forder[y] = forder[y - 1];
                 forder[y - 1] = t;

@@ -61,20 +61,22 @@ struct TetSrc {
     }
 };
 
-// Point source: an explicit V x 3 array or the grid coordinates (src/io.cpp:104-106).
+// Point source: an explicit V x 3 array or the per-axis grid coordinates (src/io.cpp:104-106),
+// coords[a * N + n] with N = res + 1.
 struct PtSrc {
-    const double* pts;  // nullptr for the grid
-    int64_t res;
-    double bmin[3], bmax[3];
+    const double* pts;     // nullptr for the grid
+    const double* coords;
+    int N;
     __device__ __forceinline__ void get(int64_t v, double p[3]) const {
         if (pts) {
             p[0] = pts[3 * v];
             p[1] = pts[3 * v + 1];
             p[2] = pts[3 * v + 2];
         } else {
-            const int64_t N = res + 1;
-            int64_t idx[3] = {v / (N * N), (v / N) % N, v % N};
-            for (int a = 0; a < 3; ++a) p[a] = ((double)idx[a] / (double)(N - 1)) * (bmax[a] - bmin[a]) + bmin[a];
+            const int vi = (int)v;
+            p[0] = coords[vi / (N * N)];
+            p[1] = coords[N + (vi / N) % N];
+            p[2] = coords[2 * N + vi % N];
         }
     }
 };

@@ -2,9 +2,10 @@
 // argmax masks, and the ordered compaction of the active tets.
 //
 //   sampling     the external implicit_functions library (app/implicit_arrangement.cpp:59);
-//                formulas in include/ria.h.  One thread per (vertex, function) element of the
-//                row-major V x F matrix, so stores are coalesced; a block stages a 32-vertex tile in
-//                shared memory and derives the per-vertex masks from it.
+//                formulas in include/ria.h.  One thread per vertex loops over the functions
+//                (no divergence across a warp), combining per-axis terms tabulated once per grid;
+//                the block's rows of the row-major V x F matrix go through shared memory so the
+//                stores stay coalesced; the per-vertex masks come out of the same loop.
 //   IA signs     src/implicit_arrangement.cpp:53-77   (pos/neg bit masks, F <= 64)
 //   IA filter    src/implicit_arrangement.cpp:82-116  (active = not all corners strictly + and not
 //                all strictly -:  ~(p0&p1&p2&p3 | n0&n1&n2&n3))
@@ -21,41 +22,6 @@ namespace {
 
 constexpr int kTileV = 32;
 constexpr int kBlock = 256;
-
-__device__ __forceinline__ double eval_function(const ria_function& f, double x, double y, double z) {
-    double v = 0.0;
-    switch (f.type) {
-        case RIA_FUNC_PLANE:
-            v = (f.p[3] * (x - f.p[0]) + f.p[4] * (y - f.p[1])) + f.p[5] * (z - f.p[2]);
-            break;
-        case RIA_FUNC_SPHERE:
-        case RIA_FUNC_SPHERE_SQUARED: {
-            double dx = x - f.p[0], dy = y - f.p[1], dz = z - f.p[2];
-            double d2 = (dx * dx + dy * dy) + dz * dz;
-            v = (f.type == RIA_FUNC_SPHERE) ? f.p[3] - sqrt(d2) : f.p[3] * f.p[3] - d2;
-            break;
-        }
-        case RIA_FUNC_CYLINDER: {
-            double vx = x - f.p[0], vy = y - f.p[1], vz = z - f.p[2];
-            double t = (vx * f.p[3] + vy * f.p[4]) + vz * f.p[5];
-            double wx = vx - t * f.p[3], wy = vy - t * f.p[4], wz = vz - t * f.p[5];
-            v = f.p[6] - sqrt((wx * wx + wy * wy) + wz * wz);
-            break;
-        }
-        case RIA_FUNC_TORUS: {
-            double vx = x - f.p[0], vy = y - f.p[1], vz = z - f.p[2];
-            double h = (vx * f.p[3] + vy * f.p[4]) + vz * f.p[5];
-            double wx = vx - h * f.p[3], wy = vy - h * f.p[4], wz = vz - h * f.p[5];
-            double rho = sqrt((wx * wx + wy * wy) + wz * wz);
-            double a = rho - f.p[6];
-            v = f.p[7] - sqrt(a * a + h * h);
-            break;
-        }
-        default:
-            v = 0.0;
-    }
-    return f.flipped ? -v : v;
-}
 
 // masks of one vertex row held in shared memory
 template <bool MI>
@@ -90,43 +56,157 @@ __device__ __forceinline__ void block_add(unsigned long long* dst, int v) {
     if ((threadIdx.x & 31) == 0 && v) atomicAdd(dst, (unsigned long long)v);
 }
 
-template <bool MI>
-__global__ void __launch_bounds__(kBlock) k_sample_grid(const ria_function* __restrict__ funcs, int F, PtSrc ps,
-                                                        int64_t V, double* __restrict__ fv,
-                                                        ulonglong2* __restrict__ vmask,
-                                                        unsigned long long* __restrict__ n_zero) {
-    extern __shared__ double tile[];
-    const int stride = F + 1;
-    const int64_t v0 = (int64_t)blockIdx.x * kTileV;
-    const int nel = kTileV * F;
-    for (int e = threadIdx.x; e < nel; e += blockDim.x) {
-        int lv = e / F, f = e - lv * F;
-        int64_t v = v0 + lv;
-        if (v < V) {
-            double p[3];
-            ps.get(v, p);
-            double val = eval_function(funcs[f], p[0], p[1], p[2]);
-            fv[v * F + f] = val;
-            tile[lv * stride + f] = val;
+// Separable evaluation.  Every function of include/ria.h starts with terms that depend on a single
+// coordinate (n_a (x_a - p_a), d_a^2, v_a = x_a - p_a and v_a u_a); on a grid they are tabulated per
+// axis once, and each vertex only performs the operations that mix the axes, in the same order as
+// the full formula, so the result is bit-identical to evaluating the formula at the vertex.
+__device__ __forceinline__ void axis_parts(const ria_function& f, int a, double x, double& w0, double& w1) {
+    switch (f.type) {
+        case RIA_FUNC_PLANE:
+            w0 = f.p[3 + a] * (x - f.p[a]);
+            w1 = 0.0;
+            break;
+        case RIA_FUNC_SPHERE:
+        case RIA_FUNC_SPHERE_SQUARED: {
+            double d = x - f.p[a];
+            w0 = d * d;
+            w1 = 0.0;
+            break;
         }
+        case RIA_FUNC_CYLINDER:
+        case RIA_FUNC_TORUS: {
+            double d = x - f.p[a];
+            w0 = d;
+            w1 = d * f.p[3 + a];
+            break;
+        }
+        default:
+            w0 = w1 = 0.0;
     }
-    __syncthreads();
-    int nz = 0;
-    if (threadIdx.x < kTileV) {
-        int64_t v = v0 + threadIdx.x;
-        if (v < V) vmask[v] = row_masks<MI>(tile + threadIdx.x * stride, F, nz);
-    }
-    if (threadIdx.x < 32) block_add(n_zero, nz);
 }
 
-__global__ void __launch_bounds__(kBlock) k_sample_points(const ria_function* __restrict__ funcs, int F,
-                                                          const double* __restrict__ pts, int64_t V,
-                                                          double* __restrict__ fv) {
-    int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= V * F) return;
-    int64_t v = e / F;
-    int f = (int)(e - v * F);
-    fv[e] = eval_function(funcs[f], pts[3 * v], pts[3 * v + 1], pts[3 * v + 2]);
+__device__ __forceinline__ double combine_parts(const ria_function& f, const double w0[3], const double w1[3]) {
+    double v;
+    switch (f.type) {
+        case RIA_FUNC_PLANE:
+            v = (w0[0] + w0[1]) + w0[2];
+            break;
+        case RIA_FUNC_SPHERE:
+            v = f.p[3] - sqrt((w0[0] + w0[1]) + w0[2]);
+            break;
+        case RIA_FUNC_SPHERE_SQUARED:
+            v = f.p[3] * f.p[3] - ((w0[0] + w0[1]) + w0[2]);
+            break;
+        case RIA_FUNC_CYLINDER: {
+            double t = (w1[0] + w1[1]) + w1[2];
+            double wx = w0[0] - t * f.p[3], wy = w0[1] - t * f.p[4], wz = w0[2] - t * f.p[5];
+            v = f.p[6] - sqrt((wx * wx + wy * wy) + wz * wz);
+            break;
+        }
+        case RIA_FUNC_TORUS: {
+            double h = (w1[0] + w1[1]) + w1[2];
+            double wx = w0[0] - h * f.p[3], wy = w0[1] - h * f.p[4], wz = w0[2] - h * f.p[5];
+            double rho = sqrt((wx * wx + wy * wy) + wz * wz);
+            double a = rho - f.p[6];
+            v = f.p[7] - sqrt(a * a + h * h);
+            break;
+        }
+        default:
+            v = 0.0;
+    }
+    return f.flipped ? -v : v;
+}
+
+// grid coordinates per axis (src/io.cpp:104-106): coords[a * N + n]
+__global__ void k_grid_coords(GridDesc g, int N, double* __restrict__ coords) {
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= 3 * N) return;
+    const int a = idx / N, n = idx - a * N;
+    coords[idx] = ((double)n / (double)(N - 1)) * (g.bmax[a] - g.bmin[a]) + g.bmin[a];
+}
+
+// per-axis terms: tab[((f * 3 + a) * 2 + w) * N + n]
+__global__ void k_axis_tables(const ria_function* __restrict__ funcs, int F, const double* __restrict__ coords, int N,
+                              double* __restrict__ tab) {
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= F * 3 * N) return;
+    const int n = idx % N, fa = idx / N, a = fa % 3, f = fa / 3;
+    double w0, w1;
+    axis_parts(funcs[f], a, coords[a * N + n], w0, w1);
+    tab[(fa * 2 + 0) * N + n] = w0;
+    tab[(fa * 2 + 1) * N + n] = w1;
+}
+
+constexpr int kSampleBlock = 128;
+
+// One thread per vertex, a loop over the functions (uniform across the warp); the block's rows are
+// staged in shared memory and stored row by row, so the V x F stores stay coalesced.
+template <bool MI, bool GRID>
+__global__ void __launch_bounds__(kSampleBlock) k_sample(const ria_function* __restrict__ funcs, int F,
+                                                         const double* __restrict__ tab, int N,
+                                                         const double* __restrict__ pts, int64_t V,
+                                                         double* __restrict__ fv, ulonglong2* __restrict__ vmask,
+                                                         unsigned long long* __restrict__ n_zero) {
+    extern __shared__ double tile[];
+    const int stride = F + 1;
+    const int64_t v0 = (int64_t)blockIdx.x * kSampleBlock;
+    const int64_t v = v0 + threadIdx.x;
+    const bool valid = v < V;
+    int ix[3] = {0, 0, 0};
+    double x[3] = {0.0, 0.0, 0.0};
+    if (valid) {
+        if (GRID) {
+            const int vi = (int)v;
+            ix[0] = vi / (N * N);
+            ix[1] = (vi / N) % N;
+            ix[2] = vi % N;
+        } else {
+            x[0] = pts[3 * v];
+            x[1] = pts[3 * v + 1];
+            x[2] = pts[3 * v + 2];
+        }
+    }
+    uint64_t m0 = 0, m1 = 0;
+    double mx = 0.0;
+    for (int f = 0; f < F; ++f) {
+        const ria_function& fn = funcs[f];
+        double w0[3], w1[3];
+        if (GRID) {
+            const double* t = tab + (size_t)f * 6 * N;
+            for (int a = 0; a < 3; ++a) {
+                w0[a] = t[(2 * a) * N + ix[a]];
+                w1[a] = t[(2 * a + 1) * N + ix[a]];
+            }
+        } else {
+            for (int a = 0; a < 3; ++a) axis_parts(fn, a, x[a], w0[a], w1[a]);
+        }
+        const double val = combine_parts(fn, w0, w1);
+        tile[threadIdx.x * stride + f] = val;
+        if (!MI) {
+            if (val > 0.0) m0 |= bit64(f);
+            else if (val < 0.0) m1 |= bit64(f);
+        } else {
+            if (f == 0 || val > mx) {
+                mx = val;
+                m0 = bit64(f);
+            } else if (val == mx) {
+                m0 |= bit64(f);
+            }
+        }
+    }
+    int nz = 0;
+    if (valid && vmask) {
+        vmask[v] = make_ulonglong2(m0, m1);
+        nz = MI ? (__popcll(m0) > 1) : (F - __popcll(m0) - __popcll(m1));
+    }
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int r = warp; r < kSampleBlock; r += kSampleBlock / 32) {
+        if (v0 + r >= V) break;
+        double* dst = fv + (v0 + r) * F;
+        for (int c = lane; c < F; c += 32) dst[c] = tile[r * stride + c];
+    }
+    if (n_zero) block_add(n_zero, nz);
 }
 
 template <bool MI>
@@ -300,44 +380,49 @@ __global__ void k_check_tets(const int64_t* __restrict__ tets, int64_t n, int64_
     }
 }
 
-PtSrc grid_pts(const GridDesc& g) {
-    PtSrc p;
-    p.pts = nullptr;
-    p.res = g.res;
-    for (int a = 0; a < 3; ++a) {
-        p.bmin[a] = g.bmin[a];
-        p.bmax[a] = g.bmax[a];
+template <bool MI, bool GRID>
+void set_sample_smem(size_t smem) {
+    static bool done = false;
+    if (!done && smem > 48 * 1024) {
+        cudaFuncSetAttribute(k_sample<MI, GRID>, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024);
+        done = true;
     }
-    return p;
 }
 
 }  // namespace
 
-void launch_sample_grid(bool mi, const ria_function* d_funcs, int F, const GridDesc& g, double* fv,
-                        ulonglong2* vmask, unsigned long long* n_zero, cudaStream_t s) {
-    const int64_t N = g.res + 1;
-    const int64_t V = N * N * N;
-    const int64_t blocks = (V + kTileV - 1) / kTileV;
-    const size_t smem = sizeof(double) * kTileV * (F + 1);
-    if (mi)
-        {
-            k_sample_grid<true><<<(unsigned)blocks, kBlock, smem, s>>>(d_funcs, F, grid_pts(g), V, fv, vmask, n_zero);
-            note_launch();
-        }
-    else
-        {
-            k_sample_grid<false><<<(unsigned)blocks, kBlock, smem, s>>>(d_funcs, F, grid_pts(g), V, fv, vmask, n_zero);
-            note_launch();
-        }
+void launch_grid_coords(const GridDesc& g, double* coords, cudaStream_t s) {
+    const int N = (int)g.res + 1;
+    k_grid_coords<<<(3 * N + 127) / 128, 128, 0, s>>>(g, N, coords);
+    note_launch();
 }
 
-void launch_sample_points(const ria_function* d_funcs, int F, const double* pts, int64_t V, double* fv, cudaStream_t s) {
-    const int64_t n = V * F;
-    if (n == 0) return;
-    {
-        k_sample_points<<<(unsigned)((n + kBlock - 1) / kBlock), kBlock, 0, s>>>(d_funcs, F, pts, V, fv);
-        note_launch();
+void launch_sample_grid(bool mi, const ria_function* d_funcs, int F, const GridDesc& g, const double* coords,
+                        double* tab, double* fv, ulonglong2* vmask, unsigned long long* n_zero, cudaStream_t s) {
+    const int N = (int)g.res + 1;
+    const int64_t V = (int64_t)N * N * N;
+    k_axis_tables<<<(F * 3 * N + 127) / 128, 128, 0, s>>>(d_funcs, F, coords, N, tab);
+    note_launch();
+    const unsigned blocks = (unsigned)((V + kSampleBlock - 1) / kSampleBlock);
+    const size_t smem = sizeof(double) * kSampleBlock * (F + 1);
+    if (mi) {
+        set_sample_smem<true, true>(smem);
+        k_sample<true, true><<<blocks, kSampleBlock, smem, s>>>(d_funcs, F, tab, N, nullptr, V, fv, vmask, n_zero);
+    } else {
+        set_sample_smem<false, true>(smem);
+        k_sample<false, true><<<blocks, kSampleBlock, smem, s>>>(d_funcs, F, tab, N, nullptr, V, fv, vmask, n_zero);
     }
+    note_launch();
+}
+
+void launch_sample_points(const ria_function* d_funcs, int F, const double* pts, int64_t V, double* fv,
+                          ulonglong2* vmask, unsigned long long* n_zero, cudaStream_t s) {
+    if (V == 0) return;
+    const unsigned blocks = (unsigned)((V + kSampleBlock - 1) / kSampleBlock);
+    const size_t smem = sizeof(double) * kSampleBlock * (F + 1);
+    set_sample_smem<false, false>(smem);
+    k_sample<false, false><<<blocks, kSampleBlock, smem, s>>>(d_funcs, F, nullptr, 0, pts, V, fv, vmask, n_zero);
+    note_launch();
 }
 
 void launch_vertex_masks(bool mi, const double* fv, int64_t V, int F, ulonglong2* vmask, unsigned long long* n_zero,

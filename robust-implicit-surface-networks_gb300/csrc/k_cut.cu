@@ -91,6 +91,30 @@ __device__ __forceinline__ void finish_cut(const CutArgs& a, uint32_t ai, Cut& c
     a.act_sum[ai] = pack_sum<Sum>(s);
 }
 
+// Tets whose planes reduce to at most one after grouping (duplicates, planes coincident with a tet
+// face, zero planes): the record comes from the one-plane lookup table, relabelled.
+__device__ __forceinline__ bool ia_try_template(const CutArgs& a, uint32_t ai, const double* planes, int k) {
+    uint8_t rep[kFastMaxK];
+    int first;
+    const int eff = ia_group_planes(planes, k, rep, first);
+    if (eff > 1 || !a.table) return false;
+    const int pattern = eff ? ia_sign_pattern(planes + 4 * first) : kTablePatterns - 1;  // all positive: uncut
+    const uint8_t* tmpl = a.table + a.table_off[pattern];
+    const int size = ia_template_record_size(tmpl, k);
+    unsigned long long off = atomicAdd(a.heap_used, (unsigned long long)size);
+    if (off + size > a.heap_cap) {
+        raise_status(a.status, ST_CAPACITY);
+        return true;
+    }
+    uint8_t* dst = a.heap + off;
+    ia_record_from_template(tmpl, k, rep, eff, first, dst);
+    IASummary s;
+    ia_record_summary(dst, s);
+    a.act_desc[ai] = off | a.desc_bit;
+    a.act_sum[ai] = pack_sum<IASummary>(s);
+    return true;
+}
+
 template <bool MI>
 __global__ void __launch_bounds__(128) k_cut_fast(CutArgs a) {
     using Fast = typename Traits<MI>::Fast;
@@ -100,6 +124,7 @@ __global__ void __launch_bounds__(128) k_cut_fast(CutArgs a) {
     const uint32_t ai = a.list[i];
     double planes[4 * kFastMaxK];
     const int k = gather_planes(a, ai, planes, kFastMaxK);
+    if (!MI && k <= kFastMaxK && ia_try_template(a, ai, planes, k)) return;
     int st = CUT_DEFER;
     Fast c;
     if (k <= kFastMaxK) st = c.run(planes, k);
@@ -113,13 +138,15 @@ __global__ void __launch_bounds__(128) k_cut_fast(CutArgs a) {
     }
 }
 
+// One tet per block at a time; its state lives in shared memory (the exact variant is a long serial
+// computation, so the latency of its state accesses sets the time of the whole stage).
 template <bool MI>
-__global__ void __launch_bounds__(64) k_cut_big(CutArgs a, BigSlot<MI>* scratch, int64_t slots) {
+__global__ void __launch_bounds__(32) k_cut_big(CutArgs a) {
     using Sum = typename Traits<MI>::Sum;
-    const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (tid >= slots) return;
-    BigSlot<MI>& S = scratch[tid];
-    for (int64_t i = tid; i < a.n; i += slots) {
+    extern __shared__ __align__(16) unsigned char big_smem[];
+    if (threadIdx.x != 0) return;
+    BigSlot<MI>& S = *reinterpret_cast<BigSlot<MI>*>(big_smem);
+    for (int64_t i = blockIdx.x; i < a.n; i += gridDim.x) {
         const uint32_t ai = a.list[i];
         const int k = gather_planes(a, ai, S.planes, 60);
         if (k > 60) {
@@ -252,21 +279,25 @@ void launch_cut_fast(const CutArgs& a, cudaStream_t s) {
         }
 }
 
-void launch_cut_big(const CutArgs& a, void* scratch, int64_t slots, cudaStream_t s) {
+template <bool MI>
+void launch_big(const CutArgs& a, cudaStream_t s) {
+    static bool attr = false;
+    const size_t smem = sizeof(BigSlot<MI>);
+    if (!attr) {
+        cudaFuncSetAttribute(k_cut_big<MI>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        attr = true;
+    }
+    const int64_t blocks = a.n < 152 * 8 ? a.n : 152 * 8;
+    k_cut_big<MI><<<(unsigned)blocks, 32, smem, s>>>(a);
+    note_launch();
+}
+
+void launch_cut_big(const CutArgs& a, cudaStream_t s) {
     if (a.n == 0) return;
-    const int bs = 64;
-    const int64_t use = a.n < slots ? a.n : slots;
-    const unsigned nb = (unsigned)((use + bs - 1) / bs);
     if (a.mi)
-        {
-            k_cut_big<true><<<nb, bs, 0, s>>>(a, (BigSlot<true>*)scratch, use);
-            note_launch();
-        }
+        launch_big<true>(a, s);
     else
-        {
-            k_cut_big<false><<<nb, bs, 0, s>>>(a, (BigSlot<false>*)scratch, use);
-            note_launch();
-        }
+        launch_big<false>(a, s);
 }
 
 void launch_build_table(bool mi, uint8_t* table, uint32_t* table_off, IASum4* table_sum, void* scratch,

@@ -227,13 +227,7 @@ __global__ void k_vert_emit(ExtractCtx C, int64_t n, int64_t* __restrict__ verts
     for (int c = 0; c < 3; ++c) rec[7 + c] = k.fn[c];
     rec[10] = -1;
     // coordinates, with the reference's formulas and operation order
-    PtSrc ps;
-    ps.pts = C.a.d_pts;
-    ps.res = C.a.g.res;
-    for (int c = 0; c < 3; ++c) {
-        ps.bmin[c] = C.a.g.bmin[c];
-        ps.bmax[c] = C.a.g.bmax[c];
-    }
+    PtSrc ps{C.a.d_pts, C.a.coords, (int)C.a.g.res + 1};
     const double* fv = C.a.fv;
     const int F = C.a.F;
     double out[3];

@@ -21,10 +21,15 @@ struct GridDesc {
 };
 
 // ---- stage a / b (k_ab.cu)
-// grid sampling fused with the per-vertex masks: IA -> (pos, neg) masks; MI -> (argmax mask, 0)
-void launch_sample_grid(bool mi, const ria_function* d_funcs, int F, const GridDesc& g, double* fv,
-                        ulonglong2* vmask, unsigned long long* n_zero, cudaStream_t s);
-void launch_sample_points(const ria_function* d_funcs, int F, const double* pts, int64_t V, double* fv, cudaStream_t s);
+// grid coordinates per axis: coords[a * (res+1) + n]
+void launch_grid_coords(const GridDesc& g, double* coords, cudaStream_t s);
+// grid sampling fused with the per-vertex masks: IA -> (pos, neg) masks; MI -> (argmax mask, 0).
+// tab: scratch of 6 * F * (res+1) doubles for the per-axis terms.
+void launch_sample_grid(bool mi, const ria_function* d_funcs, int F, const GridDesc& g, const double* coords,
+                        double* tab, double* fv, ulonglong2* vmask, unsigned long long* n_zero, cudaStream_t s);
+// sampling at explicit points (vmask / n_zero may be null)
+void launch_sample_points(const ria_function* d_funcs, int F, const double* pts, int64_t V, double* fv,
+                          ulonglong2* vmask, unsigned long long* n_zero, cudaStream_t s);
 void launch_vertex_masks(bool mi, const double* fv, int64_t V, int F, ulonglong2* vmask, unsigned long long* n_zero,
                          cudaStream_t s);
 
@@ -70,9 +75,13 @@ struct CutArgs {
     // explicit per-tet rows (the per-tet batch API): rows of tet i are value_off[i]..value_off[i+1]-1
     const double* values = nullptr;
     const uint32_t* value_off = nullptr;
+    // one-plane lookup table (implicit arrangement), used for tets with one effective plane
+    const uint8_t* table = nullptr;
+    const uint32_t* table_off = nullptr;
 };
 void launch_cut_fast(const CutArgs& a, cudaStream_t s);
-void launch_cut_big(const CutArgs& a, void* scratch, int64_t scratch_slots, cudaStream_t s);
+// exact variant: one tet per block, state in shared memory
+void launch_cut_big(const CutArgs& a, cudaStream_t s);
 size_t cut_big_slot_bytes(bool mi);
 // per-device lookup tables: IA one active plane, MI two active materials; 81 sign patterns each
 constexpr int kTablePatterns = 81;
@@ -99,6 +108,7 @@ struct ExtractArgs {
     int F;
     const int64_t* d_tets;
     const double* d_pts;
+    const double* coords;  // grid coordinates per axis (grid inputs)
     GridDesc g;
     int64_t V;
     uint32_t* status;

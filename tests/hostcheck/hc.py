@@ -36,3 +36,16 @@ def cut(mode, rows, big):
 def det_sign(M):
     M = np.ascontiguousarray(M, dtype=np.float64)
     return lib().hc_det_sign(M.ctypes.data, M.shape[0])
+
+
+def ia_template(rows):
+    """Record of the one-effective-plane path, or None when the tet has two or more planes left."""
+    rows = np.ascontiguousarray(rows, dtype=np.float64).reshape(-1, 4)
+    L = lib()
+    L.hc_ia_template.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
+    buf = np.zeros(4096, dtype=np.uint8)
+    summ = np.zeros(4, dtype=np.uint16)
+    n = L.hc_ia_template(rows.shape[0], rows.ctypes.data, buf.ctypes.data, buf.size, summ.ctypes.data)
+    if n < 0:
+        return None
+    return bytes(buf[:n]), summ.copy()

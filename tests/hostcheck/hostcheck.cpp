@@ -46,3 +46,47 @@ extern "C" int hc_mi_cut(int k, const double* mats, int big, uint8_t* buf, int c
 }
 
 extern "C" int hc_det_sign(const double* M, int n) { return det_sign_exact(M, n); }
+
+// The one-effective-plane path of the fast kernel: the one-plane table is built by the exact variant
+// from corner values in {-1, 0, 1}, as on the device.
+extern "C" int hc_ia_template(int k, const double* planes, uint8_t* buf, int cap, uint16_t* summary) {
+    static uint8_t table[81][256];
+    static bool built = false;
+    if (!built) {
+        for (int p = 0; p < 81; ++p) {
+            double pl[4];
+            int q = p;
+            for (int c = 0; c < 4; ++c) {
+                pl[c] = (double)(q % 3) - 1.0;
+                q /= 3;
+            }
+            auto* c = new IACutBig();
+            c->run(pl, 1);
+            c->canonicalize();
+            IASummary s;
+            c->emit(table[p], s);
+            delete c;
+        }
+        built = true;
+    }
+    uint8_t rep[64];
+    int first;
+    int eff = ia_group_planes(planes, k, rep, first);
+    if (eff > 1) return -1;
+    const uint8_t* tmpl = table[eff ? ia_sign_pattern(planes + 4 * first) : 80];
+    int n = ia_template_record_size(tmpl, k);
+    if (n > cap) return -3;
+    ia_record_from_template(tmpl, k, rep, eff, first, buf);
+    IASummary s;
+    ia_record_summary(buf, s);
+    std::memcpy(summary, &s, sizeof(s));
+    return n;
+}
+
+extern "C" int hc_sizes(int* out) {
+    out[0] = (int)sizeof(IACutFast);
+    out[1] = (int)sizeof(IACutBig);
+    out[2] = (int)sizeof(MICutFast);
+    out[3] = (int)sizeof(MICutBig);
+    return 0;
+}

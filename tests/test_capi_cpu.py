@@ -113,3 +113,37 @@ def test_exact_determinant_sign(hc):
 
             d = det(F)
             assert hc.det_sign(M) == (d > 0) - (d < 0)
+
+
+def test_one_effective_plane_template_path(hc, oracle):
+    """Tets whose planes reduce to one (duplicates, multiples, tet faces, zero planes) are built from
+    the one-plane table; the record must equal the generic cut's."""
+    rng = np.random.default_rng(12)
+    seen = 0
+    for _ in range(400):
+        p = rng.integers(-2, 3, size=4).astype(np.float64)
+        if rng.random() < 0.5:
+            p = rng.normal(size=4)
+        rows = [p]
+        for _ in range(int(rng.integers(0, 4))):
+            kind = rng.integers(0, 4)
+            if kind == 0:
+                rows.append(p * float(rng.choice([-2.0, 0.5, 1.0, 3.0])))
+            elif kind == 1:
+                b = np.zeros(4)
+                b[int(rng.integers(0, 4))] = float(rng.choice([-1.5, 2.0]))
+                rows.append(b)
+            elif kind == 2:
+                rows.append(np.zeros(4))
+            else:
+                rows.append(p.copy())
+        rng.shuffle(rows)
+        rows = np.array(rows)
+        got = hc.ia_template(rows)
+        if got is None:
+            continue
+        seen += 1
+        assert got[0] == oracle.ia_cut(rows)
+        big, summ = hc.cut("ia", rows, True)
+        assert got[0] == big and np.array_equal(got[1], summ[:4])
+    assert seen > 300
