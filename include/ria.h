@@ -202,6 +202,22 @@ RIA_API ria_status ria_compute_material_interface_batch(const double* values, co
                                                 uint64_t n_tets, uint8_t* records, uint64_t capacity,
                                                 uint64_t* record_offsets);
 
+/* Per-tet arrangements without any device allocation.  This entry point has no counterpart in the
+ * reference; it serves callers that cannot allocate device memory: a caller whose device memory is
+ * entirely held by its own allocator (a framework's caching allocator, an arena reserved at start-up)
+ * or a caller in a latency-critical loop where cudaMalloc / cudaFree, which can synchronize the device,
+ * are not allowed.  Inputs and outputs are the caller's device buffers (same meaning as
+ * ria_compute_arrangement_batch; d_record_offsets has n_tets + 1 entries); work is queued on `stream`
+ * and the call returns when it has finished.  Intermediate data lives in one fixed device array of
+ * about 8.5 MB inside the library, held by every GPU that loads it until the process exits.
+ * Limits: n_tets <= 4096 (RIA_EINVAL beyond) and at most 8 MiB of records per call (RIA_ECAPACITY
+ * beyond).  The first call on a device looks up that array's address there; make
+ * it before any stream capture.  Calls share the array: calls that overlap on the GPU race on it and
+ * must be serialized by the caller. */
+RIA_API ria_status ria_compute_arrangement_batch_noalloc(const double* d_values, const uint32_t* d_value_offsets,
+                                                         uint64_t n_tets, uint8_t* d_records, uint64_t capacity,
+                                                         uint64_t* d_record_offsets, void* stream);
+
 /* ---- results ---------------------------------------------------------------------------------- */
 RIA_API uint64_t ria_mesh_count(const ria_mesh* mesh, ria_mesh_field field); /* elements of the field */
 RIA_API ria_status ria_mesh_copy(const ria_mesh* mesh, ria_mesh_field field, void* host_dst);

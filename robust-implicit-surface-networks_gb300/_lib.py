@@ -73,6 +73,8 @@ def load():
         fn = getattr(L, name)
         fn.restype = i32
         fn.argtypes = [vp, vp, u64, vp, u64, vp]
+    L.ria_compute_arrangement_batch_noalloc.restype = i32
+    L.ria_compute_arrangement_batch_noalloc.argtypes = [vp, vp, u64, vp, u64, vp, vp]
     L.ria_mesh_count.restype = u64
     L.ria_mesh_count.argtypes = [vp, i32]
     L.ria_mesh_copy.restype = i32

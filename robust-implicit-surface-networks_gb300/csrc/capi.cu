@@ -672,6 +672,19 @@ ria_status ria_compute_material_interface_batch(const double* values, const uint
     return batch_run(true, values, value_offsets, n_tets, records, capacity, record_offsets);
 }
 
+ria_status ria_compute_arrangement_batch_noalloc(const double* d_values, const uint32_t* d_value_offsets,
+                                                 uint64_t n_tets, uint8_t* d_records, uint64_t capacity,
+                                                 uint64_t* d_record_offsets, void* stream) {
+    int dev = 0;
+    ria_status st = current_device(&dev);
+    if (st != RIA_OK) return st;
+    const char* msg = "";
+    int r = run_batch_noalloc(d_values, d_value_offsets, n_tets, d_records, capacity, d_record_offsets,
+                              (cudaStream_t)stream, &msg);
+    if (r != RIA_OK) return fail((ria_status)r, msg);
+    return RIA_OK;
+}
+
 static ria_status ensure_gathered(ria_mesh* m, ria_mesh_field f) {
     if ((f == RIA_MESH_REC_OFFSETS || f == RIA_MESH_REC_BYTES) && !m->have_rec) {
         cudaError_t err = cudaSuccess;

@@ -126,6 +126,11 @@ struct ExtractOut {
 // Runs the whole extraction; allocates the outputs with cudaMallocAsync on `s`.
 cudaError_t run_extract(const ExtractArgs& a, const IASum4* act_sum, ExtractOut& out, cudaStream_t s);
 
+// ria_compute_arrangement_batch_noalloc (k_noalloc.cu): returns a ria_status value and a static
+// message on failure; allocates nothing
+int run_batch_noalloc(const double* d_values, const uint32_t* d_value_offsets, uint64_t n_tets, uint8_t* d_records,
+                      uint64_t capacity, uint64_t* d_record_offsets, cudaStream_t s, const char** msg);
+
 // records in tet order (for RIA_MESH_REC_*)
 cudaError_t gather_records(bool mi, int64_t A, int64_t T, const uint32_t* act_tet, const uint64_t* act_desc,
                            const uint8_t* heap, const uint8_t* heap_big, const uint8_t* table, const uint32_t* table_off,
