@@ -579,39 +579,54 @@ bool mi_cut(int k, const double* materials, MIRecord& out, CutStats* st) {
     out.k = k;
     out.rep = rep;
     for (auto& kv : vid) out.verts.push_back({(uint8_t)kv.first[0], (uint8_t)kv.first[1], (uint8_t)kv.first[2], (uint8_t)kv.first[3]});
-    std::map<std::pair<int, int>, std::vector<int>> faces;  // (pos, neg) -> loop
+    // Interface faces are identified by their vertex sets: the face of cell m against the material
+    // j it was clipped by may border another cell when tie planes coincide (m - j parallel to
+    // m - k), so the neighbouring cell is the one holding the same polygon.  Each interface is
+    // emitted once, from the smaller material's cell (outward there, so toward the larger one).
+    struct CF {
+        int m, other;
+        std::vector<int> loop, sorted;
+    };
+    std::vector<CF> all;
     for (auto& [m, poly] : cells) {
         const auto& labs = clab[m];
         for (auto& f : poly.F) {
-            std::vector<int> loop;
-            for (int v : f.loop) loop.push_back(vid[labs[v]]);
-            if (f.other < 4) {
-                rotate_min(loop);
-                faces[{f.other, m}] = loop;
-            } else if (m < f.other) {
-                rotate_min(loop);
-                faces[{f.other, m}] = loop;
-            } else if (g_selfcheck) {
-                // the same polygon seen from the larger material, reversed
-                std::reverse(loop.begin(), loop.end());
-                rotate_min(loop);
-                auto& other = cells.at(f.other);
-                (void)other;
-                faces.emplace(std::make_pair(-1 - m, -1 - f.other), loop);  // checked below
-            }
+            CF c{m, f.other, {}, {}};
+            for (int v : f.loop) c.loop.push_back(vid[labs[v]]);
+            c.sorted = c.loop;
+            std::sort(c.sorted.begin(), c.sorted.end());
+            all.push_back(c);
         }
     }
-    if (g_selfcheck) {
-        for (auto it = faces.begin(); it != faces.end();) {
-            if (it->first.first < 0) {
-                int m = -1 - it->first.first, o = -1 - it->first.second;
-                auto f = faces.find({m, o});
-                if (f == faces.end() || f->second != it->second)
-                    throw std::runtime_error("MI interface seen differently from its two cells");
-                it = faces.erase(it);
-            } else {
-                ++it;
+    std::map<std::pair<int, int>, std::vector<int>> faces;  // (pos, neg) -> loop
+    for (size_t i = 0; i < all.size(); ++i) {
+        CF& f = all[i];
+        std::vector<int> loop = f.loop;
+        if (f.other < 4) {
+            rotate_min(loop);
+            faces[{f.other, f.m}] = loop;
+            continue;
+        }
+        int partner = -1;
+        for (size_t j = 0; j < all.size() && partner < 0; ++j)
+            if (j != i && all[j].other >= 4 && all[j].m != f.m && all[j].sorted == f.sorted) partner = (int)j;
+        if (partner >= 0) {
+            const int mo = all[partner].m;
+            if (f.m > mo) continue;
+            rotate_min(loop);
+            if (g_selfcheck) {
+                std::vector<int> rev = all[partner].loop;
+                std::reverse(rev.begin(), rev.end());
+                rotate_min(rev);
+                if (rev != loop) throw std::runtime_error("MI interface seen differently from its two cells");
             }
+            faces[{mo, f.m}] = loop;
+        } else {
+            // no cell holds the same polygon (coincident tie planes splitting the neighbour):
+            // keep the clipping label, oriented toward the larger material
+            if (f.m > f.other) std::reverse(loop.begin(), loop.end());
+            rotate_min(loop);
+            faces[{std::max(f.m, f.other), std::min(f.m, f.other)}] = loop;
         }
     }
     for (auto& kv : faces) {

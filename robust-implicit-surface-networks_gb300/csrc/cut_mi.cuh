@@ -329,7 +329,6 @@ struct MICut {
             }
             for (int f = 0; f < nf; ++f) {
                 int o = fother[f];
-                if (o >= 4 && m > o) continue;  // the interface is taken from the smaller material
                 if (onf >= OF || oloop + flen[f] > OL) return kBad;
                 opos[onf] = (uint8_t)o;
                 oneg[onf] = (uint8_t)m;
@@ -342,10 +341,65 @@ struct MICut {
         return CUT_OK;
     }
 
+    // Interface faces are identified by their vertex sets: when tie planes coincide the face of cell m
+    // against the material it was clipped by can border another cell, which holds the same polygon.
+    // Each interface is kept once, from the smaller material's cell (its loop is outward there, so
+    // it turns toward the larger material), and labelled (larger, smaller).
+    RIA_HD bool same_polygon(int a, int b) const {
+        if (olen[a] != olen[b]) return false;
+        for (int t = 0; t < olen[a]; ++t) {
+            bool in = false;
+            for (int u = 0; u < olen[b] && !in; ++u) in = oloops[ooff[a] + t] == oloops[ooff[b] + u];
+            if (!in) return false;
+        }
+        return true;
+    }
+
+    RIA_HDI void pair_faces() {
+        uint8_t keep[OF];
+        for (int i = 0; i < onf; ++i) {
+            keep[i] = 1;
+            if (opos[i] < 4) continue;
+            int partner = -1;
+            for (int j = 0; j < onf && partner < 0; ++j)
+                if (j != i && opos[j] >= 4 && oneg[j] != oneg[i] && same_polygon(i, j)) partner = j;
+            if (partner >= 0) {
+                if (oneg[i] > oneg[partner]) {
+                    keep[i] = 0;
+                } else {
+                    opos[i] = oneg[partner];
+                }
+            } else if (oneg[i] > opos[i]) {
+                // no cell holds the same polygon: keep the clipping label, toward the larger material
+                uint8_t t = opos[i];
+                opos[i] = oneg[i];
+                oneg[i] = t;
+                for (int x = 0, y = olen[i] - 1; x < y; ++x, --y) {
+                    uint8_t s = oloops[ooff[i] + x];
+                    oloops[ooff[i] + x] = oloops[ooff[i] + y];
+                    oloops[ooff[i] + y] = s;
+                }
+            }
+        }
+        int n = 0, total = 0;
+        for (int i = 0; i < onf; ++i) {
+            if (!keep[i]) continue;
+            opos[n] = opos[i];
+            oneg[n] = oneg[i];
+            ooff[n] = ooff[i];
+            olen[n] = olen[i];
+            total += olen[i];
+            ++n;
+        }
+        onf = n;
+        oloop = total;  // the record writes only the kept loops
+    }
+
     // ---- canonical form
     uint8_t vorder[OV], vnew[OV], forder[OF];
 
     RIA_HDI void canonicalize() {
+        pair_faces();
         for (int i = 0; i < onv; ++i) vorder[i] = (uint8_t)i;
         for (int x = 1; x < onv; ++x)
             for (int y = x; y > 0 && okey[vorder[y - 1]] > okey[vorder[y]]; --y) {

@@ -10,27 +10,14 @@
 // (a direct-mapped array for tet vertices, a 128-bit open-addressing hash otherwise); an occurrence
 // is new iff it owns its key, and the new occurrences are numbered by one more scan.  The result is
 // the reference's numbering exactly.
-#include <cub/cub.cuh>
-
-#include <vector>
-
-#include "device_common.cuh"
+#include "extract_common.cuh"
 #include "launch.hpp"
 
 namespace ria {
 
+using namespace xc;
+
 namespace {
-
-constexpr int kBs = 256;
-
-enum : uint64_t { OCC_SELF = 0, OCC_CORNER = 1, OCC_EDGE = 2, OCC_FACE = 3 };
-
-struct U4 {
-    uint32_t a, b, c, d;
-};
-struct U4Sum {
-    __host__ __device__ U4 operator()(const U4& x, const U4& y) const { return U4{x.a + y.a, x.b + y.b, x.c + y.c, x.d + y.d}; }
-};
 
 struct ExtractCtx {
     ExtractArgs a;
@@ -55,11 +42,6 @@ struct ExtractCtx {
     uint32_t* foff;
     uint32_t* ftoff;
 };
-
-__device__ __forceinline__ int local_func(uint64_t mask, int j) {  // j-th set bit of mask
-    for (int i = 0; i < j; ++i) mask &= mask - 1;
-    return __ffsll((long long)mask) - 1;
-}
 
 // iso flags of the local vertices of an IA record (up to 128 vertices)
 __device__ __forceinline__ void iso_vertex_flags(const IAView& r, uint64_t iso[2]) {
@@ -139,13 +121,6 @@ __device__ __forceinline__ VertKey ia_vertex_key(const IAView& r, int j, const i
             k.type = 4;
     }
     return k;
-}
-
-__global__ void k_base_in(int64_t A, const IASum4* __restrict__ sum, U4* __restrict__ out) {
-    int64_t a = (int64_t)blockIdx.x * kBs + threadIdx.x;
-    if (a >= A) return;
-    IASum4 s = sum[a];
-    out[a] = U4{s.a, s.b, s.c, s.d};
 }
 
 // D2: keys of the iso vertices
@@ -393,69 +368,12 @@ __global__ void __launch_bounds__(kBs) k_ia_face_emit(ExtractCtx C, int64_t* __r
     }
 }
 
-__global__ void k_set_last(int64_t* p, int64_t idx, const uint32_t* a, const uint32_t* b, int64_t n) {
-    // p[idx] = a[n-1] + b[n-1] (exclusive-scan total), or 0 when n == 0
-    p[idx] = n ? (int64_t)a[n - 1] + (int64_t)b[n - 1] : 0;
-}
-
-inline unsigned nblk(int64_t n) { return (unsigned)((n + kBs - 1) / kBs); }
-
-uint64_t pow2_at_least(uint64_t x) {
-    uint64_t p = 1024;
-    while (p < x) p <<= 1;
-    return p;
-}
-
-struct Pool {
-    cudaStream_t s;
-    std::vector<void*> ptrs;
-    cudaError_t err = cudaSuccess;
-    template <class T>
-    T* get(int64_t n) {
-        void* p = nullptr;
-        if (n <= 0) n = 1;
-        cudaError_t e = cudaMallocAsync(&p, sizeof(T) * (size_t)n, s);
-        if (e != cudaSuccess) {
-            err = e;
-            return nullptr;
-        }
-        ptrs.push_back(p);
-        return (T*)p;
-    }
-    ~Pool() {
-        for (void* p : ptrs) cudaFreeAsync(p, s);
-    }
-};
-
-cudaError_t exscan_u32(const uint32_t* in, uint32_t* out, int64_t n, cudaStream_t s) {
-    if (n == 0) return cudaSuccess;
-    size_t bytes = 0;
-    cub::DeviceScan::ExclusiveSum(nullptr, bytes, in, out, n, s);
-    void* tmp = nullptr;
-    cudaError_t e = cudaMallocAsync(&tmp, bytes, s);
-    if (e != cudaSuccess) return e;
-    cub::DeviceScan::ExclusiveSum(tmp, bytes, in, out, n, s);
-    return cudaFreeAsync(tmp, s);
-}
-
-// total of an exclusive scan: out[n-1] + in[n-1]
-cudaError_t scan_total(const uint32_t* in, const uint32_t* out, int64_t n, int64_t* total, cudaStream_t s) {
-    if (n == 0) {
-        *total = 0;
-        return cudaSuccess;
-    }
-    uint32_t h[2];
-    cudaError_t e = cudaMemcpyAsync(&h[0], in + n - 1, 4, cudaMemcpyDeviceToHost, s);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(&h[1], out + n - 1, 4, cudaMemcpyDeviceToHost, s);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-    *total = (int64_t)h[0] + (int64_t)h[1];
-    return e;
-}
-
 }  // namespace
 
+cudaError_t run_extract_mi(const ExtractArgs& a, const IASum4* act_sum, ExtractOut& out, cudaStream_t s);
+
 cudaError_t run_extract(const ExtractArgs& a, const IASum4* act_sum, ExtractOut& out, cudaStream_t s) {
-    if (a.mi) return cudaErrorNotSupported;
+    if (a.mi) return run_extract_mi(a, act_sum, out, s);
     Pool pool{s};
     ExtractCtx C;
     C.a = a;

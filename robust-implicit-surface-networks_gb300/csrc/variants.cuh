@@ -8,6 +8,6 @@
 namespace ria {
 using IACutFast = IACut<32, 48, 16, 192, false>;
 using IACutBig = IACut<128, 256, 64, 1024, true>;
-using MICutFast = MICut<32, 24, 160, 48, 32, 192, false>;
+using MICutFast = MICut<32, 24, 160, 48, 48, 256, false>;
 using MICutBig = MICut<96, 96, 640, 128, 128, 1024, true>;
 }  // namespace ria

@@ -168,7 +168,10 @@ def check_ia_record(planes, rec):
     return True
 
 
-def mi_vertex_labels(mats):
+def mi_vertex_labels(mats, owners=None):
+    """Vertices of the material-interface complex.  `owners` (labels of the materials that own a
+    cell) restricts the vertices to points fixed by the constraints of those materials; a material
+    that only touches the maximum adds no geometry, but it still counts among the tied labels."""
     def row(l):
         if l < 4:
             return [Fr(int(l == c)) for c in range(4)] + [Fr(0)]
@@ -197,12 +200,16 @@ def mi_vertex_labels(mats):
     for P, t in pts.items():
         tight = [b for b in range(4) if P[b] == 0]
         tight += [4 + i for i, m in enumerate(mats) if _dot([Fr(x) for x in m], P) == t]
+        if owners is not None:
+            own = [l for l in tight if l < 4 or l in owners]
+            if not any(l >= 4 for l in own) or _rank([row(l) for l in own]) < 4:
+                continue
         out[_greedy(tight, row, 4)] = P
     return out
 
 
 def check_mi_record(mats, rec):
-    expected = mi_vertex_labels(mats)
+    expected = mi_vertex_labels(mats, owners=set(rec["cells"]))
     got = [tuple(v) for v in rec["verts"]]
     assert got == sorted(got)
     assert set(got) == set(expected), (sorted(set(expected) - set(got)), sorted(set(got) - set(expected)))
