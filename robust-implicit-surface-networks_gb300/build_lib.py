@@ -1,4 +1,6 @@
-"""Build the CUDA library in-tree: robust-implicit-surface-networks_gb300/_build/libria.so.
+"""Build the CUDA library in-tree: robust-implicit-surface-networks_gb300/_build/libria.so, plus the
+C++ host layer over its C ABI (_build/libria_host.so) and the two command-line programs
+(_build/impl_arrangement, _build/material_interface).
 
 sm_103a only (GB300).  The translation units compile in parallel; every kernel is built with
 -fmad=false so that each FP64 operation is rounded on its own (the sampled values and vertex
@@ -20,6 +22,14 @@ LIB = os.path.join(OUT_DIR, "libria.so")
 SOURCES = ["k_ab.cu", "k_cut.cu", "k_extract.cu", "k_extract_mi.cu", "k_noalloc.cu", "capi.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-fmad=false", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden"]
+HOST = os.path.join(HERE, "host")
+HOST_LIB = os.path.join(OUT_DIR, "libria_host.so")
+HOST_SOURCES = ["ria_host.cpp", "mesh_io.cpp"]
+APPS = ["impl_arrangement", "material_interface"]
+CXX = os.environ.get("CXX", "g++")
+# -ffp-contract=off: the grid coordinates and unit axis vectors round as written (aarch64 g++
+# contracts a*b+c into fma by default)
+HOST_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off"]
 
 
 def nvcc() -> str:
@@ -38,6 +48,26 @@ def _stale(obj: str, src: str) -> bool:
     return any(os.path.getmtime(d) > t for d in deps)
 
 
+def _host_stale(out: str, srcs: list[str]) -> bool:
+    if not os.path.exists(out):
+        return True
+    deps = srcs + [os.path.join(HOST, f) for f in os.listdir(HOST) if f.endswith(".hpp")]
+    deps.append(os.path.join(os.path.dirname(HERE), "include", "ria.h"))
+    t = os.path.getmtime(out)
+    return any(os.path.getmtime(d) > t for d in deps)
+
+
+def _run(jobs, what, verbose):
+    if not jobs:
+        return
+    with cf.ThreadPoolExecutor(max_workers=len(jobs)) as ex:
+        for cmd, r in zip(jobs, ex.map(lambda c: subprocess.run(c, capture_output=True, text=True), jobs)):
+            if r.returncode != 0:
+                raise RuntimeError("%s failed: %s\n%s%s" % (what, " ".join(cmd), r.stdout, r.stderr))
+            if verbose and (r.stdout or r.stderr):
+                print(r.stdout + r.stderr)
+
+
 def build(verbose: bool = False) -> str:
     os.makedirs(OUT_DIR, exist_ok=True)
     cc = nvcc()
@@ -47,18 +77,30 @@ def build(verbose: bool = False) -> str:
         obj = os.path.join(OUT_DIR, s.replace(".cu", ".o"))
         if _stale(obj, src):
             jobs.append([cc, *ARCH, *FLAGS, "-c", src, "-o", obj])
-    with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
-        for cmd, r in zip(jobs, ex.map(lambda c: subprocess.run(c, capture_output=True, text=True), jobs)):
-            if r.returncode != 0:
-                raise RuntimeError("nvcc failed: %s\n%s%s" % (" ".join(cmd), r.stdout, r.stderr))
-            if verbose and (r.stdout or r.stderr):
-                print(r.stdout + r.stderr)
+    host_objs = []
+    for s in HOST_SOURCES:
+        src = os.path.join(HOST, s)
+        obj = os.path.join(OUT_DIR, s.replace(".cpp", ".o"))
+        host_objs.append(obj)
+        if _host_stale(obj, [src]):
+            jobs.append([CXX, *HOST_FLAGS, "-c", src, "-o", obj])
+    _run(jobs, "compile", verbose)
     objs = [os.path.join(OUT_DIR, s.replace(".cu", ".o")) for s in SOURCES]
-    if jobs or not os.path.exists(LIB):
-        cmd = [cc, *ARCH, "-shared", *objs, "-o", LIB]
-        r = subprocess.run(cmd, capture_output=True, text=True)
-        if r.returncode != 0:
-            raise RuntimeError("link failed: %s\n%s%s" % (" ".join(cmd), r.stdout, r.stderr))
+    relinked = False
+    if any(j[0] == cc for j in jobs) or not os.path.exists(LIB):
+        _run([[cc, *ARCH, "-shared", *objs, "-o", LIB]], "link", verbose)
+        relinked = True
+    if relinked or _host_stale(HOST_LIB, host_objs):
+        _run([[CXX, "-shared", *host_objs, "-L" + OUT_DIR, "-lria", "-Wl,-rpath,$ORIGIN", "-o", HOST_LIB]],
+             "link", verbose)
+        relinked = True
+    apps = []
+    for app in APPS:
+        src = os.path.join(HOST, "apps", app + ".cpp")
+        exe = os.path.join(OUT_DIR, app)
+        if relinked or _host_stale(exe, [src]):
+            apps.append([CXX, *HOST_FLAGS, src, "-L" + OUT_DIR, "-lria_host", "-lria", "-Wl,-rpath,$ORIGIN", "-o", exe])
+    _run(apps, "build", verbose)
     return LIB
 
 

@@ -33,8 +33,9 @@ FUNC_DTYPE = np.dtype([("type", "<i4"), ("flipped", "<i4"), ("p", "<f8", (12,))]
 
 
 def _unit(v):
+    # fixed evaluation order (x*x + y*y) + z*z, rounded after each operation, as the C++ loader
     v = np.asarray(v, dtype=np.float64)
-    n = float(np.sqrt(np.dot(v, v)))
+    n = float(np.sqrt((v[0] * v[0] + v[1] * v[1]) + v[2] * v[2]))
     if n == 0.0:
         raise ValueError("zero axis vector")
     return v / n

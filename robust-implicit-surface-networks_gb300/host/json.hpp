@@ -1,0 +1,216 @@
+// Minimal JSON reader and number formatting for the host layer (configs, function files, tet-mesh
+// files, mesh.json).  The reference uses nlohmann-json (absent here); this reader covers the
+// documents the reference reads: objects, arrays, strings, numbers, booleans and null.
+#pragma once
+#include <cctype>
+#include <charconv>
+#include <cstdint>
+#include <map>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+namespace ria_host {
+
+struct Json {
+    enum Type { Null, Bool, Number, String, Array, Object } type = Null;
+    bool b = false;
+    double num = 0.0;
+    std::string str;
+    std::vector<Json> arr;
+    std::map<std::string, Json> obj;
+
+    bool contains(const std::string& k) const { return type == Object && obj.count(k) > 0; }
+    const Json& operator[](const std::string& k) const {
+        auto it = obj.find(k);
+        if (type != Object || it == obj.end()) throw std::runtime_error("missing JSON key: " + k);
+        return it->second;
+    }
+    const Json& operator[](size_t i) const {
+        if (type != Array || i >= arr.size()) throw std::runtime_error("JSON index out of range");
+        return arr[i];
+    }
+    size_t size() const { return type == Array ? arr.size() : (type == Object ? obj.size() : 0); }
+    double as_double() const {
+        if (type != Number) throw std::runtime_error("JSON value is not a number");
+        return num;
+    }
+    bool as_bool() const {
+        if (type == Bool) return b;
+        if (type == Number) return num != 0.0;
+        throw std::runtime_error("JSON value is not a boolean");
+    }
+    const std::string& as_string() const {
+        if (type != String) throw std::runtime_error("JSON value is not a string");
+        return str;
+    }
+};
+
+class JsonParser {
+   public:
+    explicit JsonParser(const std::string& s) : s_(s) {}
+    Json parse() {
+        Json v = value();
+        ws();
+        if (p_ != s_.size()) fail("trailing characters");
+        return v;
+    }
+
+   private:
+    const std::string& s_;
+    size_t p_ = 0;
+
+    [[noreturn]] void fail(const char* what) {
+        throw std::runtime_error(std::string("JSON parse error (") + what + ") at offset " + std::to_string(p_));
+    }
+    void ws() {
+        while (p_ < s_.size() && (s_[p_] == ' ' || s_[p_] == '\n' || s_[p_] == '\r' || s_[p_] == '\t')) ++p_;
+    }
+    bool lit(const char* w) {
+        size_t n = std::char_traits<char>::length(w);
+        if (s_.compare(p_, n, w) == 0) {
+            p_ += n;
+            return true;
+        }
+        return false;
+    }
+    Json value() {
+        ws();
+        if (p_ >= s_.size()) fail("unexpected end");
+        Json v;
+        char c = s_[p_];
+        if (c == '{') {
+            v.type = Json::Object;
+            ++p_;
+            ws();
+            if (p_ < s_.size() && s_[p_] == '}') {
+                ++p_;
+                return v;
+            }
+            for (;;) {
+                ws();
+                Json k = value();
+                if (k.type != Json::String) fail("object key");
+                ws();
+                if (p_ >= s_.size() || s_[p_] != ':') fail("expected ':'");
+                ++p_;
+                v.obj[k.str] = value();
+                ws();
+                if (p_ < s_.size() && s_[p_] == ',') {
+                    ++p_;
+                    continue;
+                }
+                if (p_ < s_.size() && s_[p_] == '}') {
+                    ++p_;
+                    return v;
+                }
+                fail("expected ',' or '}'");
+            }
+        }
+        if (c == '[') {
+            v.type = Json::Array;
+            ++p_;
+            ws();
+            if (p_ < s_.size() && s_[p_] == ']') {
+                ++p_;
+                return v;
+            }
+            for (;;) {
+                v.arr.push_back(value());
+                ws();
+                if (p_ < s_.size() && s_[p_] == ',') {
+                    ++p_;
+                    continue;
+                }
+                if (p_ < s_.size() && s_[p_] == ']') {
+                    ++p_;
+                    return v;
+                }
+                fail("expected ',' or ']'");
+            }
+        }
+        if (c == '"') {
+            v.type = Json::String;
+            ++p_;
+            while (p_ < s_.size() && s_[p_] != '"') {
+                if (s_[p_] == '\\') {
+                    ++p_;
+                    if (p_ >= s_.size()) fail("escape");
+                    char e = s_[p_];
+                    v.str.push_back(e == 'n' ? '\n' : e == 't' ? '\t' : e == 'r' ? '\r' : e);
+                } else {
+                    v.str.push_back(s_[p_]);
+                }
+                ++p_;
+            }
+            if (p_ >= s_.size()) fail("unterminated string");
+            ++p_;
+            return v;
+        }
+        if (lit("true")) {
+            v.type = Json::Bool;
+            v.b = true;
+            return v;
+        }
+        if (lit("false")) {
+            v.type = Json::Bool;
+            return v;
+        }
+        if (lit("null")) return v;
+        size_t q = p_;
+        while (q < s_.size() && (std::isdigit((unsigned char)s_[q]) || s_[q] == '-' || s_[q] == '+' || s_[q] == '.' ||
+                                 s_[q] == 'e' || s_[q] == 'E'))
+            ++q;
+        if (q == p_) fail("unexpected character");
+        v.type = Json::Number;
+        auto r = std::from_chars(s_.data() + p_, s_.data() + q, v.num);
+        if (r.ec != std::errc()) fail("number");
+        p_ = q;
+        return v;
+    }
+};
+
+// A double as the reference's JSON library prints it: the shortest round-trip digits d1..dk with
+// decimal exponent n (value = 0.d1..dk x 10^n), written
+//   d1..dk 0..0 ".0"      if k <= n <= 15
+//   d1..dn "." dn+1..dk   if 0 < n <= 15
+//   "0." 0..0 d1..dk      if -4 < n <= 0
+//   d1 "." d2..dk "e" +-XX   otherwise (exponent n-1, at least two digits; no "." when k = 1)
+// and "null" for a NaN or an infinity.
+inline std::string json_double(double x) {
+    if (x != x || x - x != 0.0) return "null";
+    char buf[64];
+    auto r = std::to_chars(buf, buf + sizeof(buf), x, std::chars_format::scientific);
+    std::string s(buf, r.ptr), out;
+    size_t i = 0;
+    if (s[0] == '-') {
+        out.push_back('-');
+        i = 1;
+    }
+    size_t e = s.find('e');
+    std::string digits;
+    for (size_t j = i; j < e; ++j)
+        if (s[j] != '.') digits.push_back(s[j]);
+    const int n = std::stoi(s.substr(e + 1)) + 1;
+    const int k = (int)digits.size();
+    if (digits == "0") return out + "0.0";
+    if (k <= n && n <= 15) {
+        out += digits + std::string((size_t)(n - k), '0') + ".0";
+    } else if (0 < n && n <= 15) {
+        out += digits.substr(0, (size_t)n) + "." + digits.substr((size_t)n);
+    } else if (-4 < n && n <= 0) {
+        out += "0." + std::string((size_t)(-n), '0') + digits;
+    } else {
+        out += digits.substr(0, 1);
+        if (k > 1) out += "." + digits.substr(1);
+        const int ex = n - 1;
+        out += ex < 0 ? "e-" : "e+";
+        const int a = ex < 0 ? -ex : ex;
+        if (a < 10) out.push_back('0');
+        out += std::to_string(a);
+    }
+    return out;
+}
+
+}  // namespace ria_host

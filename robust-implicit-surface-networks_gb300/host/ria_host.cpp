@@ -1,0 +1,198 @@
+// GPU half of the host layer: stages a-d through the C ABI, then the CPU connectivity stages.
+#include <chrono>
+#include <iostream>
+
+#include "ria_host.hpp"
+
+namespace ria_host {
+
+namespace {
+
+double now() {
+    return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+size_t none_or(int64_t x) { return x < 0 ? Mesh_None : (size_t)x; }
+
+struct DeviceMesh {
+    ria_mesh* m = nullptr;
+    ~DeviceMesh() {
+        if (m) ria_mesh_free(m);
+    }
+    std::vector<int64_t> i64(ria_mesh_field f) const {
+        std::vector<int64_t> v(ria_mesh_count(m, f));
+        if (!v.empty()) ria_mesh_copy(m, f, v.data());
+        return v;
+    }
+};
+
+void fetch_faces(const DeviceMesh& dm, std::vector<PolygonFace>& faces) {
+    auto fo = dm.i64(RIA_MESH_FACE_OFFSETS), fv = dm.i64(RIA_MESH_FACE_VERTS);
+    auto to = dm.i64(RIA_MESH_FACE_TET_OFFSETS), tf = dm.i64(RIA_MESH_FACE_TETS), fn = dm.i64(RIA_MESH_FACE_FUNC);
+    faces.assign(fo.empty() ? 0 : fo.size() - 1, PolygonFace());
+    for (size_t f = 0; f < faces.size(); ++f) {
+        for (int64_t i = fo[f]; i < fo[f + 1]; ++i) faces[f].vert_indices.push_back((size_t)fv[i]);
+        for (int64_t t = to[f]; t < to[f + 1]; ++t) faces[f].tet_face_indices.emplace_back(tf[2 * t], tf[2 * t + 1]);
+        faces[f].func_index = {none_or(fn[2 * f]), none_or(fn[2 * f + 1])};
+    }
+}
+
+void fetch_points(const DeviceMesh& dm, std::vector<std::array<double, 3>>& pts) {
+    pts.resize(ria_mesh_count(dm.m, RIA_MESH_POINTS) / 3);
+    if (!pts.empty()) ria_mesh_copy(dm.m, RIA_MESH_POINTS, pts.data());
+}
+
+// shared part of the two pipelines: GPU stages a-d, then edges / patches / chains on the host
+template <class Label>
+bool run_pipeline(bool mi, bool robust_test, bool use_lookup, bool use_secondary_lookup,
+                  const std::vector<std::array<double, 3>>& pts, const std::vector<std::array<size_t, 4>>& tets,
+                  const double* funcVals, size_t n_func, std::vector<std::array<double, 3>>& out_pts,
+                  std::vector<PolygonFace>& faces, std::vector<std::vector<size_t>>& patches,
+                  std::vector<Label>& patch_function_label, std::vector<Edge>& edges,
+                  std::vector<std::vector<size_t>>& chains, std::vector<std::vector<size_t>>& nm_edges_of_vert,
+                  std::vector<std::string>& timing_labels, std::vector<double>& timings,
+                  std::vector<std::string>& stats_labels, std::vector<size_t>& stats) {
+    if (!use_lookup) use_secondary_lookup = false;
+    ria_config cfg{use_lookup ? 1 : 0, use_secondary_lookup ? 1 : 0, 1, robust_test ? 1 : 0, 0};
+    DeviceMesh dm;
+    static_assert(sizeof(size_t) == sizeof(int64_t), "tet vertex ids are passed as int64");
+    const double t0 = now();
+    ria_status st = mi ? ria_compute_material_interface(&cfg, pts.empty() ? nullptr : pts[0].data(), pts.size(),
+                                                         tets.empty() ? nullptr : (const int64_t*)tets[0].data(),
+                                                         tets.size(), funcVals, (uint32_t)n_func, &dm.m)
+                       : ria_compute_implicit_arrangement(&cfg, pts.empty() ? nullptr : pts[0].data(), pts.size(),
+                                                          tets.empty() ? nullptr : (const int64_t*)tets[0].data(),
+                                                          tets.size(), funcVals, (uint32_t)n_func, &dm.m);
+    if (robust_test) {
+        int64_t s[RIA_NUM_STATS] = {0};
+        if (dm.m) ria_mesh_copy(dm.m, RIA_MESH_STATS, s);
+        if (st != RIA_OK && !dm.m) {
+            std::cout << ria_last_error() << std::endl;
+            return false;
+        }
+        std::cout << (s[RIA_STAT_ROBUST_FAILURES] ? "type 1 failure (inconsistency)." : "success.") << std::endl;
+        return s[RIA_STAT_ROBUST_FAILURES] == 0 && st == RIA_OK;
+    }
+    if (st != RIA_OK) {
+        std::cout << ria_last_error() << std::endl;
+        return false;
+    }
+    int64_t s[RIA_NUM_STATS];
+    double tm[RIA_NUM_TIMINGS];
+    ria_mesh_copy(dm.m, RIA_MESH_STATS, s);
+    ria_mesh_copy(dm.m, RIA_MESH_TIMINGS, tm);
+    fetch_points(dm, out_pts);
+    fetch_faces(dm, faces);
+    const double t1 = now();
+    const char* ia_names[] = {"num_pts", "num_tets", "num_degenerate_vertex", "num_intersecting_tet",
+                              "num_1_func", "num_2_func", "num_more_func", "num_iso_verts", "num_iso_faces"};
+    const char* mi_names[] = {"num_pts", "num_tets", "num_degenerate_vertex", "num_intersecting_tet",
+                              "num_2_func", "num_3_func", "num_more_func", "num_MI_verts", "num_MI_faces"};
+    for (int i = 0; i < 9; ++i) {
+        stats_labels.emplace_back(mi ? mi_names[i] : ia_names[i]);
+        stats.push_back((size_t)s[i]);
+    }
+    const char* tnames[] = {"GPU sample/upload", "GPU signs+filter", "GPU per-tet cut", "GPU extract mesh+xyz"};
+    for (int i = 0; i < 4; ++i) {
+        timing_labels.emplace_back(tnames[i]);
+        timings.push_back(tm[i]);
+    }
+    timing_labels.emplace_back("device to host");
+    timings.push_back(t1 - t0 - tm[RIA_TIME_TOTAL]);
+    // host stages
+    double h0 = now();
+    std::vector<std::vector<size_t>> edges_of_face;
+    compute_mesh_edges(faces, edges_of_face, edges);
+    double h1 = now();
+    timing_labels.emplace_back(mi ? "MIEdge-face connectivity" : "isoEdge-face connectivity");
+    timings.push_back(h1 - h0);
+    stats_labels.emplace_back(mi ? "num_MI_edges" : "num_iso_edges");
+    stats.push_back(edges.size());
+    std::vector<std::pair<size_t, size_t>> labels;
+    compute_patches(edges_of_face, edges, faces, patches, labels);
+    patch_function_label.clear();
+    for (auto& l : labels) {
+        if constexpr (std::is_same<Label, size_t>::value)
+            patch_function_label.push_back(l.first);
+        else
+            patch_function_label.push_back(l);
+    }
+    double h2 = now();
+    timing_labels.emplace_back("patches");
+    timings.push_back(h2 - h1);
+    stats_labels.emplace_back("num_patches");
+    stats.push_back(patches.size());
+    nm_edges_of_vert.assign(out_pts.size(), {});
+    for (size_t i = 0; i < edges.size(); ++i)
+        if (edges[i].face_edge_indices.size() > 2) {
+            nm_edges_of_vert[edges[i].v1].push_back(i);
+            nm_edges_of_vert[edges[i].v2].push_back(i);
+        }
+    compute_chains(edges, nm_edges_of_vert, chains);
+    timing_labels.emplace_back("chains");
+    timings.push_back(now() - h2);
+    stats_labels.emplace_back("num_chains");
+    stats.push_back(chains.size());
+    return true;
+}
+
+}  // namespace
+
+bool sample_functions(const std::vector<ria_function>& funcs, const std::vector<std::array<double, 3>>& pts,
+                      FuncVals& fv) {
+    fv.n_rows = pts.size();
+    fv.n_cols = funcs.size();
+    fv.v.assign(fv.n_rows * fv.n_cols, 0.0);
+    ria_status st = ria_sample_functions(funcs.data(), (uint32_t)funcs.size(), pts.empty() ? nullptr : pts[0].data(),
+                                         pts.size(), fv.v.data());
+    if (st != RIA_OK) {
+        std::cout << ria_last_error() << std::endl;
+        return false;
+    }
+    return true;
+}
+
+bool load_functions(const std::string& filename, const std::vector<std::array<double, 3>>& pts, FuncVals& fv) {
+    std::vector<ria_function> funcs;
+    return load_functions(filename, funcs) && sample_functions(funcs, pts, fv);
+}
+
+bool implicit_arrangement(bool robust_test, bool use_lookup, bool use_secondary_lookup, bool,
+                          const std::vector<std::array<double, 3>>& pts, const std::vector<std::array<size_t, 4>>& tets,
+                          const double* funcVals, size_t n_func, std::vector<std::array<double, 3>>& iso_pts,
+                          std::vector<PolygonFace>& iso_faces, std::vector<std::vector<size_t>>& patches,
+                          std::vector<size_t>& patch_function_label, std::vector<Edge>& iso_edges,
+                          std::vector<std::vector<size_t>>& chains,
+                          std::vector<std::vector<size_t>>& non_manifold_edges_of_vert,
+                          std::vector<std::vector<size_t>>& shells, std::vector<std::vector<size_t>>& arrangement_cells,
+                          std::vector<std::vector<bool>>& cell_function_label, std::vector<std::string>& timing_labels,
+                          std::vector<double>& timings, std::vector<std::string>& stats_labels,
+                          std::vector<size_t>& stats) {
+    shells.clear();
+    arrangement_cells.clear();
+    cell_function_label.clear();
+    return run_pipeline<size_t>(false, robust_test, use_lookup, use_secondary_lookup, pts, tets, funcVals, n_func, iso_pts,
+                                iso_faces, patches, patch_function_label, iso_edges, chains, non_manifold_edges_of_vert,
+                                timing_labels, timings, stats_labels, stats);
+}
+
+bool material_interface(bool robust_test, bool use_lookup, bool use_secondary_lookup, bool,
+                        const std::vector<std::array<double, 3>>& pts, const std::vector<std::array<size_t, 4>>& tets,
+                        const double* funcVals, size_t n_func, std::vector<std::array<double, 3>>& MI_pts,
+                        std::vector<PolygonFace>& MI_faces, std::vector<std::vector<size_t>>& patches,
+                        std::vector<std::pair<size_t, size_t>>& patch_function_label, std::vector<Edge>& MI_edges,
+                        std::vector<std::vector<size_t>>& chains,
+                        std::vector<std::vector<size_t>>& non_manifold_edges_of_vert,
+                        std::vector<std::vector<size_t>>& shells, std::vector<std::vector<size_t>>& material_cells,
+                        std::vector<size_t>& cell_function_label, std::vector<std::string>& timing_labels,
+                        std::vector<double>& timings, std::vector<std::string>& stats_labels, std::vector<size_t>& stats) {
+    shells.clear();
+    material_cells.clear();
+    cell_function_label.clear();
+    return run_pipeline<std::pair<size_t, size_t>>(true, robust_test, use_lookup, use_secondary_lookup, pts, tets,
+                                                   funcVals, n_func, MI_pts, MI_faces, patches, patch_function_label,
+                                                   MI_edges, chains, non_manifold_edges_of_vert, timing_labels, timings,
+                                                   stats_labels, stats);
+}
+
+}  // namespace ria_host

@@ -1,0 +1,157 @@
+// Host C++ layer with the reference's names and signatures over the C ABI (include/ria.h).
+//
+//   implicit_arrangement(...)   src/implicit_arrangement.h:39-62
+//   material_interface(...)     src/material_interface.h:38-61
+//   parse_config_file / load_tet_mesh / generate_tet_mesh / save_result* / save_timings /
+//   save_statistics             src/io.h:30-92
+//   compute_mesh_edges / compute_patches / compute_chains
+//                               src/mesh_connectivity.h (restated host stages that consume the
+//                               extracted mesh; src/mesh_connectivity.cpp:10-242)
+// Stages a-d run on the GPU.  Face pairing, shells, topological ray shooting, cell grouping and
+// sign propagation are not part of this build: `shells`, `arrangement_cells` and
+// `cell_function_label` come back empty.
+#pragma once
+#include <array>
+#include <cstddef>
+#include <limits>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "../../include/ria.h"
+
+namespace ria_host {
+
+constexpr size_t Mesh_None = std::numeric_limits<size_t>::max();
+
+struct PolygonFace {  // src/mesh.h:15-25
+    std::vector<size_t> vert_indices;
+    std::vector<std::pair<size_t, size_t>> tet_face_indices;
+    std::pair<size_t, size_t> func_index{Mesh_None, Mesh_None};
+};
+
+struct IsoVert {  // src/mesh.h:28-41
+    size_t tet_index;
+    size_t tet_vert_index;
+    size_t simplex_size;
+    std::array<size_t, 4> simplex_vert_indices;
+    std::array<size_t, 3> func_indices = {Mesh_None, Mesh_None, Mesh_None};
+};
+
+struct MI_Vert {  // src/mesh.h:45-58
+    size_t tet_index;
+    size_t tet_vert_index;
+    size_t simplex_size;
+    std::array<size_t, 4> simplex_vert_indices;
+    std::array<size_t, 4> material_indices;
+};
+
+struct Edge {  // src/mesh.h:63-72
+    size_t v1, v2;
+    std::vector<std::pair<size_t, size_t>> face_edge_indices;
+};
+
+struct Config {  // src/io.h:12-28; missing lookup switches default to true (README)
+    std::string tet_mesh_file;
+    std::string func_file;
+    std::string output_dir;
+    bool use_lookup = true;
+    bool use_secondary_lookup = true;
+    bool use_topo_ray_shooting = true;
+    size_t tet_mesh_resolution = 0;
+    std::array<double, 3> tet_mesh_bbox_min{-1, -1, -1};
+    std::array<double, 3> tet_mesh_bbox_max{1, 1, 1};
+};
+
+// Row-major n_pts x n_func values (the reference's Eigen RowMajor funcVals)
+struct FuncVals {
+    size_t n_rows = 0, n_cols = 0;
+    std::vector<double> v;
+    size_t rows() const { return n_rows; }
+    size_t cols() const { return n_cols; }
+    const double* data() const { return v.data(); }
+};
+
+Config parse_config_file(const std::string& filename);
+bool load_tet_mesh(const std::string& filename, std::vector<std::array<double, 3>>& pts,
+                   std::vector<std::array<size_t, 4>>& tets);
+bool generate_tet_mesh(size_t resolution, const std::array<double, 3>& bbox_min, const std::array<double, 3>& bbox_max,
+                       std::vector<std::array<double, 3>>& pts, std::vector<std::array<size_t, 4>>& tets);
+// reference function files (plane, sphere, cylinder, torus, zero); false on an unsupported type
+bool load_functions(const std::string& filename, std::vector<ria_function>& funcs);
+// stage a on the GPU
+bool sample_functions(const std::vector<ria_function>& funcs, const std::vector<std::array<double, 3>>& pts,
+                      FuncVals& funcVals);
+// load + sample, the reference's load_functions(file, pts, funcVals) (src/implicit_functions.h)
+bool load_functions(const std::string& filename, const std::vector<std::array<double, 3>>& pts, FuncVals& funcVals);
+
+bool implicit_arrangement(bool robust_test, bool use_lookup, bool use_secondary_lookup, bool use_topo_ray_shooting,
+                          const std::vector<std::array<double, 3>>& pts, const std::vector<std::array<size_t, 4>>& tets,
+                          const double* funcVals, size_t n_func,
+                          std::vector<std::array<double, 3>>& iso_pts, std::vector<PolygonFace>& iso_faces,
+                          std::vector<std::vector<size_t>>& patches, std::vector<size_t>& patch_function_label,
+                          std::vector<Edge>& iso_edges, std::vector<std::vector<size_t>>& chains,
+                          std::vector<std::vector<size_t>>& non_manifold_edges_of_vert,
+                          std::vector<std::vector<size_t>>& shells, std::vector<std::vector<size_t>>& arrangement_cells,
+                          std::vector<std::vector<bool>>& cell_function_label, std::vector<std::string>& timing_labels,
+                          std::vector<double>& timings, std::vector<std::string>& stats_labels,
+                          std::vector<size_t>& stats);
+
+bool material_interface(bool robust_test, bool use_lookup, bool use_secondary_lookup, bool use_topo_ray_shooting,
+                        const std::vector<std::array<double, 3>>& pts, const std::vector<std::array<size_t, 4>>& tets,
+                        const double* funcVals, size_t n_func,
+                        std::vector<std::array<double, 3>>& MI_pts, std::vector<PolygonFace>& MI_faces,
+                        std::vector<std::vector<size_t>>& patches,
+                        std::vector<std::pair<size_t, size_t>>& patch_function_label, std::vector<Edge>& MI_edges,
+                        std::vector<std::vector<size_t>>& chains,
+                        std::vector<std::vector<size_t>>& non_manifold_edges_of_vert,
+                        std::vector<std::vector<size_t>>& shells, std::vector<std::vector<size_t>>& material_cells,
+                        std::vector<size_t>& cell_function_label, std::vector<std::string>& timing_labels,
+                        std::vector<double>& timings, std::vector<std::string>& stats_labels, std::vector<size_t>& stats);
+
+// Matrix types with data() / cols() and row-major storage (Eigen RowMajor, FuncVals)
+template <class M, class... Rest>
+bool implicit_arrangement(bool robust_test, bool use_lookup, bool use_secondary_lookup, bool use_topo_ray_shooting,
+                          const std::vector<std::array<double, 3>>& pts, const std::vector<std::array<size_t, 4>>& tets,
+                          const M& funcVals, Rest&... rest) {
+    return implicit_arrangement(robust_test, use_lookup, use_secondary_lookup, use_topo_ray_shooting, pts, tets,
+                                funcVals.data(), (size_t)funcVals.cols(), rest...);
+}
+template <class M, class... Rest>
+bool material_interface(bool robust_test, bool use_lookup, bool use_secondary_lookup, bool use_topo_ray_shooting,
+                        const std::vector<std::array<double, 3>>& pts, const std::vector<std::array<size_t, 4>>& tets,
+                        const M& funcVals, Rest&... rest) {
+    return material_interface(robust_test, use_lookup, use_secondary_lookup, use_topo_ray_shooting, pts, tets,
+                              funcVals.data(), (size_t)funcVals.cols(), rest...);
+}
+
+// host stages that consume the mesh (src/mesh_connectivity.cpp:10-242)
+void compute_mesh_edges(const std::vector<PolygonFace>& mesh_faces, std::vector<std::vector<size_t>>& edges_of_face,
+                        std::vector<Edge>& mesh_edges);
+void compute_patches(const std::vector<std::vector<size_t>>& edges_of_face, const std::vector<Edge>& mesh_edges,
+                     const std::vector<PolygonFace>& mesh_faces, std::vector<std::vector<size_t>>& patches,
+                     std::vector<std::pair<size_t, size_t>>& patch_label);
+void compute_chains(const std::vector<Edge>& mesh_edges, const std::vector<std::vector<size_t>>& non_manifold_edges_of_vert,
+                    std::vector<std::vector<size_t>>& chains);
+
+// writers (src/io.cpp:154-312, 554-588): same keys and value types as the reference's files
+bool save_result(const std::string& filename, const std::vector<std::array<double, 3>>& mesh_pts,
+                 const std::vector<PolygonFace>& mesh_faces, const std::vector<std::vector<size_t>>& patches,
+                 const std::vector<size_t>& patch_function_label, const std::vector<Edge>& edges,
+                 const std::vector<std::vector<size_t>>& chains,
+                 const std::vector<std::vector<size_t>>& non_manifold_edges_of_vert,
+                 const std::vector<std::vector<size_t>>& shells, const std::vector<std::vector<size_t>>& cells,
+                 const std::vector<std::vector<bool>>& cell_function_label);
+bool save_result_MI(const std::string& filename, const std::vector<std::array<double, 3>>& mesh_pts,
+                    const std::vector<PolygonFace>& mesh_faces, const std::vector<std::vector<size_t>>& patches,
+                    const std::vector<std::pair<size_t, size_t>>& patch_function_label, const std::vector<Edge>& edges,
+                    const std::vector<std::vector<size_t>>& chains,
+                    const std::vector<std::vector<size_t>>& non_manifold_edges_of_vert,
+                    const std::vector<std::vector<size_t>>& shells, const std::vector<std::vector<size_t>>& cells,
+                    const std::vector<size_t>& cell_function_label);
+bool save_timings(const std::string& filename, const std::vector<std::string>& timing_labels,
+                  const std::vector<double>& timings);
+bool save_statistics(const std::string& filename, const std::vector<std::string>& stats_labels,
+                     const std::vector<size_t>& stats);
+
+}  // namespace ria_host

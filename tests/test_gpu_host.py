@@ -1,0 +1,135 @@
+"""The C++ host layer and its command-line programs on the GPU (app/implicit_arrangement.cpp and
+app/material_interface.cpp of the reference): mesh.json, stats.json and timings.json against the
+oracle, and the reference's known answers (tests/test_implicit_networks.cpp) through the programs."""
+import json
+import os
+import shutil
+import subprocess
+from collections import Counter
+
+import numpy as np
+import pytest
+
+import meshjson
+from conftest import GOLDEN
+
+pytestmark = pytest.mark.gpu
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+BIN = os.path.join(REPO, "robust-implicit-surface-networks_gb300", "_build")
+APP = {"ia": "impl_arrangement", "mi": "material_interface"}
+
+with open(os.path.join(GOLDEN, "kat.json")) as _f:
+    KATS = json.load(_f)
+
+
+@pytest.fixture(scope="module")
+def built(pkg):
+    pkg.build()
+    return BIN
+
+
+def _config(tmp_path, name, res=None, mesh_file=None, **switches):
+    shutil.copy(os.path.join(GOLDEN, "functions", name + ".json"), tmp_path / "fn.json")
+    os.makedirs(tmp_path / "out", exist_ok=True)
+    body = {"funcFile": "fn.json", "outputDir": "out"}
+    if mesh_file:
+        body["tetMeshFile"] = mesh_file
+    else:
+        body.update({"gridResolution": res, "gridBbox": [[-1.0, -1.0, -1.0], [1.0, 1.0, 1.0]]})
+    body.update(switches)
+    (tmp_path / "config.json").write_text(json.dumps(body))
+    return tmp_path / "config.json"
+
+
+def _run(mode, cfg, *flags):
+    r = subprocess.run([os.path.join(BIN, APP[mode]), str(cfg), *flags], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    return r.stdout
+
+
+@pytest.mark.parametrize("mode,name,res,lookup", [("ia", "3-sphere-3", 24, True), ("ia", "2-planesphere", 20, False),
+                                                  ("mi", "3-sphere-1", 22, True), ("mi", "8-sphere", 18, False)])
+def test_cli_matches_oracle(built, fns, oracle, tmp_path, mode, name, res, lookup):
+    cfg = _config(tmp_path, name, res, useLookup=lookup)
+    _run(mode, cfg)
+    funcs = fns.load_functions(os.path.join(GOLDEN, "functions", name + ".json"))
+    pts, tets = fns.generate_tet_mesh(res)
+    ref = oracle.run(mode, pts, tets, oracle.sample(funcs, pts), connectivity=True)
+    got = meshjson.load_mesh_json(tmp_path / "out" / "mesh.json")
+    meshjson.compare(got, meshjson.expected_mesh_json(ref, mode), xyz_rtol=1e-12)
+    stats = json.load(open(tmp_path / "out" / "stats.json"))
+    rs = ref["stats_named"]
+    tag = "iso" if mode == "ia" else "MI"
+    assert stats["num_pts"] == rs["num_pts"] and stats["num_tets"] == rs["num_tets"]
+    assert stats["num_intersecting_tet"] == rs["num_intersecting_tet"]
+    assert stats[f"num_{tag}_verts"] == rs["num_verts"] and stats[f"num_{tag}_faces"] == rs["num_faces"]
+    assert stats[f"num_{tag}_edges"] == len(ref["edges"])
+    assert stats["num_patches"] == len(ref["patch_offsets"]) - 1
+    assert stats["num_chains"] == len(ref["chain_offsets"]) - 1
+    timings = json.load(open(tmp_path / "out" / "timings.json"))
+    assert "patches" in timings and "chains" in timings and all(v >= 0 for v in timings.values())
+
+
+def test_cli_tet_mesh_file(built, fns, oracle, tmp_path):
+    m = np.load(os.path.join(GOLDEN, "mesh_8sphere.npz"))
+    (tmp_path / "tets.json").write_text(json.dumps([m["pts"].tolist(), m["tets"].tolist()]))
+    cfg = _config(tmp_path, "8-sphere", mesh_file="tets.json")
+    _run("mi", cfg)
+    funcs = fns.load_functions(os.path.join(GOLDEN, "functions", "8-sphere.json"))
+    ref = oracle.run("mi", m["pts"], m["tets"], oracle.sample(funcs, m["pts"]), connectivity=True)
+    got = meshjson.load_mesh_json(tmp_path / "out" / "mesh.json")
+    meshjson.compare(got, meshjson.expected_mesh_json(ref, "mi"), xyz_rtol=1e-12)
+
+
+def test_cli_flags(built, tmp_path):
+    cfg = _config(tmp_path, "2-sphere", 16)
+    _run("ia", cfg, "-T")
+    assert not (tmp_path / "out" / "mesh.json").exists()
+    assert (tmp_path / "out" / "timings.json").exists() and (tmp_path / "out" / "stats.json").exists()
+    out = _run("ia", cfg, "--robust-test")
+    assert "success." in out
+    out = _run("mi", cfg, "-R")
+    assert "success." in out
+
+
+def test_cli_bad_function_file(built, tmp_path):
+    cfg = _config(tmp_path, "2-sphere", 8)
+    (tmp_path / "fn.json").write_text(json.dumps([{"type": "cone"}]))
+    r = subprocess.run([os.path.join(BIN, APP["ia"]), str(cfg)], capture_output=True, text=True, timeout=120)
+    assert r.returncode != 0 and "function loading failed." in r.stdout
+
+
+def _corners(mesh):
+    """Vertices with more than two incident non-manifold edges, from mesh.json alone."""
+    count = Counter()
+    for f in mesh["faces"] or []:
+        for i in range(len(f)):
+            a, b = f[i], f[(i + 1) % len(f)]
+            count[(min(a, b), max(a, b))] += 1
+    deg = Counter()
+    for (a, b), c in count.items():
+        if c > 2:
+            deg[a] += 1
+            deg[b] += 1
+    return sum(1 for d in deg.values() if d > 2)
+
+
+@pytest.mark.parametrize("kat", KATS, ids=[f"{k['mode']}-{k['functions']}" for k in KATS])
+def test_cli_known_answers(built, tmp_path, kat):
+    if kat["mesh"] == "mesh":
+        m = np.load(os.path.join(GOLDEN, "mesh_8sphere.npz"))
+        (tmp_path / "tets.json").write_text(json.dumps([m["pts"].tolist(), m["tets"].tolist()]))
+        cfg = _config(tmp_path, kat["functions"], mesh_file="tets.json")
+    else:
+        cfg = _config(tmp_path, kat["functions"], 101)
+    _run(kat["mode"], cfg)
+    mesh = meshjson.load_mesh_json(tmp_path / "out" / "mesh.json")
+    stats = json.load(open(tmp_path / "out" / "stats.json"))
+    if "patches" in kat:
+        assert stats["num_patches"] == kat["patches"] == len(mesh["patches"] or [])
+    if "chains" in kat:
+        assert stats["num_chains"] == kat["chains"] == len(mesh["chains"] or [])
+    if "corners" in kat:
+        assert _corners(mesh) == kat["corners"]
+    assert mesh["patches_label"] == [kat["patch_label"]]
