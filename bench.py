@@ -14,6 +14,10 @@ entry points: ria_sample_functions (host points in, host values out, as the refe
 load_functions) and ria_compute_implicit_arrangement (host pts / tets / values in), then copies the
 mesh (points, vertex records, faces) back; host<->device copies are inside its timed region.
 
+--config batch runs the batched form: 4096 independent grids (vertices per axis uniform in 9..33,
+2..24 functions of mixed kinds; about 2.3x10^8 tets) through ria_grid_batch, one pass of every stage
+over all of them, and beside it the plain drop-in called once per grid (`per_problem_plain`).
+
 --impl reference times the CPU restatement of the reference path (oracle/) on this host's cores on a
 bounded slab of the same workload (the reference itself depends on absent third-party libraries and
 cannot be built).  Under torchrun only rank 0 runs it.
@@ -99,15 +103,92 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def workload(name):
+def workload(name, res=None):
+    """The named workload; `res` (cubes per axis) overrides its grid size for profiling captures."""
     fns = importlib.import_module(PKG + ".functions")
+    kw = {} if res is None else {"res": res}
     if name == "ia-degenerate":
-        return fns.workload_ia_degenerate()
+        return fns.workload_ia_degenerate(**kw)
     if name == "mi":
-        return fns.workload_mi()
+        return fns.workload_mi(**kw)
     if name == "ia-small":
-        return fns.workload_ia_small()
+        return fns.workload_ia_small(**kw)
     raise SystemExit(f"unknown config {name}")
+
+
+def run_batch(args, world, local):
+    """The batched form against the plain drop-in called per problem."""
+    import numpy as np
+    import torch
+
+    torch.cuda.set_device(local)
+    fns = importlib.import_module(PKG + ".functions")
+    pkg = importlib.import_module(PKG)
+    pkg.build()
+    L = pkg.load()
+    wl = fns.workload_batch(n=args.batch_n)
+    probs = wl.problems
+    for _ in range(args.warmup):
+        pkg.grid_batch(probs).close()
+    launches0 = int(L.ria_kernel_launches())
+    dev_ms, stage = [], {"sample": [], "filter": [], "cut": [], "extract": []}
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            m = pkg.grid_batch(probs)
+            tm = m.timings
+            dev_ms.append(tm["total"] * 1e3)
+            for k in stage:
+                stage[k].append(tm[k] * 1e3)
+            st = m.stats
+            m.close()
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+    launches = int(L.ria_kernel_launches()) - launches0
+    ms = statistics.mean(dev_ms)
+    value = wl.n_tets / (ms * 1e-3)
+    # end to end: descriptors in, the whole mesh of every problem back on the host
+    e2e_t = []
+    d2h = 0
+    for it in range(0 if args.no_e2e else 1 + args.steps):
+        t0 = time.perf_counter()
+        m = pkg.grid_batch(probs)
+        outs = [m["xyz"], m["verts"], m["face_offsets"], m["face_verts"], m["face_tets"], m["face_func"]]
+        m.close()
+        if it > 0:
+            e2e_t.append(time.perf_counter() - t0)
+        d2h = sum(o.nbytes for o in outs)
+    h2d = sum(f.nbytes for _, f in probs) + 56 * len(probs)
+    # the plain drop-in, one call per problem (same descriptors, same results)
+    t0 = time.perf_counter()
+    plain_dev = 0.0
+    for r, f in probs:
+        m = pkg.grid_implicit_arrangement(r, f)
+        plain_dev += m.timings["total"]
+        m.close()
+    plain_wall = time.perf_counter() - t0
+    peak, peak_kind = _peaks()
+    stage_ms = {k: statistics.mean(v) for k, v in stage.items()}
+    line = {
+        "metric": METRIC, "value": value, "unit": "tets/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+        "config": {"workload": wl.name, "tets": wl.n_tets, "verts": wl.n_verts, "problems": len(probs),
+                   "functions_per_problem": "2..24", "mode": "ia",
+                   "l2": "inputs larger than L2 (padded values %.1f GB)" %
+                   (8 * wl.n_verts * max(len(f) for _, f in probs) / 1e9), "parallelism": "single"},
+        "stage_ms": stage_ms, "stats": st, "wall_ms_per_step": wall / args.steps * 1e3,
+        "e2e": {"value": wl.n_tets / statistics.median(e2e_t) if e2e_t else None, "unit": "tets/s",
+                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+        "gpu_launches": launches,
+        "per_problem_plain": {"tets_per_s_wall": wl.n_tets / plain_wall, "wall_s": plain_wall,
+                              "device_s": plain_dev, "batch_speedup_wall": plain_wall / (wall / args.steps)},
+        "roofline": {"bound": "hbm", "kernel_stage": "total", "achieved": None, "peak": peak, "unit": "GB/s",
+                     "frac": None, "peak_kind": peak_kind, "traffic": None},
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line))
 
 
 def algorithmic_bytes(wl, st):
@@ -176,7 +257,9 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="ia-degenerate", choices=["ia-degenerate", "mi", "ia-small"])
+    ap.add_argument("--config", default="ia-degenerate", choices=["ia-degenerate", "mi", "ia-small", "batch"])
+    ap.add_argument("--batch-n", type=int, default=4096, help="problems of --config batch")
+    ap.add_argument("--res", type=int, default=None, help="grid resolution override (small profiling cases)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer end-to-end leg (profiling runs)")
     args = ap.parse_args()
@@ -186,7 +269,14 @@ def main():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
-    wl = workload(args.config)
+    if args.config == "batch":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "the batched form has no CPU reference arm; "
+                              "run --impl reference on the other configs"}))
+        elif rank == 0:
+            run_batch(args, world, local)
+        return
+    wl = workload(args.config, args.res)
 
     if args.impl == "reference":
         if rank == 0:

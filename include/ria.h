@@ -41,7 +41,8 @@ typedef enum ria_status {
     RIA_OK = 0,
     RIA_EINVAL = 1,       /* bad argument (null pointer, n_func > 64, index out of range, ...) */
     RIA_ENOMEM = 2,       /* device or host allocation failed */
-    RIA_ECAPACITY = 3,    /* a tet's arrangement exceeds the per-tet capacity (about 10 active functions in general position) */
+    RIA_ECAPACITY = 3,    /* a tet's arrangement exceeds the per-tet capacity (255 vertices or 254 cells: about
+                             13 planes in general position; 60 active functions) */
     RIA_EDEGENERATE = 4,  /* an exact predicate exceeded its expansion capacity (extreme dynamic range) */
     RIA_ETIMEOUT = 5,     /* reserved for bounded device waits */
     RIA_ECUDA = 6,        /* a CUDA runtime call failed */
@@ -129,7 +130,8 @@ typedef enum ria_mesh_field {
     RIA_MESH_REC_BYTES = 10,      /* uint8 [...] */
     RIA_MESH_STATS = 11,          /* int64 [RIA_NUM_STATS] */
     RIA_MESH_TIMINGS = 12,        /* double [RIA_NUM_TIMINGS]: seconds of each device stage */
-    RIA_MESH_FUNC_VALS = 13       /* double [n_pts][n_func]: the sampled values (grid entry points) */
+    RIA_MESH_FUNC_VALS = 13       /* double [n_pts][n_func]: the values the mesh was computed from (device
+                                     entry points: read from the caller's buffer, which must still exist) */
 } ria_mesh_field;
 
 /* RIA_MESH_STATS entries, named as in the reference's stats.json
@@ -187,6 +189,50 @@ RIA_API ria_status ria_grid_implicit_arrangement(const ria_config* cfg, uint32_t
 RIA_API ria_status ria_grid_material_interface(const ria_config* cfg, uint32_t resolution, const double* bbox_min,
                                        const double* bbox_max, const ria_function* funcs, uint32_t n_func,
                                        ria_mesh** out);
+
+/* ---- batched grids -------------------------------------------------------------------------------
+ * Many independent grid problems in one pass of every stage.  The problems' grids are concatenated
+ * (vertices and tets numbered problem after problem), the general-case tets of all problems are cut
+ * together in bins of equal active-function count, and the mesh numbering stays per problem: each
+ * problem's fields, read with ria_batch_copy, equal those of its own ria_grid_* call.  No counterpart
+ * in the reference, which solves one grid per call.  Limits: 2^31 points and tets in total. */
+typedef struct ria_grid_problem {
+    uint32_t resolution;        /* cubes per axis, 1..1200 */
+    uint32_t n_func;            /* 1..64 */
+    double bbox_min[3];
+    double bbox_max[3];
+    const ria_function* funcs;  /* host array of n_func */
+} ria_grid_problem;
+
+RIA_API ria_status ria_grid_batch(const ria_config* cfg, int32_t material_interface, const ria_grid_problem* problems,
+                                  uint32_t n_problems, ria_mesh** out);
+/* Number of problems of a batch mesh (0 for a mesh of any other entry point). */
+RIA_API uint32_t ria_batch_size(const ria_mesh* mesh);
+/* One problem's part of a field, with vertex, tet, mesh-vertex and offset values relative to the
+ * problem.  RIA_MESH_STATS are the problem's own counts (RIA_STAT_NUM_DEFERRED and
+ * RIA_STAT_ROBUST_FAILURES are 0); RIA_MESH_TIMINGS are the batch's. */
+RIA_API uint64_t ria_batch_count(const ria_mesh* mesh, uint32_t problem, ria_mesh_field field);
+RIA_API ria_status ria_batch_copy(const ria_mesh* mesh, uint32_t problem, ria_mesh_field field, void* host_dst);
+
+/* ---- CSG pruning (src/csg.cpp:55-116; replaces the lambda on cell labels) ----------------------------
+ * For each face of an implicit-arrangement mesh: 0 if the CSG shape is on both sides or on neither,
+ * 1 if its inside is on the positive side of the face's function (func_index.first), 2 if on the
+ * negative side.  tree: n_units units of three int32 {op, a, b} as the reference's CSG tree files
+ * (app/csg.cpp:15-52): op 0 Intersection, 1 Union, 2 Negation (b unused); an element e > 0 is unit e
+ * (1-based), e < 0 is function -e-1; unit 1 is the root.  n_units = 0: the union of all functions
+ * (the reference's default lambda).  Function j is inside where it is positive (positive_inside != 0)
+ * or negative.  The reference instead negates every function when positive_inside is false, which
+ * also reverses the faces' positive sides.  face_labels: host array of n_faces bytes (for a batch,
+ * of the problem's faces).  Meshes from the *_device entry points read the caller's tets and values,
+ * which must still exist. */
+RIA_API ria_status ria_mesh_csg(const ria_mesh* mesh, const int32_t* tree, uint32_t n_units, int32_t positive_inside,
+                                uint8_t* face_labels);
+RIA_API ria_status ria_batch_csg(const ria_mesh* mesh, uint32_t problem, const int32_t* tree, uint32_t n_units,
+                                 int32_t positive_inside, uint8_t* face_labels);
+/* For an arbitrary membership function (the reference's std::function lambda over cell labels): the
+ * sign vectors of the two sides of each face, sides[2f] on the positive and sides[2f+1] on the
+ * negative side of the face's function (bit j set where function j is positive; n_func <= 64). */
+RIA_API ria_status ria_mesh_face_sides(const ria_mesh* mesh, uint64_t* sides);
 
 /* Stage a alone: func_vals[n_pts][n_func] = funcs evaluated at pts (host buffers). */
 RIA_API ria_status ria_sample_functions(const ria_function* funcs, uint32_t n_func, const double* pts, uint64_t n_pts,

@@ -30,6 +30,12 @@ class RiaError(RuntimeError):
         self.status = status
 
 
+class GridProblem(ctypes.Structure):
+    """ria_grid_problem of include/ria.h."""
+    _fields_ = [("resolution", ctypes.c_uint32), ("n_func", ctypes.c_uint32), ("bbox_min", ctypes.c_double * 3),
+                ("bbox_max", ctypes.c_double * 3), ("funcs", ctypes.c_void_p)]
+
+
 class Config(ctypes.Structure):
     _fields_ = [("use_lookup", ctypes.c_int32), ("use_secondary_lookup", ctypes.c_int32),
                 ("use_topo_ray_shooting", ctypes.c_int32), ("robust_test", ctypes.c_int32),
@@ -75,6 +81,20 @@ def load():
         fn.argtypes = [vp, vp, u64, vp, u64, vp]
     L.ria_compute_arrangement_batch_noalloc.restype = i32
     L.ria_compute_arrangement_batch_noalloc.argtypes = [vp, vp, u64, vp, u64, vp, vp]
+    L.ria_grid_batch.restype = i32
+    L.ria_grid_batch.argtypes = [cfgp, i32, vp, u32, ctypes.POINTER(vp)]
+    L.ria_batch_size.restype = u32
+    L.ria_batch_size.argtypes = [vp]
+    L.ria_batch_count.restype = u64
+    L.ria_batch_count.argtypes = [vp, u32, i32]
+    L.ria_batch_copy.restype = i32
+    L.ria_batch_copy.argtypes = [vp, u32, i32, vp]
+    L.ria_mesh_csg.restype = i32
+    L.ria_mesh_csg.argtypes = [vp, vp, u32, i32, vp]
+    L.ria_mesh_face_sides.restype = i32
+    L.ria_mesh_face_sides.argtypes = [vp, vp]
+    L.ria_batch_csg.restype = i32
+    L.ria_batch_csg.argtypes = [vp, u32, vp, u32, i32, vp]
     L.ria_mesh_count.restype = u64
     L.ria_mesh_count.argtypes = [vp, i32]
     L.ria_mesh_copy.restype = i32

@@ -79,6 +79,38 @@ class Mesh:
     def timings(self) -> dict:
         return dict(zip(_lib.TIMING_NAMES, self["timings"].tolist()))
 
+    def csg(self, tree=None, positive_inside=True) -> np.ndarray:
+        """Per-face CSG label (0 not on the boundary, 1 inside on the positive side, 2 on the negative
+        side); tree: list of (op, a, b) units as the reference's CSG tree files, None = union."""
+        t, n = _csg_tree(tree)
+        out = np.zeros(int(_lib.load().ria_mesh_count(self._h, _lib.FIELD_FACE_FUNC)) // 2, dtype=np.uint8)
+        _lib.check(_lib.load().ria_mesh_csg(self._h, t.ctypes.data if n else None, n, int(positive_inside),
+                                            out.ctypes.data))
+        return out
+
+
+    def face_sides(self) -> np.ndarray:
+        """n_faces x 2 sign vectors (bit j: function j positive) on the positive / negative side."""
+        n = int(_lib.load().ria_mesh_count(self._h, _lib.FIELD_FACE_FUNC)) // 2
+        out = np.zeros((n, 2), dtype=np.uint64)
+        _lib.check(_lib.load().ria_mesh_face_sides(self._h, out.ctypes.data))
+        return out
+
+
+CSG_OPS = {"Intersection": 0, "Union": 1, "Negation": 2}
+
+
+def _csg_tree(tree):
+    if not tree:
+        return np.zeros(3, dtype=np.int32), 0
+    rows = []
+    for u in tree:
+        if isinstance(u, dict):
+            rows.append((CSG_OPS[u["type"]], int(u["elements"][0]), int(u["elements"][1])))
+        else:
+            rows.append(tuple(int(x) for x in u))
+    return np.ascontiguousarray(rows, dtype=np.int32), len(rows)
+
 
 def _config(use_lookup=True, use_secondary_lookup=True, use_topo_ray_shooting=True, robust_test=False):
     if not use_lookup:
@@ -128,6 +160,80 @@ def grid_implicit_arrangement(res, funcs, **kw) -> Mesh:
 
 def grid_material_interface(res, funcs, **kw) -> Mesh:
     return _run_grid("ria_grid_material_interface", res, funcs, **kw)
+
+
+class BatchMesh(Mesh):
+    """A ria_grid_batch result; `problem(i)` views one problem's fields, numbered as in its own grid
+    call."""
+
+    def __len__(self):
+        return int(_lib.load().ria_batch_size(self._h))
+
+    def problem(self, i):
+        return _ProblemView(self, int(i))
+
+
+class _ProblemView:
+    def __init__(self, batch, i):
+        self._b = batch
+        self._i = i
+        self._cache = {}
+
+    def __getitem__(self, name):
+        if name not in self._cache:
+            L = _lib.load()
+            h = self._b._h
+            if name == "stats":
+                a = np.zeros(len(_lib.STAT_NAMES), dtype=np.int64)
+                _lib.check(L.ria_batch_copy(h, self._i, _lib.FIELD_STATS, a.ctypes.data))
+            elif name == "timings":
+                a = np.zeros(len(_lib.TIMING_NAMES), dtype=np.float64)
+                _lib.check(L.ria_batch_copy(h, self._i, _lib.FIELD_TIMINGS, a.ctypes.data))
+            else:
+                field, dt, shape = Mesh._FIELDS[name]
+                n = int(L.ria_batch_count(h, self._i, field))
+                a = np.zeros(n, dtype=dt)
+                if n:
+                    _lib.check(L.ria_batch_copy(h, self._i, field, a.ctypes.data))
+                if shape:
+                    a = a.reshape(shape)
+            self._cache[name] = a
+        return self._cache[name]
+
+    @property
+    def stats(self) -> dict:
+        return dict(zip(_lib.STAT_NAMES, self["stats"].tolist()))
+
+    def csg(self, tree=None, positive_inside=True) -> np.ndarray:
+        t, n = _csg_tree(tree)
+        out = np.zeros(len(self["face_func"]), dtype=np.uint8)
+        _lib.check(_lib.load().ria_batch_csg(self._b._h, self._i, t.ctypes.data if n else None, n,
+                                             int(positive_inside), out.ctypes.data))
+        return out
+
+
+def grid_batch(problems, mode="ia", **kw) -> BatchMesh:
+    """Solve many grid problems in one pass of every stage.  problems: iterable of
+    (res, funcs) or (res, funcs, bbox_min, bbox_max)."""
+    L = _lib.load()
+    problems = list(problems)
+    arr = (_lib.GridProblem * len(problems))()
+    keep = []
+    for i, pr in enumerate(problems):
+        res, funcs = pr[0], np.ascontiguousarray(pr[1], dtype=FUNC_DTYPE)
+        bmin = pr[2] if len(pr) > 2 else (-1.0, -1.0, -1.0)
+        bmax = pr[3] if len(pr) > 3 else (1.0, 1.0, 1.0)
+        keep.append(funcs)
+        arr[i].resolution = int(res)
+        arr[i].n_func = len(funcs)
+        for a in range(3):
+            arr[i].bbox_min[a] = float(bmin[a])
+            arr[i].bbox_max[a] = float(bmax[a])
+        arr[i].funcs = funcs.ctypes.data
+    cfg = _config(**kw)
+    h = ctypes.c_void_p()
+    _lib.check(L.ria_grid_batch(ctypes.byref(cfg), 1 if mode == "mi" else 0, arr, len(problems), ctypes.byref(h)))
+    return BatchMesh(h)
 
 
 def sample_functions(funcs, pts) -> np.ndarray:

@@ -7,6 +7,7 @@
 #include <cuda_runtime.h>
 
 #include <cub/cub.cuh>
+#include <algorithm>
 #include <atomic>
 #include <chrono>
 #include <cstring>
@@ -42,16 +43,18 @@ ria_status fail(ria_status s, const std::string& msg) {
 
 struct DeviceCtx {
     bool ready[2] = {false, false};
-    uint8_t* table[2] = {nullptr, nullptr};
-    uint32_t* table_off[2] = {nullptr, nullptr};
+    uint8_t* table[2] = {nullptr, nullptr};      // 81 patterns, then the secondary-lookup templates
+    uint32_t* table_off[2] = {nullptr, nullptr};  // 81 + kCacheEntries
     IASum4* table_sum[2] = {nullptr, nullptr};
+    unsigned long long* cache_slots[2] = {nullptr, nullptr};
+    unsigned long long* cache_cnt[2] = {nullptr, nullptr};  // [0] entries used, [1] template bytes used
 };
 
 std::mutex g_mu;
 std::vector<DeviceCtx> g_ctx;
 
 constexpr int64_t kFastRecordBytes = 1024;  // bound of a record of the fast variants
-constexpr int64_t kBigRecordBytes = 5120;   // bound of a record of the exact variants
+constexpr int64_t kBigRecordBytes = 28672;  // bound of a record of the exact variants
 constexpr int64_t kBigSlots = 152 * 64;     // concurrent exact-variant threads
 
 ria_status current_device(int* dev) {
@@ -62,6 +65,21 @@ ria_status current_device(int* dev) {
     }
     RIA_CUDA(cudaGetDevice(dev));
     return RIA_OK;
+}
+
+// the secondary lookup of one mode (its entries share the mode's table region)
+void set_cache(CutArgs& a, DeviceCtx* ctx, bool mi) {
+    const int m = mi ? 1 : 0;
+    a.cache.slots = ctx->cache_slots[m];
+    a.cache.slot_mask = kCacheSlots - 1;
+    a.cache.cap = kCacheEntries;
+    a.cache.next = ctx->cache_cnt[m];
+    a.cache.heap_used = ctx->cache_cnt[m] + 1;
+    a.cache.heap_base = (uint64_t)kTablePatterns * kTableStride;
+    a.cache.heap_cap = kCacheHeapBytes;
+    a.cache.table = ctx->table[m];
+    a.cache.table_off = ctx->table_off[m];
+    a.cache.table_sum = ctx->table_sum[m];
 }
 
 // Build (once per device) the lookup table of one mode with the exact per-tet cut.
@@ -82,9 +100,13 @@ ria_status ensure_table(bool mi, cudaStream_t s, DeviceCtx** out) {
         }
     }
     if (!c.ready[m]) {
-        RIA_CUDA(cudaMalloc(&c.table[m], (size_t)kTablePatterns * kTableStride));
-        RIA_CUDA(cudaMalloc(&c.table_off[m], sizeof(uint32_t) * kTablePatterns));
-        RIA_CUDA(cudaMalloc(&c.table_sum[m], sizeof(IASum4) * kTablePatterns));
+        RIA_CUDA(cudaMalloc(&c.table[m], (size_t)kTablePatterns * kTableStride + kCacheHeapBytes));
+        RIA_CUDA(cudaMalloc(&c.table_off[m], sizeof(uint32_t) * (kTablePatterns + kCacheEntries)));
+        RIA_CUDA(cudaMalloc(&c.table_sum[m], sizeof(IASum4) * (kTablePatterns + kCacheEntries)));
+        RIA_CUDA(cudaMalloc(&c.cache_slots[m], sizeof(unsigned long long) * kCacheSlots));
+        RIA_CUDA(cudaMalloc(&c.cache_cnt[m], sizeof(unsigned long long) * 2));
+        RIA_CUDA(cudaMemsetAsync(c.cache_slots[m], 0, sizeof(unsigned long long) * kCacheSlots, s));
+        RIA_CUDA(cudaMemsetAsync(c.cache_cnt[m], 0, sizeof(unsigned long long) * 2, s));
         void* scratch = nullptr;
         uint32_t* status = nullptr;
         RIA_CUDA(cudaMalloc(&scratch, cut_big_slot_bytes(mi) * kTablePatterns));
@@ -122,6 +144,16 @@ struct Inputs {
     const int64_t* d_tets = nullptr;
     const double* d_fv = nullptr;       // explicit values, or
     const ria_function* funcs = nullptr;  // functions sampled on the grid (host array)
+    ulonglong2* d_vmask = nullptr;      // vertex masks computed with the values (batched grids)
+    bool trusted_tets = false;          // tets generated here: no range check
+};
+
+// one problem of a batched-grid mesh
+struct BatchInfo {
+    int64_t vbase = 0, tbase = 0, V = 0, T = 0;
+    int F = 0, res = 0;
+    int64_t vfirst = 0, vlast = 0, ffirst = 0, flast = 0;  // mesh vertices / faces of the problem
+    int64_t stats[RIA_NUM_STATS] = {0};
 };
 
 // device allocations of one call
@@ -173,6 +205,9 @@ struct ria_mesh {
     int64_t n_fit = 0;
     int64_t stats[RIA_NUM_STATS] = {0};
     double timings[RIA_NUM_TIMINGS] = {0};
+    std::vector<BatchInfo> batch;  // batched grids: per-problem ranges (empty otherwise)
+    const int64_t* d_tets = nullptr;  // explicit tets (kept by the mesh or the caller), or the grid:
+    int64_t res = 0;
 };
 
 namespace {
@@ -181,7 +216,8 @@ ria_status run_pipeline(const ria_config* cfg, const Inputs& in, cudaStream_t s,
     if (!cfg || !out) return fail(RIA_EINVAL, "null argument");
     if (in.F < 1 || in.F > 64) return fail(RIA_EINVAL, "n_func must be in 1..64");
     if (in.V <= 0 || in.V >= (1ll << 31)) return fail(RIA_EINVAL, "n_pts must be in 1..2^31-1");
-    if (in.T < 0 || in.T >= (1ll << 32)) return fail(RIA_EINVAL, "n_tets must be below 2^32");
+    // active and general-case lists share one 32-bit scan: A + G <= 2 n_tets
+    if (in.T < 0 || in.T >= (1ll << 31)) return fail(RIA_EINVAL, "n_tets must be below 2^31");
     const bool mi = in.mi;
     const bool use_table = cfg->use_lookup != 0;
     DeviceCtx* ctx = nullptr;
@@ -198,6 +234,9 @@ ria_status run_pipeline(const ria_config* cfg, const Inputs& in, cudaStream_t s,
     M->keep.s = s;
     M->table = ctx->table[mi];
     M->table_off = ctx->table_off[mi];
+    M->d_tets = in.d_tets;
+    M->res = in.g.res;
+    M->fv = const_cast<double*>(in.d_fv);  // explicit values (the grid path replaces it with its own)
     Allocs tmp{s, {}};
     cudaError_t err = cudaSuccess;
     cudaEvent_t ev[5];
@@ -220,7 +259,7 @@ ria_status run_pipeline(const ria_config* cfg, const Inputs& in, cudaStream_t s,
     uint32_t* status = (uint32_t*)cnt;
     if (err != cudaSuccess) return bail(fail(RIA_ENOMEM, "device allocation failed"));
     cudaMemsetAsync(cnt, 0, sizeof(unsigned long long) * 16, s);
-    if (in.d_tets) {
+    if (in.d_tets && !in.trusted_tets) {
         // every kernel below indexes through the tets: check them before any of them runs
         launch_check_tets(in.d_tets, in.T, in.V, status, s);
         uint32_t hst = 0;
@@ -230,7 +269,7 @@ ria_status run_pipeline(const ria_config* cfg, const Inputs& in, cudaStream_t s,
     }
 
     // ---- stage a
-    ulonglong2* vmask = tmp.get<ulonglong2>(in.V, &err);
+    ulonglong2* vmask = in.d_vmask ? in.d_vmask : tmp.get<ulonglong2>(in.V, &err);
     const double* fv = in.d_fv;
     double* coords = nullptr;
     if (in.funcs) {
@@ -247,27 +286,28 @@ ria_status run_pipeline(const ria_config* cfg, const Inputs& in, cudaStream_t s,
         M->fv = d_fv;
     } else {
         if (err != cudaSuccess) return bail(fail(RIA_ENOMEM, "device allocation failed"));
-        launch_vertex_masks(mi, fv, in.V, in.F, vmask, cnt + 1, s);
+        if (!in.d_vmask) launch_vertex_masks(mi, fv, in.V, in.F, vmask, cnt + 1, s);
     }
     cudaEventRecord(ev[1], s);
 
     // ---- stage b
     const int64_t nb = filter_num_blocks(in.T);
-    uint32_t* blk = tmp.get<uint32_t>(2 * nb, &err);
-    uint32_t* blk_off = tmp.get<uint32_t>(2 * nb, &err);
+    const int64_t nscan = (1 + kGenBins) * nb;  // active counts, then the per-bin general-case counts
+    uint32_t* blk = tmp.get<uint32_t>(nscan, &err);
+    uint32_t* blk_off = tmp.get<uint32_t>(nscan, &err);
     if (err != cudaSuccess) return bail(fail(RIA_ENOMEM, "device allocation failed"));
     int64_t A = 0, G = 0;
     if (nb > 0) {
         launch_filter_count(mi, vmask, fv, in.F, in.d_tets, in.g, in.T, use_table, blk, cnt + 2, s);
         size_t bytes = 0;
-        cub::DeviceScan::ExclusiveSum(nullptr, bytes, blk, blk_off, 2 * nb, s);
+        cub::DeviceScan::ExclusiveSum(nullptr, bytes, blk, blk_off, nscan, s);
         uint8_t* scan_tmp = tmp.get<uint8_t>((int64_t)bytes, &err);
         if (err != cudaSuccess) return bail(fail(RIA_ENOMEM, "device allocation failed"));
-        cub::DeviceScan::ExclusiveSum(scan_tmp, bytes, blk, blk_off, 2 * nb, s);
+        cub::DeviceScan::ExclusiveSum(scan_tmp, bytes, blk, blk_off, nscan, s);
         uint32_t h[3];
         cudaMemcpyAsync(&h[0], blk_off + nb, 4, cudaMemcpyDeviceToHost, s);
-        cudaMemcpyAsync(&h[1], blk_off + 2 * nb - 1, 4, cudaMemcpyDeviceToHost, s);
-        cudaMemcpyAsync(&h[2], blk + 2 * nb - 1, 4, cudaMemcpyDeviceToHost, s);
+        cudaMemcpyAsync(&h[1], blk_off + nscan - 1, 4, cudaMemcpyDeviceToHost, s);
+        cudaMemcpyAsync(&h[2], blk + nscan - 1, 4, cudaMemcpyDeviceToHost, s);
         if (cudaStreamSynchronize(s) != cudaSuccess) return bail(fail(RIA_ECUDA, cudaGetErrorString(cudaGetLastError())));
         A = h[0];
         G = (int64_t)h[1] + h[2] - A;
@@ -326,6 +366,7 @@ ria_status run_pipeline(const ria_config* cfg, const Inputs& in, cudaStream_t s,
             ca.table = ctx->table[0];
             ca.table_off = ctx->table_off[0];
         }
+        if (cfg->use_lookup && cfg->use_secondary_lookup) set_cache(ca, ctx, mi);
         launch_cut_fast(ca, s);
         unsigned long long h = 0;
         cudaMemcpyAsync(&h, cnt + 7, 8, cudaMemcpyDeviceToHost, s);
@@ -476,6 +517,164 @@ ria_status grid_run(bool mi, const ria_config* cfg, uint32_t res, const double* 
     st = run_pipeline(cfg, in, s, true, out);
     if (st != RIA_OK) cudaStreamDestroy(s);
     return st;
+}
+
+// Many grid problems through one pass of each stage: the grids are concatenated problem-major, the
+// values padded to the widest function count with a constant that is never active, and the
+// pipeline runs once over the whole batch.  Mesh keys always contain a vertex or tet id of their
+// own problem, so first-occurrence numbering in tet order numbers each problem's vertices and faces
+// contiguously, in the order of its own grid call.
+ria_status grid_batch_run(bool mi, const ria_config* cfg, const ria_grid_problem* probs, uint32_t n, ria_mesh** out) {
+    if (!cfg || !probs || !out || n == 0) return fail(RIA_EINVAL, "null argument or empty batch");
+    std::vector<BatchProblem> hp(n);
+    std::vector<int64_t> tb(n + 1);
+    std::vector<uint32_t> bo(n + 1);
+    std::vector<ria_function> funcs;
+    int Fmax = 0;
+    int64_t V = 0, T = 0, blocks = 0;
+    for (uint32_t p = 0; p < n; ++p) {
+        const ria_grid_problem& q = probs[p];
+        if (q.resolution == 0 || q.resolution > 1200) return fail(RIA_EINVAL, "resolution must be in 1..1200");
+        if (q.n_func < 1 || q.n_func > 64 || !q.funcs) return fail(RIA_EINVAL, "n_func must be in 1..64");
+        const int64_t N = (int64_t)q.resolution + 1;
+        BatchProblem b{};
+        b.vbase = V;
+        b.tbase = T;
+        b.res = (int32_t)q.resolution;
+        b.F = (int32_t)q.n_func;
+        b.foff = (int32_t)funcs.size();
+        for (int a = 0; a < 3; ++a) {
+            b.bmin[a] = q.bbox_min[a];
+            b.bmax[a] = q.bbox_max[a];
+        }
+        hp[p] = b;
+        tb[p] = T;
+        bo[p] = (uint32_t)blocks;
+        V += N * N * N;
+        T += 5 * (int64_t)q.resolution * q.resolution * q.resolution;
+        blocks += (N * N * N + kBatchSampleBlock - 1) / kBatchSampleBlock;
+        funcs.insert(funcs.end(), q.funcs, q.funcs + q.n_func);
+        Fmax = std::max(Fmax, (int)q.n_func);
+        if (V >= (1ll << 31) || T >= (1ll << 31)) return fail(RIA_EINVAL, "batch too large: 2^31 points or tets");
+    }
+    tb[n] = T;
+    bo[n] = (uint32_t)blocks;
+    int dev = 0;
+    ria_status st = current_device(&dev);
+    if (st != RIA_OK) return st;
+    cudaStream_t s;
+    RIA_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    Allocs tmp{s, {}};
+    cudaError_t err = cudaSuccess;
+    BatchProblem* d_probs = tmp.get<BatchProblem>(n, &err);
+    int64_t* d_tb = tmp.get<int64_t>(n + 1, &err);
+    uint32_t* d_bo = tmp.get<uint32_t>(n + 1, &err);
+    ria_function* d_funcs = tmp.get<ria_function>((int64_t)funcs.size(), &err);
+    double* d_pts = tmp.get<double>(3 * V, &err);
+    ulonglong2* d_vmask = tmp.get<ulonglong2>(V, &err);
+    int64_t* d_tets = tmp.get<int64_t>(4 * T, &err);
+    unsigned long long* d_cnt = tmp.get<unsigned long long>(5 * (int64_t)n + 1, &err);  // n_zero per problem, total, 4 stats
+    double* d_fv = nullptr;
+    if (err == cudaSuccess) err = cudaMallocAsync(&d_fv, sizeof(double) * (size_t)V * Fmax, s);
+    auto bail = [&](ria_status r) {
+        tmp.release();
+        if (d_fv) cudaFreeAsync(d_fv, s);
+        cudaStreamSynchronize(s);
+        cudaStreamDestroy(s);
+        return r;
+    };
+    if (err != cudaSuccess) return bail(fail(RIA_ENOMEM, "device allocation failed"));
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, s);
+    cudaMemcpyAsync(d_probs, hp.data(), sizeof(BatchProblem) * n, cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(d_tb, tb.data(), sizeof(int64_t) * (n + 1), cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(d_bo, bo.data(), sizeof(uint32_t) * (n + 1), cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(d_funcs, funcs.data(), sizeof(ria_function) * funcs.size(), cudaMemcpyHostToDevice, s);
+    cudaMemsetAsync(d_cnt, 0, sizeof(unsigned long long) * (5 * (size_t)n + 1), s);
+    launch_batch_sample(mi, d_probs, (int)n, d_bo, (uint32_t)blocks, d_funcs, Fmax, d_pts, d_fv, d_vmask, d_cnt + n,
+                        d_cnt, s);
+    launch_batch_tets(d_probs, d_tb, (int)n, T, d_tets, s);
+    cudaEventRecord(e1, s);
+    Inputs in;
+    in.mi = mi;
+    in.V = V;
+    in.T = T;
+    in.F = Fmax;
+    in.d_pts = d_pts;
+    in.d_tets = d_tets;
+    in.d_fv = d_fv;
+    in.d_vmask = d_vmask;
+    in.trusted_tets = true;
+    st = run_pipeline(cfg, in, s, true, out);
+    if (st != RIA_OK) {
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        return bail(st);
+    }
+    ria_mesh* M = *out;
+    M->keep.v.push_back(d_fv);
+    M->fv = d_fv;
+    M->d_tets = nullptr;  // released below; per-problem grids are rebuilt from BatchInfo
+    d_fv = nullptr;
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    M->timings[RIA_TIME_SAMPLE] += ms * 1e-3;
+    M->timings[RIA_TIME_TOTAL] += ms * 1e-3;
+    // per-problem ranges and statistics
+    int64_t* d_first = tmp.get<int64_t>(2 * ((int64_t)n + 1), &err);
+    if (err != cudaSuccess) {
+        tmp.release();
+        ria_mesh_free(M);
+        *out = nullptr;
+        return fail(RIA_ENOMEM, "device allocation failed");
+    }
+    if (!cfg->robust_test)
+        launch_batch_ranges(d_tb, (int)n, M->ex.verts, M->ex.n_verts, M->ex.face_tet_offsets, M->ex.face_tets,
+                            M->ex.n_faces, d_first, d_first + n + 1, s);
+    launch_batch_active_stats(mi, d_tb, (int)n, M->act_tet, M->act_mask, M->A, d_cnt + n + 1, s);
+    std::vector<int64_t> first(2 * ((size_t)n + 1), 0);
+    std::vector<unsigned long long> cnt(5 * (size_t)n + 1);
+    if (!cfg->robust_test)
+        cudaMemcpyAsync(first.data(), d_first, sizeof(int64_t) * first.size(), cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(cnt.data(), d_cnt, sizeof(unsigned long long) * cnt.size(), cudaMemcpyDeviceToHost, s);
+    tmp.release();
+    cudaError_t se = cudaStreamSynchronize(s);
+    if (se != cudaSuccess) {
+        ria_mesh_free(M);
+        *out = nullptr;
+        return fail(RIA_ECUDA, cudaGetErrorString(se));
+    }
+    M->stats[RIA_STAT_NUM_DEGENERATE_VERTEX] = (int64_t)cnt[n];
+    M->batch.resize(n);
+    for (uint32_t p = 0; p < n; ++p) {
+        BatchInfo& b = M->batch[p];
+        const int64_t N = (int64_t)hp[p].res + 1;
+        b.vbase = hp[p].vbase;
+        b.tbase = hp[p].tbase;
+        b.V = N * N * N;
+        b.T = tb[p + 1] - tb[p];
+        b.F = hp[p].F;
+        b.res = hp[p].res;
+        b.vfirst = first[p];
+        b.vlast = first[p + 1];
+        b.ffirst = first[n + 1 + p];
+        b.flast = first[n + 1 + p + 1];
+        const unsigned long long* a4 = &cnt[n + 1 + 4 * (size_t)p];
+        b.stats[RIA_STAT_NUM_PTS] = b.V;
+        b.stats[RIA_STAT_NUM_TETS] = b.T;
+        b.stats[RIA_STAT_NUM_DEGENERATE_VERTEX] = (int64_t)cnt[p];
+        b.stats[RIA_STAT_NUM_INTERSECTING_TET] = (int64_t)a4[0];
+        b.stats[RIA_STAT_NUM_A_FUNC] = (int64_t)a4[1];
+        b.stats[RIA_STAT_NUM_B_FUNC] = (int64_t)a4[2];
+        b.stats[RIA_STAT_NUM_MORE_FUNC] = (int64_t)a4[3];
+        b.stats[RIA_STAT_NUM_VERTS] = b.vlast - b.vfirst;
+        b.stats[RIA_STAT_NUM_FACES] = b.flast - b.ffirst;
+    }
+    return RIA_OK;
 }
 
 ria_status batch_run(bool mi, const double* values, const uint32_t* value_offsets, uint64_t n_tets,
@@ -682,6 +881,248 @@ ria_status ria_compute_arrangement_batch_noalloc(const double* d_values, const u
     int r = run_batch_noalloc(d_values, d_value_offsets, n_tets, d_records, capacity, d_record_offsets,
                               (cudaStream_t)stream, &msg);
     if (r != RIA_OK) return fail((ria_status)r, msg);
+    return RIA_OK;
+}
+
+ria_status ria_grid_batch(const ria_config* cfg, int32_t material_interface, const ria_grid_problem* problems,
+                          uint32_t n_problems, ria_mesh** out) {
+    return grid_batch_run(material_interface != 0, cfg, problems, n_problems, out);
+}
+
+static ria_status ensure_gathered(ria_mesh* m, ria_mesh_field f);
+
+namespace {
+
+// The reference's CSG tree (app/csg.cpp:15-52): units {op, a, b}, op 0 intersection, 1 union,
+// 2 negation (b unused); an element > 0 is a unit (1-based), < 0 is function -e-1; unit 1 is the
+// root.  Emitted as a postfix program for the device.
+bool csg_emit(const int32_t* tree, uint32_t n, int F, int32_t e, int depth, std::vector<int32_t>& prog) {
+    if (depth > 60) return false;
+    if (e < 0) {
+        const int f = -e - 1;
+        if (f >= F) return false;
+        prog.push_back(f);
+        return true;
+    }
+    if (e == 0 || (uint32_t)e > n) return false;
+    const int32_t* u = tree + 3 * (e - 1);
+    if (u[0] < 0 || u[0] > 2) return false;
+    if (!csg_emit(tree, n, F, u[1], depth + 1, prog)) return false;
+    if (u[0] != 2 && !csg_emit(tree, n, F, u[2], depth + 1, prog)) return false;
+    prog.push_back(u[0] == 0 ? -1 : (u[0] == 1 ? -2 : -3));
+    return true;
+}
+
+ria_status run_csg(ria_mesh* m, int64_t f0, int64_t f1, int nfunc, int64_t res, int64_t tbase, int64_t vbase,
+                   const int32_t* tree, uint32_t n_units, int32_t positive_inside, uint8_t* labels,
+                   uint64_t* sides = nullptr) {
+    if (m->mi) return fail(RIA_EINVAL, "CSG needs an implicit-arrangement mesh");
+    if (!m->fv || (!m->d_tets && res == 0)) return fail(RIA_EINVAL, "the mesh keeps no function values");
+    std::vector<int32_t> prog;
+    if (n_units && !csg_emit(tree, n_units, nfunc, 1, 0, prog)) return fail(RIA_EINVAL, "invalid CSG tree");
+    Allocs tmp{m->s, {}};
+    cudaError_t err = cudaSuccess;
+    int32_t* d_prog = tmp.get<int32_t>((int64_t)prog.size(), &err);
+    uint8_t* d_out = tmp.get<uint8_t>(f1 - f0, &err);
+    uint64_t* d_sides = sides ? tmp.get<uint64_t>(2 * (f1 - f0), &err) : nullptr;
+    if (err != cudaSuccess) {
+        tmp.release();
+        return fail(RIA_ENOMEM, "device allocation failed");
+    }
+    if (!prog.empty())
+        cudaMemcpyAsync(d_prog, prog.data(), sizeof(int32_t) * prog.size(), cudaMemcpyHostToDevice, m->s);
+    CsgArgs a{};
+    a.f0 = f0;
+    a.f1 = f1;
+    a.face_tet_offsets = m->ex.face_tet_offsets;
+    a.face_tets = m->ex.face_tets;
+    a.face_func = m->ex.face_func;
+    a.act_tet = m->act_tet;
+    a.A = m->A;
+    a.act_desc = m->act_desc;
+    a.act_mask = m->act_mask;
+    a.heap = m->heap;
+    a.heap_big = m->heap_big;
+    a.table = m->table;
+    a.table_off = m->table_off;
+    a.fv = m->fv;
+    a.F = m->F;
+    a.nfunc = nfunc;
+    a.d_tets = m->d_tets;
+    a.res = res;
+    a.tbase = tbase;
+    a.vbase = vbase;
+    a.prog = d_prog;
+    a.nprog = (int)prog.size();
+    a.pos_inside = positive_inside ? 1 : 0;
+    a.out = d_out;
+    a.sides = d_sides;
+    launch_csg(a, m->s);
+    if (f1 > f0 && sides)
+        cudaMemcpyAsync(sides, d_sides, sizeof(uint64_t) * 2 * (size_t)(f1 - f0), cudaMemcpyDeviceToHost, m->s);
+    else if (f1 > f0)
+        cudaMemcpyAsync(labels, d_out, (size_t)(f1 - f0), cudaMemcpyDeviceToHost, m->s);
+    tmp.release();
+    cudaError_t e = cudaStreamSynchronize(m->s);
+    if (e != cudaSuccess) return fail(RIA_ECUDA, cudaGetErrorString(e));
+    return RIA_OK;
+}
+
+}  // namespace
+
+ria_status ria_mesh_csg(const ria_mesh* mc, const int32_t* tree, uint32_t n_units, int32_t positive_inside,
+                        uint8_t* face_labels) {
+    ria_mesh* m = const_cast<ria_mesh*>(mc);
+    if (!m || !face_labels || (n_units && !tree)) return fail(RIA_EINVAL, "null argument");
+    if (!m->batch.empty()) return fail(RIA_EINVAL, "a batch mesh: use ria_batch_csg");
+    return run_csg(m, 0, m->ex.n_faces, m->F, m->d_tets ? 0 : m->res, 0, 0, tree, n_units, positive_inside,
+                   face_labels);
+}
+
+ria_status ria_mesh_face_sides(const ria_mesh* mc, uint64_t* sides) {
+    ria_mesh* m = const_cast<ria_mesh*>(mc);
+    if (!m || !sides) return fail(RIA_EINVAL, "null argument");
+    if (!m->batch.empty()) return fail(RIA_EINVAL, "a batch mesh: not supported");
+    return run_csg(m, 0, m->ex.n_faces, m->F, m->d_tets ? 0 : m->res, 0, 0, nullptr, 0, 1, nullptr, sides);
+}
+
+ria_status ria_batch_csg(const ria_mesh* mc, uint32_t problem, const int32_t* tree, uint32_t n_units,
+                         int32_t positive_inside, uint8_t* face_labels) {
+    ria_mesh* m = const_cast<ria_mesh*>(mc);
+    if (!m || !face_labels || (n_units && !tree)) return fail(RIA_EINVAL, "null argument");
+    if (problem >= m->batch.size()) return fail(RIA_EINVAL, "problem index out of range (or not a batch mesh)");
+    const BatchInfo& b = m->batch[problem];
+    return run_csg(m, b.ffirst, b.flast, b.F, b.res, b.tbase, b.vbase, tree, n_units, positive_inside, face_labels);
+}
+
+uint32_t ria_batch_size(const ria_mesh* m) { return m ? (uint32_t)m->batch.size() : 0; }
+
+namespace {
+
+int64_t read_i64(const ria_mesh* m, const int64_t* p) {
+    int64_t v = 0;
+    cudaMemcpyAsync(&v, p, 8, cudaMemcpyDeviceToHost, m->s);
+    cudaStreamSynchronize(m->s);
+    return v;
+}
+
+// element range [b, e) of a per-problem slice, in units of the field's elements
+ria_status batch_slice(ria_mesh* m, const BatchInfo& b, ria_mesh_field f, int64_t* lo, int64_t* hi) {
+    switch (f) {
+        case RIA_MESH_POINTS: *lo = 3 * b.vfirst; *hi = 3 * b.vlast; return RIA_OK;
+        case RIA_MESH_VERTS: *lo = 11 * b.vfirst; *hi = 11 * b.vlast; return RIA_OK;
+        case RIA_MESH_FACE_OFFSETS:
+        case RIA_MESH_FACE_TET_OFFSETS: *lo = b.ffirst; *hi = b.flast + 1; return RIA_OK;
+        case RIA_MESH_FACE_FUNC: *lo = 2 * b.ffirst; *hi = 2 * b.flast; return RIA_OK;
+        case RIA_MESH_FACE_VERTS:
+            *lo = read_i64(m, m->ex.face_offsets + b.ffirst);
+            *hi = read_i64(m, m->ex.face_offsets + b.flast);
+            return RIA_OK;
+        case RIA_MESH_FACE_TETS:
+            *lo = 2 * read_i64(m, m->ex.face_tet_offsets + b.ffirst);
+            *hi = 2 * read_i64(m, m->ex.face_tet_offsets + b.flast);
+            return RIA_OK;
+        case RIA_MESH_START_INDEX:
+        case RIA_MESH_REC_OFFSETS: *lo = b.tbase; *hi = b.tbase + b.T + 1; return RIA_OK;
+        case RIA_MESH_FUNC_IN_TET:
+            *lo = read_i64(m, m->start_index + b.tbase);
+            *hi = read_i64(m, m->start_index + b.tbase + b.T);
+            return RIA_OK;
+        case RIA_MESH_REC_BYTES:
+            *lo = read_i64(m, m->rec_offsets + b.tbase);
+            *hi = read_i64(m, m->rec_offsets + b.tbase + b.T);
+            return RIA_OK;
+        case RIA_MESH_FUNC_VALS: *lo = 0; *hi = b.V * b.F; return RIA_OK;
+        case RIA_MESH_STATS: *lo = 0; *hi = RIA_NUM_STATS; return RIA_OK;
+        case RIA_MESH_TIMINGS: *lo = 0; *hi = RIA_NUM_TIMINGS; return RIA_OK;
+    }
+    return fail(RIA_EINVAL, "unknown field");
+}
+
+}  // namespace
+
+uint64_t ria_batch_count(const ria_mesh* mc, uint32_t problem, ria_mesh_field f) {
+    ria_mesh* m = const_cast<ria_mesh*>(mc);
+    if (!m || problem >= m->batch.size()) return 0;
+    if (ensure_gathered(m, f) != RIA_OK) return 0;
+    int64_t lo = 0, hi = 0;
+    if (batch_slice(m, m->batch[problem], f, &lo, &hi) != RIA_OK) return 0;
+    return (uint64_t)(hi - lo);
+}
+
+ria_status ria_batch_copy(const ria_mesh* mc, uint32_t problem, ria_mesh_field f, void* dst) {
+    ria_mesh* m = const_cast<ria_mesh*>(mc);
+    if (!m || !dst) return fail(RIA_EINVAL, "null argument");
+    if (problem >= m->batch.size()) return fail(RIA_EINVAL, "problem index out of range (or not a batch mesh)");
+    const BatchInfo& b = m->batch[problem];
+    ria_status st = ensure_gathered(m, f);
+    if (st != RIA_OK) return st;
+    if (f == RIA_MESH_STATS) {
+        std::memcpy(dst, b.stats, sizeof(b.stats));
+        return RIA_OK;
+    }
+    if (f == RIA_MESH_TIMINGS) {
+        std::memcpy(dst, m->timings, sizeof(m->timings));
+        return RIA_OK;
+    }
+    if (f == RIA_MESH_FUNC_VALS) {
+        if (!m->fv) return fail(RIA_EINVAL, "field not available on this mesh");
+        RIA_CUDA(cudaMemcpy2DAsync(dst, sizeof(double) * b.F, m->fv + b.vbase * m->F, sizeof(double) * m->F,
+                                   sizeof(double) * b.F, (size_t)b.V, cudaMemcpyDeviceToHost, m->s));
+        RIA_CUDA(cudaStreamSynchronize(m->s));
+        return RIA_OK;
+    }
+    int64_t lo = 0, hi = 0;
+    st = batch_slice(m, b, f, &lo, &hi);
+    if (st != RIA_OK) return st;
+    const void* src = nullptr;
+    size_t esz = 8;
+    switch (f) {
+        case RIA_MESH_POINTS: src = m->ex.xyz; break;
+        case RIA_MESH_VERTS: src = m->ex.verts; break;
+        case RIA_MESH_FACE_OFFSETS: src = m->ex.face_offsets; break;
+        case RIA_MESH_FACE_VERTS: src = m->ex.face_verts; break;
+        case RIA_MESH_FACE_TET_OFFSETS: src = m->ex.face_tet_offsets; break;
+        case RIA_MESH_FACE_TETS: src = m->ex.face_tets; break;
+        case RIA_MESH_FACE_FUNC: src = m->ex.face_func; break;
+        case RIA_MESH_FUNC_IN_TET: src = m->func_in_tet; break;
+        case RIA_MESH_START_INDEX: src = m->start_index; break;
+        case RIA_MESH_REC_OFFSETS: src = m->rec_offsets; break;
+        case RIA_MESH_REC_BYTES: src = m->rec_bytes; esz = 1; break;
+        default: return fail(RIA_EINVAL, "unknown field");
+    }
+    if (hi <= lo) return RIA_OK;
+    if (!src) return fail(RIA_EINVAL, "field not available on this mesh");
+    RIA_CUDA(cudaMemcpyAsync(dst, (const uint8_t*)src + esz * lo, esz * (size_t)(hi - lo), cudaMemcpyDeviceToHost, m->s));
+    RIA_CUDA(cudaStreamSynchronize(m->s));
+    // ids relative to the problem
+    int64_t* d = (int64_t*)dst;
+    const int64_t n = hi - lo;
+    switch (f) {
+        case RIA_MESH_VERTS:
+            for (int64_t i = 0; i < n; i += 11) {
+                d[i] -= b.tbase;
+                for (int j = 3; j < 7; ++j)
+                    if (d[i + j] >= 0) d[i + j] -= b.vbase;
+            }
+            break;
+        case RIA_MESH_FACE_OFFSETS:
+        case RIA_MESH_FACE_TET_OFFSETS:
+        case RIA_MESH_START_INDEX:
+        case RIA_MESH_REC_OFFSETS: {
+            const int64_t base = d[0];
+            for (int64_t i = 0; i < n; ++i) d[i] -= base;
+            break;
+        }
+        case RIA_MESH_FACE_VERTS:
+            for (int64_t i = 0; i < n; ++i) d[i] -= b.vfirst;
+            break;
+        case RIA_MESH_FACE_TETS:
+            for (int64_t i = 0; i < n; i += 2) d[i] -= b.tbase;
+            break;
+        default:
+            break;
+    }
     return RIA_OK;
 }
 

@@ -459,7 +459,7 @@ struct IACut {
     // ---- canonical form
     uint8_t vorder[MV], vnew[MV];
     uint8_t corder[MC], cnew[MC];
-    uint8_t forder[MF];
+    uint16_t forder[MF];  // face ids exceed 8 bits in the exact variant
     int loop_total;
 
     RIA_HD uint32_t vkey(int v) const { return ((uint32_t)lab[v][0] << 16) | ((uint32_t)lab[v][1] << 8) | lab[v][2]; }
@@ -512,12 +512,12 @@ struct IACut {
         for (int i = 0; i < nc; ++i) cnew[corder[i]] = (uint8_t)i;
         uint32_t fkey[MF];
         for (int f = 0; f < nf; ++f) {
-            forder[f] = (uint8_t)f;
+            forder[f] = (uint16_t)f;
             fkey[f] = face_key(f);
         }
         for (int x = 1; x < nf; ++x)
             for (int y = x; y > 0 && fkey[forder[y - 1]] > fkey[forder[y]]; --y) {
-                uint8_t t = forder[y];
+                uint16_t t = forder[y];
                 forder[y] = forder[y - 1];
                 forder[y - 1] = t;
             }

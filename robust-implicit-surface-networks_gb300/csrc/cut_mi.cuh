@@ -138,9 +138,26 @@ struct MICut {
         k = kk;
         if (k > 60) return CUT_FAIL;
         group_materials();
+        // A material b >= a at all four corners leaves the half-space a >= b without interior in the
+        // tet (values are linear), so a owns no cell; if b > a at all corners, a never reaches the
+        // maximum anywhere in the tet and its half-space clips nothing.  Both are skipped; the result
+        // is the same as clipping with them.
+        uint64_t no_cell = 0, no_clip = 0;
+        for (int a = 0; a < k; ++a) {
+            if (rep[a] != 4 + a) continue;
+            const double* x = mt + 4 * a;
+            for (int b = 0; b < k; ++b) {
+                if (b == a || rep[b] != 4 + b) continue;
+                const double* y = mt + 4 * b;
+                if (y[0] >= x[0] && y[1] >= x[1] && y[2] >= x[2] && y[3] >= x[3]) {
+                    no_cell |= bit64(a);
+                    if (y[0] > x[0] && y[1] > x[1] && y[2] > x[2] && y[3] > x[3]) no_clip |= bit64(a);
+                }
+            }
+        }
         onv = onf = onc = oloop = 0;
         for (int m = 4; m < 4 + k; ++m) {
-            if (rep[m - 4] != m) continue;
+            if (rep[m - 4] != m || (no_cell & bit64(m - 4))) continue;
             // the whole tet, labelled with material m
             nv = 4;
             for (int c = 0; c < 4; ++c) {
@@ -161,7 +178,7 @@ struct MICut {
             }
             bool empty = false;
             for (int j = 4; j < 4 + k; ++j) {
-                if (j == m || rep[j - 4] != j) continue;
+                if (j == m || rep[j - 4] != j || (no_clip & bit64(j - 4))) continue;
                 const double* qv = row_of(j);
                 uint8_t live[PV];
                 for (int v = 0; v < nv; ++v) live[v] = 0;
@@ -396,7 +413,8 @@ struct MICut {
     }
 
     // ---- canonical form
-    uint8_t vorder[OV], vnew[OV], forder[OF];
+    uint8_t vorder[OV], vnew[OV];
+    uint16_t forder[OF];  // face ids exceed 8 bits in the exact variant
 
     RIA_HDI void canonicalize() {
         pair_faces();
@@ -408,11 +426,11 @@ struct MICut {
                 vorder[y - 1] = t;
             }
         for (int i = 0; i < onv; ++i) vnew[vorder[i]] = (uint8_t)i;
-        for (int i = 0; i < onf; ++i) forder[i] = (uint8_t)i;
+        for (int i = 0; i < onf; ++i) forder[i] = (uint16_t)i;
         auto fk = [&](int f) { return ((int)opos[f] << 8) | oneg[f]; };
         for (int x = 1; x < onf; ++x)
             for (int y = x; y > 0 && fk(forder[y - 1]) > fk(forder[y]); --y) {
-                uint8_t t = forder[y];
+                uint16_t t = forder[y];
                 forder[y] = forder[y - 1];
                 forder[y - 1] = t;
             }

@@ -102,7 +102,16 @@ struct IAView {
     }
     __device__ __forceinline__ int supp(int f) const { return faces[8 * f]; }
     __device__ __forceinline__ bool bnd(int f) const { return faces[8 * f + 1] & 1; }
+    __device__ __forceinline__ int pos(int f) const { return rd16(faces + 8 * f + 2); }
+    __device__ __forceinline__ int neg(int f) const { return rd16(faces + 8 * f + 4); }
     __device__ __forceinline__ int len(int f) const { return rd16(faces + 8 * f + 6); }
+    // sign vector of cell c (bit 4+j: positive side of inserted plane 4+j); b is the record start
+    __device__ __forceinline__ uint64_t cell(const uint8_t* b, int c) const {
+        const uint8_t* p = loops + 2 * rd16(b + 8) + 8 * c;
+        uint64_t x = 0;
+        for (int i = 7; i >= 0; --i) x = (x << 8) | p[i];
+        return x;
+    }
     __device__ __forceinline__ int loopv(int idx) const { return rd16(loops + 2 * idx); }
     __device__ __forceinline__ bool plane_is_iso(int p) const {
         if (p > 3) return true;

@@ -14,6 +14,7 @@
 #pragma once
 #include <cstdint>
 #include <cmath>
+#include <cstring>
 
 #if defined(__CUDACC__)
 #define RIA_HD __host__ __device__ __forceinline__
@@ -266,27 +267,112 @@ RIA_HD double det_err_coeff(int n) {
 // For a query row r: det([A; r]) = sum_i r_i N_i and the sign of the query at P is
 // sign(det([A; r])) * sigma with sigma = sign(det([A; z])), z = (1 on S, 0 on the level column).
 struct VCache {
-    double N[5];
-    double E[5];
+    float N[5];  // sigma * cofactors from the FP32 filter (valid when f32)
+    float E[5];  // their error bounds against the exact cofactors of the FP64 inputs
     int8_t s, m;
     int8_t mi;
     int8_t sigma;
     uint8_t S[4];
+    uint8_t f32;
 };
 
-// rows[r] points at the 4 corner values of defining row r.  Returns false when sigma cannot be
-// decided by the filter and `exact` is false (or the exact evaluation overflowed).
-RIA_HD bool vcache_build(VCache& c, bool mi, int s, const uint8_t* S, int m, const double* const* rows, bool exact) {
-    c.mi = mi;
-    c.s = (int8_t)s;
-    c.m = (int8_t)m;
-    for (int i = 0; i < 4; ++i) c.S[i] = i < s ? S[i] : 0;
-    const int nc = m + 1;
-    double A[4 * 5];
-    for (int r = 0; r < m; ++r) {
-        for (int i = 0; i < s; ++i) A[r * nc + i] = rows[r][S[i]];
-        if (mi) A[r * nc + s] = 1.0;
+// ---- FP32 filter
+//
+// GB300 issues FP32 at many times its FP64 rate, so the predicates are tried in FP32 first.  Inputs
+// are truncated to FP32 bit-exactly with integer operations (relative error below 2^-23); a
+// nonzero input outside [2^-24, 2^24) leaves the FP32 filter out for that vertex or query.  With
+// every input in that range no product of up to five inputs leaves the normal FP32 range; products
+// of inputs with cancelled (possibly subnormal) minors are covered by an absolute term 2^-60 that
+// exceeds the worst accumulated underflow error (fewer than 2^7 products, each off by at most
+// 2^-150 and scaled by at most 2^72 through the remaining levels).
+
+constexpr float kU32 = 5.9604644775390625e-8f;       // 2^-24
+constexpr float kAbs32 = 8.673617379884035e-19f;      // 2^-60
+
+RIA_HD bool to_f32(double x, float& f) {
+#if defined(__CUDA_ARCH__)
+    const uint64_t b = (uint64_t)__double_as_longlong(x);
+#else
+    uint64_t b;
+    std::memcpy(&b, &x, 8);
+#endif
+    const uint64_t mag = b & 0x7FFFFFFFFFFFFFFFull;
+    if (mag == 0) {
+        f = 0.0f;
+        return true;
     }
+    const int e = (int)(mag >> 52) - 1023;
+    if (e < -24 || e > 23) return false;
+    const uint32_t fb = ((uint32_t)(b >> 32) & 0x80000000u) | ((uint32_t)(e + 127) << 23) |
+                        ((uint32_t)(mag >> 29) & 0x7FFFFFu);
+#if defined(__CUDA_ARCH__)
+    f = __int_as_float((int)fb);
+#else
+    std::memcpy(&f, &fb, 4);
+#endif
+    return true;
+}
+
+RIA_HD int popc32(unsigned x) {
+#if defined(__CUDA_ARCH__)
+    return __popc(x);
+#else
+    return __builtin_popcount(x);
+#endif
+}
+
+// All M+1 maximal minors of an M x (M+1) matrix (signed as cofactors of an appended row) and their
+// permanents, from shared minors of the bottom rows: the minor of rows M-j..M-1 on a column set is
+// the Laplace expansion along row M-j, so each value is the same expansion as a full recursive
+// Laplace evaluation, with its error bound (c_1 = 0, c_j = c_{j-1} + j).
+template <int M>
+RIA_HD void cofactors_f32(const float* A, float* N, float* P) {
+    constexpr int NC = M + 1;
+    float D[1 << NC], Q[1 << NC];
+#pragma unroll
+    for (int mask = 1; mask < (1 << NC); ++mask) {
+        const int j = popc32((unsigned)mask);
+        if (j > M) continue;
+        const int row = M - j;
+        float acc = 0.0f, pacc = 0.0f;
+        int t = 0;
+#pragma unroll
+        for (int c = 0; c < NC; ++c) {
+            if (!(mask & (1 << c))) continue;
+            const float a = A[row * NC + c];
+            const int sub = mask & ~(1 << c);
+            if (j == 1) {
+                acc = a;
+                pacc = fabsf(a);
+            } else {
+                const float term = a * D[sub];
+                acc = (t & 1) ? acc - term : acc + term;
+                pacc = pacc + fabsf(a) * Q[sub];
+            }
+            ++t;
+        }
+        D[mask] = acc;
+        Q[mask] = pacc;
+    }
+#pragma unroll
+    for (int i = 0; i < NC; ++i) {
+        const int mask = ((1 << NC) - 1) & ~(1 << i);
+        const float v = (M == 0) ? 1.0f : D[mask];
+        N[i] = ((M + i) & 1) ? -v : v;
+        P[i] = (M == 0) ? 0.0f : Q[mask];
+    }
+}
+
+// (2M + c_M) u with 2% headroom: 2M u for the truncated inputs, c_M u for the evaluation
+RIA_HD float err_coeff_f32(int m) {
+    const float k = m <= 0 ? 0.0f : (m == 1 ? 2.0f : (m == 2 ? 6.0f : (m == 3 ? 11.0f : 17.0f)));
+    return 1.02f * k * kU32;
+}
+
+// ---- FP64 filter (the fallback when the FP32 filter cannot decide)
+
+RIA_HD void cofactors_f64(const double* A, int m, double* N, double* E) {
+    const int nc = m + 1;
     for (int i = 0; i < nc; ++i) {
         double minor[16];
         for (int r = 0; r < m; ++r) {
@@ -296,15 +382,60 @@ RIA_HD bool vcache_build(VCache& c, bool mi, int s, const uint8_t* S, int m, con
         }
         double perm = 0.0;
         double v = (m == 0) ? 1.0 : det_fp(minor, m, perm);
-        c.N[i] = ((m + i) & 1) ? -v : v;
-        c.E[i] = det_err_coeff(m) * perm;
+        N[i] = ((m + i) & 1) ? -v : v;
+        E[i] = det_err_coeff(m) * perm;
     }
+}
+
+RIA_HD void vcache_matrix(const VCache& c, const double* const* rows, double* A) {
+    const int nc = c.m + 1;
+    for (int r = 0; r < c.m; ++r) {
+        for (int i = 0; i < c.s; ++i) A[r * nc + i] = rows[r][c.S[i]];
+        if (c.mi) A[r * nc + c.s] = 1.0;
+    }
+}
+
+// rows[r] points at the 4 corner values of defining row r.  Returns false when sigma cannot be
+// decided by the filters and `exact` is false (or the exact evaluation overflowed).
+RIA_HD bool vcache_build(VCache& c, bool mi, int s, const uint8_t* S, int m, const double* const* rows, bool exact) {
+    c.mi = mi;
+    c.s = (int8_t)s;
+    c.m = (int8_t)m;
+    for (int i = 0; i < 4; ++i) c.S[i] = i < s ? S[i] : 0;
+    const int nc = m + 1;
+    double A[4 * 5];
+    vcache_matrix(c, rows, A);
+    float A32[4 * 5];
+    bool ok = true;
+    for (int k = 0; k < m * nc; ++k) ok = to_f32(A[k], A32[k]) && ok;
+    c.f32 = ok ? 1 : 0;
     int sig = 0;
-    for (int i = 0; i < s; ++i)
-        if (fabs(c.N[i]) > c.E[i]) {
-            sig = c.N[i] > 0 ? 1 : -1;
-            break;
+    if (ok) {
+        float P[5];
+        switch (m) {
+            case 0: cofactors_f32<0>(A32, c.N, P); break;
+            case 1: cofactors_f32<1>(A32, c.N, P); break;
+            case 2: cofactors_f32<2>(A32, c.N, P); break;
+            case 3: cofactors_f32<3>(A32, c.N, P); break;
+            default: cofactors_f32<4>(A32, c.N, P); break;
         }
+        const float k = err_coeff_f32(m);
+        for (int i = 0; i < nc; ++i) c.E[i] = P[i] == 0.0f ? 0.0f : k * P[i] + kAbs32;
+        for (int i = 0; i < s; ++i)
+            if (fabsf(c.N[i]) > c.E[i]) {
+                sig = c.N[i] > 0.0f ? 1 : -1;
+                break;
+            }
+    }
+    if (sig == 0) {
+        double N[5], E[5];
+        cofactors_f64(A, m, N, E);
+        for (int i = 0; i < s; ++i)
+            if (fabs(N[i]) > E[i]) {
+                sig = N[i] > 0 ? 1 : -1;
+                break;
+            }
+    }
     if (sig == 0) {
         if (!exact) return false;
         double M[25];
@@ -315,23 +446,50 @@ RIA_HD bool vcache_build(VCache& c, bool mi, int s, const uint8_t* S, int m, con
         if (sig == 0 || sig == 2) return false;
     }
     c.sigma = (int8_t)sig;
-    for (int i = 0; i < nc; ++i) c.N[i] *= (double)sig;
+    if (ok)
+        for (int i = 0; i < nc; ++i) c.N[i] = sig > 0 ? c.N[i] : -c.N[i];
     return true;
 }
 
-// Sign of the query row q (4 corner values) at the vertex: -1, 0, 1; or 2 when the filter cannot
+// Sign of the query row q (4 corner values) at the vertex: -1, 0, 1; or 2 when the filters cannot
 // decide and `exact` is false (or the exact evaluation overflowed).  `rows` are the defining rows.
 RIA_HD int vcache_query(const VCache& c, const double* q, const double* const* rows, bool exact) {
     const int nc = c.m + 1;
     double r[5];
     for (int i = 0; i < c.s; ++i) r[i] = q[c.S[i]];
     if (c.mi) r[c.s] = 1.0;
+    if (c.f32) {
+        float r32[5];
+        bool ok = true;
+        for (int i = 0; i < nc; ++i) ok = to_f32(r[i], r32[i]) && ok;
+        if (ok) {
+            // |v32 - v| <= 1.02 ((nc + 2) u mag + sum |r_i| E_i) + 2^-60: nc u for the evaluation, 2u for
+            // the truncated query, the cofactor bounds E for the rest
+            float v = 0.0f, mag = 0.0f, err = 0.0f;
+            bool zero = true;
+            for (int i = 0; i < nc; ++i) {
+                const float t = r32[i] * c.N[i];
+                v = v + t;
+                mag = mag + fabsf(t);
+                err = err + fabsf(r32[i]) * c.E[i];
+                zero = zero && (r32[i] == 0.0f || (c.N[i] == 0.0f && c.E[i] == 0.0f));
+            }
+            if (zero) return 0;  // every term is exactly zero
+            const float bound = 1.02f * ((float)(nc + 2) * kU32 * mag + err) + kAbs32;
+            if (v > bound) return 1;
+            if (v < -bound) return -1;
+        }
+    }
+    double A[4 * 5];
+    vcache_matrix(c, rows, A);
+    double N[5], E[5];
+    cofactors_f64(A, c.m, N, E);
     double v = 0.0, mag = 0.0, err = 0.0;
     for (int i = 0; i < nc; ++i) {
-        double t = r[i] * c.N[i];
+        double t = r[i] * (N[i] * (double)c.sigma);
         v += t;
         mag += fabs(t);
-        err += fabs(r[i]) * c.E[i];
+        err += fabs(r[i]) * E[i];
     }
     double bound = 1.01 * ((double)(nc + 1) * kU * mag + err);
     if (v > bound) return 1;
@@ -339,10 +497,8 @@ RIA_HD int vcache_query(const VCache& c, const double* q, const double* const* r
     if (bound == 0.0) return 0;
     if (!exact) return 2;
     double M[25];
-    for (int rr = 0; rr < c.m; ++rr) {
-        for (int i = 0; i < c.s; ++i) M[rr * nc + i] = rows[rr][c.S[i]];
-        if (c.mi) M[rr * nc + c.s] = 1.0;
-    }
+    for (int rr = 0; rr < c.m; ++rr)
+        for (int j = 0; j < nc; ++j) M[rr * nc + j] = A[rr * nc + j];
     for (int j = 0; j < nc; ++j) M[c.m * nc + j] = r[j];
     int sg = det_sign_exact(M, nc);
     if (sg == 2) return 2;

@@ -13,6 +13,8 @@
 //   MI filter    src/material_interface.cpp:94-152
 // The compaction keeps tet order (per-block counts, an exclusive scan, warp-ballot ranks) so the
 // active-function CRS and the first-occurrence numbering of the extraction follow the reference.
+#include <math_constants.h>
+
 #include "device_common.cuh"
 #include "launch.hpp"
 
@@ -293,11 +295,22 @@ __device__ __forceinline__ int tet_pattern(const ulonglong2* __restrict__ vmask,
     return p;
 }
 
+// bin of a general-case tet: the heaviest (most active functions) first, so that a warp cuts tets of
+// one size and the longest cuts start first
+template <bool MI>
+__device__ __forceinline__ int gen_bin(int k) {
+    const int kk = k - (MI ? 1 : 0);
+    return kGenBins - (kk < kGenBins ? kk : kGenBins);
+}
+
+// per block: the active count, then the general-case count of each bin; layout [1 + kGenBins][nb]
 template <bool MI>
 __global__ void __launch_bounds__(kBlock) k_filter_count(const ulonglong2* __restrict__ vmask,
                                                          const double* __restrict__ fv, int F, TetSrc ts, int64_t T,
                                                          bool use_table, uint32_t* __restrict__ blk,
                                                          unsigned long long* __restrict__ khist) {
+    __shared__ uint32_t bins[kGenBins];
+    if (threadIdx.x < kGenBins) bins[threadIdx.x] = 0;
     const int64_t t = (int64_t)blockIdx.x * kBlock + threadIdx.x;
     int k = 0;
     if (t < T) {
@@ -308,18 +321,21 @@ __global__ void __launch_bounds__(kBlock) k_filter_count(const ulonglong2* __res
     const int ka = MI ? 2 : 1;
     int act = k > 0;
     int gen = act && !(use_table && k == ka);
-    int na = __syncthreads_count(act);
-    int ng = __syncthreads_count(gen);
+    int na = __syncthreads_count(act);  // also orders the zeroing of bins before the adds
+    const unsigned full = 0xFFFFFFFFu;
+    const int lane = threadIdx.x & 31;
+    const unsigned same = __match_any_sync(full, gen ? gen_bin<MI>(k) : -1);
+    if (gen && lane == __ffs(same) - 1) atomicAdd(&bins[gen_bin<MI>(k)], (uint32_t)__popc(same));
     int h0 = __syncthreads_count(k == ka);
     int h1 = __syncthreads_count(k == ka + 1);
     int h2 = __syncthreads_count(k > ka + 1);
     if (threadIdx.x == 0) {
         blk[blockIdx.x] = (uint32_t)na;
-        blk[gridDim.x + blockIdx.x] = (uint32_t)ng;
         if (h0) atomicAdd(&khist[0], (unsigned long long)h0);
         if (h1) atomicAdd(&khist[1], (unsigned long long)h1);
         if (h2) atomicAdd(&khist[2], (unsigned long long)h2);
     }
+    if (threadIdx.x < kGenBins) blk[(1 + threadIdx.x) * (int64_t)gridDim.x + blockIdx.x] = bins[threadIdx.x];
 }
 
 template <bool MI>
@@ -328,7 +344,9 @@ __global__ void __launch_bounds__(kBlock) k_filter_scatter(const ulonglong2* __r
                                                            int64_t T, bool use_table,
                                                            const uint32_t* __restrict__ blk_off,
                                                            const IASum4* __restrict__ table_sum, FilterOut out) {
-    __shared__ int wa[kBlock / 32], wg[kBlock / 32];
+    __shared__ int wa[kBlock / 32];
+    __shared__ int wg[kGenBins][kBlock / 32];
+    for (int i = threadIdx.x; i < kGenBins * (kBlock / 32); i += kBlock) (&wg[0][0])[i] = 0;
     const int64_t t = (int64_t)blockIdx.x * kBlock + threadIdx.x;
     uint64_t act = 0;
     int64_t v[4] = {0, 0, 0, 0};
@@ -340,27 +358,27 @@ __global__ void __launch_bounds__(kBlock) k_filter_scatter(const ulonglong2* __r
     const int ka = MI ? 2 : 1;
     const bool isact = k > 0;
     const bool isgen = isact && !(use_table && k == ka);
+    const int bin = isgen ? gen_bin<MI>(k) : -1;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const unsigned lt = (1u << lane) - 1;
-    unsigned ba = __ballot_sync(0xFFFFFFFFu, isact), bg = __ballot_sync(0xFFFFFFFFu, isgen);
-    if (lane == 0) {
-        wa[warp] = __popc(ba);
-        wg[warp] = __popc(bg);
-    }
+    const unsigned ba = __ballot_sync(0xFFFFFFFFu, isact);
+    const unsigned same = __match_any_sync(0xFFFFFFFFu, bin);
+    __syncthreads();  // wg zeroed
+    if (lane == 0) wa[warp] = __popc(ba);
+    if (isgen && lane == __ffs(same) - 1) wg[bin][warp] = __popc(same);
     __syncthreads();
     int pa = 0, pg = 0;
     for (int w = 0; w < warp; ++w) {
         pa += wa[w];
-        pg += wg[w];
+        if (isgen) pg += wg[bin][w];
     }
-    const uint32_t base_a = blk_off[blockIdx.x];
-    const uint32_t base_g = blk_off[gridDim.x + blockIdx.x] - blk_off[gridDim.x];
     if (isact) {
-        uint32_t a = base_a + pa + __popc(ba & lt);
+        uint32_t a = blk_off[blockIdx.x] + pa + __popc(ba & lt);
         out.act_tet[a] = (uint32_t)t;
         out.act_mask[a] = act;
         if (isgen) {
-            out.gen[base_g + pg + __popc(bg & lt)] = a;
+            const uint32_t base_g = blk_off[(1 + bin) * (int64_t)gridDim.x + blockIdx.x] - blk_off[gridDim.x];
+            out.gen[base_g + pg + __popc(same & lt)] = a;
             out.act_desc[a] = 0;
         } else {
             int p = tet_pattern<MI>(vmask, fv, F, v, act);
@@ -377,6 +395,155 @@ __global__ void k_check_tets(const int64_t* __restrict__ tets, int64_t n, int64_
             raise_status(status, ST_BADINPUT);
             return;
         }
+    }
+}
+
+// ---- batched grids
+
+__device__ __forceinline__ int upper_index(const int64_t* base, int n, int64_t x) {
+    // largest p in [0, n) with base[p] <= x (base ascending, base[0] = 0)
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (base[mid] <= x) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ int upper_index32(const uint32_t* base, int n, uint32_t x) {
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (base[mid] <= x) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+// One block holds vertices of one problem.  Coordinates follow src/io.cpp:104-106 and every value
+// is the full formula at the vertex (the same operations, in the same order, as the separable grid
+// sampler), so each problem's values equal those of its own grid call.
+template <bool MI>
+__global__ void __launch_bounds__(kBatchSampleBlock)
+    k_batch_sample(const BatchProblem* __restrict__ probs, int n, const uint32_t* __restrict__ blk_off,
+                   const ria_function* __restrict__ funcs, int Fmax, double* __restrict__ pts,
+                   double* __restrict__ fv, ulonglong2* __restrict__ vmask, unsigned long long* __restrict__ n_zero,
+                   unsigned long long* __restrict__ n_zero_p) {
+    extern __shared__ double tile[];
+    const int stride = Fmax + 1;
+    const int p = upper_index32(blk_off, n, blockIdx.x);
+    const BatchProblem pr = probs[p];
+    const int N = pr.res + 1;
+    const int64_t Vp = (int64_t)N * N * N;
+    const int64_t l0 = (int64_t)(blockIdx.x - blk_off[p]) * kBatchSampleBlock;
+    const int64_t lv = l0 + threadIdx.x;
+    const bool valid = lv < Vp;
+    double x[3] = {0.0, 0.0, 0.0};
+    if (valid) {
+        const int vi = (int)lv;
+        const int ix[3] = {vi / (N * N), (vi / N) % N, vi % N};
+        for (int a = 0; a < 3; ++a)
+            x[a] = ((double)ix[a] / (double)(N - 1)) * (pr.bmax[a] - pr.bmin[a]) + pr.bmin[a];
+        double* dst = pts + 3 * (pr.vbase + lv);
+        dst[0] = x[0];
+        dst[1] = x[1];
+        dst[2] = x[2];
+    }
+    uint64_t m0 = 0, m1 = 0;
+    double mx = 0.0;
+    for (int f = 0; f < Fmax; ++f) {
+        double val;
+        if (f < pr.F) {
+            const ria_function& fn = funcs[pr.foff + f];
+            double w0[3], w1[3];
+            for (int a = 0; a < 3; ++a) axis_parts(fn, a, x[a], w0[a], w1[a]);
+            val = combine_parts(fn, w0, w1);
+        } else {
+            val = MI ? -CUDART_INF : 1.0;
+        }
+        tile[threadIdx.x * stride + f] = val;
+        if (!MI) {
+            if (val > 0.0) m0 |= bit64(f);
+            else if (val < 0.0) m1 |= bit64(f);
+        } else {
+            if (f == 0 || val > mx) {
+                mx = val;
+                m0 = bit64(f);
+            } else if (val == mx) {
+                m0 |= bit64(f);
+            }
+        }
+    }
+    int nz = 0;
+    if (valid) {
+        vmask[pr.vbase + lv] = make_ulonglong2(m0, m1);
+        nz = MI ? (__popcll(m0) > 1) : (Fmax - __popcll(m0) - __popcll(m1));
+    }
+    __syncthreads();
+    const int warp = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31;
+    for (int r = warp; r < kBatchSampleBlock; r += kBatchSampleBlock / 32) {
+        if (l0 + r >= Vp) break;
+        double* dst = fv + (pr.vbase + l0 + r) * Fmax;
+        for (int c = lane; c < Fmax; c += 32) dst[c] = tile[r * stride + c];
+    }
+    block_add(n_zero, nz);
+    block_add(n_zero_p + p, nz);
+}
+
+__global__ void k_batch_tets(const BatchProblem* __restrict__ probs, const int64_t* __restrict__ tet_base, int n,
+                             int64_t T, int64_t* __restrict__ tets) {
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < T; t += (int64_t)gridDim.x * blockDim.x) {
+        const int p = upper_index(tet_base, n, t);
+        int64_t v[4];
+        grid_tet(t - tet_base[p], probs[p].res, v);
+        const int64_t vb = probs[p].vbase;
+        longlong2* dst = reinterpret_cast<longlong2*>(tets + 4 * t);
+        dst[0] = make_longlong2(v[0] + vb, v[1] + vb);
+        dst[1] = make_longlong2(v[2] + vb, v[3] + vb);
+    }
+}
+
+// first index i in [0, m) with key(i) >= x (key non-decreasing), or m
+template <class Key>
+__device__ __forceinline__ int64_t lower_index(int64_t m, int64_t x, Key key) {
+    int64_t lo = 0, hi = m;
+    while (lo < hi) {
+        const int64_t mid = (lo + hi) >> 1;
+        if (key(mid) < x) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
+}
+
+__global__ void k_batch_ranges(const int64_t* __restrict__ tet_base, int n, const int64_t* __restrict__ verts,
+                               int64_t n_verts, const int64_t* __restrict__ fto, const int64_t* __restrict__ ftets,
+                               int64_t n_faces, int64_t* __restrict__ vert_first, int64_t* __restrict__ face_first) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p > n) return;
+    if (p == n) {
+        vert_first[n] = n_verts;
+        face_first[n] = n_faces;
+        return;
+    }
+    const int64_t tb = tet_base[p];
+    vert_first[p] = lower_index(n_verts, tb, [&](int64_t i) { return verts[11 * i]; });
+    face_first[p] = lower_index(n_faces, tb, [&](int64_t f) { return ftets[2 * fto[f]]; });
+}
+
+// stats4[4 p + 0..3]: active tets, k == a, k == a + 1, k > a + 1 (a = 1 IA, 2 MI)
+template <bool MI>
+__global__ void k_batch_active_stats(const int64_t* __restrict__ tet_base, int n, const uint32_t* __restrict__ act_tet,
+                                     const uint64_t* __restrict__ act_mask, int64_t A,
+                                     unsigned long long* __restrict__ stats4) {
+    const int ka = MI ? 2 : 1;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < A; i += (int64_t)gridDim.x * blockDim.x) {
+        const int p = upper_index(tet_base, n, (int64_t)act_tet[i]);
+        const int k = __popcll(act_mask[i]);
+        unsigned long long* st = stats4 + 4 * p;
+        atomicAdd(st, 1ull);
+        atomicAdd(st + (k == ka ? 1 : (k == ka + 1 ? 2 : 3)), 1ull);
     }
 }
 
@@ -440,6 +607,53 @@ void launch_vertex_masks(bool mi, const double* fv, int64_t V, int F, ulonglong2
             k_vertex_masks<false><<<(unsigned)blocks, kBlock, smem, s>>>(fv, V, F, vmask, n_zero);
             note_launch();
         }
+}
+
+void launch_batch_sample(bool mi, const BatchProblem* probs, int n, const uint32_t* blk_off, uint32_t n_blocks,
+                         const ria_function* funcs, int Fmax, double* pts, double* fv, ulonglong2* vmask,
+                         unsigned long long* n_zero, unsigned long long* n_zero_p, cudaStream_t s) {
+    if (n_blocks == 0) return;
+    const size_t smem = sizeof(double) * kBatchSampleBlock * (Fmax + 1);
+    static bool attr[2] = {false, false};
+    if (!attr[mi] && smem > 48 * 1024) {
+        if (mi) cudaFuncSetAttribute(k_batch_sample<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024);
+        else cudaFuncSetAttribute(k_batch_sample<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024);
+        attr[mi] = true;
+    }
+    if (mi)
+        k_batch_sample<true><<<n_blocks, kBatchSampleBlock, smem, s>>>(probs, n, blk_off, funcs, Fmax, pts, fv, vmask,
+                                                                       n_zero, n_zero_p);
+    else
+        k_batch_sample<false><<<n_blocks, kBatchSampleBlock, smem, s>>>(probs, n, blk_off, funcs, Fmax, pts, fv, vmask,
+                                                                        n_zero, n_zero_p);
+    note_launch();
+}
+
+void launch_batch_tets(const BatchProblem* probs, const int64_t* tet_base, int n, int64_t T, int64_t* tets,
+                       cudaStream_t s) {
+    if (T == 0) return;
+    int64_t blocks = (T + 255) / 256;
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    k_batch_tets<<<(unsigned)blocks, 256, 0, s>>>(probs, tet_base, n, T, tets);
+    note_launch();
+}
+
+void launch_batch_ranges(const int64_t* tet_base, int n, const int64_t* verts, int64_t n_verts,
+                         const int64_t* face_tet_offsets, const int64_t* face_tets, int64_t n_faces,
+                         int64_t* vert_first, int64_t* face_first, cudaStream_t s) {
+    k_batch_ranges<<<(unsigned)((n + 1 + 127) / 128), 128, 0, s>>>(tet_base, n, verts, n_verts, face_tet_offsets,
+                                                                    face_tets, n_faces, vert_first, face_first);
+    note_launch();
+}
+
+void launch_batch_active_stats(bool mi, const int64_t* tet_base, int n, const uint32_t* act_tet,
+                               const uint64_t* act_mask, int64_t A, unsigned long long* stats4, cudaStream_t s) {
+    if (A == 0) return;
+    int64_t blocks = (A + 255) / 256;
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    if (mi) k_batch_active_stats<true><<<(unsigned)blocks, 256, 0, s>>>(tet_base, n, act_tet, act_mask, A, stats4);
+    else k_batch_active_stats<false><<<(unsigned)blocks, 256, 0, s>>>(tet_base, n, act_tet, act_mask, A, stats4);
+    note_launch();
 }
 
 void launch_check_tets(const int64_t* d_tets, int64_t T, int64_t V, uint32_t* status, cudaStream_t s) {

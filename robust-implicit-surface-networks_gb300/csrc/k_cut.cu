@@ -3,8 +3,8 @@
 //   k_cut_fast   one thread per tet, state in local memory, FP64-filtered predicates only.  A tet
 //                whose predicate the filter cannot decide, or that outgrows the small capacities,
 //                is appended to a deferred list.
-//   k_cut_big    a fixed pool of threads, each with a state slot in global scratch memory, exact
-//                predicates and large capacities, walks the deferred list.
+//   k_cut_big    one tet per block at a time, its state in dynamic shared memory, exact
+//                predicates and large capacities; walks the deferred list.
 //   k_build_table  the 81-pattern lookup tables (IA: one active plane; MI: two active
 //                materials), computed on the device by the exact variant from one representative
 //                tet per sign pattern (corner values in {-1, 0, 1}).
@@ -12,6 +12,7 @@
 // the result, which only depends on the per-tet record contents.
 #include "device_common.cuh"
 #include "launch.hpp"
+#include "lookup2.cuh"
 
 namespace ria {
 
@@ -76,27 +77,79 @@ __device__ __forceinline__ int gather_planes(const CutArgs& a, uint32_t ai, doub
     return k;
 }
 
+// returns the record's place in the heap (nullptr on overflow)
 template <class Cut, class Sum>
-__device__ __forceinline__ void finish_cut(const CutArgs& a, uint32_t ai, Cut& c) {
+__device__ __forceinline__ const uint8_t* finish_cut(const CutArgs& a, uint32_t ai, Cut& c, int* size_out,
+                                                     IASum4* sum_out) {
     c.canonicalize();
     const int size = c.record_size();
     unsigned long long off = atomicAdd(a.heap_used, (unsigned long long)size);
     if (off + size > a.heap_cap) {
         raise_status(a.status, ST_CAPACITY);
-        return;
+        return nullptr;
     }
     Sum s;
     c.emit(a.heap + off, s);
+    const IASum4 ps = pack_sum<Sum>(s);
     a.act_desc[ai] = off | a.desc_bit;
-    a.act_sum[ai] = pack_sum<Sum>(s);
+    a.act_sum[ai] = ps;
+    *size_out = size;
+    *sum_out = ps;
+    return a.heap + off;
+}
+
+// ---- secondary lookup: a device-wide cache of canonical records keyed by the combinatorial type
+// (lookup2.cuh), filled on first sight by the general cut and kept for the life of the process.
+// An entry is published after its bytes (fence, then CAS of its slot); readers fence after seeing
+// the slot.  Records depend only on the key, so racing inserts of one key are interchangeable.
+constexpr int kCacheProbes = 32;
+
+__device__ __forceinline__ uint32_t cache_hash(uint32_t key, uint32_t mask) {
+    return (uint32_t)mix64((uint64_t)key) & mask;
+}
+
+__device__ __forceinline__ int cache_find(const CutArgs::Cache& c, uint32_t key) {
+    const unsigned long long tag = (unsigned long long)(key + 1u) << 32;
+    const uint32_t h = cache_hash(key, c.slot_mask);
+    for (int p = 0; p < kCacheProbes; ++p) {
+        const unsigned long long v = *reinterpret_cast<volatile const unsigned long long*>(&c.slots[(h + p) & c.slot_mask]);
+        if (v == 0) return -1;
+        if ((v & 0xFFFFFFFF00000000ull) == tag) {
+            __threadfence();
+            return (int)(v & 0xFFFFFFFFull);
+        }
+    }
+    return -1;
+}
+
+__device__ __forceinline__ void cache_insert(const CutArgs::Cache& c, uint32_t key, const uint8_t* rec, int size,
+                                             IASum4 sum) {
+    const unsigned long long j = atomicAdd(c.next, 1ull);
+    if (j >= c.cap) return;
+    const unsigned long long off = atomicAdd(c.heap_used, (unsigned long long)((size + 7) & ~7));
+    if (off + size > c.heap_cap) return;
+    uint8_t* dst = c.table + c.heap_base + off;
+    for (int i = 0; i < size; ++i) dst[i] = rec[i];
+    c.table_off[kTablePatterns + j] = (uint32_t)(c.heap_base + off);
+    c.table_sum[kTablePatterns + j] = sum;
+    __threadfence();
+    const unsigned long long v = ((unsigned long long)(key + 1u) << 32) | j;
+    const uint32_t h = cache_hash(key, c.slot_mask);
+    for (int p = 0; p < kCacheProbes; ++p) {
+        const unsigned long long old = atomicCAS(&c.slots[(h + p) & c.slot_mask], 0ull, v);
+        if (old == 0 || (old >> 32) == (unsigned long long)(key + 1u)) return;
+    }
 }
 
 // Tets whose planes reduce to at most one after grouping (duplicates, planes coincident with a tet
-// face, zero planes): the record comes from the one-plane lookup table, relabelled.
-__device__ __forceinline__ bool ia_try_template(const CutArgs& a, uint32_t ai, const double* planes, int k) {
+// face, zero planes): the record comes from the one-plane lookup table, relabelled.  `two` reports
+// two distinct planes that are neither zero nor a tet face (labels 4, 5: secondary lookup).
+__device__ __forceinline__ bool ia_try_template(const CutArgs& a, uint32_t ai, const double* planes, int k,
+                                                bool* two) {
     uint8_t rep[kFastMaxK];
     int first;
     const int eff = ia_group_planes(planes, k, rep, first);
+    *two = k == 2 && eff == 2 && rep[0] == 4 && rep[1] == 5;
     if (eff > 1 || !a.table) return false;
     const int pattern = eff ? ia_sign_pattern(planes + 4 * first) : kTablePatterns - 1;  // all positive: uncut
     const uint8_t* tmpl = a.table + a.table_off[pattern];
@@ -124,12 +177,31 @@ __global__ void __launch_bounds__(128) k_cut_fast(CutArgs a) {
     const uint32_t ai = a.list[i];
     double planes[4 * kFastMaxK];
     const int k = gather_planes(a, ai, planes, kFastMaxK);
-    if (!MI && k <= kFastMaxK && ia_try_template(a, ai, planes, k)) return;
+    bool keyed = false;
+    if (!MI && k <= kFastMaxK && ia_try_template(a, ai, planes, k, &keyed)) return;
+    if (MI) keyed = k == 3 && mi_distinct3(planes);
+    uint32_t key = 0;
+    if (keyed && a.cache.slots) {
+        keyed = MI ? mi_key3(planes, key) : ia_key2(planes, key);
+        if (keyed) {
+            const int j = cache_find(a.cache, key);
+            if (j >= 0) {
+                a.act_desc[ai] = kTableBit | (uint64_t)(kTablePatterns + j);
+                a.act_sum[ai] = a.cache.table_sum[kTablePatterns + j];
+                return;
+            }
+        }
+    } else {
+        keyed = false;
+    }
     int st = CUT_DEFER;
     Fast c;
     if (k <= kFastMaxK) st = c.run(planes, k);
     if (st == CUT_OK) {
-        finish_cut<Fast, Sum>(a, ai, c);
+        int size = 0;
+        IASum4 sum;
+        const uint8_t* rec = finish_cut<Fast, Sum>(a, ai, c, &size, &sum);
+        if (rec && keyed) cache_insert(a.cache, key, rec, size, sum);
     } else if (st == CUT_DEFER) {
         unsigned int d = atomicAdd(a.n_deferred, 1u);
         a.deferred[d] = ai;
@@ -158,7 +230,9 @@ __global__ void __launch_bounds__(32) k_cut_big(CutArgs a) {
             raise_status(a.status, ST_CAPACITY);
             continue;
         }
-        finish_cut<typename Traits<MI>::Big, Sum>(a, ai, S.cut);
+        int size = 0;
+        IASum4 sum;
+        finish_cut<typename Traits<MI>::Big, Sum>(a, ai, S.cut, &size, &sum);
     }
 }
 
@@ -265,7 +339,10 @@ size_t cut_big_slot_bytes(bool mi) { return mi ? sizeof(BigSlot<true>) : sizeof(
 
 void launch_cut_fast(const CutArgs& a, cudaStream_t s) {
     if (a.n == 0) return;
-    const int bs = 128;
+    // each thread runs one long serial cut: with few tets, smaller blocks spread them over all SMs
+    // (the FP64 pipe of one SM is shared by its resident warps)
+    int bs = 128;
+    while (bs > 32 && (a.n + bs - 1) / bs < 4 * 152) bs >>= 1;
     const unsigned nb = (unsigned)((a.n + bs - 1) / bs);
     if (a.mi)
         {

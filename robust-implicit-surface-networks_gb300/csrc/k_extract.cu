@@ -500,6 +500,115 @@ cudaError_t run_extract(const ExtractArgs& a, const IASum4* act_sum, ExtractOut&
     return cudaGetLastError();
 }
 
+// ---- CSG pruning (src/csg.cpp:55-116): a face separates the shape's inside from its outside when the
+// CSG membership differs on its two sides.  The signs of every function on one side come from the
+// face's tet: inserted planes from the record's cell sign vector, grouped duplicates from their
+// representative and the sign of the ratio, planes on a tet face from the opposite corner, inactive
+// functions from any corner (their sign is constant in the tet).  The other side differs exactly in
+// the functions coincident with the face.
+
+namespace {
+
+__device__ __forceinline__ int local_sign(const IAView& r, uint64_t cs, int li, uint64_t mask, const double* fv,
+                                          int F, const int64_t v[4]) {
+    const int rp = r.rep[li];
+    if (rp == 4 + li) return (cs >> rp) & 1 ? 1 : -1;
+    const int gj = local_func(mask, li);
+    if (rp == 0xFF) return -1;  // the zero function: never inside
+    if (rp < 4) return fv[v[rp] * F + gj] > 0.0 ? 1 : -1;
+    const int g0 = local_func(mask, rp - 4);
+    const int s0 = (cs >> rp) & 1 ? 1 : -1;
+    for (int c = 0; c < 4; ++c) {
+        const double x0 = fv[v[c] * F + g0];
+        if (x0 != 0.0) return ((x0 > 0.0) == (fv[v[c] * F + gj] > 0.0)) ? s0 : -s0;
+    }
+    return -1;
+}
+
+__device__ __forceinline__ bool csg_inside(const CsgArgs& a, uint64_t S, uint64_t full) {
+    const uint64_t in = a.pos_inside ? S : (~S & full);
+    if (a.nprog == 0) return in != 0;
+    uint64_t st = 0;  // stack of booleans, top at bit depth-1
+    int depth = 0;
+    for (int i = 0; i < a.nprog; ++i) {
+        const int t = a.prog[i];
+        if (t >= 0) {
+            st = (st & ~bit64(depth)) | (((in >> t) & 1) << depth);
+            ++depth;
+        } else if (t == -3) {
+            st ^= bit64(depth - 1);
+        } else {
+            const uint64_t x = (st >> (depth - 2)) & 1, y = (st >> (depth - 1)) & 1;
+            const uint64_t z = t == -1 ? (x & y) : (x | y);
+            --depth;
+            st = (st & ~bit64(depth - 1)) | (z << (depth - 1));
+        }
+    }
+    return st & 1;
+}
+
+__global__ void k_csg(CsgArgs a) {
+    const int64_t g = a.f0 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= a.f1) return;
+    const int64_t to = a.face_tet_offsets[g];
+    const int64_t t = a.face_tets[2 * to];
+    const int rf = (int)a.face_tets[2 * to + 1];
+    int64_t lo = 0, hi = a.A;  // active index of t (the active list is in tet order)
+    while (lo < hi) {
+        const int64_t mid = (lo + hi) >> 1;
+        if ((int64_t)a.act_tet[mid] < t) lo = mid + 1;
+        else hi = mid;
+    }
+    const RecSrc rs{a.heap, a.heap_big, a.table, a.table_off};
+    const uint8_t* b = rs.get(a.act_desc[lo]);
+    IAView r;
+    r.init(b);
+    const uint64_t mask = a.act_mask[lo];
+    int64_t v[4];
+    TetSrc ts{a.d_tets, a.res};
+    ts.get(t - a.tbase, v);
+    for (int q = 0; q < 4; ++q) v[q] += a.vbase;
+    const int c = r.pos(rf) != 0xFFFF ? r.pos(rf) : r.neg(rf);
+    const uint64_t cs = r.cell(b, c);
+    const uint64_t full = a.nfunc == 64 ? ~0ull : (bit64(a.nfunc) - 1);
+    uint64_t S = 0;
+    int li = 0;
+    for (int j = 0; j < a.nfunc; ++j) {
+        int sg;
+        if (mask & bit64(j)) sg = local_sign(r, cs, li++, mask, a.fv, a.F, v);
+        else sg = a.fv[v[0] * a.F + j] > 0.0 ? 1 : -1;
+        if (sg > 0) S |= bit64(j);
+    }
+    const int jstar = (int)a.face_func[2 * g];
+    if (jstar < 0) {
+        if (a.sides) a.sides[2 * (g - a.f0)] = a.sides[2 * (g - a.f0) + 1] = S;
+        else a.out[g - a.f0] = 0;
+        return;
+    }
+    const int ls = __popcll(mask & (bit64(jstar) - 1));
+    const int grp = r.rep[ls];
+    uint64_t X = 0;
+    for (int l = 0; l < r.k; ++l)
+        if (r.rep[l] == grp) X |= bit64(local_func(mask, l));
+    const uint64_t Sp = (S >> jstar) & 1 ? S : (S ^ X);
+    if (a.sides) {
+        a.sides[2 * (g - a.f0)] = Sp;
+        a.sides[2 * (g - a.f0) + 1] = Sp ^ X;
+        return;
+    }
+    const bool ip = csg_inside(a, Sp, full), in_ = csg_inside(a, Sp ^ X, full);
+    a.out[g - a.f0] = ip == in_ ? 0 : (ip ? 1 : 2);
+}
+
+}  // namespace
+
+void launch_csg(const CsgArgs& a, cudaStream_t s) {
+    const int64_t n = a.f1 - a.f0;
+    if (n <= 0) return;
+    k_csg<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(a);
+    note_launch();
+}
+
 // ---- per-tet records and the active-function CRS, in tet order
 
 namespace {

@@ -33,8 +33,69 @@ void launch_sample_points(const ria_function* d_funcs, int F, const double* pts,
 void launch_vertex_masks(bool mi, const double* fv, int64_t V, int F, ulonglong2* vmask, unsigned long long* n_zero,
                          cudaStream_t s);
 
+// ---- CSG pruning (k_extract.cu): per face of an implicit-arrangement mesh in [f0, f1): 0 not on the
+// boundary of the shape, 1 inside on the positive side of the face's function, 2 on its negative
+// side.  prog: postfix tokens (>= 0 function, -1 intersection, -2 union, -3 negation); nprog = 0: the
+// union of all functions.  Function j is inside where its sign is positive (pos_inside) or negative.
+struct CsgArgs {
+    int64_t f0, f1;
+    const int64_t* face_tet_offsets;
+    const int64_t* face_tets;
+    const int64_t* face_func;
+    const uint32_t* act_tet;
+    int64_t A;
+    const uint64_t* act_desc;
+    const uint64_t* act_mask;
+    const uint8_t* heap;
+    const uint8_t* heap_big;
+    const uint8_t* table;
+    const uint32_t* table_off;
+    const double* fv;
+    int F;                  // row stride of fv
+    int nfunc;              // functions of the problem (F, or fewer in a batch)
+    const int64_t* d_tets;  // explicit tets, or the grid of `res` cubes with ids offset by tbase / vbase
+    int64_t res, tbase, vbase;
+    const int32_t* prog;
+    int nprog;
+    int pos_inside;
+    uint8_t* out;
+    uint64_t* sides = nullptr;  // instead of labels: per face the sign vectors (bit j: function j > 0)
+                                // on the positive and on the negative side of the face's function
+};
+void launch_csg(const CsgArgs& a, cudaStream_t s);
+
+// ---- batched grids (k_ab.cu): many independent tet5 grids concatenated problem-major
+struct BatchProblem {
+    int64_t vbase, tbase;  // first vertex / tet of the problem in the batch numbering
+    int32_t res, F;        // cubes per axis, functions
+    int32_t foff, pad;     // first function in the concatenated function array
+    double bmin[3], bmax[3];
+};
+// Grid points, values (stride Fmax; columns F..Fmax-1 hold a constant that is never active: +1 for
+// the implicit arrangement, -inf for the material interface) and vertex masks of every problem.
+// blk_off[p] is the first sampling block of problem p (n + 1 entries, blocks of kBatchSampleBlock
+// vertices); n_zero_p receives each problem's degenerate-vertex count.
+constexpr int kBatchSampleBlock = 128;
+void launch_batch_sample(bool mi, const BatchProblem* probs, int n, const uint32_t* blk_off, uint32_t n_blocks,
+                         const ria_function* funcs, int Fmax, double* pts, double* fv, ulonglong2* vmask,
+                         unsigned long long* n_zero, unsigned long long* n_zero_p, cudaStream_t s);
+// explicit tets of every problem (global vertex ids); tet_base[p] = probs[p].tbase, n + 1 entries
+void launch_batch_tets(const BatchProblem* probs, const int64_t* tet_base, int n, int64_t T, int64_t* tets,
+                       cudaStream_t s);
+// per problem: first mesh vertex and first face (n + 1 entries each) and the active-tet statistics
+// (active count, k histogram) from the active lists
+void launch_batch_ranges(const int64_t* tet_base, int n, const int64_t* verts, int64_t n_verts,
+                         const int64_t* face_tet_offsets, const int64_t* face_tets, int64_t n_faces,
+                         int64_t* vert_first, int64_t* face_first, cudaStream_t s);
+void launch_batch_active_stats(bool mi, const int64_t* tet_base, int n, const uint32_t* act_tet,
+                               const uint64_t* act_mask, int64_t A, unsigned long long* stats4, cudaStream_t s);
+
 // Ordered compaction of the active tets.  Pass 1 counts per block (active, generic) and the k
 // histogram; pass 2 writes, in tet order, the active tets and the tets that need the generic cut.
+// general-case tets are listed in bins of equal active-function count, the heaviest first: bin 0
+// holds k >= kGenBins (+1 for MI), bin kGenBins-1 the lightest; the count kernel writes, per block,
+// the active count and then one count per bin ([1 + kGenBins][blocks], scanned as one array)
+constexpr int kGenBins = 8;
 struct FilterOut {
     uint32_t* act_tet;    // [A]
     uint64_t* act_mask;   // [A] active functions (bit j = function j)
@@ -78,6 +139,18 @@ struct CutArgs {
     // one-plane lookup table (implicit arrangement), used for tets with one effective plane
     const uint8_t* table = nullptr;
     const uint32_t* table_off = nullptr;
+    // secondary lookup (two planes / three materials): disabled when slots is null
+    struct Cache {
+        unsigned long long* slots = nullptr;  // (key + 1) << 32 | entry; 0 = empty
+        uint32_t slot_mask = 0;
+        uint32_t cap = 0;                     // entries
+        unsigned long long* next = nullptr;   // entries taken (64-bit: never wraps)
+        unsigned long long* heap_used = nullptr;
+        uint64_t heap_base = 0, heap_cap = 0; // template bytes in the table region
+        uint8_t* table = nullptr;             // the mode's table region (entries follow the 81 patterns)
+        uint32_t* table_off = nullptr;
+        IASum4* table_sum = nullptr;
+    } cache;
 };
 void launch_cut_fast(const CutArgs& a, cudaStream_t s);
 // exact variant: one tet per block, state in shared memory
@@ -86,6 +159,10 @@ size_t cut_big_slot_bytes(bool mi);
 // per-device lookup tables: IA one active plane, MI two active materials; 81 sign patterns each
 constexpr int kTablePatterns = 81;
 constexpr int kTableStride = 256;
+// secondary lookup entries per mode and their template bytes (after the 81 patterns)
+constexpr uint32_t kCacheEntries = 1u << 18;
+constexpr uint32_t kCacheSlots = 1u << 20;
+constexpr uint64_t kCacheHeapBytes = 64ull << 20;
 void launch_build_table(bool mi, uint8_t* table, uint32_t* table_off, IASum4* table_sum, void* scratch,
                         uint32_t* status, cudaStream_t s);
 // robust test: cut every listed tet with its rows in the given and in the reversed order with the

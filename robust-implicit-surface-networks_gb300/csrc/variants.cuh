@@ -7,7 +7,9 @@
 
 namespace ria {
 using IACutFast = IACut<32, 48, 16, 192, false>;
-using IACutBig = IACut<128, 256, 64, 1024, true>;
+// exact variants: the full range of the 8-bit vertex and cell ids (255 vertices, 254 cells); one tet
+// per block with the state in shared memory (about 44 KB / 31 KB)
+using IACutBig = IACut<255, 1024, 254, 8192, true>;
 using MICutFast = MICut<32, 24, 160, 48, 48, 256, false>;
-using MICutBig = MICut<96, 96, 640, 128, 128, 1024, true>;
+using MICutBig = MICut<255, 255, 2048, 255, 512, 4096, true>;
 }  // namespace ria

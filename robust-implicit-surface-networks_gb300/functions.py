@@ -258,6 +258,50 @@ def workload_ia_degenerate(seed=3, res=128):
     return Workload("ia-degenerate-32func-res%d" % res, "ia", res, make_functions(specs), meta={"seed": seed})
 
 
+def random_function_spec(rng, kind):
+    """One function of the given kind with the parameter distributions of the workloads above."""
+    if kind == "plane":
+        n = _rand_unit(rng)
+        return _plane(-rng.uniform(-0.5, 0.5) * n, n)
+    if kind == "sphere":
+        return {"type": "sphere", "center": list(rng.uniform(-0.7, 0.7, 3)), "radius": float(rng.uniform(0.2, 0.6))}
+    if kind == "cylinder":
+        return {"type": "cylinder", "axis_point": list(rng.uniform(-0.5, 0.5, 3)), "axis_vector": list(_rand_unit(rng)),
+                "radius": float(rng.uniform(0.1, 0.4))}
+    return {"type": "torus", "center": list(rng.uniform(-0.5, 0.5, 3)), "axis_vector": list(_rand_unit(rng)),
+            "major_radius": float(rng.uniform(0.3, 0.6)), "minor_radius": float(rng.uniform(0.05, 0.2))}
+
+
+@dataclass
+class BatchWorkload:
+    name: str
+    mode: str
+    problems: list  # (res, funcs) pairs
+
+    @property
+    def n_tets(self):
+        return sum(5 * r ** 3 for r, _ in self.problems)
+
+    @property
+    def n_verts(self):
+        return sum((r + 1) ** 3 for r, _ in self.problems)
+
+
+def workload_batch(seed=4, n=4096, mode="ia", verts_per_axis=(9, 33), funcs=(2, 24)):
+    """Batched form: n independent grids over [-1,1]^3 with vertices per axis uniform in
+    verts_per_axis, a function count uniform in `funcs` and the function kinds uniform over
+    plane / sphere / cylinder / torus."""
+    rng = np.random.default_rng(seed)
+    kinds = ["plane", "sphere", "cylinder", "torus"]
+    probs = []
+    for _ in range(n):
+        res = int(rng.integers(verts_per_axis[0], verts_per_axis[1] + 1)) - 1
+        F = int(rng.integers(funcs[0], funcs[1] + 1))
+        specs = [random_function_spec(rng, kinds[int(rng.integers(0, 4))]) for _ in range(F)]
+        probs.append((res, make_functions(specs)))
+    return BatchWorkload("batch-%d-grids" % n, mode, probs)
+
+
 WORKLOADS = {
     "ia-small": workload_ia_small,
     "mi": workload_mi,

@@ -18,6 +18,8 @@ def lib():
         for f in (L.hc_ia_cut, L.hc_mi_cut):
             f.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
         L.hc_det_sign.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        for f in (L.hc_ia_key2, L.hc_mi_key3):
+            f.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
         _lib = L
     return _lib
 
@@ -49,3 +51,11 @@ def ia_template(rows):
     if n < 0:
         return None
     return bytes(buf[:n]), summ.copy()
+
+
+def key(mode, rows):
+    """Secondary lookup key of two planes (ia) or three materials (mi), or None."""
+    rows = np.ascontiguousarray(rows, dtype=np.float64).reshape(-1)
+    out = np.zeros(1, dtype=np.uint32)
+    f = lib().hc_ia_key2 if mode == "ia" else lib().hc_mi_key3
+    return int(out[0]) if f(rows.ctypes.data, out.ctypes.data) else None

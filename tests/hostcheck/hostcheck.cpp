@@ -4,6 +4,7 @@
 
 #include "../../robust-implicit-surface-networks_gb300/csrc/cut_mi.cuh"
 #include "../../robust-implicit-surface-networks_gb300/csrc/variants.cuh"
+#include "../../robust-implicit-surface-networks_gb300/csrc/lookup2.cuh"
 
 using namespace ria;
 
@@ -46,6 +47,10 @@ extern "C" int hc_mi_cut(int k, const double* mats, int big, uint8_t* buf, int c
 }
 
 extern "C" int hc_det_sign(const double* M, int n) { return det_sign_exact(M, n); }
+
+// secondary lookup keys: returns 1 and the key, or 0 when no key is formed
+extern "C" int hc_ia_key2(const double* rows, uint32_t* key) { return ia_key2(rows, *key) ? 1 : 0; }
+extern "C" int hc_mi_key3(const double* rows, uint32_t* key) { return mi_key3(rows, *key) ? 1 : 0; }
 
 // The one-effective-plane path of the fast kernel: the one-plane table is built by the exact variant
 // from corner values in {-1, 0, 1}, as on the device.

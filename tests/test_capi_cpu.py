@@ -12,6 +12,7 @@ import numpy as np
 import pytest
 
 from conftest import REPO
+from records import decode_ia, decode_mi
 
 sys.path.insert(0, os.path.join(REPO, "tests", "hostcheck"))
 
@@ -77,6 +78,34 @@ def test_device_cut_logic_degenerate(hc, oracle):
         k = int(rng.integers(2, 5))
         deferred += _agree(hc, oracle, "mi", rng.integers(-2, 3, size=(k, 4)).astype(np.float64))
     assert deferred > 0  # exact ties must reach the exact variant
+
+
+def test_device_cut_near_degenerate(hc, oracle):
+    """Exact degeneracies perturbed at and below FP32 resolution (2^-24 relative): the FP32 filter
+    must hand these predicates on to the FP64 filter or the exact evaluation, never decide them."""
+    rng = np.random.default_rng(10)
+    for _ in range(300):
+        k = int(rng.integers(1, 5))
+        base = rng.integers(-2, 3, size=(k, 4)).astype(np.float64)
+        eps = 10.0 ** rng.uniform(-9, -5, size=(k, 4)) * rng.choice([-1.0, 0.0, 1.0], size=(k, 4))
+        _agree(hc, oracle, "ia", base + eps)
+        base = rng.integers(-2, 3, size=(k + 1, 4)).astype(np.float64)
+        eps = 10.0 ** rng.uniform(-9, -5, size=(k + 1, 4)) * rng.choice([-1.0, 0.0, 1.0], size=(k + 1, 4))
+        _agree(hc, oracle, "mi", base + eps)
+
+
+def test_device_mi_dominated_materials(hc, oracle):
+    """Materials below another at every corner (strictly, or with ties at some corners) are skipped by
+    the device cut; the records must still equal the oracle's full clipping."""
+    rng = np.random.default_rng(9)
+    for _ in range(200):
+        k = int(rng.integers(3, 7))
+        m = rng.integers(-3, 4, size=(k, 4)).astype(np.float64)
+        a, b = rng.choice(k, size=2, replace=False)
+        m[a] = m[b] - rng.integers(0, 2, size=4)  # a <= b everywhere, strict where 1
+        if rng.random() < 0.5:
+            m[a] = m[b] - 1.0 - rng.random(4)      # strictly below
+        _agree(hc, oracle, "mi", m)
 
 
 def test_device_cut_logic_on_workload_tets(hc, oracle, fns):
@@ -147,3 +176,72 @@ def test_one_effective_plane_template_path(hc, oracle):
         big, summ = hc.cut("ia", rows, True)
         assert got[0] == big and np.array_equal(got[1], summ[:4])
     assert seen > 300
+
+
+def _exact_key(mode, rows):
+    """The secondary-lookup key restated with rational arithmetic."""
+    from fractions import Fraction as Fr
+    from itertools import combinations
+
+    def sgn(x):
+        return (x > 0) - (x < 0)
+    R = [[Fr(x) for x in r] for r in np.asarray(rows, dtype=np.float64)]
+    t = []
+    if mode == "ia":
+        P, Q = R
+        t = [sgn(x) for x in P] + [sgn(x) for x in Q]
+        t += [sgn(P[i] * Q[j] - P[j] * Q[i]) for i, j in combinations(range(4), 2)]
+    else:
+        for a, b in ((0, 1), (0, 2), (1, 2)):
+            t += [sgn(R[b][c] - R[a][c]) for c in range(4)]
+        t += [sgn((R[1][c] - R[0][c]) * (R[2][d] - R[0][d]) - (R[2][c] - R[0][c]) * (R[1][d] - R[0][d]))
+              for c, d in combinations(range(4), 2)]
+    k = 0
+    for s in t:
+        k = 3 * k + s + 1
+    return k
+
+
+def test_secondary_lookup_keys(hc, oracle):
+    """The device keys equal their rational restatement, and equal keys always carry equal records
+    (the combinatorial type fixes the canonical record), for generic and degenerate inputs."""
+    rng = np.random.default_rng(12)
+    seen = {}
+    for it in range(6000):
+        mode = "ia" if it % 2 == 0 else "mi"
+        n = 2 if mode == "ia" else 3
+        kind = (it // 2) % 3
+        if kind == 0:
+            rows = rng.normal(size=(n, 4))
+        elif kind == 1:
+            rows = rng.integers(-2, 3, size=(n, 4)).astype(np.float64)
+        else:
+            rows = rng.integers(-1, 2, size=(n, 4)).astype(np.float64) + rng.normal(size=(n, 4)) * 1e-9
+        k = hc.key(mode, rows)
+        assert k == _exact_key(mode, rows)
+        rec = oracle.ia_cut(rows) if mode == "ia" else oracle.mi_cut(rows)
+        d = decode_ia(rec) if mode == "ia" else decode_mi(rec)
+        if d["rep"] != list(range(4, 4 + n)):
+            continue
+        assert seen.setdefault((mode, k), rec) == rec
+    assert hc.key("ia", [[1e-80, 1, 1, 1], [1, 2, 3, 4]]) is None
+
+
+def test_heavy_tets_exact_variant(hc, oracle):
+    """Up to 14 planes (more than 256 faces) and 16 materials in one tet: the exact variant either
+    reports its capacity or reproduces the oracle's record."""
+    rng = np.random.default_rng(13)
+    done = 0
+    for k in (10, 12, 14):
+        for _ in range(6):
+            rows = rng.normal(size=(k, 4))
+            out, _ = hc.cut("ia", rows, True)
+            if not isinstance(out, int):
+                assert out == oracle.ia_cut(rows)
+                done += 1
+    for k in (8, 12, 16):
+        for _ in range(4):
+            rows = rng.normal(size=(k, 4)) * 0.3
+            out, _ = hc.cut("mi", rows, True)
+            assert not isinstance(out, int) and out == oracle.mi_cut(rows)
+    assert done >= 8

@@ -124,3 +124,25 @@ def test_repeatable(pkg, fns, lib):
     b = pkg.grid_implicit_arrangement(wl.res, wl.funcs)
     for k in ("verts", "face_verts", "face_tets", "xyz", "rec_bytes"):
         assert np.array_equal(a[k], b[k]), k
+
+
+@pytest.mark.parametrize("mode", ["ia", "mi"])
+def test_secondary_lookup_cache(pkg, fns, oracle, lib, mode):
+    """Two-plane (IA) / three-material (MI) tets come from the device cache of records keyed by
+    their combinatorial type once seen.  The first call fills the cache, the second reads it; both
+    equal the general cut (useSecondaryLookup off) and the oracle."""
+    if mode == "ia":
+        wl = fns.workload_ia_degenerate(res=40)
+        grid = pkg.grid_implicit_arrangement
+    else:
+        wl = fns.workload_mi(res=40)
+        grid = pkg.grid_material_interface
+    pts, tets = fns.generate_tet_mesh(wl.res)
+    fv = oracle.sample(wl.funcs, pts)
+    ref = oracle.run(mode, pts, tets, fv)
+    off = grid(wl.res, wl.funcs, use_secondary_lookup=False)
+    for _ in range(2):
+        on = grid(wl.res, wl.funcs, use_secondary_lookup=True)
+        assert_mesh_equal(on, ref)
+        for k in ("rec_bytes", "verts", "face_verts", "xyz"):
+            assert np.array_equal(on[k], off[k]), k
