@@ -191,6 +191,94 @@ def run_batch(args, world, local):
     print(json.dumps(line))
 
 
+def run_serve(args, world, local):
+    """The served form against the plain drop-in on the same Poisson request stream."""
+    import numpy as np
+    import torch
+
+    torch.cuda.set_device(local)
+    fns = importlib.import_module(PKG + ".functions")
+    pkg = importlib.import_module(PKG)
+    pkg.build()
+    L = pkg.load()
+    n = max(1, int(args.rate * args.duration))
+    reqs = fns.workload_serve(n=n)
+    rng = np.random.default_rng(6)
+    gaps = rng.exponential(1.0 / args.rate, size=n)
+    arrivals = np.cumsum(gaps) - gaps[0]
+    total_tets = sum(r.n_tets for r in reqs)
+    # warm-up: every kind once through both paths (tables, caches, pools)
+    srv = pkg.Server(budget_bytes=int(args.budget_gb * 2 ** 30), streams=args.streams, max_batch=256)
+    for r in reqs[:6]:
+        t = srv.submit(r.kind, r.res, r.funcs, tree=r.tree)
+        srv.wait(t)
+        srv.release(t)
+        m = (pkg.grid_material_interface if r.kind == "mi" else pkg.grid_implicit_arrangement)(r.res, r.funcs)
+        if r.kind == "csg":
+            m.csg(r.tree)
+        m.close()
+    launches0 = int(L.ria_kernel_launches())
+    # served: a submitter replays the arrival times; results are consumed as they complete
+    tickets = [None] * n
+    with ClockSampler(local) as clk:
+        t0 = time.perf_counter()
+
+        def submit():
+            for i, r in enumerate(reqs):
+                d = t0 + arrivals[i] - time.perf_counter()
+                if d > 0:
+                    time.sleep(d)
+                tickets[i] = srv.submit(r.kind, r.res, r.funcs, tree=r.tree)
+        th = threading.Thread(target=submit)
+        th.start()
+        lat = []
+        for i in range(n):
+            while tickets[i] is None:
+                time.sleep(0.0002)
+            _, l = srv.wait(tickets[i])
+            lat.append(l)
+            srv.release(tickets[i])
+        th.join()
+        served_wall = time.perf_counter() - t0
+    launches = int(L.ria_kernel_launches()) - launches0
+    srv.close()
+    # plain: one request at a time in arrival order; latency counts the wait in the queue
+    plain_lat = []
+    t0 = time.perf_counter()
+    for i, r in enumerate(reqs):
+        d = t0 + arrivals[i] - time.perf_counter()
+        if d > 0:
+            time.sleep(d)
+        m = (pkg.grid_material_interface if r.kind == "mi" else pkg.grid_implicit_arrangement)(r.res, r.funcs)
+        if r.kind == "csg":
+            m.csg(r.tree)
+        m.close()
+        plain_lat.append(time.perf_counter() - (t0 + arrivals[i]))
+    plain_wall = time.perf_counter() - t0
+    pct = lambda v, q: float(np.percentile(np.asarray(v) * 1e3, q))
+    peak, peak_kind = _peaks()
+    line = {
+        "metric": METRIC, "value": total_tets / served_wall, "unit": "tets/s", "n_gpus": world, "steps": 1,
+        "warmup": 1, "ms_per_step": served_wall * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+        "config": {"workload": "served-poisson", "requests": n, "rate_per_s": args.rate, "duration_s": args.duration,
+                   "mix": "60% ia / 30% mi / 10% csg", "tets": "log-uniform 10k..2M (total %d)" % total_tets,
+                   "functions": "2..16", "budget_gb": args.budget_gb, "streams": args.streams,
+                   "l2": "inputs generated per request on the device", "parallelism": "single"},
+        "latency_ms": {"p50": pct(lat, 50), "p99": pct(lat, 99), "max": pct(lat, 100)},
+        "plain": {"p50_ms": pct(plain_lat, 50), "p99_ms": pct(plain_lat, 99), "tets_per_s": total_tets / plain_wall,
+                  "wall_s": plain_wall},
+        "p99_ratio_plain_over_served": pct(plain_lat, 99) / pct(lat, 99),
+        "e2e": {"value": total_tets / served_wall, "unit": "tets/s",
+                "h2d_bytes_per_step": int(sum(r.funcs.nbytes for r in reqs)), "d2h_bytes_per_step": 0},
+        "gpu_launches": launches,
+        "roofline": {"bound": "hbm", "kernel_stage": "total", "achieved": None, "peak": peak, "unit": "GB/s",
+                     "frac": None, "peak_kind": peak_kind, "traffic": None},
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line))
+
+
 def algorithmic_bytes(wl, st):
     """Bytes each stage must move at least (per-unit figures in the design doc)."""
     V, T, F = wl.n_verts, wl.n_tets, len(wl.funcs)
@@ -257,8 +345,12 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="ia-degenerate", choices=["ia-degenerate", "mi", "ia-small", "batch"])
+    ap.add_argument("--config", default="ia-degenerate", choices=["ia-degenerate", "mi", "ia-small", "batch", "serve"])
     ap.add_argument("--batch-n", type=int, default=4096, help="problems of --config batch")
+    ap.add_argument("--rate", type=float, default=100.0, help="--config serve: requests per second")
+    ap.add_argument("--duration", type=float, default=10.0, help="--config serve: seconds of arrivals")
+    ap.add_argument("--budget-gb", type=float, default=120.0, help="--config serve: HBM budget")
+    ap.add_argument("--streams", type=int, default=3, help="--config serve: worker streams")
     ap.add_argument("--res", type=int, default=None, help="grid resolution override (small profiling cases)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer end-to-end leg (profiling runs)")
@@ -269,12 +361,12 @@ def main():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
-    if args.config == "batch":
+    if args.config in ("batch", "serve"):
         if args.impl == "reference":
-            print(json.dumps({"impl": "reference", "unavailable": "the batched form has no CPU reference arm; "
-                              "run --impl reference on the other configs"}))
+            print(json.dumps({"impl": "reference", "unavailable": "the batched and served forms have no CPU "
+                              "reference arm; run --impl reference on the other configs"}))
         elif rank == 0:
-            run_batch(args, world, local)
+            (run_batch if args.config == "batch" else run_serve)(args, world, local)
         return
     wl = workload(args.config, args.res)
 
@@ -328,24 +420,38 @@ def main():
         ms = float(t.item())
     value = world * wl.n_tets / (ms * 1e-3)
 
-    # ---- end to end through the host-buffer entry points
+    # ---- end to end through the host-buffer entry points, host buffers in pinned memory
     fns = importlib.import_module(PKG + ".functions")
     pts, tets = fns.generate_tet_mesh(wl.res, wl.bbox_min, wl.bbox_max)
-    pts = np.ascontiguousarray(pts)
-    tets = np.ascontiguousarray(tets)
+
+    def pinned(shape, dtype):
+        t = torch.empty(int(np.prod(shape)) * np.dtype(dtype).itemsize, dtype=torch.uint8, pin_memory=True)
+        return t.numpy().view(dtype).reshape(shape)
+
+    pts_h = pinned(pts.shape, np.float64)
+    pts_h[...] = pts
+    tets_h = pinned(tets.shape, np.int64)
+    tets_h[...] = tets
+    fv_h = pinned((len(pts), len(wl.funcs)), np.float64)
+    out_bufs = {}
+    names = ["xyz", "verts", "face_offsets", "face_verts", "face_tets", "face_func"]
     e2e_times = []
     h2d = d2h = 0
     for it in range(0 if args.no_e2e else 1 + args.steps):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        fv = pkg.sample_functions(wl.funcs, pts)
-        m = host(pts, tets, fv)
-        outs = [m["xyz"], m["verts"], m["face_offsets"], m["face_verts"], m["face_tets"], m["face_func"]]
+        fv = pkg.sample_functions(wl.funcs, pts_h, out=fv_h)
+        m = host(pts_h, tets_h, fv)
+        if it == 0:  # size the pinned result buffers once (untimed iteration)
+            for k in names:
+                n = int(L.ria_mesh_count(m._h, pkg.Mesh._FIELDS[k][0]))
+                out_bufs[k] = pinned((max(n, 1) * 2,), pkg.Mesh._FIELDS[k][1])
+        outs = [m.copy_into(k, out_bufs[k]) for k in names]
         m.close()
         dt = time.perf_counter() - t0
         if it > 0:
             e2e_times.append(dt)
-        h2d = pts.nbytes + wl.funcs.nbytes + pts.nbytes + tets.nbytes + fv.nbytes
+        h2d = pts_h.nbytes + wl.funcs.nbytes + pts_h.nbytes + tets_h.nbytes + fv.nbytes
         d2h = fv.nbytes + sum(o.nbytes for o in outs)
     e2e = world * wl.n_tets / statistics.median(e2e_times) if e2e_times else None
 

@@ -234,6 +234,39 @@ RIA_API ria_status ria_batch_csg(const ria_mesh* mesh, uint32_t problem, const i
  * negative side of the face's function (bit j set where function j is positive; n_func <= 64). */
 RIA_API ria_status ria_mesh_face_sides(const ria_mesh* mesh, uint64_t* sides);
 
+/* ---- served form ----------------------------------------------------------------------------------
+ * A request loop for arrangement, material-interface and CSG solves.  Requests are admitted against
+ * an HBM budget as they arrive; each of `streams` worker threads takes the oldest waiting request and
+ * every other waiting request of the same class (material interface, or arrangement and CSG) that
+ * fits the remaining budget, and solves them as one batch (ria_grid_batch) on its own stream, so
+ * batches overlap on the device.  A request's result is its problem of that batch mesh, resident on
+ * the device until ria_server_release; its budget share is returned when the last request of the
+ * batch is released.  Results equal those of the plain calls on the same inputs.  No counterpart in
+ * the reference. */
+enum { RIA_REQ_IA = 0, RIA_REQ_MI = 1, RIA_REQ_CSG = 2 };
+typedef struct ria_request {
+    int32_t kind;              /* RIA_REQ_* */
+    ria_grid_problem grid;     /* copied at submission */
+    const int32_t* csg_tree;   /* CSG: n_units x 3 as ria_mesh_csg (copied); NULL: union of all */
+    uint32_t csg_units;
+    int32_t positive_inside;
+} ria_request;
+typedef struct ria_server ria_server;
+
+RIA_API ria_status ria_server_create(const ria_config* cfg, uint64_t hbm_budget_bytes, uint32_t streams,
+                                     uint32_t max_batch, ria_server** out);
+RIA_API ria_status ria_server_submit(ria_server* server, const ria_request* request, uint64_t* ticket);
+/* Waits up to timeout_s seconds (< 0: no limit; RIA_ETIMEOUT when it runs out) for a request; gives the
+ * batch mesh holding its result (read with ria_batch_count / ria_batch_copy at `problem`) and the
+ * time from submission to completion. */
+RIA_API ria_status ria_server_wait(ria_server* server, uint64_t ticket, double timeout_s, const ria_mesh** mesh,
+                                   uint32_t* problem, double* latency_s);
+/* CSG requests: the face labels of ria_mesh_csg (host_dst may be NULL to ask for the count). */
+RIA_API uint64_t ria_server_labels(ria_server* server, uint64_t ticket, uint8_t* host_dst);
+RIA_API void ria_server_release(ria_server* server, uint64_t ticket);
+/* Stops the workers after their current batch and frees every result. */
+RIA_API void ria_server_destroy(ria_server* server);
+
 /* Stage a alone: func_vals[n_pts][n_func] = funcs evaluated at pts (host buffers). */
 RIA_API ria_status ria_sample_functions(const ria_function* funcs, uint32_t n_func, const double* pts, uint64_t n_pts,
                                 double* func_vals);

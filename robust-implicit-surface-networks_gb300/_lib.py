@@ -36,6 +36,15 @@ class GridProblem(ctypes.Structure):
                 ("bbox_max", ctypes.c_double * 3), ("funcs", ctypes.c_void_p)]
 
 
+class Request(ctypes.Structure):
+    """ria_request of include/ria.h."""
+    _fields_ = [("kind", ctypes.c_int32), ("grid", GridProblem), ("csg_tree", ctypes.c_void_p),
+                ("csg_units", ctypes.c_uint32), ("positive_inside", ctypes.c_int32)]
+
+
+REQ_IA, REQ_MI, REQ_CSG = 0, 1, 2
+
+
 class Config(ctypes.Structure):
     _fields_ = [("use_lookup", ctypes.c_int32), ("use_secondary_lookup", ctypes.c_int32),
                 ("use_topo_ray_shooting", ctypes.c_int32), ("robust_test", ctypes.c_int32),
@@ -95,6 +104,19 @@ def load():
     L.ria_mesh_face_sides.argtypes = [vp, vp]
     L.ria_batch_csg.restype = i32
     L.ria_batch_csg.argtypes = [vp, u32, vp, u32, i32, vp]
+    L.ria_server_create.restype = i32
+    L.ria_server_create.argtypes = [cfgp, u64, u32, u32, ctypes.POINTER(vp)]
+    L.ria_server_submit.restype = i32
+    L.ria_server_submit.argtypes = [vp, ctypes.POINTER(Request), ctypes.POINTER(u64)]
+    L.ria_server_wait.restype = i32
+    L.ria_server_wait.argtypes = [vp, u64, ctypes.c_double, ctypes.POINTER(vp), ctypes.POINTER(u32),
+                                  ctypes.POINTER(ctypes.c_double)]
+    L.ria_server_labels.restype = u64
+    L.ria_server_labels.argtypes = [vp, u64, vp]
+    L.ria_server_release.restype = None
+    L.ria_server_release.argtypes = [vp, u64]
+    L.ria_server_destroy.restype = None
+    L.ria_server_destroy.argtypes = [vp]
     L.ria_mesh_count.restype = u64
     L.ria_mesh_count.argtypes = [vp, i32]
     L.ria_mesh_copy.restype = i32

@@ -55,6 +55,19 @@ class Mesh:
             _lib.check(L.ria_mesh_copy(self._h, field, out.ctypes.data))
         return out
 
+    def copy_into(self, name, out):
+        """Copy a field into a caller buffer (e.g. pinned host memory); returns the filled view."""
+        field, dt, shape = self._FIELDS[name]
+        L = _lib.load()
+        n = int(L.ria_mesh_count(self._h, field))
+        flat = out.reshape(-1).view(dt)
+        if flat.size < n:
+            raise ValueError("buffer too small for %s: %d < %d" % (name, flat.size, n))
+        if n:
+            _lib.check(L.ria_mesh_copy(self._h, field, flat.ctypes.data))
+        v = flat[:n]
+        return v.reshape(shape) if shape else v
+
     def __getitem__(self, name):
         if name not in self._cache:
             if name == "stats":
@@ -236,11 +249,79 @@ def grid_batch(problems, mode="ia", **kw) -> BatchMesh:
     return BatchMesh(h)
 
 
-def sample_functions(funcs, pts) -> np.ndarray:
+class _Borrowed:
+    """A mesh handle owned by the server (not freed here)."""
+
+    def __init__(self, h):
+        self._h = h
+
+
+class Server:
+    """The served form (ria_server_*): submit requests as they arrive, wait for their results."""
+
+    KINDS = {"ia": _lib.REQ_IA, "mi": _lib.REQ_MI, "csg": _lib.REQ_CSG}
+
+    def __init__(self, budget_bytes, streams=3, max_batch=256, **kw):
+        cfg = _config(**kw)
+        self._h = ctypes.c_void_p()
+        _lib.check(_lib.load().ria_server_create(ctypes.byref(cfg), int(budget_bytes), int(streams), int(max_batch),
+                                                 ctypes.byref(self._h)))
+        self._keep = {}
+
+    def submit(self, kind, res, funcs, bbox_min=(-1.0, -1.0, -1.0), bbox_max=(1.0, 1.0, 1.0), tree=None,
+               positive_inside=True) -> int:
+        funcs = np.ascontiguousarray(funcs, dtype=FUNC_DTYPE)
+        t, n = _csg_tree(tree)
+        q = _lib.Request()
+        q.kind = self.KINDS[kind]
+        q.grid.resolution = int(res)
+        q.grid.n_func = len(funcs)
+        for a in range(3):
+            q.grid.bbox_min[a] = float(bbox_min[a])
+            q.grid.bbox_max[a] = float(bbox_max[a])
+        q.grid.funcs = funcs.ctypes.data
+        q.csg_tree = t.ctypes.data if n else None
+        q.csg_units = n
+        q.positive_inside = int(positive_inside)
+        ticket = ctypes.c_uint64()
+        _lib.check(_lib.load().ria_server_submit(self._h, ctypes.byref(q), ctypes.byref(ticket)))
+        return int(ticket.value)
+
+    def wait(self, ticket, timeout=-1.0):
+        """(view of the result, latency in seconds); the view reads like a grid call's mesh."""
+        h, prob, lat = ctypes.c_void_p(), ctypes.c_uint32(), ctypes.c_double()
+        _lib.check(_lib.load().ria_server_wait(self._h, int(ticket), float(timeout), ctypes.byref(h),
+                                               ctypes.byref(prob), ctypes.byref(lat)))
+        return _ProblemView(_Borrowed(h), prob.value), lat.value
+
+    def labels(self, ticket) -> np.ndarray:
+        L = _lib.load()
+        n = int(L.ria_server_labels(self._h, int(ticket), None))
+        out = np.zeros(n, dtype=np.uint8)
+        if n:
+            L.ria_server_labels(self._h, int(ticket), out.ctypes.data)
+        return out
+
+    def release(self, ticket):
+        _lib.load().ria_server_release(self._h, int(ticket))
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _lib.load().ria_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+
+def sample_functions(funcs, pts, out=None) -> np.ndarray:
     L = _lib.load()
     funcs = np.ascontiguousarray(funcs, dtype=FUNC_DTYPE)
     pts = np.ascontiguousarray(pts, dtype=np.float64).reshape(-1, 3)
-    out = np.zeros((pts.shape[0], len(funcs)))
+    if out is None:
+        out = np.zeros((pts.shape[0], len(funcs)))
+    elif out.dtype != np.float64 or out.shape != (pts.shape[0], len(funcs)) or not out.flags.c_contiguous:
+        raise ValueError("out must be a contiguous n_pts x n_func float64 array")
     _lib.check(L.ria_sample_functions(funcs.ctypes.data, len(funcs), pts.ctypes.data, pts.shape[0], out.ctypes.data))
     return out
 

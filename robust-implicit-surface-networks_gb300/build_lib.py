@@ -25,7 +25,7 @@ FLAGS = ["-O3", "-std=c++17", "-fmad=false", "-lineinfo", "-Xcompiler", "-fPIC",
 HOST = os.path.join(HERE, "host")
 HOST_LIB = os.path.join(OUT_DIR, "libria_host.so")
 HOST_SOURCES = ["ria_host.cpp", "mesh_io.cpp"]
-APPS = ["impl_arrangement", "material_interface"]
+APPS = ["impl_arrangement", "material_interface", "csg"]
 CXX = os.environ.get("CXX", "g++")
 # -ffp-contract=off: the grid coordinates and unit axis vectors round as written (aarch64 g++
 # contracts a*b+c into fma by default)

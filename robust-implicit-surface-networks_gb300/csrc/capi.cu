@@ -11,7 +11,12 @@
 #include <atomic>
 #include <chrono>
 #include <cstring>
+#include <condition_variable>
+#include <deque>
+#include <map>
+#include <memory>
 #include <mutex>
+#include <thread>
 #include <string>
 #include <vector>
 
@@ -53,7 +58,8 @@ struct DeviceCtx {
 std::mutex g_mu;
 std::vector<DeviceCtx> g_ctx;
 
-constexpr int64_t kFastRecordBytes = 1024;  // bound of a record of the fast variants
+constexpr int64_t kFastRecordBytes = 1024;  // heap bytes per tet of the small filtered variant
+constexpr int64_t kMidRecordBytes = 4096;   // per tet of the mid variant (fuller records go to the exact kernel)
 constexpr int64_t kBigRecordBytes = 28672;  // bound of a record of the exact variants
 constexpr int64_t kBigSlots = 152 * 64;     // concurrent exact-variant threads
 
@@ -296,7 +302,7 @@ ria_status run_pipeline(const ria_config* cfg, const Inputs& in, cudaStream_t s,
     uint32_t* blk = tmp.get<uint32_t>(nscan, &err);
     uint32_t* blk_off = tmp.get<uint32_t>(nscan, &err);
     if (err != cudaSuccess) return bail(fail(RIA_ENOMEM, "device allocation failed"));
-    int64_t A = 0, G = 0;
+    int64_t A = 0, G = 0, G_mid = 0;
     if (nb > 0) {
         launch_filter_count(mi, vmask, fv, in.F, in.d_tets, in.g, in.T, use_table, blk, cnt + 2, s);
         size_t bytes = 0;
@@ -304,13 +310,15 @@ ria_status run_pipeline(const ria_config* cfg, const Inputs& in, cudaStream_t s,
         uint8_t* scan_tmp = tmp.get<uint8_t>((int64_t)bytes, &err);
         if (err != cudaSuccess) return bail(fail(RIA_ENOMEM, "device allocation failed"));
         cub::DeviceScan::ExclusiveSum(scan_tmp, bytes, blk, blk_off, nscan, s);
-        uint32_t h[3];
+        uint32_t h[4];
         cudaMemcpyAsync(&h[0], blk_off + nb, 4, cudaMemcpyDeviceToHost, s);
         cudaMemcpyAsync(&h[1], blk_off + nscan - 1, 4, cudaMemcpyDeviceToHost, s);
         cudaMemcpyAsync(&h[2], blk + nscan - 1, 4, cudaMemcpyDeviceToHost, s);
+        cudaMemcpyAsync(&h[3], blk_off + (1 + kFirstSmallBin(mi)) * nb, 4, cudaMemcpyDeviceToHost, s);
         if (cudaStreamSynchronize(s) != cudaSuccess) return bail(fail(RIA_ECUDA, cudaGetErrorString(cudaGetLastError())));
         A = h[0];
         G = (int64_t)h[1] + h[2] - A;
+        G_mid = (int64_t)h[3] - A;  // the heavy bins come first in the general-case list
     }
     M->A = A;
     M->act_tet = M->keep.get<uint32_t>(A, &err);
@@ -351,14 +359,15 @@ ria_status run_pipeline(const ria_config* cfg, const Inputs& in, cudaStream_t s,
         launch_robust(ca, scratch, kBigSlots, cnt + 8, s);
         cudaStreamSynchronize(s);
     } else if (G > 0) {
-        M->heap = M->keep.get<uint8_t>(G * kFastRecordBytes, &err);
+        const uint64_t heap_bytes = (uint64_t)(G - G_mid) * kFastRecordBytes + (uint64_t)G_mid * kMidRecordBytes;
+        M->heap = M->keep.get<uint8_t>((int64_t)heap_bytes, &err);
         uint32_t* deferred = tmp.get<uint32_t>(G, &err);
         if (err != cudaSuccess) return bail(fail(RIA_ENOMEM, "device allocation failed"));
         ca.list = gen;
         ca.n = G;
         ca.heap = M->heap;
         ca.heap_used = cnt + 5;
-        ca.heap_cap = (uint64_t)G * kFastRecordBytes;
+        ca.heap_cap = heap_bytes;
         ca.desc_bit = 0;
         ca.deferred = deferred;
         ca.n_deferred = (unsigned int*)(cnt + 7);
@@ -367,7 +376,12 @@ ria_status run_pipeline(const ria_config* cfg, const Inputs& in, cudaStream_t s,
             ca.table_off = ctx->table_off[0];
         }
         if (cfg->use_lookup && cfg->use_secondary_lookup) set_cache(ca, ctx, mi);
-        launch_cut_fast(ca, s);
+        CutArgs cm = ca;  // heavy bins: mid-size variant
+        cm.n = G_mid;
+        launch_cut_fast(cm, s, true);
+        ca.list = gen + G_mid;
+        ca.n = G - G_mid;
+        launch_cut_fast(ca, s, false);
         unsigned long long h = 0;
         cudaMemcpyAsync(&h, cnt + 7, 8, cudaMemcpyDeviceToHost, s);
         if (cudaStreamSynchronize(s) != cudaSuccess) return bail(fail(RIA_ECUDA, cudaGetErrorString(cudaGetLastError())));
@@ -1216,6 +1230,264 @@ void ria_mesh_free(ria_mesh* m) {
     cudaStreamSynchronize(m->s);
     if (m->own_stream) cudaStreamDestroy(m->s);
     delete m;
+}
+
+// ---- served form ------------------------------------------------------------------------------
+
+}  // extern "C"
+
+namespace {
+
+struct ServerBatch {
+    ria_mesh* mesh = nullptr;
+    int refs = 0;
+    uint64_t bytes = 0;  // reserved budget, returned when the last request is released
+};
+
+struct ServerReq {
+    uint64_t ticket = 0;
+    int kind = 0;
+    uint32_t res = 0;
+    double bmin[3], bmax[3];
+    std::vector<ria_function> funcs;
+    std::vector<int32_t> tree;
+    int32_t positive_inside = 1;
+    uint64_t bytes = 0;
+    std::chrono::steady_clock::time_point arrival;
+    // result
+    bool done = false;
+    ria_status status = RIA_OK;
+    std::string error;
+    std::shared_ptr<ServerBatch> batch;
+    uint32_t problem = 0;
+    std::vector<uint8_t> labels;
+    double latency = 0.0;
+};
+
+// device bytes one problem can hold at its peak: values and masks per vertex, generated tets and
+// filter lists per tet, records and mesh per tet as an upper estimate
+uint64_t request_bytes(uint32_t res, uint32_t F) {
+    const uint64_t N = (uint64_t)res + 1, V = N * N * N, T = 5ull * res * res * res;
+    return V * (8ull * F + 64) + T * 256;
+}
+
+}  // namespace
+
+struct ria_server {
+    ria_config cfg{};
+    int dev = 0;
+    uint64_t budget = 0, used = 0;
+    uint32_t max_batch = 256;
+    std::mutex mu;
+    std::condition_variable cv_work, cv_done;
+    std::deque<std::shared_ptr<ServerReq>> pending;
+    std::map<uint64_t, std::shared_ptr<ServerReq>> reqs;
+    uint64_t next_ticket = 1;
+    bool stop = false;
+    std::vector<std::thread> workers;
+
+    void work() {
+        cudaSetDevice(dev);
+        for (;;) {
+            std::vector<std::shared_ptr<ServerReq>> take;
+            uint64_t bytes = 0;
+            {
+                std::unique_lock<std::mutex> lk(mu);
+                cv_work.wait(lk, [&] { return stop || (!pending.empty() && used + pending.front()->bytes <= budget); });
+                if (stop) return;
+                // the oldest request decides the class (material interface, or arrangement and CSG);
+                // later requests of that class join while the budget allows
+                const bool mi = pending.front()->kind == RIA_REQ_MI;
+                for (auto it = pending.begin(); it != pending.end() && take.size() < max_batch;) {
+                    if (((*it)->kind == RIA_REQ_MI) != mi) {
+                        ++it;
+                        continue;
+                    }
+                    if (used + bytes + (*it)->bytes > budget) break;
+                    bytes += (*it)->bytes;
+                    take.push_back(*it);
+                    it = pending.erase(it);
+                }
+                used += bytes;
+            }
+            run(take, bytes);
+        }
+    }
+
+    void run(std::vector<std::shared_ptr<ServerReq>>& take, uint64_t bytes) {
+        std::vector<ria_grid_problem> probs(take.size());
+        for (size_t i = 0; i < take.size(); ++i) {
+            ria_grid_problem& p = probs[i];
+            p.resolution = take[i]->res;
+            p.n_func = (uint32_t)take[i]->funcs.size();
+            for (int a = 0; a < 3; ++a) {
+                p.bbox_min[a] = take[i]->bmin[a];
+                p.bbox_max[a] = take[i]->bmax[a];
+            }
+            p.funcs = take[i]->funcs.data();
+        }
+        const bool mi = take.front()->kind == RIA_REQ_MI;
+        ria_mesh* m = nullptr;
+        ria_status st = grid_batch_run(mi, &cfg, probs.data(), (uint32_t)probs.size(), &m);
+        const std::string err = st == RIA_OK ? std::string() : g_err;
+        auto batch = std::make_shared<ServerBatch>();
+        batch->mesh = m;
+        batch->bytes = bytes;
+        std::vector<ria_status> rs(take.size(), st);
+        std::vector<std::vector<uint8_t>> labels(take.size());
+        if (st == RIA_OK)
+            for (size_t i = 0; i < take.size(); ++i)
+                if (take[i]->kind == RIA_REQ_CSG) {
+                    const BatchInfo& b = m->batch[i];
+                    labels[i].resize((size_t)(b.flast - b.ffirst));
+                    rs[i] = run_csg(m, b.ffirst, b.flast, b.F, b.res, b.tbase, b.vbase,
+                                    take[i]->tree.empty() ? nullptr : take[i]->tree.data(),
+                                    (uint32_t)(take[i]->tree.size() / 3), take[i]->positive_inside, labels[i].data());
+                }
+        const auto now = std::chrono::steady_clock::now();
+        std::lock_guard<std::mutex> lk(mu);
+        if (st != RIA_OK) used -= bytes;
+        for (size_t i = 0; i < take.size(); ++i) {
+            ServerReq& r = *take[i];
+            r.status = rs[i];
+            r.error = rs[i] == RIA_OK ? std::string() : (st != RIA_OK ? err : g_err);
+            if (st == RIA_OK) {
+                r.batch = batch;
+                ++batch->refs;
+            }
+            r.problem = (uint32_t)i;
+            r.labels.swap(labels[i]);
+            r.latency = std::chrono::duration<double>(now - r.arrival).count();
+            r.done = true;
+        }
+        cv_done.notify_all();
+        cv_work.notify_all();
+    }
+
+    // caller holds mu
+    void release_batch(const std::shared_ptr<ServerBatch>& b) {
+        if (--b->refs == 0) {
+            ria_mesh_free(b->mesh);
+            b->mesh = nullptr;
+            used -= b->bytes;
+            cv_work.notify_all();
+        }
+    }
+};
+
+extern "C" {
+
+ria_status ria_server_create(const ria_config* cfg, uint64_t hbm_budget_bytes, uint32_t streams, uint32_t max_batch,
+                             ria_server** out) {
+    if (!cfg || !out || hbm_budget_bytes == 0 || streams == 0 || streams > 16) return fail(RIA_EINVAL, "bad argument");
+    int dev = 0;
+    ria_status st = current_device(&dev);
+    if (st != RIA_OK) return st;
+    DeviceCtx* ctx = nullptr;
+    cudaStream_t s;
+    RIA_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    st = ensure_table(false, s, &ctx);
+    if (st == RIA_OK) st = ensure_table(true, s, &ctx);
+    cudaStreamDestroy(s);
+    if (st != RIA_OK) return st;
+    ria_server* sv = new ria_server();
+    sv->cfg = *cfg;
+    sv->cfg.robust_test = 0;
+    sv->dev = dev;
+    sv->budget = hbm_budget_bytes;
+    sv->max_batch = max_batch ? max_batch : 256;
+    for (uint32_t i = 0; i < streams; ++i) sv->workers.emplace_back([sv] { sv->work(); });
+    *out = sv;
+    return RIA_OK;
+}
+
+ria_status ria_server_submit(ria_server* sv, const ria_request* q, uint64_t* ticket) {
+    if (!sv || !q || !ticket || !q->grid.funcs) return fail(RIA_EINVAL, "null argument");
+    if (q->kind < RIA_REQ_IA || q->kind > RIA_REQ_CSG) return fail(RIA_EINVAL, "unknown request kind");
+    if (q->grid.resolution == 0 || q->grid.resolution > 1200) return fail(RIA_EINVAL, "resolution must be in 1..1200");
+    if (q->grid.n_func < 1 || q->grid.n_func > 64) return fail(RIA_EINVAL, "n_func must be in 1..64");
+    if (q->csg_units && !q->csg_tree) return fail(RIA_EINVAL, "null CSG tree");
+    if (q->kind == RIA_REQ_CSG && q->csg_units) {
+        std::vector<int32_t> prog;
+        if (!csg_emit(q->csg_tree, q->csg_units, (int)q->grid.n_func, 1, 0, prog))
+            return fail(RIA_EINVAL, "invalid CSG tree");
+    }
+    auto r = std::make_shared<ServerReq>();
+    r->kind = q->kind;
+    r->res = q->grid.resolution;
+    for (int a = 0; a < 3; ++a) {
+        r->bmin[a] = q->grid.bbox_min[a];
+        r->bmax[a] = q->grid.bbox_max[a];
+    }
+    r->funcs.assign(q->grid.funcs, q->grid.funcs + q->grid.n_func);
+    if (q->kind == RIA_REQ_CSG && q->csg_units) r->tree.assign(q->csg_tree, q->csg_tree + 3 * (size_t)q->csg_units);
+    r->positive_inside = q->positive_inside;
+    r->bytes = request_bytes(q->grid.resolution, q->grid.n_func);
+    if (r->bytes > sv->budget) return fail(RIA_ENOMEM, "request larger than the server's HBM budget");
+    r->arrival = std::chrono::steady_clock::now();
+    {
+        std::lock_guard<std::mutex> lk(sv->mu);
+        r->ticket = sv->next_ticket++;
+        sv->reqs[r->ticket] = r;
+        sv->pending.push_back(r);
+    }
+    sv->cv_work.notify_one();
+    *ticket = r->ticket;
+    return RIA_OK;
+}
+
+ria_status ria_server_wait(ria_server* sv, uint64_t ticket, double timeout_s, const ria_mesh** mesh, uint32_t* problem,
+                           double* latency_s) {
+    if (!sv) return fail(RIA_EINVAL, "null argument");
+    std::unique_lock<std::mutex> lk(sv->mu);
+    auto it = sv->reqs.find(ticket);
+    if (it == sv->reqs.end()) return fail(RIA_EINVAL, "unknown ticket");
+    std::shared_ptr<ServerReq> r = it->second;
+    auto ready = [&] { return r->done; };
+    if (timeout_s < 0) {
+        sv->cv_done.wait(lk, ready);
+    } else if (!sv->cv_done.wait_for(lk, std::chrono::duration<double>(timeout_s), ready)) {
+        return fail(RIA_ETIMEOUT, "request not finished");
+    }
+    if (r->status != RIA_OK) return fail(r->status, r->error);
+    if (mesh) *mesh = r->batch->mesh;
+    if (problem) *problem = r->problem;
+    if (latency_s) *latency_s = r->latency;
+    return RIA_OK;
+}
+
+uint64_t ria_server_labels(ria_server* sv, uint64_t ticket, uint8_t* dst) {
+    if (!sv) return 0;
+    std::lock_guard<std::mutex> lk(sv->mu);
+    auto it = sv->reqs.find(ticket);
+    if (it == sv->reqs.end() || !it->second->done) return 0;
+    const std::vector<uint8_t>& l = it->second->labels;
+    if (dst && !l.empty()) std::memcpy(dst, l.data(), l.size());
+    return l.size();
+}
+
+void ria_server_release(ria_server* sv, uint64_t ticket) {
+    if (!sv) return;
+    std::lock_guard<std::mutex> lk(sv->mu);
+    auto it = sv->reqs.find(ticket);
+    if (it == sv->reqs.end() || !it->second->done) return;
+    if (it->second->batch) sv->release_batch(it->second->batch);
+    sv->reqs.erase(it);
+}
+
+void ria_server_destroy(ria_server* sv) {
+    if (!sv) return;
+    {
+        std::lock_guard<std::mutex> lk(sv->mu);
+        sv->stop = true;
+    }
+    sv->cv_work.notify_all();
+    for (auto& t : sv->workers) t.join();
+    std::lock_guard<std::mutex> lk(sv->mu);
+    for (auto& kv : sv->reqs)
+        if (kv.second->batch) sv->release_batch(kv.second->batch);
+    sv->reqs.clear();
+    delete sv;
 }
 
 const char* ria_last_error(void) { return g_err.c_str(); }

@@ -19,6 +19,13 @@ enum : int { CUT_OK = 0, CUT_DEFER = 1, CUT_FAIL = 2 };
 constexpr uint8_t kNoCell = 0xFF;
 
 RIA_HD uint64_t bit64(int l) { return uint64_t(1) << l; }
+RIA_HD int popc64u(uint64_t x) {
+#if defined(__CUDA_ARCH__)
+    return __popcll(x);
+#else
+    return __builtin_popcountll(x);
+#endif
+}
 RIA_HD int ctz64(uint64_t x) {
 #if defined(__CUDA_ARCH__)
     return __ffsll((long long)x) - 1;
@@ -26,6 +33,25 @@ RIA_HD int ctz64(uint64_t x) {
     return __builtin_ctzll(x);
 #endif
 }
+
+// A set of cells (ids below N), one 64-bit word per 64 cells.
+template <int N>
+struct CellSet {
+    uint64_t w[(N + 63) / 64];
+    RIA_HD void clear() {
+        for (int i = 0; i < (N + 63) / 64; ++i) w[i] = 0;
+    }
+    RIA_HD void set(int c) { w[c >> 6] |= uint64_t(1) << (c & 63); }
+    RIA_HD bool test(int c) const { return (w[c >> 6] >> (c & 63)) & 1; }
+    RIA_HD void meet(const CellSet& a, const CellSet& b) {
+        for (int i = 0; i < (N + 63) / 64; ++i) w[i] = a.w[i] & b.w[i];
+    }
+    RIA_HD bool any() const {
+        uint64_t o = 0;
+        for (int i = 0; i < (N + 63) / 64; ++i) o |= w[i];
+        return o != 0;
+    }
+};
 
 // Tet face b is opposite corner b; loops run counter-clockwise seen from inside the tet in the
 // reference frame x = (P1, P2, P3).
@@ -113,7 +139,7 @@ RIA_HD void ia_record_summary(const uint8_t* b, IASummary& sum) {
     const uint8_t* rep = b + 10;
     const uint8_t* faces = rep + k + 3 * nv;
     const uint8_t* loops = faces + 8 * nf;
-    uint64_t iso[2] = {0, 0};
+    uint64_t iso[4] = {0, 0, 0, 0};
     int nisof = 0, nloop = 0, nbnd = 0, off = 0;
     for (int f = 0; f < nf; ++f) {
         const int p = faces[8 * f];
@@ -131,11 +157,9 @@ RIA_HD void ia_record_summary(const uint8_t* b, IASummary& sum) {
         }
         off += L;
     }
-#if defined(__CUDA_ARCH__)
-    sum.n_iso_v = (uint16_t)(__popcll(iso[0]) + __popcll(iso[1]));
-#else
-    sum.n_iso_v = (uint16_t)(__builtin_popcountll(iso[0]) + __builtin_popcountll(iso[1]));
-#endif
+    int niso = 0;
+    for (int w = 0; w < 4; ++w) niso += popc64u(iso[w]);
+    sum.n_iso_v = (uint16_t)niso;
     sum.n_iso_f = (uint16_t)nisof;
     sum.n_iso_loop = (uint16_t)nloop;
     sum.n_bnd_f = (uint16_t)nbnd;
@@ -265,19 +289,29 @@ struct IACut {
                 sg[v] = (int8_t)s;
                 if (s == 0) mask[v] |= bit64(q);
             }
-            uint64_t cpos = 0, cneg = 0;
+            CellSet<MC> cpos, cneg, strad;
+            cpos.clear();
+            cneg.clear();
             for (int f = 0; f < nf; ++f) {
-                uint64_t cm = bit64(fpos[f]) | (fneg[f] != kNoCell ? bit64(fneg[f]) : 0);
+                bool hp = false, hn = false;
                 for (int j = 0; j < flen[f]; ++j) {
                     int s = sg[loops[cur][foff[f] + j]];
-                    if (s > 0) cpos |= cm;
-                    if (s < 0) cneg |= cm;
+                    hp = hp || s > 0;
+                    hn = hn || s < 0;
+                }
+                if (hp) {
+                    cpos.set(fpos[f]);
+                    if (fneg[f] != kNoCell) cpos.set(fneg[f]);
+                }
+                if (hn) {
+                    cneg.set(fpos[f]);
+                    if (fneg[f] != kNoCell) cneg.set(fneg[f]);
                 }
             }
-            uint64_t strad = cpos & cneg;
+            strad.meet(cpos, cneg);
             for (int c = 0; c < nc; ++c)
-                if (!(strad & bit64(c)) && (cpos & bit64(c))) csign[c] |= bit64(q);
-            if (!strad) continue;
+                if (!strad.test(c) && cpos.test(c)) csign[c] |= bit64(q);
+            if (!strad.any()) continue;
 
             // new vertices on crossing edges
             int ne = 0;
@@ -398,7 +432,7 @@ struct IACut {
             const int nc0 = nc;
             for (int c = 0; c < nc0; ++c) {
                 cneg_of[c] = kNoCell;
-                if (!(strad & bit64(c))) continue;
+                if (!strad.test(c)) continue;
                 if (nc >= MC) return kBad;
                 cneg_of[c] = (uint8_t)nc;
                 csign[nc] = csign[c];
@@ -406,7 +440,7 @@ struct IACut {
                 ++nc;
             }
             for (int c = 0; c < nc0; ++c) {
-                if (!(strad & bit64(c))) continue;
+                if (!strad.test(c)) continue;
                 uint8_t et[MF], eh[MF];
                 int nedge = 0;
                 for (int f = 0; f < nf0; ++f) {

@@ -10,6 +10,8 @@
 //                tet per sign pattern (corner values in {-1, 0, 1}).
 // Records are appended to a byte heap with an atomic bump pointer; their placement does not affect
 // the result, which only depends on the per-tet record contents.
+#include <type_traits>
+
 #include "device_common.cuh"
 #include "launch.hpp"
 #include "lookup2.cuh"
@@ -36,15 +38,18 @@ struct Traits;
 template <>
 struct Traits<false> {
     using Fast = IACutFast;
+    using Mid = IACutMid;
     using Big = IACutBig;
     using Sum = IASummary;
 };
 template <>
 struct Traits<true> {
     using Fast = MICutFast;
+    using Mid = MICutMid;
     using Big = MICutBig;
     using Sum = MISummary;
 };
+constexpr int kMidMaxK = 16;
 
 template <bool MI>
 struct BigSlot {
@@ -77,15 +82,17 @@ __device__ __forceinline__ int gather_planes(const CutArgs& a, uint32_t ai, doub
     return k;
 }
 
-// returns the record's place in the heap (nullptr on overflow)
+// returns the record's place in the heap; nullptr when the heap is full (the exact kernel then
+// reports the capacity; the filtered kernels hand the tet to the exact kernel, whose heap is sized
+// by the record bound)
 template <class Cut, class Sum>
 __device__ __forceinline__ const uint8_t* finish_cut(const CutArgs& a, uint32_t ai, Cut& c, int* size_out,
-                                                     IASum4* sum_out) {
+                                                     IASum4* sum_out, bool defer_when_full = false) {
     c.canonicalize();
     const int size = c.record_size();
     unsigned long long off = atomicAdd(a.heap_used, (unsigned long long)size);
     if (off + size > a.heap_cap) {
-        raise_status(a.status, ST_CAPACITY);
+        if (!defer_when_full) raise_status(a.status, ST_CAPACITY);
         return nullptr;
     }
     Sum s;
@@ -168,17 +175,18 @@ __device__ __forceinline__ bool ia_try_template(const CutArgs& a, uint32_t ai, c
     return true;
 }
 
-template <bool MI>
+template <bool MI, bool MID>
 __global__ void __launch_bounds__(128) k_cut_fast(CutArgs a) {
-    using Fast = typename Traits<MI>::Fast;
+    using Fast = typename std::conditional<MID, typename Traits<MI>::Mid, typename Traits<MI>::Fast>::type;
     using Sum = typename Traits<MI>::Sum;
+    constexpr int kMax = MID ? kMidMaxK : kFastMaxK;
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.n) return;
     const uint32_t ai = a.list[i];
-    double planes[4 * kFastMaxK];
-    const int k = gather_planes(a, ai, planes, kFastMaxK);
+    double planes[4 * kMax];
+    const int k = gather_planes(a, ai, planes, kMax);
     bool keyed = false;
-    if (!MI && k <= kFastMaxK && ia_try_template(a, ai, planes, k, &keyed)) return;
+    if (!MI && k <= kMax && k <= kFastMaxK && ia_try_template(a, ai, planes, k, &keyed)) return;
     if (MI) keyed = k == 3 && mi_distinct3(planes);
     uint32_t key = 0;
     if (keyed && a.cache.slots) {
@@ -196,12 +204,15 @@ __global__ void __launch_bounds__(128) k_cut_fast(CutArgs a) {
     }
     int st = CUT_DEFER;
     Fast c;
-    if (k <= kFastMaxK) st = c.run(planes, k);
+    if (k <= kMax) st = c.run(planes, k);
     if (st == CUT_OK) {
         int size = 0;
         IASum4 sum;
-        const uint8_t* rec = finish_cut<Fast, Sum>(a, ai, c, &size, &sum);
+        const uint8_t* rec = finish_cut<Fast, Sum>(a, ai, c, &size, &sum, true);
         if (rec && keyed) cache_insert(a.cache, key, rec, size, sum);
+        if (!rec) st = CUT_DEFER;
+    }
+    if (st == CUT_OK) {
     } else if (st == CUT_DEFER) {
         unsigned int d = atomicAdd(a.n_deferred, 1u);
         a.deferred[d] = ai;
@@ -337,23 +348,20 @@ void launch_robust(const CutArgs& a, void* scratch, int64_t slots, unsigned long
 
 size_t cut_big_slot_bytes(bool mi) { return mi ? sizeof(BigSlot<true>) : sizeof(BigSlot<false>); }
 
-void launch_cut_fast(const CutArgs& a, cudaStream_t s) {
+void launch_cut_fast(const CutArgs& a, cudaStream_t s, bool mid) {
     if (a.n == 0) return;
     // each thread runs one long serial cut: with few tets, smaller blocks spread them over all SMs
-    // (the FP64 pipe of one SM is shared by its resident warps)
     int bs = 128;
     while (bs > 32 && (a.n + bs - 1) / bs < 4 * 152) bs >>= 1;
     const unsigned nb = (unsigned)((a.n + bs - 1) / bs);
-    if (a.mi)
-        {
-            k_cut_fast<true><<<nb, bs, 0, s>>>(a);
-            note_launch();
-        }
-    else
-        {
-            k_cut_fast<false><<<nb, bs, 0, s>>>(a);
-            note_launch();
-        }
+    if (a.mi) {
+        if (mid) k_cut_fast<true, true><<<nb, bs, 0, s>>>(a);
+        else k_cut_fast<true, false><<<nb, bs, 0, s>>>(a);
+    } else {
+        if (mid) k_cut_fast<false, true><<<nb, bs, 0, s>>>(a);
+        else k_cut_fast<false, false><<<nb, bs, 0, s>>>(a);
+    }
+    note_launch();
 }
 
 template <bool MI>

@@ -43,9 +43,9 @@ struct ExtractCtx {
     uint32_t* ftoff;
 };
 
-// iso flags of the local vertices of an IA record (up to 128 vertices)
-__device__ __forceinline__ void iso_vertex_flags(const IAView& r, uint64_t iso[2]) {
-    iso[0] = iso[1] = 0;
+// iso flags of the local vertices of an IA record (vertex ids below 256)
+__device__ __forceinline__ void iso_vertex_flags(const IAView& r, uint64_t iso[4]) {
+    iso[0] = iso[1] = iso[2] = iso[3] = 0;
     int off = 0;
     for (int f = 0; f < r.nf; ++f) {
         int L = r.len(f);
@@ -58,9 +58,10 @@ __device__ __forceinline__ void iso_vertex_flags(const IAView& r, uint64_t iso[2
     }
 }
 
-__device__ __forceinline__ int iso_rank(const uint64_t iso[2], int v) {
-    if (v < 64) return __popcll(iso[0] & ((1ull << v) - 1));
-    return __popcll(iso[0]) + __popcll(iso[1] & ((1ull << (v - 64)) - 1));
+__device__ __forceinline__ int iso_rank(const uint64_t iso[4], int v) {
+    int n = 0;
+    for (int w = 0; w < (v >> 6); ++w) n += __popcll(iso[w]);
+    return n + __popcll(iso[v >> 6] & ((1ull << (v & 63)) - 1));
 }
 
 struct VertKey {
@@ -133,7 +134,7 @@ __global__ void __launch_bounds__(kBs) k_ia_vert_keys(ExtractCtx C) {
     TetSrc ts{C.a.d_tets, C.a.g.res};
     ts.get(C.a.act_tet[a], tv);
     const uint64_t mask = C.a.act_mask[a];
-    uint64_t iso[2];
+    uint64_t iso[4];
     iso_vertex_flags(r, iso);
     uint32_t pos = C.base[a].a;
     for (int j = 0; j < r.nv; ++j) {
@@ -267,7 +268,7 @@ __global__ void __launch_bounds__(kBs) k_ia_face_keys(ExtractCtx C) {
     if (a >= C.a.A) return;
     IAView r;
     r.init(C.rs.get(C.a.act_desc[a]));
-    uint64_t iso[2];
+    uint64_t iso[4];
     iso_vertex_flags(r, iso);
     const uint32_t vb = C.base[a].a;
     uint32_t fpos = C.base[a].b;
@@ -334,7 +335,7 @@ __global__ void __launch_bounds__(kBs) k_ia_face_emit(ExtractCtx C, int64_t* __r
     if (a >= C.a.A) return;
     IAView r;
     r.init(C.rs.get(C.a.act_desc[a]));
-    uint64_t iso[2];
+    uint64_t iso[4];
     iso_vertex_flags(r, iso);
     const uint32_t vb = C.base[a].a;
     uint32_t fpos = C.base[a].b;
@@ -449,8 +450,12 @@ cudaError_t run_extract(const ExtractArgs& a, const IASum4* act_sum, ExtractOut&
     e = scan_total(C.vflag, C.vgid_new, NV, &n_verts, s);
     if (e != cudaSuccess) return e;
     out.n_verts = n_verts;
-    cudaMallocAsync((void**)&out.xyz, sizeof(double) * 3 * (size_t)(n_verts > 0 ? n_verts : 1), s);
-    cudaMallocAsync((void**)&out.verts, sizeof(int64_t) * 11 * (size_t)(n_verts > 0 ? n_verts : 1), s);
+    if ((e = cudaMallocAsync((void**)&out.xyz, sizeof(double) * 3 * (size_t)(n_verts > 0 ? n_verts : 1), s)) !=
+        cudaSuccess)
+        return e;
+    if ((e = cudaMallocAsync((void**)&out.verts, sizeof(int64_t) * 11 * (size_t)(n_verts > 0 ? n_verts : 1), s)) !=
+        cudaSuccess)
+        return e;
     if (NV > 0) {
         k_vert_emit<<<nblk(NV), kBs, 0, s>>>(C, NV, out.verts, out.xyz);
         note_launch();
@@ -478,11 +483,16 @@ cudaError_t run_extract(const ExtractArgs& a, const IASum4* act_sum, ExtractOut&
     out.n_faces = n_faces;
     out.n_face_verts = n_fv;
     out.n_face_tets = n_ft;
-    cudaMallocAsync((void**)&out.face_offsets, sizeof(int64_t) * (size_t)(n_faces + 1), s);
-    cudaMallocAsync((void**)&out.face_verts, sizeof(int64_t) * (size_t)(n_fv > 0 ? n_fv : 1), s);
-    cudaMallocAsync((void**)&out.face_tet_offsets, sizeof(int64_t) * (size_t)(n_faces + 1), s);
-    cudaMallocAsync((void**)&out.face_tets, sizeof(int64_t) * 2 * (size_t)(n_ft > 0 ? n_ft : 1), s);
-    cudaMallocAsync((void**)&out.face_func, sizeof(int64_t) * 2 * (size_t)(n_faces > 0 ? n_faces : 1), s);
+    if ((e = cudaMallocAsync((void**)&out.face_offsets, sizeof(int64_t) * (size_t)(n_faces + 1), s)) != cudaSuccess ||
+        (e = cudaMallocAsync((void**)&out.face_verts, sizeof(int64_t) * (size_t)(n_fv > 0 ? n_fv : 1), s)) !=
+            cudaSuccess ||
+        (e = cudaMallocAsync((void**)&out.face_tet_offsets, sizeof(int64_t) * (size_t)(n_faces + 1), s)) !=
+            cudaSuccess ||
+        (e = cudaMallocAsync((void**)&out.face_tets, sizeof(int64_t) * 2 * (size_t)(n_ft > 0 ? n_ft : 1), s)) !=
+            cudaSuccess ||
+        (e = cudaMallocAsync((void**)&out.face_func, sizeof(int64_t) * 2 * (size_t)(n_faces > 0 ? n_faces : 1), s)) !=
+            cudaSuccess)
+        return e;
     if (A > 0)
         {
             k_ia_face_emit<<<nblk(A), kBs, 0, s>>>(C, out.face_offsets, out.face_verts, out.face_tet_offsets, out.face_tets,

@@ -130,9 +130,9 @@ __device__ __forceinline__ MIKey mi_vertex_key(const MIView& r, int j, const int
     return k;
 }
 
-// flags of the local vertices on an interface face (records have at most 128 vertices)
-__device__ __forceinline__ void mi_vertex_flags(const MIView& r, uint64_t f[2]) {
-    f[0] = f[1] = 0;
+// flags of the local vertices on an interface face (vertex ids below 256)
+__device__ __forceinline__ void mi_vertex_flags(const MIView& r, uint64_t f[4]) {
+    f[0] = f[1] = f[2] = f[3] = 0;
     int off = 0;
     for (int i = 0; i < r.nf; ++i) {
         const int L = r.len(i);
@@ -145,9 +145,10 @@ __device__ __forceinline__ void mi_vertex_flags(const MIView& r, uint64_t f[2]) 
     }
 }
 
-__device__ __forceinline__ int flag_rank(const uint64_t f[2], int v) {
-    if (v < 64) return __popcll(f[0] & ((1ull << v) - 1));
-    return __popcll(f[0]) + __popcll(f[1] & ((1ull << (v - 64)) - 1));
+__device__ __forceinline__ int flag_rank(const uint64_t f[4], int v) {
+    int n = 0;
+    for (int w = 0; w < (v >> 6); ++w) n += __popcll(f[w]);
+    return n + __popcll(f[v >> 6] & ((1ull << (v & 63)) - 1));
 }
 
 __device__ __forceinline__ bool is_corner(const MIView& r, int v) {
@@ -173,7 +174,7 @@ __global__ void __launch_bounds__(kBs) k_mi_vert_keys(MICtx C) {
     TetSrc ts{C.a.d_tets, C.a.g.res};
     ts.get(C.a.act_tet[a], tv);
     const uint64_t mask = C.a.act_mask[a];
-    uint64_t fl[2];
+    uint64_t fl[4];
     mi_vertex_flags(r, fl);
     uint32_t pos = C.base0[a].a;
     for (int j = 0; j < r.nv; ++j) {
@@ -228,7 +229,7 @@ __device__ __forceinline__ void pack3(int64_t a, int64_t b, int64_t c, uint64_t&
 
 // encoded vertex of a boundary-face loop: tet corners -v-1, interface vertices their identity
 __device__ __forceinline__ int64_t bnd_code(const MICtx& C, const MIView& r, int lv, const int64_t tv[4],
-                                            const uint64_t fl[2], uint32_t b0) {
+                                            const uint64_t fl[4], uint32_t b0) {
     if (is_corner(r, lv)) return -tv[corner_of(r.vlab + 4 * lv, 3)] - 1;
     if (!((fl[lv >> 6] >> (lv & 63)) & 1)) {  // every other boundary vertex lies on an interface
         raise_status(C.a.status, ST_INTERNAL);
@@ -247,7 +248,7 @@ __global__ void __launch_bounds__(kBs) k_mi_bnd_keys(MICtx C) {
     TetSrc ts{C.a.d_tets, C.a.g.res};
     ts.get(C.a.act_tet[a], tv);
     const uint64_t mask = C.a.act_mask[a];
-    uint64_t fl[2];
+    uint64_t fl[4];
     mi_vertex_flags(r, fl);
     const uint32_t b0 = C.base0[a].a;
     uint32_t bpos = C.base0[a].d;
@@ -345,7 +346,7 @@ __global__ void __launch_bounds__(kBs) k_mi_final_occ(MICtx C) {
     ts.get(C.a.act_tet[a], tv);
     const uint32_t b0 = C.base0[a].a;
     uint32_t pos = C.vbase[a].a;
-    uint64_t fl[2];
+    uint64_t fl[4];
     mi_vertex_flags(r, fl);
     const int cnt0 = __popcll(fl[0]) + __popcll(fl[1]);
     for (int i = 0; i < cnt0; ++i) {
@@ -487,7 +488,7 @@ __global__ void __launch_bounds__(kBs) k_mi_face_emit(MICtx C, bool with_extra, 
     const uint32_t tet = C.a.act_tet[a];
     ts.get(tet, tv);
     const uint64_t mask = C.a.act_mask[a];
-    uint64_t fl[2];
+    uint64_t fl[4];
     mi_vertex_flags(r, fl);
     const uint32_t vb = C.vbase[a].a;
     uint32_t fpos = C.vbase[a].b;
@@ -650,13 +651,18 @@ cudaError_t run_extract_mi(const ExtractArgs& a, const IASum4* act_sum, ExtractO
     out.n_faces = NF;
     out.n_face_verts = NL;
     out.n_face_tets = NF;
-    cudaMallocAsync((void**)&out.xyz, sizeof(double) * 3 * (size_t)(n_verts > 0 ? n_verts : 1), s);
-    cudaMallocAsync((void**)&out.verts, sizeof(int64_t) * 11 * (size_t)(n_verts > 0 ? n_verts : 1), s);
-    cudaMallocAsync((void**)&out.face_offsets, sizeof(int64_t) * (size_t)(NF + 1), s);
-    cudaMallocAsync((void**)&out.face_verts, sizeof(int64_t) * (size_t)(NL > 0 ? NL : 1), s);
-    cudaMallocAsync((void**)&out.face_tet_offsets, sizeof(int64_t) * (size_t)(NF + 1), s);
-    cudaMallocAsync((void**)&out.face_tets, sizeof(int64_t) * 2 * (size_t)(NF > 0 ? NF : 1), s);
-    cudaMallocAsync((void**)&out.face_func, sizeof(int64_t) * 2 * (size_t)(NF > 0 ? NF : 1), s);
+    if ((e = cudaMallocAsync((void**)&out.xyz, sizeof(double) * 3 * (size_t)(n_verts > 0 ? n_verts : 1), s)) !=
+            cudaSuccess ||
+        (e = cudaMallocAsync((void**)&out.verts, sizeof(int64_t) * 11 * (size_t)(n_verts > 0 ? n_verts : 1), s)) !=
+            cudaSuccess ||
+        (e = cudaMallocAsync((void**)&out.face_offsets, sizeof(int64_t) * (size_t)(NF + 1), s)) != cudaSuccess ||
+        (e = cudaMallocAsync((void**)&out.face_verts, sizeof(int64_t) * (size_t)(NL > 0 ? NL : 1), s)) != cudaSuccess ||
+        (e = cudaMallocAsync((void**)&out.face_tet_offsets, sizeof(int64_t) * (size_t)(NF + 1), s)) != cudaSuccess ||
+        (e = cudaMallocAsync((void**)&out.face_tets, sizeof(int64_t) * 2 * (size_t)(NF > 0 ? NF : 1), s)) !=
+            cudaSuccess ||
+        (e = cudaMallocAsync((void**)&out.face_func, sizeof(int64_t) * 2 * (size_t)(NF > 0 ? NF : 1), s)) !=
+            cudaSuccess)
+        return e;
     if (NV > 0) {
         k_mi_vert_emit<<<nblk(NV), kBs, 0, s>>>(C, NV, out.verts, out.xyz);
         note_launch();

@@ -152,7 +152,12 @@ struct CutArgs {
         IASum4* table_sum = nullptr;
     } cache;
 };
-void launch_cut_fast(const CutArgs& a, cudaStream_t s);
+// filtered variants, one thread per tet: `mid` for the heavy bins (four or more active functions,
+// up to 16), the small one otherwise; a tet that outgrows them, or whose record does not fit the
+// heap, goes to the deferred list
+void launch_cut_fast(const CutArgs& a, cudaStream_t s, bool mid = false);
+// first bin of tets for the small filtered variant (three or fewer active functions)
+constexpr int kFirstSmallBin(bool mi) { return mi ? 6 : 5; }
 // exact variant: one tet per block, state in shared memory
 void launch_cut_big(const CutArgs& a, cudaStream_t s);
 size_t cut_big_slot_bytes(bool mi);

@@ -11,5 +11,9 @@ using IACutFast = IACut<32, 48, 16, 192, false>;
 // per block with the state in shared memory (about 44 KB / 31 KB)
 using IACutBig = IACut<255, 1024, 254, 8192, true>;
 using MICutFast = MICut<32, 24, 160, 48, 48, 256, false>;
+// mid-size filtered variants for the heavy bins (four or more active functions): one thread per tet,
+// state in local memory, about four times the fast capacity
+using IACutMid = IACut<128, 256, 64, 1024, false>;
+using MICutMid = MICut<96, 96, 640, 128, 128, 1024, false>;
 using MICutBig = MICut<255, 255, 2048, 255, 512, 4096, true>;
 }  // namespace ria

@@ -302,6 +302,65 @@ def workload_batch(seed=4, n=4096, mode="ia", verts_per_axis=(9, 33), funcs=(2, 
     return BatchWorkload("batch-%d-grids" % n, mode, probs)
 
 
+def random_csg_tree(rng, n_func, depth=4):
+    """A random CSG tree (units {op, a, b}: 0 intersection, 1 union, 2 negation) of depth <= `depth`
+    over functions 0..n_func-1, unit 1 the root."""
+    units = []
+
+    def node(d):
+        if d >= depth or rng.random() < 0.3:
+            return -int(rng.integers(0, n_func)) - 1
+        op = int(rng.choice([0, 1, 1, 2]))
+        units.append(None)
+        me = len(units)
+        a = node(d + 1)
+        b = node(d + 1) if op != 2 else 0
+        units[me - 1] = (op, a, b)
+        return me
+
+    root = node(0)
+    if root < 0:  # a lone function: wrap it so that unit 1 exists
+        return [(1, root, root)]
+    return units
+
+
+@dataclass
+class Request:
+    kind: str  # "ia", "mi" or "csg"
+    res: int
+    funcs: np.ndarray
+    tree: list = None
+
+    @property
+    def n_tets(self):
+        return 5 * self.res ** 3
+
+
+def workload_serve(seed=5, n=1000, tets=(10_000, 2_000_000), funcs=(2, 16), mix=(0.6, 0.3, 0.1)):
+    """Served form: requests of the three kinds, tet counts log-uniform in `tets` (grid resolution
+    rounded from it), function counts uniform in `funcs`."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n):
+        u = rng.random()
+        kind = "ia" if u < mix[0] else ("mi" if u < mix[0] + mix[1] else "csg")
+        T = float(np.exp(rng.uniform(np.log(tets[0]), np.log(tets[1]))))
+        res = max(1, int(round((T / 5.0) ** (1.0 / 3.0))))
+        F = int(rng.integers(funcs[0], funcs[1] + 1))
+        tree = None
+        if kind == "mi":
+            specs = [{"type": "sphere", "center": list(rng.uniform(-0.8, 0.8, 3)),
+                      "radius": float(rng.uniform(0.0, 0.2))} for _ in range(F)]
+        elif kind == "csg":
+            specs = [random_function_spec(rng, ["sphere", "cylinder"][int(rng.integers(0, 2))]) for _ in range(F)]
+            tree = random_csg_tree(rng, F)
+        else:
+            kinds = ["plane", "sphere", "cylinder", "torus"]
+            specs = [random_function_spec(rng, kinds[int(rng.integers(0, 4))]) for _ in range(F)]
+        out.append(Request(kind, res, make_functions(specs), tree))
+    return out
+
+
 WORKLOADS = {
     "ia-small": workload_ia_small,
     "mi": workload_mi,

@@ -401,4 +401,101 @@ bool save_statistics(const std::string& filename, const std::vector<std::string>
     return true;
 }
 
+bool save_result_CSG(const std::string& filename, const std::vector<std::array<double, 3>>& pts,
+                     const std::vector<PolygonFace>& faces, const std::vector<std::vector<size_t>>& patches,
+                     const std::vector<bool>& patch_sign_label, const std::vector<Edge>& edges,
+                     const std::vector<std::vector<size_t>>& chains,
+                     const std::vector<std::vector<size_t>>& nm_edges_of_vert) {
+    // src/io.cpp:314-372: no shells, cells or cell labels
+    std::ostringstream o;
+    o << "{\"chains\":";
+    put_lists(o, chains);
+    std::vector<size_t> corners;
+    for (size_t i = 0; i < nm_edges_of_vert.size(); ++i)
+        if (nm_edges_of_vert[i].size() > 2 || nm_edges_of_vert[i].size() == 1) corners.push_back(i);
+    o << ",\"corners\":";
+    if (corners.empty())
+        o << "null";
+    else
+        put_list(o, corners);
+    o << ",\"edges\":";
+    if (edges.empty()) {
+        o << "null";
+    } else {
+        o << '[';
+        for (size_t i = 0; i < edges.size(); ++i) o << (i ? "," : "") << '[' << edges[i].v1 << ',' << edges[i].v2 << ']';
+        o << ']';
+    }
+    o << ",\"faces\":";
+    if (faces.empty()) {
+        o << "null";
+    } else {
+        o << '[';
+        for (size_t i = 0; i < faces.size(); ++i) {
+            if (i) o << ',';
+            put_list(o, faces[i].vert_indices);
+        }
+        o << ']';
+    }
+    o << ",\"patches\":";
+    put_lists(o, patches);
+    o << ",\"patches_label\":[[";
+    for (size_t i = 0; i < patch_sign_label.size(); ++i) o << (i ? "," : "") << (patch_sign_label[i] ? "true" : "false");
+    o << "]],\"points\":";
+    if (pts.empty()) {
+        o << "null";
+    } else {
+        o << '[';
+        for (size_t i = 0; i < pts.size(); ++i)
+            o << (i ? "," : "") << '[' << json_double(pts[i][0]) << ',' << json_double(pts[i][1]) << ','
+              << json_double(pts[i][2]) << ']';
+        o << ']';
+    }
+    o << "}\n";
+    std::ofstream f(filename);
+    f << o.str();
+    return true;
+}
+
+bool load_csg_tree(const std::string& filename, std::vector<CsgUnit>& tree) {
+    std::ifstream fin(filename);
+    if (!fin) {
+        std::cout << "function file not exist!" << std::endl;
+        return false;
+    }
+    Json d = JsonParser(read_file(filename)).parse();
+    tree.clear();
+    for (size_t j = 0; j < d.size(); ++j) {
+        const std::string& t = d[j]["type"].as_string();
+        CsgUnit u;
+        u.op = t == "Intersection" ? 0 : (t == "Union" ? 1 : (t == "Negation" ? 2 : -1));
+        if (u.op < 0) throw std::runtime_error("not a valid CSG operation: " + t);
+        for (int i = 0; i < 2; ++i) u.elements[i] = (int)d[j]["elements"][i].as_double();
+        tree.push_back(u);
+    }
+    return true;
+}
+
+std::function<bool(std::vector<bool>)> csg_lambda(const std::vector<CsgUnit>& tree) {
+    if (tree.empty())
+        return [](std::vector<bool> labels) {
+            for (bool b : labels)
+                if (b) return true;
+            return false;
+        };
+    return [tree](std::vector<bool> labels) {
+        // app/csg.cpp:54-136: function j is [1, 2] where positive, [-1, -2] elsewhere; union is the
+        // maximum, intersection the minimum, negation the mirror; inside where the root is positive
+        std::function<bool(int, int)> ev = [&](int e, int depth) -> bool {
+            if (depth > 1000) throw std::runtime_error("CSG tree too deep or cyclic");
+            if (e < 0) return labels.at((size_t)(-e - 1));
+            const CsgUnit& u = tree.at((size_t)(e - 1));
+            if (u.op == 2) return !ev(u.elements[0], depth + 1);
+            const bool a = ev(u.elements[0], depth + 1), b = ev(u.elements[1], depth + 1);
+            return u.op == 0 ? (a && b) : (a || b);
+        };
+        return ev(1, 0);
+    };
+}
+
 }  // namespace ria_host

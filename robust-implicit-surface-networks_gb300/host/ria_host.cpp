@@ -51,7 +51,8 @@ bool run_pipeline(bool mi, bool robust_test, bool use_lookup, bool use_secondary
                   std::vector<Label>& patch_function_label, std::vector<Edge>& edges,
                   std::vector<std::vector<size_t>>& chains, std::vector<std::vector<size_t>>& nm_edges_of_vert,
                   std::vector<std::string>& timing_labels, std::vector<double>& timings,
-                  std::vector<std::string>& stats_labels, std::vector<size_t>& stats) {
+                  std::vector<std::string>& stats_labels, std::vector<size_t>& stats,
+                  std::vector<uint64_t>* face_sides = nullptr) {
     if (!use_lookup) use_secondary_lookup = false;
     ria_config cfg{use_lookup ? 1 : 0, use_secondary_lookup ? 1 : 0, 1, robust_test ? 1 : 0, 0};
     DeviceMesh dm;
@@ -83,6 +84,13 @@ bool run_pipeline(bool mi, bool robust_test, bool use_lookup, bool use_secondary
     ria_mesh_copy(dm.m, RIA_MESH_TIMINGS, tm);
     fetch_points(dm, out_pts);
     fetch_faces(dm, faces);
+    if (face_sides) {
+        face_sides->assign(2 * faces.size(), 0);
+        if (!faces.empty() && ria_mesh_face_sides(dm.m, face_sides->data()) != RIA_OK) {
+            std::cout << ria_last_error() << std::endl;
+            return false;
+        }
+    }
     const double t1 = now();
     const char* ia_names[] = {"num_pts", "num_tets", "num_degenerate_vertex", "num_intersecting_tet",
                               "num_1_func", "num_2_func", "num_more_func", "num_iso_verts", "num_iso_faces"};
@@ -193,6 +201,70 @@ bool material_interface(bool robust_test, bool use_lookup, bool use_secondary_lo
                                                    funcVals, n_func, MI_pts, MI_faces, patches, patch_function_label,
                                                    MI_edges, chains, non_manifold_edges_of_vert, timing_labels, timings,
                                                    stats_labels, stats);
+}
+
+bool csg(bool robust_test, bool use_lookup, bool use_secondary_lookup, bool, bool positive_inside,
+         const std::vector<std::array<double, 3>>& pts, const std::vector<std::array<size_t, 4>>& tets,
+         const double* funcVals, size_t n_func, const std::function<bool(std::vector<bool>)>& lambda,
+         std::vector<std::array<double, 3>>& mesh_pts, std::vector<PolygonFace>& mesh_faces,
+         std::vector<std::vector<size_t>>& patches, std::vector<size_t>& patch_function_label,
+         std::vector<bool>& patch_sign_label, std::vector<Edge>& edges, std::vector<std::vector<size_t>>& chains,
+         std::vector<std::vector<size_t>>& non_manifold_edges_of_vert, std::vector<std::vector<size_t>>& shells,
+         std::vector<std::vector<size_t>>& cells, std::vector<std::vector<bool>>& cell_function_label,
+         std::vector<std::string>& timing_labels, std::vector<double>& timings, std::vector<std::string>& stats_labels,
+         std::vector<size_t>& stats) {
+    shells.clear();
+    cells.clear();
+    cell_function_label.clear();
+    std::vector<double> negated;
+    if (!positive_inside) {  // src/csg.cpp:36
+        negated.assign(funcVals, funcVals + pts.size() * n_func);
+        for (double& x : negated) x = -x;
+        funcVals = negated.data();
+    }
+    std::vector<uint64_t> sides;
+    if (!run_pipeline<size_t>(false, robust_test, use_lookup, use_secondary_lookup, pts, tets, funcVals, n_func,
+                              mesh_pts, mesh_faces, patches, patch_function_label, edges, chains,
+                              non_manifold_edges_of_vert, timing_labels, timings, stats_labels, stats,
+                              robust_test ? nullptr : &sides))
+        return false;
+    if (robust_test) return true;
+    const double t0 = now();
+    // src/csg.cpp:55-116 with each patch's two cells labelled from the sides of its first face
+    auto labels = [&](uint64_t bits) {
+        std::vector<bool> v(n_func);
+        for (size_t j = 0; j < n_func; ++j) v[j] = (bits >> j) & 1;
+        return v;
+    };
+    std::vector<std::vector<size_t>> kept;
+    patch_sign_label.clear();
+    std::vector<size_t> vertex_to_patch_count(mesh_pts.size(), 0);
+    for (auto& patch : patches) {
+        const size_t f = patch.front();
+        const bool in_pos = lambda(labels(sides[2 * f])), in_neg = lambda(labels(sides[2 * f + 1]));
+        if (in_pos == in_neg) continue;
+        kept.push_back(patch);
+        patch_sign_label.push_back(in_pos);
+        for (size_t face : patch)
+            for (size_t v : mesh_faces[face].vert_indices) ++vertex_to_patch_count[v];
+    }
+    std::vector<std::vector<size_t>> kept_chains;
+    for (auto& chain : chains) {
+        bool active = true;
+        for (size_t e : chain)
+            if (vertex_to_patch_count[edges[e].v1] < 2 || vertex_to_patch_count[edges[e].v2] < 2) {
+                active = false;
+                break;
+            }
+        if (active) kept_chains.push_back(chain);
+    }
+    for (size_t v = 0; v < non_manifold_edges_of_vert.size(); ++v)
+        if (vertex_to_patch_count[v] <= 2) non_manifold_edges_of_vert[v].clear();
+    patches.swap(kept);
+    chains.swap(kept_chains);
+    timing_labels.emplace_back("csg prune");
+    timings.push_back(now() - t0);
+    return true;
 }
 
 }  // namespace ria_host

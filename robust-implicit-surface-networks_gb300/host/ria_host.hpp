@@ -13,6 +13,7 @@
 #pragma once
 #include <array>
 #include <cstddef>
+#include <functional>
 #include <limits>
 #include <string>
 #include <utility>
@@ -109,6 +110,39 @@ bool material_interface(bool robust_test, bool use_lookup, bool use_secondary_lo
                         std::vector<size_t>& cell_function_label, std::vector<std::string>& timing_labels,
                         std::vector<double>& timings, std::vector<std::string>& stats_labels, std::vector<size_t>& stats);
 
+// src/csg.h:46-72: the implicit arrangement, then the patches that separate the shape's inside
+// (lambda over a cell's function labels: true where the function is positive) from its outside;
+// chains and corners are pruned to the kept patches.  positive_inside = false negates the functions
+// first, as the reference does.  Cell labels come from the device (each face's two sides), not from
+// shells and cells.
+bool csg(bool robust_test, bool use_lookup, bool use_secondary_lookup, bool use_topo_ray_shooting, bool positive_inside,
+         const std::vector<std::array<double, 3>>& pts, const std::vector<std::array<size_t, 4>>& tets,
+         const double* funcVals, size_t n_func, const std::function<bool(std::vector<bool>)>& lambda,
+         std::vector<std::array<double, 3>>& mesh_pts, std::vector<PolygonFace>& mesh_faces,
+         std::vector<std::vector<size_t>>& patches, std::vector<size_t>& patch_function_label,
+         std::vector<bool>& patch_sign_label, std::vector<Edge>& edges, std::vector<std::vector<size_t>>& chains,
+         std::vector<std::vector<size_t>>& non_manifold_edges_of_vert, std::vector<std::vector<size_t>>& shells,
+         std::vector<std::vector<size_t>>& cells, std::vector<std::vector<bool>>& cell_function_label,
+         std::vector<std::string>& timing_labels, std::vector<double>& timings, std::vector<std::string>& stats_labels,
+         std::vector<size_t>& stats);
+template <class M, class... Rest>
+bool csg(bool robust_test, bool use_lookup, bool use_secondary_lookup, bool use_topo_ray_shooting, bool positive_inside,
+         const std::vector<std::array<double, 3>>& pts, const std::vector<std::array<size_t, 4>>& tets, const M& funcVals,
+         const std::function<bool(std::vector<bool>)>& lambda, Rest&... rest) {
+    return csg(robust_test, use_lookup, use_secondary_lookup, use_topo_ray_shooting, positive_inside, pts, tets,
+               funcVals.data(), (size_t)funcVals.cols(), lambda, rest...);
+}
+
+// CSG tree files (app/csg.cpp:15-52): units {type: Intersection | Union | Negation, elements: [a, b]};
+// element e > 0 is unit e (1-based), e < 0 is function -e-1; unit 1 is the root.
+struct CsgUnit {
+    int op;  // 0 Intersection, 1 Union, 2 Negation
+    std::array<int, 2> elements;
+};
+bool load_csg_tree(const std::string& filename, std::vector<CsgUnit>& tree);
+// membership over cell labels (true: function positive); an empty tree is the union of all functions
+std::function<bool(std::vector<bool>)> csg_lambda(const std::vector<CsgUnit>& tree);
+
 // Matrix types with data() / cols() and row-major storage (Eigen RowMajor, FuncVals)
 template <class M, class... Rest>
 bool implicit_arrangement(bool robust_test, bool use_lookup, bool use_secondary_lookup, bool use_topo_ray_shooting,
@@ -149,6 +183,11 @@ bool save_result_MI(const std::string& filename, const std::vector<std::array<do
                     const std::vector<std::vector<size_t>>& non_manifold_edges_of_vert,
                     const std::vector<std::vector<size_t>>& shells, const std::vector<std::vector<size_t>>& cells,
                     const std::vector<size_t>& cell_function_label);
+bool save_result_CSG(const std::string& filename, const std::vector<std::array<double, 3>>& mesh_pts,
+                     const std::vector<PolygonFace>& mesh_faces, const std::vector<std::vector<size_t>>& patches,
+                     const std::vector<bool>& patch_sign_label, const std::vector<Edge>& edges,
+                     const std::vector<std::vector<size_t>>& chains,
+                     const std::vector<std::vector<size_t>>& non_manifold_edges_of_vert);
 bool save_timings(const std::string& filename, const std::vector<std::string>& timing_labels,
                   const std::vector<double>& timings);
 bool save_statistics(const std::string& filename, const std::vector<std::string>& stats_labels,

@@ -20,7 +20,14 @@ static int finish(C* c, int st, uint8_t* buf, int cap, uint16_t* summary) {
     return n;
 }
 
+// big: 0 the small filtered variant, 1 the exact variant, 2 the mid-size filtered variant
 extern "C" int hc_ia_cut(int k, const double* planes, int big, uint8_t* buf, int cap, uint16_t* summary) {
+    if (big == 2) {
+        auto* c = new IACutMid();
+        int r = finish<IACutMid, IASummary>(c, c->run(planes, k), buf, cap, summary);
+        delete c;
+        return r;
+    }
     if (big) {
         auto* c = new IACutBig();
         int r = finish<IACutBig, IASummary>(c, c->run(planes, k), buf, cap, summary);
@@ -34,6 +41,12 @@ extern "C" int hc_ia_cut(int k, const double* planes, int big, uint8_t* buf, int
 }
 
 extern "C" int hc_mi_cut(int k, const double* mats, int big, uint8_t* buf, int cap, uint16_t* summary) {
+    if (big == 2) {
+        auto* c = new MICutMid();
+        int r = finish<MICutMid, MISummary>(c, c->run(mats, k), buf, cap, summary);
+        delete c;
+        return r;
+    }
     if (big) {
         auto* c = new MICutBig();
         int r = finish<MICutBig, MISummary>(c, c->run(mats, k), buf, cap, summary);

@@ -58,6 +58,8 @@ def _agree(hc, oracle, mode, rows):
     assert big == ref
     fast, _ = hc.cut(mode, rows, False)
     assert isinstance(fast, int) or fast == ref
+    mid, _ = hc.cut(mode, rows, "mid")
+    assert isinstance(mid, int) or mid == ref
     return isinstance(fast, int)
 
 

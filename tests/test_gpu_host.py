@@ -133,3 +133,34 @@ def test_cli_known_answers(built, tmp_path, kat):
     if "corners" in kat:
         assert _corners(mesh) == kat["corners"]
     assert mesh["patches_label"] == [kat["patch_label"]]
+
+
+def test_cli_csg(built, pkg, fns, oracle, tmp_path):
+    """app/csg.cpp through the C++ host layer: the kept patches are those whose faces separate the
+    CSG shape's inside from its outside (device labels), with chains and corners pruned to them."""
+    specs = [{"type": "sphere", "center": [0.1, 0.0, 0.05], "radius": 0.55},
+             {"type": "cylinder", "axis_point": [0.0, 0.1, 0.0], "axis_vector": [0.2, 1.0, 0.1], "radius": 0.3},
+             {"type": "sphere", "center": [-0.3, 0.2, -0.1], "radius": 0.4}]
+    (tmp_path / "fn.json").write_text(json.dumps(specs))
+    tree = [{"type": "Union", "elements": [2, -3]}, {"type": "Intersection", "elements": [-1, 3]},
+            {"type": "Negation", "elements": [-2, 0]}]  # (f0 - f1) | f2
+    (tmp_path / "tree.json").write_text(json.dumps(tree))
+    os.makedirs(tmp_path / "out", exist_ok=True)
+    res = 20
+    (tmp_path / "config.json").write_text(json.dumps({"gridResolution": res, "gridBbox": [[-1, -1, -1], [1, 1, 1]],
+                                                       "funcFile": "fn.json", "outputDir": "out"}))
+    r = subprocess.run([os.path.join(BIN, "csg"), str(tmp_path / "config.json"), "--tree", str(tmp_path / "tree.json")],
+                       capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    text = open(tmp_path / "out" / "mesh.json").read()
+    got = json.loads(text)
+    assert list(got) == ["chains", "corners", "edges", "faces", "patches", "patches_label", "points"]
+    funcs = fns.make_functions(specs)
+    pts, tets = fns.generate_tet_mesh(res)
+    ref = oracle.run("ia", pts, tets, oracle.sample(funcs, pts), connectivity=True)
+    full = meshjson.expected_mesh_json(ref, "ia")
+    labels = pkg.grid_implicit_arrangement(res, funcs).csg([(1, 2, -3), (0, -1, 3), (2, -2, 0)])
+    kept = [p for p in full["patches"] if labels[p[0]] != 0]
+    assert got["patches"] == kept and len(kept) > 0
+    assert got["patches_label"] == [[bool(labels[p[0]] == 1) for p in kept]]
+    assert got["faces"] == full["faces"] and got["edges"] == full["edges"]

@@ -146,3 +146,32 @@ def test_secondary_lookup_cache(pkg, fns, oracle, lib, mode):
         assert_mesh_equal(on, ref)
         for k in ("rec_bytes", "verts", "face_verts", "xyz"):
             assert np.array_equal(on[k], off[k]), k
+
+
+@pytest.mark.parametrize("mode", ["ia", "mi"])
+def test_heavy_single_tets_through_extraction(pkg, fns, oracle, lib, mode):
+    """Single tets whose arrangements exceed 128 vertices and 64 cells (the exact variant's range
+    reaches 255 / 254), through sampling-free host entry points, filter, cut and extraction."""
+    rng = np.random.default_rng(80)
+    pts = np.array([[0.0, 0.0, 0.0], [1.0, 0.0, 0.0], [0.0, 1.0, 0.0], [0.0, 0.0, 1.0]])
+    tets = np.array([[0, 1, 2, 3]])
+    big = 0
+    for it in range(16):
+        if mode == "ia":
+            k = int(rng.integers(9, 15))
+            fv = rng.normal(size=(4, k))
+        else:
+            # every material owns a cell: tangent planes of |x|^2 at sites inside the tet (Voronoi)
+            k = int(rng.integers(30, 45))
+            sites = rng.dirichlet(np.ones(4), size=k) @ pts
+            fv = np.stack([2 * pts @ c - c @ c for c in sites], axis=1)
+        call = pkg.implicit_arrangement if mode == "ia" else pkg.material_interface
+        try:
+            mesh = call(pts, tets, fv)
+        except pkg.RiaError as e:
+            assert e.status == pkg._lib.RIA_ECAPACITY
+            continue
+        ref = oracle.run(mode, pts, tets, fv)
+        assert_mesh_equal(mesh, ref)
+        big += int(len(mesh["verts"]) > 128)
+    assert big > 0
