@@ -306,6 +306,11 @@ RIA_API void ria_mesh_free(ria_mesh* mesh);
 RIA_API const char* ria_last_error(void);
 /* Diagnostics: number of kernels this library has launched in this process. */
 RIA_API uint64_t ria_kernel_launches(void);
+/* Empties the current device's secondary-lookup caches (two-plane and three-material records kept
+ * by their combinatorial type; results never depend on them).  Callers that must not reuse work
+ * across calls (for example a benchmark timing single calls) clear them first.  Must not overlap
+ * with running calls on the device. */
+RIA_API ria_status ria_lookup_cache_clear(void);
 RIA_API int ria_device_count(void);
 
 #ifdef __cplusplus

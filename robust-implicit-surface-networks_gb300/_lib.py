@@ -127,6 +127,8 @@ def load():
     L.ria_last_error.argtypes = []
     L.ria_device_count.restype = ctypes.c_int
     L.ria_device_count.argtypes = []
+    L.ria_lookup_cache_clear.restype = i32
+    L.ria_lookup_cache_clear.argtypes = []
     L.ria_kernel_launches.restype = u64
     L.ria_kernel_launches.argtypes = []
     _lib = L

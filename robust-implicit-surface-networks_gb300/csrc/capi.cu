@@ -60,8 +60,32 @@ std::vector<DeviceCtx> g_ctx;
 
 constexpr int64_t kFastRecordBytes = 1024;  // heap bytes per tet of the small filtered variant
 constexpr int64_t kMidRecordBytes = 4096;   // per tet of the mid variant (fuller records go to the exact kernel)
+constexpr int64_t kMidThreshold = 4 * 152 * 5;  // deferred tets the exact kernel takes in about one wave
 constexpr int64_t kBigRecordBytes = 28672;  // bound of a record of the exact variants
 constexpr int64_t kBigSlots = 152 * 64;     // concurrent exact-variant threads
+
+// A second stream per host thread and device, for work that overlaps the caller's stream inside one
+// call; created on first use and kept for the life of the thread's process, like the tables.
+struct AuxStream {
+    cudaStream_t s = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
+};
+
+cudaError_t aux_stream(AuxStream** out) {
+    thread_local std::vector<AuxStream> aux;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if ((int)aux.size() <= dev) aux.resize(dev + 1);
+    AuxStream& a = aux[dev];
+    if (!a.s) {
+        if ((e = cudaStreamCreateWithFlags(&a.s, cudaStreamNonBlocking)) != cudaSuccess) return e;
+        if ((e = cudaEventCreateWithFlags(&a.fork, cudaEventDisableTiming)) != cudaSuccess) return e;
+        if ((e = cudaEventCreateWithFlags(&a.join, cudaEventDisableTiming)) != cudaSuccess) return e;
+    }
+    *out = &a;
+    return cudaSuccess;
+}
 
 ria_status current_device(int* dev) {
     int n = 0;
@@ -260,7 +284,8 @@ ria_status run_pipeline(const ria_config* cfg, const Inputs& in, cudaStream_t s,
     };
     cudaEventRecord(ev[0], s);
 
-    // counters: 0 status, 1 n_zero, 2..4 k histogram, 5 heap used, 6 big heap used, 7 deferred, 8 robust failures
+    // counters: 0 status, 1 n_zero, 2..4 k histogram, 5 heap used, 6 big heap used, 7 deferred by the small
+    // variant, 8 robust failures, 9 deferred by the mid variant
     unsigned long long* cnt = tmp.get<unsigned long long>(16, &err);
     uint32_t* status = (uint32_t*)cnt;
     if (err != cudaSuccess) return bail(fail(RIA_ENOMEM, "device allocation failed"));
@@ -359,9 +384,13 @@ ria_status run_pipeline(const ria_config* cfg, const Inputs& in, cudaStream_t s,
         launch_robust(ca, scratch, kBigSlots, cnt + 8, s);
         cudaStreamSynchronize(s);
     } else if (G > 0) {
+        // one heap for both filtered variants: the small records of every tet plus room for the mid
+        // variant's larger records of the heavy bins (a record that does not fit goes on to the exact
+        // variant, whose heap is sized by its bound)
         const uint64_t heap_bytes = (uint64_t)(G - G_mid) * kFastRecordBytes + (uint64_t)G_mid * kMidRecordBytes;
         M->heap = M->keep.get<uint8_t>((int64_t)heap_bytes, &err);
         uint32_t* deferred = tmp.get<uint32_t>(G, &err);
+        uint32_t* deferred2 = tmp.get<uint32_t>(G, &err);
         if (err != cudaSuccess) return bail(fail(RIA_ENOMEM, "device allocation failed"));
         ca.list = gen;
         ca.n = G;
@@ -376,21 +405,76 @@ ria_status run_pipeline(const ria_config* cfg, const Inputs& in, cudaStream_t s,
             ca.table_off = ctx->table_off[0];
         }
         if (cfg->use_lookup && cfg->use_secondary_lookup) set_cache(ca, ctx, mi);
-        CutArgs cm = ca;  // heavy bins: mid-size variant
-        cm.n = G_mid;
-        launch_cut_fast(cm, s, true);
-        ca.list = gen + G_mid;
-        ca.n = G - G_mid;
-        launch_cut_fast(ca, s, false);
+        // The general-case list is heaviest first.  Its heavy bins (four or more active functions)
+        // are a few long cuts, its light bins many short lookups and cuts: the two parts run at the
+        // same time on two streams.  Heavy: the small variant (implicit arrangement), or one block
+        // per tet clipping the materials' cells in parallel (material interface).  Light: the
+        // lookup pass, then the small variant over the tets it did not finish.  The tets the small
+        // variant cannot finish go to the mid-size variant, and what that cannot finish to the
+        // exact variant.
+        const int64_t G_light = G - G_mid;
+        const bool prep = G_light > 0 && (ca.table || ca.cache.slots);
+        uint32_t* rest = prep ? tmp.get<uint32_t>(G_light, &err) : nullptr;
+        if (err != cudaSuccess) return bail(fail(RIA_ENOMEM, "device allocation failed"));
+        AuxStream* aux = nullptr;
+        if (G_mid > 0 && G_light > 0) {
+            if (aux_stream(&aux) != cudaSuccess) return bail(fail(RIA_ECUDA, "stream creation failed"));
+            cudaEventRecord(aux->fork, s);
+            cudaStreamWaitEvent(aux->s, aux->fork, 0);
+        }
+        if (G_mid > 0) {
+            CutArgs ch = ca;
+            ch.n = G_mid;
+            if (mi)
+                launch_cut_mi_split(ch, s);
+            else
+                launch_cut_fast(ch, s, false);
+        }
+        if (G_light > 0) {
+            cudaStream_t sl = aux ? aux->s : s;
+            CutArgs cl = ca;
+            cl.list = gen + G_mid;
+            cl.n = G_light;
+            if (prep) {
+                CutArgs cp = cl;
+                cp.deferred = rest;
+                cp.n_deferred = (unsigned int*)(cnt + 10);
+                launch_cut_prep(cp, sl);
+                cl.list = rest;
+                cl.n_dev = cp.n_deferred;
+            }
+            launch_cut_fast(cl, sl, false);
+        }
+        if (aux) {
+            cudaEventRecord(aux->join, aux->s);
+            cudaStreamWaitEvent(s, aux->join, 0);
+        }
         unsigned long long h = 0;
         cudaMemcpyAsync(&h, cnt + 7, 8, cudaMemcpyDeviceToHost, s);
         if (cudaStreamSynchronize(s) != cudaSuccess) return bail(fail(RIA_ECUDA, cudaGetErrorString(cudaGetLastError())));
-        n_def = (int64_t)(h & 0xFFFFFFFFull);
+        const int64_t n_def1 = (int64_t)(h & 0xFFFFFFFFull);
+        // a few deferred tets: straight to the exact kernel (state in shared memory, one tet per
+        // block, the shortest per-tet time); many: the mid-size variant first (one tet per thread,
+        // every SM full), the exact kernel for what remains
+        n_def = n_def1;
+        if (n_def1 > kMidThreshold) {
+            CutArgs cm = ca;
+            cm.list = deferred;
+            cm.n = n_def1;
+            cm.deferred = deferred2;
+            cm.n_deferred = (unsigned int*)(cnt + 9);
+            launch_cut_fast(cm, s, true);
+            cudaMemcpyAsync(&h, cnt + 9, 8, cudaMemcpyDeviceToHost, s);
+            if (cudaStreamSynchronize(s) != cudaSuccess)
+                return bail(fail(RIA_ECUDA, cudaGetErrorString(cudaGetLastError())));
+            n_def = (int64_t)(h & 0xFFFFFFFFull);
+        }
+        uint32_t* big_list = n_def1 > kMidThreshold ? deferred2 : deferred;
         if (n_def > 0) {
             M->heap_big = M->keep.get<uint8_t>(n_def * kBigRecordBytes, &err);
             if (err != cudaSuccess) return bail(fail(RIA_ENOMEM, "device allocation failed"));
             CutArgs cb = ca;
-            cb.list = deferred;
+            cb.list = big_list;
             cb.n = n_def;
             cb.heap = M->heap_big;
             cb.heap_used = cnt + 6;
@@ -1493,6 +1577,22 @@ void ria_server_destroy(ria_server* sv) {
 const char* ria_last_error(void) { return g_err.c_str(); }
 
 uint64_t ria_kernel_launches(void) { return g_launches.load(); }
+
+ria_status ria_lookup_cache_clear(void) {
+    int dev = 0;
+    ria_status st = current_device(&dev);
+    if (st != RIA_OK) return st;
+    std::lock_guard<std::mutex> lk(g_mu);
+    if ((int)g_ctx.size() <= dev) return RIA_OK;
+    DeviceCtx& c = g_ctx[dev];
+    for (int m = 0; m < 2; ++m) {
+        if (!c.ready[m]) continue;
+        RIA_CUDA(cudaMemset(c.cache_slots[m], 0, sizeof(unsigned long long) * kCacheSlots));
+        RIA_CUDA(cudaMemset(c.cache_cnt[m], 0, sizeof(unsigned long long) * 2));
+    }
+    RIA_CUDA(cudaDeviceSynchronize());
+    return RIA_OK;
+}
 
 int ria_device_count(void) {
     int n = 0;

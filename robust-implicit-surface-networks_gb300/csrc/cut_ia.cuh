@@ -196,6 +196,38 @@ RIA_HD void ia_record_from_template(const uint8_t* tmpl, int k, const uint8_t* r
     }
 }
 
+// The record of a tet whose planes reduce to two groups with representatives r1 < r2 (local
+// indices): the canonical record `tmpl` of the two representative planes alone (k = 2, labels 4 and
+// 5) with 4 renamed 4+r1 and 5 renamed 4+r2, the cell sign bits moved accordingly, and the tet's own
+// groups.  The renaming keeps every order the canonical form sorts by, and the generic cut inserts
+// exactly the representatives, so the result equals the generic cut's record.
+RIA_HD void ia_record_from_template2(const uint8_t* tmpl, int k, const uint8_t* rep, int r1, int r2, uint8_t* dst) {
+    const int nv = rd16h(tmpl + 2), nf = rd16h(tmpl + 4), nc = rd16h(tmpl + 6), nl = rd16h(tmpl + 8);
+    const uint8_t l1 = (uint8_t)(4 + r1), l2 = (uint8_t)(4 + r2);
+    auto ren = [&](uint8_t x) -> uint8_t { return x == 4 ? l1 : (x == 5 ? l2 : x); };
+    for (int t = 0; t < 10; ++t) dst[t] = tmpl[t];
+    dst[1] = (uint8_t)k;
+    for (int j = 0; j < k; ++j) dst[10 + j] = rep[j];
+    const uint8_t* s = tmpl + 12;
+    uint8_t* d = dst + 10 + k;
+    for (int t = 0; t < 3 * nv; ++t) d[t] = ren(s[t]);
+    s += 3 * nv;
+    d += 3 * nv;
+    for (int f = 0; f < nf; ++f)
+        for (int t = 0; t < 8; ++t) d[8 * f + t] = t == 0 ? ren(s[8 * f]) : s[8 * f + t];
+    s += 8 * nf;
+    d += 8 * nf;
+    for (int t = 0; t < 2 * nl; ++t) d[t] = s[t];
+    s += 2 * nl;
+    d += 2 * nl;
+    for (int c = 0; c < nc; ++c) {
+        uint64_t sig = 0;
+        for (int t = 0; t < 8; ++t) sig |= (uint64_t)s[8 * c + t] << (8 * t);
+        const uint64_t out = ((sig >> 4) & 1 ? (1ull << l1) : 0ull) | ((sig >> 5) & 1 ? (1ull << l2) : 0ull);
+        for (int t = 0; t < 8; ++t) d[8 * c + t] = (uint8_t)((out >> (8 * t)) & 0xFF);
+    }
+}
+
 template <int MV, int MF, int MC, int ML, bool EXACT>
 struct IACut {
     const double* pl;  // k x 4 corner values

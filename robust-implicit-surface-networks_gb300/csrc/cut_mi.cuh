@@ -33,6 +33,17 @@ RIA_HD int popc64(uint64_t x) {
 #endif
 }
 
+// One material's cell, exported from its clipped polytope (vertex keys: four sorted labels).
+template <int V, int F, int L>
+struct MICell {
+    static constexpr int kV = V, kF = F, kL = L;
+    uint8_t nv, nf;
+    uint32_t vkey[V];
+    uint8_t fother[F];
+    uint8_t flen[F];
+    uint8_t loops[L];
+};
+
 template <int PV, int PF, int PL, int OV, int OF, int OL, bool EXACT>
 struct MICut {
     const double* mt;  // k x 4 corner values
@@ -132,8 +143,10 @@ struct MICut {
         }
     }
 
-    RIA_HDI int run(const double* mats, int kk) {
-        const int kBad = EXACT ? CUT_FAIL : CUT_DEFER;
+    uint64_t no_cell, no_clip;
+
+    // materials, grouping of identical materials, dominated materials; empty output
+    RIA_HDI int prepare(const double* mats, int kk) {
         mt = mats;
         k = kk;
         if (k > 60) return CUT_FAIL;
@@ -142,7 +155,8 @@ struct MICut {
         // tet (values are linear), so a owns no cell; if b > a at all corners, a never reaches the
         // maximum anywhere in the tet and its half-space clips nothing.  Both are skipped; the result
         // is the same as clipping with them.
-        uint64_t no_cell = 0, no_clip = 0;
+        no_cell = 0;
+        no_clip = 0;
         for (int a = 0; a < k; ++a) {
             if (rep[a] != 4 + a) continue;
             const double* x = mt + 4 * a;
@@ -156,8 +170,17 @@ struct MICut {
             }
         }
         onv = onf = onc = oloop = 0;
-        for (int m = 4; m < 4 + k; ++m) {
-            if (rep[m - 4] != m || (no_cell & bit64(m - 4))) continue;
+        return CUT_OK;
+    }
+
+    // does material m (label) own a cell that has to be computed?
+    RIA_HD bool has_cell(int m) const { return rep[m - 4] == m && !(no_cell & bit64(m - 4)); }
+
+    // The cell of material m: the tet clipped by m >= j for every other material j.  Leaves the
+    // polytope (nv, mask, faces, loops[cur]) for export_cell; `empty` when it has no interior.
+    RIA_HDI int clip(int m, bool& empty) {
+        const int kBad = EXACT ? CUT_FAIL : CUT_DEFER;
+        {
             // the whole tet, labelled with material m
             nv = 4;
             for (int c = 0; c < 4; ++c) {
@@ -176,7 +199,7 @@ struct MICut {
                 flen[b] = 3;
                 for (int j = 0; j < 3; ++j) loops[0][3 * b + j] = (uint8_t)tet_face_outward(b, j);
             }
-            bool empty = false;
+            empty = false;
             for (int j = 4; j < 4 + k; ++j) {
                 if (j == m || rep[j - 4] != j || (no_clip & bit64(j - 4))) continue;
                 const double* qv = row_of(j);
@@ -320,40 +343,88 @@ struct MICut {
                 }
                 cur = nb;
             }
+        }
+        return CUT_OK;
+    }
+
+    // The clipped polytope as a self-contained cell: the keys of its live vertices (the four sorted
+    // labels of each, in polytope order) and its faces with loops over those vertices.
+    template <class Cell>
+    RIA_HDI int export_cell(Cell& out) const {
+        const int kBad = EXACT ? CUT_FAIL : CUT_DEFER;
+        uint8_t id[PV];
+        uint8_t live[PV];
+        for (int v = 0; v < nv; ++v) live[v] = 0;
+        for (int f = 0; f < nf; ++f)
+            for (int t = 0; t < flen[f]; ++t) live[loops[cur][foff[f] + t]] = 1;
+        int n = 0;
+        for (int v = 0; v < nv; ++v) {
+            if (!live[v]) continue;
+            uint8_t lb[4];
+            if (!labels_of_mask(mask[v], lb)) return kBad;
+            if (n >= Cell::kV) return kBad;
+            out.vkey[n] = ((uint32_t)lb[0] << 24) | ((uint32_t)lb[1] << 16) | ((uint32_t)lb[2] << 8) | lb[3];
+            id[v] = (uint8_t)n++;
+        }
+        out.nv = (uint8_t)n;
+        if (nf > Cell::kF) return kBad;
+        int used = 0;
+        for (int f = 0; f < nf; ++f) {
+            if (used + flen[f] > Cell::kL) return kBad;
+            out.fother[f] = fother[f];
+            out.flen[f] = (uint8_t)flen[f];
+            for (int t = 0; t < flen[f]; ++t) out.loops[used++] = id[loops[cur][foff[f] + t]];
+        }
+        out.nf = (uint8_t)nf;
+        return CUT_OK;
+    }
+
+    // Appends cell m to the output: its vertices are merged with those of earlier cells by key.
+    template <class Cell>
+    RIA_HDI int append_cell(int m, const Cell& cell) {
+        const int kBad = EXACT ? CUT_FAIL : CUT_DEFER;
+        if (onc >= 64) return kBad;
+        ocell[onc++] = (uint8_t)m;
+        uint8_t oid[Cell::kV];
+        for (int v = 0; v < cell.nv; ++v) {
+            const uint32_t key = cell.vkey[v];
+            int id = -1;
+            for (int x = 0; x < onv; ++x)
+                if (okey[x] == key) id = x;
+            if (id < 0) {
+                if (onv >= OV) return kBad;
+                id = onv;
+                okey[onv++] = key;
+            }
+            oid[v] = (uint8_t)id;
+        }
+        int used = 0;
+        for (int f = 0; f < cell.nf; ++f) {
+            if (onf >= OF || oloop + cell.flen[f] > OL) return kBad;
+            opos[onf] = cell.fother[f];
+            oneg[onf] = (uint8_t)m;
+            ooff[onf] = (uint16_t)oloop;
+            olen[onf] = cell.flen[f];
+            for (int t = 0; t < cell.flen[f]; ++t) oloops[oloop++] = oid[cell.loops[used++]];
+            ++onf;
+        }
+        return CUT_OK;
+    }
+
+    RIA_HDI int run(const double* mats, int kk) {
+        int st = prepare(mats, kk);
+        if (st != CUT_OK) return st;
+        for (int m = 4; m < 4 + k; ++m) {
+            if (!has_cell(m)) continue;
+            bool empty = false;
+            st = clip(m, empty);
+            if (st != CUT_OK) return st;
             if (empty) continue;
-            // append the cell to the output
-            if (onc >= 64) return kBad;
-            ocell[onc++] = (uint8_t)m;
-            uint8_t oid[PV];
-            uint8_t live[PV];
-            for (int v = 0; v < nv; ++v) live[v] = 0;
-            for (int f = 0; f < nf; ++f)
-                for (int t = 0; t < flen[f]; ++t) live[loops[cur][foff[f] + t]] = 1;
-            for (int v = 0; v < nv; ++v) {
-                if (!live[v]) continue;
-                uint8_t lb[4];
-                if (!labels_of_mask(mask[v], lb)) return kBad;
-                uint32_t key = ((uint32_t)lb[0] << 24) | ((uint32_t)lb[1] << 16) | ((uint32_t)lb[2] << 8) | lb[3];
-                int id = -1;
-                for (int x = 0; x < onv; ++x)
-                    if (okey[x] == key) id = x;
-                if (id < 0) {
-                    if (onv >= OV) return kBad;
-                    id = onv;
-                    okey[onv++] = key;
-                }
-                oid[v] = (uint8_t)id;
-            }
-            for (int f = 0; f < nf; ++f) {
-                int o = fother[f];
-                if (onf >= OF || oloop + flen[f] > OL) return kBad;
-                opos[onf] = (uint8_t)o;
-                oneg[onf] = (uint8_t)m;
-                ooff[onf] = (uint16_t)oloop;
-                olen[onf] = flen[f];
-                for (int t = 0; t < flen[f]; ++t) oloops[oloop++] = oid[loops[cur][foff[f] + t]];
-                ++onf;
-            }
+            MICell<PV, PF, PL> cell;
+            st = export_cell(cell);
+            if (st != CUT_OK) return st;
+            st = append_cell(m, cell);
+            if (st != CUT_OK) return st;
         }
         return CUT_OK;
     }

@@ -148,15 +148,72 @@ __device__ __forceinline__ void cache_insert(const CutArgs::Cache& c, uint32_t k
     }
 }
 
+// writes a relabelled two-plane record for tet ai (false: the heap is full)
+__device__ __forceinline__ bool ia_emit_template2(const CutArgs& a, uint32_t ai, const uint8_t* tmpl, int k,
+                                                  const uint8_t* rep, int r1, int r2) {
+    const int size = ia_template_record_size(tmpl, k);
+    unsigned long long off = atomicAdd(a.heap_used, (unsigned long long)size);
+    if (off + size > a.heap_cap) return false;
+    uint8_t* dst = a.heap + off;
+    ia_record_from_template2(tmpl, k, rep, r1, r2, dst);
+    IASummary s;
+    ia_record_summary(dst, s);
+    a.act_desc[ai] = off | a.desc_bit;
+    a.act_sum[ai] = pack_sum<IASummary>(s);
+    return true;
+}
+
+// Tets whose planes reduce to two groups (duplicates, multiples, planes on a tet face, zero planes
+// besides two distinct planes): the secondary lookup of the two representatives, whose record is
+// relabelled for the tet (on a miss, with `cut_on_miss`, the two planes alone are cut and the record
+// cached).  Returns CUT_OK when the tet's record is written, CUT_DEFER to fall back to the general cut.
+__device__ int ia_try_two_groups(const CutArgs& a, uint32_t ai, const double* planes, int k, const uint8_t* rep,
+                                 bool cut_on_miss) {
+    int r[2], n = 0;
+    for (int i = 0; i < k; ++i)
+        if (rep[i] == 4 + i) {
+            if (n == 2) return CUT_DEFER;
+            r[n++] = i;
+        }
+    if (n != 2) return CUT_DEFER;
+    double two[8];
+    for (int c = 0; c < 4; ++c) {
+        two[c] = planes[4 * r[0] + c];
+        two[4 + c] = planes[4 * r[1] + c];
+    }
+    uint32_t key = 0;
+    if (!ia_key2(two, key)) return CUT_DEFER;
+    const int j = cache_find(a.cache, key);
+    if (j >= 0) {
+        const uint8_t* tmpl = a.cache.table + a.cache.table_off[kTablePatterns + j];
+        if (k == 2) {  // the record itself
+            a.act_desc[ai] = kTableBit | (uint64_t)(kTablePatterns + j);
+            a.act_sum[ai] = a.cache.table_sum[kTablePatterns + j];
+            return CUT_OK;
+        }
+        return ia_emit_template2(a, ai, tmpl, k, rep, r[0], r[1]) ? CUT_OK : CUT_DEFER;
+    }
+    if (!cut_on_miss) return CUT_DEFER;
+    IACutFast c;
+    if (c.run(two, 2) != CUT_OK) return CUT_DEFER;
+    c.canonicalize();
+    const int size = c.record_size();
+    uint8_t rec2[1024];
+    if (size > (int)sizeof(rec2)) return CUT_DEFER;
+    IASummary s2;
+    c.emit(rec2, s2);
+    cache_insert(a.cache, key, rec2, size, pack_sum<IASummary>(s2));
+    return ia_emit_template2(a, ai, rec2, k, rep, r[0], r[1]) ? CUT_OK : CUT_DEFER;
+}
+
 // Tets whose planes reduce to at most one after grouping (duplicates, planes coincident with a tet
 // face, zero planes): the record comes from the one-plane lookup table, relabelled.  `two` reports
-// two distinct planes that are neither zero nor a tet face (labels 4, 5: secondary lookup).
+// exactly two groups with distinct representatives (secondary lookup).
 __device__ __forceinline__ bool ia_try_template(const CutArgs& a, uint32_t ai, const double* planes, int k,
-                                                bool* two) {
-    uint8_t rep[kFastMaxK];
+                                                bool* two, uint8_t* rep) {
     int first;
     const int eff = ia_group_planes(planes, k, rep, first);
-    *two = k == 2 && eff == 2 && rep[0] == 4 && rep[1] == 5;
+    *two = eff == 2;
     if (eff > 1 || !a.table) return false;
     const int pattern = eff ? ia_sign_pattern(planes + 4 * first) : kTablePatterns - 1;  // all positive: uncut
     const uint8_t* tmpl = a.table + a.table_off[pattern];
@@ -176,17 +233,20 @@ __device__ __forceinline__ bool ia_try_template(const CutArgs& a, uint32_t ai, c
 }
 
 template <bool MI, bool MID>
-__global__ void __launch_bounds__(128) k_cut_fast(CutArgs a) {
+__device__ __forceinline__ void cut_one(const CutArgs& a, int64_t i) {
     using Fast = typename std::conditional<MID, typename Traits<MI>::Mid, typename Traits<MI>::Fast>::type;
     using Sum = typename Traits<MI>::Sum;
     constexpr int kMax = MID ? kMidMaxK : kFastMaxK;
-    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= a.n) return;
     const uint32_t ai = a.list[i];
     double planes[4 * kMax];
     const int k = gather_planes(a, ai, planes, kMax);
     bool keyed = false;
-    if (!MI && k <= kMax && k <= kFastMaxK && ia_try_template(a, ai, planes, k, &keyed)) return;
+    if (!MI && k <= kMax && k <= kFastMaxK) {
+        uint8_t rep[kFastMaxK];
+        if (ia_try_template(a, ai, planes, k, &keyed, rep)) return;
+        if (keyed && a.cache.slots && ia_try_two_groups(a, ai, planes, k, rep, true) == CUT_OK) return;
+        keyed = false;  // the general cut below; its record is not a two-plane template
+    }
     if (MI) keyed = k == 3 && mi_distinct3(planes);
     uint32_t key = 0;
     if (keyed && a.cache.slots) {
@@ -218,6 +278,110 @@ __global__ void __launch_bounds__(128) k_cut_fast(CutArgs a) {
         a.deferred[d] = ai;
     } else {
         raise_status(a.status, ST_INTERNAL);
+    }
+}
+
+// One thread per tet.
+template <bool MI, bool MID>
+__global__ void __launch_bounds__(128) k_cut_fast(CutArgs a) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n || (a.n_dev && i >= (int64_t)*a.n_dev)) return;
+    cut_one<MI, MID>(a, i);
+}
+
+// The lookup pass: a tet the one-plane table or the secondary cache finishes is done here; every
+// other tet is appended to a.deferred (one atomic per warp, so the general pass keeps the list's
+// heaviest-first order per warp).  A warp of the general pass then holds cuts only, rather than a
+// mix of short lookups and long cuts that run one after the other.
+template <bool MI>
+__global__ void __launch_bounds__(128) k_cut_prep(CutArgs a) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n) return;
+    const uint32_t ai = a.list[i];
+    double planes[4 * kFastMaxK];
+    const int k = gather_planes(a, ai, planes, kFastMaxK);
+    bool done = false;
+    if (k <= kFastMaxK) {
+        if (!MI) {
+            uint8_t rep[kFastMaxK];
+            bool two = false;
+            done = ia_try_template(a, ai, planes, k, &two, rep);
+            if (!done && two && a.cache.slots) done = ia_try_two_groups(a, ai, planes, k, rep, false) == CUT_OK;
+        } else if (k == 3 && a.cache.slots && mi_distinct3(planes)) {
+            uint32_t key = 0;
+            if (mi_key3(planes, key)) {
+                const int j = cache_find(a.cache, key);
+                if (j >= 0) {
+                    a.act_desc[ai] = kTableBit | (uint64_t)(kTablePatterns + j);
+                    a.act_sum[ai] = a.cache.table_sum[kTablePatterns + j];
+                    done = true;
+                }
+            }
+        }
+    }
+    const unsigned act = __activemask();
+    const unsigned rest = __ballot_sync(act, !done);
+    if (!done) {
+        const int lane = threadIdx.x & 31;
+        const int leader = __ffs(rest) - 1;
+        unsigned int base = 0;
+        if (lane == leader) base = atomicAdd(a.n_deferred, (unsigned int)__popc(rest));
+        base = __shfl_sync(rest, base, leader);
+        a.deferred[base + __popc(rest & ((1u << lane) - 1u))] = ai;
+    }
+}
+
+// Material interface with many materials: one block per tet, one thread per material.  A material's
+// cell is the tet clipped by its half-spaces against every other material, independent of the other
+// cells, so the threads clip in parallel and export their cells to shared memory; thread 0 then
+// merges them in material order, canonicalises and emits, exactly as the serial cut does.
+constexpr int kSplitMaxK = 32;
+using SplitCut = MICutMid;
+using SplitCell = MICell<96, 96, 640>;
+
+__global__ void __launch_bounds__(kSplitMaxK) k_cut_mi_split(CutArgs a) {
+    __shared__ double planes[4 * kSplitMaxK];
+    __shared__ SplitCell cells[kSplitMaxK];
+    __shared__ int8_t cst[kSplitMaxK];  // 0 cell, 1 no cell, 2 defer
+    __shared__ int kk;
+    const int lane = threadIdx.x;
+    for (int64_t i = blockIdx.x; i < a.n; i += gridDim.x) {
+        const uint32_t ai = a.list[i];
+        if (lane == 0) kk = gather_planes(a, ai, planes, kSplitMaxK);
+        __syncthreads();
+        const int k = kk;
+        if (k > kSplitMaxK) {
+            if (lane == 0) a.deferred[atomicAdd(a.n_deferred, 1u)] = ai;
+            __syncthreads();
+            continue;
+        }
+        SplitCut c;
+        int st = c.prepare(planes, k);
+        cst[lane] = 1;
+        if (st == CUT_OK && lane < k && c.has_cell(4 + lane)) {
+            bool empty = false;
+            st = c.clip(4 + lane, empty);
+            if (st == CUT_OK && !empty) st = c.export_cell(cells[lane]);
+            cst[lane] = st != CUT_OK ? 2 : (empty ? 1 : 0);
+        } else if (st != CUT_OK) {
+            cst[lane] = 2;
+        }
+        __syncthreads();
+        if (lane == 0) {
+            bool ok = true;
+            for (int j = 0; j < k; ++j) ok = ok && cst[j] != 2;
+            if (ok) ok = c.prepare(planes, k) == CUT_OK;
+            for (int m = 4; m < 4 + k && ok; ++m)
+                if (cst[m - 4] == 0) ok = c.append_cell(m, cells[m - 4]) == CUT_OK;
+            const uint8_t* rec = nullptr;
+            if (ok) {
+                int size = 0;
+                IASum4 sum;
+                rec = finish_cut<SplitCut, MISummary>(a, ai, c, &size, &sum, true);
+            }
+            if (!rec) a.deferred[atomicAdd(a.n_deferred, 1u)] = ai;
+        }
+        __syncthreads();
     }
 }
 
@@ -347,6 +511,23 @@ void launch_robust(const CutArgs& a, void* scratch, int64_t slots, unsigned long
 }
 
 size_t cut_big_slot_bytes(bool mi) { return mi ? sizeof(BigSlot<true>) : sizeof(BigSlot<false>); }
+
+void launch_cut_mi_split(const CutArgs& a, cudaStream_t s) {
+    if (a.n == 0) return;
+    const int64_t blocks = a.n < 152 * 32 ? a.n : 152 * 32;
+    k_cut_mi_split<<<(unsigned)blocks, kSplitMaxK, 0, s>>>(a);
+    note_launch();
+}
+
+void launch_cut_prep(const CutArgs& a, cudaStream_t s) {
+    if (a.n == 0) return;
+    const unsigned nb = (unsigned)((a.n + 127) / 128);
+    if (a.mi)
+        k_cut_prep<true><<<nb, 128, 0, s>>>(a);
+    else
+        k_cut_prep<false><<<nb, 128, 0, s>>>(a);
+    note_launch();
+}
 
 void launch_cut_fast(const CutArgs& a, cudaStream_t s, bool mid) {
     if (a.n == 0) return;

@@ -132,6 +132,7 @@ struct CutArgs {
     uint64_t desc_bit;           // or-ed into the descriptors written (0 or kBigHeapBit)
     uint32_t* deferred;          // fast variant: tets handed to the exact variant
     unsigned int* n_deferred;
+    const unsigned int* n_dev = nullptr;  // when set, the list holds min(n, *n_dev) tets (a count on the device)
     uint32_t* status;
     // explicit per-tet rows (the per-tet batch API): rows of tet i are value_off[i]..value_off[i+1]-1
     const double* values = nullptr;
@@ -152,10 +153,17 @@ struct CutArgs {
         IASum4* table_sum = nullptr;
     } cache;
 };
+// tets the lookup tables finish without a cut (IA: one or two effective planes found in the table
+// or the secondary cache; MI: three materials found in the cache); the others are appended, in list
+// order per warp, to `deferred` for the cut kernels
+void launch_cut_prep(const CutArgs& a, cudaStream_t s);
 // filtered variants, one thread per tet: `mid` for the heavy bins (four or more active functions,
 // up to 16), the small one otherwise; a tet that outgrows them, or whose record does not fit the
 // heap, goes to the deferred list
 void launch_cut_fast(const CutArgs& a, cudaStream_t s, bool mid = false);
+// material interface, tets with many materials: one thread per material's cell (filtered), merged per
+// tet; tets it cannot finish go to the deferred list
+void launch_cut_mi_split(const CutArgs& a, cudaStream_t s);
 // first bin of tets for the small filtered variant (three or fewer active functions)
 constexpr int kFirstSmallBin(bool mi) { return mi ? 6 : 5; }
 // exact variant: one tet per block, state in shared memory

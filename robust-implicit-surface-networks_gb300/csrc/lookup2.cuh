@@ -68,6 +68,39 @@ RIA_HD bool ia_key2(const double* rows, uint32_t& key) {
     return true;
 }
 
+// three planes P, Q, R = rows[0..3], rows[4..7], rows[8..11]: their signs at the corners, the 2x2
+// minors of each pair on each corner pair, and the 3x3 minors of (P, Q, R) on each corner triple
+// (the 4x4 determinants {e_a, P, Q, R}); 34 base-3 digits
+RIA_HD bool ia_key3(const double* rows, uint64_t& key) {
+    if (!key_range(rows, 12)) return false;
+    uint64_t k = 0;
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 4; ++c) k = 3 * k + (uint64_t)(sign_of(rows[4 * r + c]) + 1);
+    const int pa[3] = {0, 0, 1}, pb[3] = {1, 2, 2};
+    for (int p = 0; p < 3; ++p)
+        for (int i = 0; i < 4; ++i)
+            for (int j = i + 1; j < 4; ++j) {
+                const double* X = rows + 4 * pa[p];
+                const double* Y = rows + 4 * pb[p];
+                const int s = sign_det2(X[i], X[j], Y[i], Y[j]);
+                if (s == 2) return false;
+                k = 3 * k + (uint64_t)(s + 1);
+            }
+    for (int skip = 0; skip < 4; ++skip) {
+        double M[9];
+        for (int r = 0; r < 3; ++r) {
+            int cc = 0;
+            for (int c = 0; c < 4; ++c)
+                if (c != skip) M[3 * r + cc++] = rows[4 * r + c];
+        }
+        const int s = sign_det3(M);
+        if (s == 2) return false;
+        k = 3 * k + (uint64_t)(s + 1);
+    }
+    key = k;
+    return true;
+}
+
 // three materials, rows m[0..3], m[4..7], m[8..11]
 RIA_HD bool mi_key3(const double* m, uint32_t& key) {
     if (!key_range(m, 12)) return false;

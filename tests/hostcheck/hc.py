@@ -18,7 +18,7 @@ def lib():
         for f in (L.hc_ia_cut, L.hc_mi_cut):
             f.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
         L.hc_det_sign.argtypes = [ctypes.c_void_p, ctypes.c_int]
-        for f in (L.hc_ia_key2, L.hc_mi_key3):
+        for f in (L.hc_ia_key2, L.hc_mi_key3, L.hc_ia_key3):
             f.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
         _lib = L
     return _lib
@@ -54,9 +54,23 @@ def ia_template(rows):
     return bytes(buf[:n]), summ.copy()
 
 
+def ia_template2(rows):
+    """Record of the two-group path (the two representatives cut alone, relabelled), or None when the
+    tet's planes do not reduce to exactly two groups."""
+    rows = np.ascontiguousarray(rows, dtype=np.float64).reshape(-1, 4)
+    L = lib()
+    L.hc_ia_template2.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
+    buf = np.zeros(4096, dtype=np.uint8)
+    summ = np.zeros(4, dtype=np.uint16)
+    n = L.hc_ia_template2(rows.shape[0], rows.ctypes.data, buf.ctypes.data, buf.size, summ.ctypes.data)
+    if n < 0:
+        return None
+    return bytes(buf[:n]), summ.copy()
+
+
 def key(mode, rows):
-    """Secondary lookup key of two planes (ia) or three materials (mi), or None."""
+    """Lookup key of two planes (ia), three planes (ia3) or three materials (mi), or None."""
     rows = np.ascontiguousarray(rows, dtype=np.float64).reshape(-1)
-    out = np.zeros(1, dtype=np.uint32)
-    f = lib().hc_ia_key2 if mode == "ia" else lib().hc_mi_key3
+    out = np.zeros(1, dtype=np.uint64 if mode == "ia3" else np.uint32)
+    f = {"ia": lib().hc_ia_key2, "mi": lib().hc_mi_key3, "ia3": lib().hc_ia_key3}[mode]
     return int(out[0]) if f(rows.ctypes.data, out.ctypes.data) else None

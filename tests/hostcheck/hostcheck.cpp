@@ -64,6 +64,7 @@ extern "C" int hc_det_sign(const double* M, int n) { return det_sign_exact(M, n)
 // secondary lookup keys: returns 1 and the key, or 0 when no key is formed
 extern "C" int hc_ia_key2(const double* rows, uint32_t* key) { return ia_key2(rows, *key) ? 1 : 0; }
 extern "C" int hc_mi_key3(const double* rows, uint32_t* key) { return mi_key3(rows, *key) ? 1 : 0; }
+extern "C" int hc_ia_key3(const double* rows, uint64_t* key) { return ia_key3(rows, *key) ? 1 : 0; }
 
 // The one-effective-plane path of the fast kernel: the one-plane table is built by the exact variant
 // from corner values in {-1, 0, 1}, as on the device.
@@ -99,6 +100,37 @@ extern "C" int hc_ia_template(int k, const double* planes, uint8_t* buf, int cap
     ia_record_summary(buf, s);
     std::memcpy(summary, &s, sizeof(s));
     return n;
+}
+
+// The two-group path of the fast kernel: the two representative planes cut alone (k = 2), their
+// record relabelled for the tet, as on a secondary-lookup hit or miss.
+extern "C" int hc_ia_template2(int k, const double* planes, uint8_t* buf, int cap, uint16_t* summary) {
+    uint8_t rep[64];
+    int first;
+    if (ia_group_planes(planes, k, rep, first) != 2) return -1;
+    int r[2], n = 0;
+    for (int i = 0; i < k; ++i)
+        if (rep[i] == 4 + i) {
+            if (n == 2) return -2;
+            r[n++] = i;
+        }
+    if (n != 2) return -2;
+    double two[8];
+    for (int c = 0; c < 4; ++c) {
+        two[c] = planes[4 * r[0] + c];
+        two[4 + c] = planes[4 * r[1] + c];
+    }
+    static uint8_t rec2[1024];
+    uint16_t s2[16];
+    const int size2 = hc_ia_cut(2, two, 0, rec2, sizeof(rec2), s2);
+    if (size2 < 0) return size2;
+    const int size = ia_template_record_size(rec2, k);
+    if (size > cap) return -3;
+    ia_record_from_template2(rec2, k, rep, r[0], r[1], buf);
+    IASummary s;
+    ia_record_summary(buf, s);
+    std::memcpy(summary, &s, sizeof(s));
+    return size;
 }
 
 extern "C" int hc_sizes(int* out) {

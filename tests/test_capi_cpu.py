@@ -180,6 +180,44 @@ def test_one_effective_plane_template_path(hc, oracle):
     assert seen > 300
 
 
+def test_two_group_template_path(hc, oracle):
+    """Tets whose planes reduce to two groups (duplicates, multiples, tet faces, zero planes besides two
+    distinct planes) take the two representatives' record, relabelled; it must equal the generic cut's."""
+    rng = np.random.default_rng(13)
+    seen = 0
+    for _ in range(400):
+        base = []
+        for _ in range(2):
+            p = rng.integers(-2, 3, size=4).astype(np.float64)
+            if rng.random() < 0.5:
+                p = rng.normal(size=4)
+            base.append(p)
+        rows = list(base)
+        for _ in range(int(rng.integers(0, 5))):
+            kind = rng.integers(0, 4)
+            p = base[int(rng.integers(0, 2))]
+            if kind == 0:
+                rows.append(p * float(rng.choice([-2.0, 0.5, 1.0, 3.0])))
+            elif kind == 1:
+                b = np.zeros(4)
+                b[int(rng.integers(0, 4))] = float(rng.choice([-1.5, 2.0]))
+                rows.append(b)
+            elif kind == 2:
+                rows.append(np.zeros(4))
+            else:
+                rows.append(p.copy())
+        rng.shuffle(rows)
+        rows = np.array(rows)
+        got = hc.ia_template2(rows)
+        if got is None:
+            continue
+        seen += 1
+        assert got[0] == oracle.ia_cut(rows)
+        big, summ = hc.cut("ia", rows, True)
+        assert got[0] == big and np.array_equal(got[1], summ[:4])
+    assert seen > 250
+
+
 def _exact_key(mode, rows):
     """The secondary-lookup key restated with rational arithmetic."""
     from fractions import Fraction as Fr
