@@ -63,6 +63,7 @@ constexpr int64_t kMidRecordBytes = 4096;   // per tet of the mid variant (fulle
 constexpr int64_t kMidThreshold = 4 * 152 * 5;  // deferred tets the exact kernel takes in about one wave
 constexpr int64_t kBigRecordBytes = 28672;  // bound of a record of the exact variants
 constexpr int64_t kBigSlots = 152 * 64;     // concurrent exact-variant threads
+constexpr int64_t kWarpCutTets = 152 * 20 * 8;  // heaviest tets cut a warp each (about 8 waves of resident warps)
 
 // A second stream per host thread and device, for work that overlaps the caller's stream inside one
 // call; created on first use and kept for the life of the thread's process, like the tables.
@@ -98,8 +99,11 @@ ria_status current_device(int* dev) {
 }
 
 // the secondary lookup of one mode (its entries share the mode's table region)
+std::atomic<uint32_t> g_cache_gen{0};
+
 void set_cache(CutArgs& a, DeviceCtx* ctx, bool mi) {
     const int m = mi ? 1 : 0;
+    a.cache.gen = g_cache_gen.fetch_add(1, std::memory_order_relaxed) + 1;
     a.cache.slots = ctx->cache_slots[m];
     a.cache.slot_mask = kCacheSlots - 1;
     a.cache.cap = kCacheEntries;
@@ -415,6 +419,7 @@ ria_status run_pipeline(const ria_config* cfg, const Inputs& in, cudaStream_t s,
         const int64_t G_light = G - G_mid;
         const bool prep = G_light > 0 && (ca.table || ca.cache.slots);
         uint32_t* rest = prep ? tmp.get<uint32_t>(G_light, &err) : nullptr;
+        WaitRec* waitl = prep ? tmp.get<WaitRec>(G_light, &err) : nullptr;
         if (err != cudaSuccess) return bail(fail(RIA_ENOMEM, "device allocation failed"));
         AuxStream* aux = nullptr;
         if (G_mid > 0 && G_light > 0) {
@@ -425,10 +430,20 @@ ria_status run_pipeline(const ria_config* cfg, const Inputs& in, cudaStream_t s,
         if (G_mid > 0) {
             CutArgs ch = ca;
             ch.n = G_mid;
-            if (mi)
+            if (mi) {
                 launch_cut_mi_split(ch, s);
-            else
-                launch_cut_fast(ch, s, false);
+            } else {
+                // a warp per tet for the heaviest (their latency sets the stage's time when they are
+                // few); past a few waves of resident warps a thread per tet has the higher throughput
+                ch.n = G_mid < kWarpCutTets ? G_mid : kWarpCutTets;
+                launch_cut_warp(ch, s);
+                if (G_mid > ch.n) {
+                    CutArgs cf = ca;
+                    cf.list = gen + ch.n;
+                    cf.n = G_mid - ch.n;
+                    launch_cut_fast(cf, s, false);
+                }
+            }
         }
         if (G_light > 0) {
             cudaStream_t sl = aux ? aux->s : s;
@@ -439,11 +454,20 @@ ria_status run_pipeline(const ria_config* cfg, const Inputs& in, cudaStream_t s,
                 CutArgs cp = cl;
                 cp.deferred = rest;
                 cp.n_deferred = (unsigned int*)(cnt + 10);
+                cp.wait = waitl;
+                cp.n_wait = (unsigned int*)(cnt + 11);
                 launch_cut_prep(cp, sl);
                 cl.list = rest;
                 cl.n_dev = cp.n_deferred;
             }
             launch_cut_fast(cl, sl, false);
+            if (prep) {
+                CutArgs cw = ca;
+                cw.n = G_light;
+                cw.wait = waitl;
+                cw.n_wait = (unsigned int*)(cnt + 11);
+                launch_cut_wait(cw, sl);
+            }
         }
         if (aux) {
             cudaEventRecord(aux->join, aux->s);

@@ -106,15 +106,21 @@ __device__ __forceinline__ const uint8_t* finish_cut(const CutArgs& a, uint32_t 
 }
 
 // ---- secondary lookup: a device-wide cache of canonical records keyed by the combinatorial type
-// (lookup2.cuh), filled on first sight by the general cut and kept for the life of the process.
-// An entry is published after its bytes (fence, then CAS of its slot); readers fence after seeing
-// the slot.  Records depend only on the key, so racing inserts of one key are interchangeable.
+// (lookup2.cuh), kept for the life of the process.  A slot holds (key + 1) << 32 and either the
+// entry of the published record or a claim (kClaim | call number): the lookup pass lets the first
+// tet of a key claim it, that tet's cut publishes the record, and the key's other tets take the
+// record afterwards, so a key is cut once per call however many tets share it.  A record is
+// published after its bytes (fence, then CAS of its slot); readers fence after seeing the slot.
+// Records depend only on the key, so racing publications of one key are interchangeable.  A claim
+// left by another call (whose cut could not publish) may be taken over.
 constexpr int kCacheProbes = 32;
+constexpr uint32_t kClaim = 0xFFFF0000u;  // entries stay far below (kCacheEntries)
 
 __device__ __forceinline__ uint32_t cache_hash(uint32_t key, uint32_t mask) {
     return (uint32_t)mix64((uint64_t)key) & mask;
 }
 
+// the entry of the key's record; -1 when absent, -2 when claimed and not yet published
 __device__ __forceinline__ int cache_find(const CutArgs::Cache& c, uint32_t key) {
     const unsigned long long tag = (unsigned long long)(key + 1u) << 32;
     const uint32_t h = cache_hash(key, c.slot_mask);
@@ -122,6 +128,7 @@ __device__ __forceinline__ int cache_find(const CutArgs::Cache& c, uint32_t key)
         const unsigned long long v = *reinterpret_cast<volatile const unsigned long long*>(&c.slots[(h + p) & c.slot_mask]);
         if (v == 0) return -1;
         if ((v & 0xFFFFFFFF00000000ull) == tag) {
+            if ((uint32_t)v >= kClaim) return -2;
             __threadfence();
             return (int)(v & 0xFFFFFFFFull);
         }
@@ -129,6 +136,44 @@ __device__ __forceinline__ int cache_find(const CutArgs::Cache& c, uint32_t key)
     return -1;
 }
 
+enum : int { CLAIM_OWNER = 0, CLAIM_PUBLISHED = 1, CLAIM_WAIT = 2, CLAIM_NONE = 3 };
+
+// CLAIM_OWNER: this tet claimed the key (its cut publishes the record); CLAIM_PUBLISHED: the record
+// is entry *j; CLAIM_WAIT: another tet of this call claimed it; CLAIM_NONE: no free slot in reach.
+__device__ __forceinline__ int cache_claim(const CutArgs::Cache& c, uint32_t key, int* j) {
+    const unsigned long long tag = (unsigned long long)(key + 1u) << 32;
+    const unsigned long long mine = tag | (kClaim | (c.gen & 0xFFFFu));
+    const uint32_t h = cache_hash(key, c.slot_mask);
+    for (int p = 0; p < kCacheProbes; ++p) {
+        unsigned long long* slot = &c.slots[(h + p) & c.slot_mask];
+        unsigned long long v = *reinterpret_cast<volatile unsigned long long*>(slot);
+        if (v == 0) {
+            v = atomicCAS(slot, 0ull, mine);
+            if (v == 0) return CLAIM_OWNER;
+        }
+        if ((v & 0xFFFFFFFF00000000ull) != tag) continue;
+        if ((uint32_t)v < kClaim) {
+            __threadfence();
+            *j = (int)(uint32_t)v;
+            return CLAIM_PUBLISHED;
+        }
+        if (v == mine) return CLAIM_WAIT;
+        // a claim of another call: take it over, or learn what replaced it
+        const unsigned long long w = atomicCAS(slot, v, mine);
+        if (w == v) return CLAIM_OWNER;
+        if (w == mine) return CLAIM_WAIT;
+        if ((uint32_t)w < kClaim) {
+            __threadfence();
+            *j = (int)(uint32_t)w;
+            return CLAIM_PUBLISHED;
+        }
+        return CLAIM_NONE;
+    }
+    return CLAIM_NONE;
+}
+
+// publish a record for the key: into an empty slot, over a claim, or not at all when the key is
+// already published
 __device__ __forceinline__ void cache_insert(const CutArgs::Cache& c, uint32_t key, const uint8_t* rec, int size,
                                              IASum4 sum) {
     const unsigned long long j = atomicAdd(c.next, 1ull);
@@ -140,11 +185,20 @@ __device__ __forceinline__ void cache_insert(const CutArgs::Cache& c, uint32_t k
     c.table_off[kTablePatterns + j] = (uint32_t)(c.heap_base + off);
     c.table_sum[kTablePatterns + j] = sum;
     __threadfence();
-    const unsigned long long v = ((unsigned long long)(key + 1u) << 32) | j;
+    const unsigned long long tag = (unsigned long long)(key + 1u) << 32;
+    const unsigned long long v = tag | j;
     const uint32_t h = cache_hash(key, c.slot_mask);
     for (int p = 0; p < kCacheProbes; ++p) {
-        const unsigned long long old = atomicCAS(&c.slots[(h + p) & c.slot_mask], 0ull, v);
-        if (old == 0 || (old >> 32) == (unsigned long long)(key + 1u)) return;
+        unsigned long long* slot = &c.slots[(h + p) & c.slot_mask];
+        unsigned long long old = atomicCAS(slot, 0ull, v);
+        if (old == 0) return;
+        for (int t = 0; t < 4 && (old & 0xFFFFFFFF00000000ull) == tag; ++t) {
+            if ((uint32_t)old < kClaim) return;  // published already
+            const unsigned long long w = atomicCAS(slot, old, v);
+            if (w == old) return;
+            old = w;
+        }
+        if ((old & 0xFFFFFFFF00000000ull) == tag) return;
     }
 }
 
@@ -163,36 +217,48 @@ __device__ __forceinline__ bool ia_emit_template2(const CutArgs& a, uint32_t ai,
     return true;
 }
 
-// Tets whose planes reduce to two groups (duplicates, multiples, planes on a tet face, zero planes
-// besides two distinct planes): the secondary lookup of the two representatives, whose record is
-// relabelled for the tet (on a miss, with `cut_on_miss`, the two planes alone are cut and the record
-// cached).  Returns CUT_OK when the tet's record is written, CUT_DEFER to fall back to the general cut.
-__device__ int ia_try_two_groups(const CutArgs& a, uint32_t ai, const double* planes, int k, const uint8_t* rep,
-                                 bool cut_on_miss) {
-    int r[2], n = 0;
+// the two representatives of a tet whose planes form two groups, and the key of their pair
+__device__ __forceinline__ bool ia_two_group_key(const double* planes, int k, const uint8_t* rep, int r[2],
+                                                 double two[8], uint32_t& key) {
+    int n = 0;
     for (int i = 0; i < k; ++i)
         if (rep[i] == 4 + i) {
-            if (n == 2) return CUT_DEFER;
+            if (n == 2) return false;
             r[n++] = i;
         }
-    if (n != 2) return CUT_DEFER;
-    double two[8];
+    if (n != 2) return false;
     for (int c = 0; c < 4; ++c) {
         two[c] = planes[4 * r[0] + c];
         two[4 + c] = planes[4 * r[1] + c];
     }
-    uint32_t key = 0;
-    if (!ia_key2(two, key)) return CUT_DEFER;
-    const int j = cache_find(a.cache, key);
-    if (j >= 0) {
-        const uint8_t* tmpl = a.cache.table + a.cache.table_off[kTablePatterns + j];
-        if (k == 2) {  // the record itself
-            a.act_desc[ai] = kTableBit | (uint64_t)(kTablePatterns + j);
-            a.act_sum[ai] = a.cache.table_sum[kTablePatterns + j];
-            return CUT_OK;
-        }
-        return ia_emit_template2(a, ai, tmpl, k, rep, r[0], r[1]) ? CUT_OK : CUT_DEFER;
+    return ia_key2(two, key);
+}
+
+// the tet's record from published entry j of its two-group key
+__device__ __forceinline__ bool ia_from_entry(const CutArgs& a, uint32_t ai, int j, int k, const uint8_t* rep, int r0,
+                                              int r1) {
+    if (k == 2) {  // the record itself
+        a.act_desc[ai] = kTableBit | (uint64_t)(kTablePatterns + j);
+        a.act_sum[ai] = a.cache.table_sum[kTablePatterns + j];
+        return true;
     }
+    const uint8_t* tmpl = a.cache.table + a.cache.table_off[kTablePatterns + j];
+    return ia_emit_template2(a, ai, tmpl, k, rep, r0, r1);
+}
+
+// Tets whose planes reduce to two groups (duplicates, multiples, planes on a tet face, zero planes
+// besides two distinct planes): the secondary lookup of the two representatives, whose record is
+// relabelled for the tet (on a miss, with `cut_on_miss`, the two planes alone are cut and the record
+// published).  Returns CUT_OK when the tet's record is written, CUT_DEFER to fall back to the
+// general cut.
+__device__ int ia_try_two_groups(const CutArgs& a, uint32_t ai, const double* planes, int k, const uint8_t* rep,
+                                 bool cut_on_miss) {
+    int r[2];
+    double two[8];
+    uint32_t key = 0;
+    if (!ia_two_group_key(planes, k, rep, r, two, key)) return CUT_DEFER;
+    const int j = cache_find(a.cache, key);
+    if (j >= 0) return ia_from_entry(a, ai, j, k, rep, r[0], r[1]) ? CUT_OK : CUT_DEFER;
     if (!cut_on_miss) return CUT_DEFER;
     IACutFast c;
     if (c.run(two, 2) != CUT_OK) return CUT_DEFER;
@@ -289,10 +355,25 @@ __global__ void __launch_bounds__(128) k_cut_fast(CutArgs a) {
     cut_one<MI, MID>(a, i);
 }
 
-// The lookup pass: a tet the one-plane table or the secondary cache finishes is done here; every
-// other tet is appended to a.deferred (one atomic per warp, so the general pass keeps the list's
-// heaviest-first order per warp).  A warp of the general pass then holds cuts only, rather than a
-// mix of short lookups and long cuts that run one after the other.
+// The lookup pass.  A tet the one-plane table finishes, or whose secondary-lookup key is published,
+// is done here.  The first tet of an unpublished key claims it and goes on to the cut kernels,
+// whose cut publishes the record; the key's other tets wait (a.wait) for launch_cut_wait.  Every
+// other tet is appended to a.deferred for the cut kernels (one atomic per warp, so the list keeps
+// its heaviest-first order per warp).  A warp of the cut kernels then holds cuts only, and a key is
+// cut once per call.
+__device__ __forceinline__ void append_warp(bool mine, uint32_t ai, uint32_t* list, unsigned int* count) {
+    const unsigned act = __activemask();
+    const unsigned m = __ballot_sync(act, mine);
+    if (mine) {
+        const int lane = threadIdx.x & 31;
+        const int leader = __ffs(m) - 1;
+        unsigned int base = 0;
+        if (lane == leader) base = atomicAdd(count, (unsigned int)__popc(m));
+        base = __shfl_sync(m, base, leader);
+        list[base + __popc(m & ((1u << lane) - 1u))] = ai;
+    }
+}
+
 template <bool MI>
 __global__ void __launch_bounds__(128) k_cut_prep(CutArgs a) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -300,35 +381,72 @@ __global__ void __launch_bounds__(128) k_cut_prep(CutArgs a) {
     const uint32_t ai = a.list[i];
     double planes[4 * kFastMaxK];
     const int k = gather_planes(a, ai, planes, kFastMaxK);
-    bool done = false;
+    bool done = false, wait = false;
+    WaitRec w{};
     if (k <= kFastMaxK) {
         if (!MI) {
             uint8_t rep[kFastMaxK];
             bool two = false;
             done = ia_try_template(a, ai, planes, k, &two, rep);
-            if (!done && two && a.cache.slots) done = ia_try_two_groups(a, ai, planes, k, rep, false) == CUT_OK;
+            int r[2];
+            double tw[8];
+            uint32_t key = 0;
+            if (!done && two && a.cache.slots && ia_two_group_key(planes, k, rep, r, tw, key)) {
+                int j = -1;
+                const int c = cache_claim(a.cache, key, &j);
+                if (c == CLAIM_PUBLISHED) {
+                    done = ia_from_entry(a, ai, j, k, rep, r[0], r[1]);
+                } else if (c == CLAIM_WAIT) {
+                    wait = true;
+                    w.ai = ai;
+                    w.key = key;
+                    w.k = (uint8_t)k;
+                    w.r0 = (uint8_t)r[0];
+                    w.r1 = (uint8_t)r[1];
+                    for (int t = 0; t < k; ++t) w.rep[t] = rep[t];
+                }
+            }
         } else if (k == 3 && a.cache.slots && mi_distinct3(planes)) {
             uint32_t key = 0;
             if (mi_key3(planes, key)) {
-                const int j = cache_find(a.cache, key);
-                if (j >= 0) {
+                int j = -1;
+                const int c = cache_claim(a.cache, key, &j);
+                if (c == CLAIM_PUBLISHED) {
                     a.act_desc[ai] = kTableBit | (uint64_t)(kTablePatterns + j);
                     a.act_sum[ai] = a.cache.table_sum[kTablePatterns + j];
                     done = true;
+                } else if (c == CLAIM_WAIT) {
+                    wait = true;
+                    w.ai = ai;
+                    w.key = key;
+                    w.k = 3;
                 }
             }
         }
     }
-    const unsigned act = __activemask();
-    const unsigned rest = __ballot_sync(act, !done);
-    if (!done) {
-        const int lane = threadIdx.x & 31;
-        const int leader = __ffs(rest) - 1;
-        unsigned int base = 0;
-        if (lane == leader) base = atomicAdd(a.n_deferred, (unsigned int)__popc(rest));
-        base = __shfl_sync(rest, base, leader);
-        a.deferred[base + __popc(rest & ((1u << lane) - 1u))] = ai;
+    if (wait) a.wait[atomicAdd(a.n_wait, 1u)] = w;
+    append_warp(!done && !wait, ai, a.deferred, a.n_deferred);
+}
+
+// The waiting tets: their keys' records are published by now (or the claiming tet's cut could not
+// publish, and the tet goes to the exact kernel).
+template <bool MI>
+__global__ void __launch_bounds__(128) k_cut_wait(CutArgs a) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n || i >= (int64_t)*a.n_wait) return;
+    const WaitRec w = a.wait[i];
+    const int j = cache_find(a.cache, w.key);
+    bool done = false;
+    if (j >= 0) {
+        if (MI) {
+            a.act_desc[w.ai] = kTableBit | (uint64_t)(kTablePatterns + j);
+            a.act_sum[w.ai] = a.cache.table_sum[kTablePatterns + j];
+            done = true;
+        } else {
+            done = ia_from_entry(a, w.ai, j, w.k, w.rep, w.r0, w.r1);
+        }
     }
+    if (!done) a.deferred[atomicAdd(a.n_deferred, 1u)] = w.ai;
 }
 
 // Material interface with many materials: one block per tet, one thread per material.  A material's
@@ -382,6 +500,67 @@ __global__ void __launch_bounds__(kSplitMaxK) k_cut_mi_split(CutArgs a) {
             if (!rec) a.deferred[atomicAdd(a.n_deferred, 1u)] = ai;
         }
         __syncthreads();
+    }
+}
+
+// One warp per tet, its state in shared memory (IAWarpCutDev, cut_ia_warp.cuh): the heavy bins of
+// the implicit arrangement.  A tet beyond the warp variant's capacity goes to the deferred list.
+constexpr int kCutWarps = 4;  // warps per block
+
+__global__ void __launch_bounds__(32 * kCutWarps) k_cut_warp(CutArgs a) {
+    extern __shared__ __align__(16) unsigned char warp_smem[];
+    const int wib = threadIdx.x >> 5;
+    IAWarpCutDev& S = reinterpret_cast<IAWarpCutDev*>(warp_smem)[wib];
+    const Lanes L{(int)(threadIdx.x & 31)};
+    const int lane = L.lane;
+    const int64_t warps = (int64_t)gridDim.x * kCutWarps;
+    for (int64_t i = (int64_t)blockIdx.x * kCutWarps + wib; i < a.n; i += warps) {
+        const uint32_t ai = a.list[i];
+        int k;
+        if (a.values) {
+            const uint32_t r0 = a.value_off[ai];
+            k = (int)(a.value_off[ai + 1] - r0);
+            if (k <= kWarpMaxK)
+                for (int x = lane; x < 4 * k; x += 32) S.pl[x] = a.values[4 * (size_t)r0 + x];
+        } else {
+            const uint64_t m = a.act_mask[ai];
+            k = __popcll(m);
+            if (k <= kWarpMaxK) {
+                int64_t v[4];
+                TetSrc ts{a.d_tets, a.g.res};
+                ts.get(a.act_tet[ai], v);
+                for (int x = lane; x < 4 * k; x += 32) {
+                    // plane x/4 is the (x/4)-th active function, at corner x%4
+                    uint64_t mm = m;
+                    for (int p = 0; p < (x >> 2); ++p) mm &= mm - 1;
+                    const int fn = __ffsll((long long)mm) - 1;
+                    S.pl[x] = a.fv[v[x & 3] * a.F + fn];
+                }
+            }
+        }
+        L.sync();
+        int st = k <= kWarpMaxK ? S.run(L, k) : CUT_DEFER;
+        unsigned long long off = 0;
+        int size = 0;
+        if (st == CUT_OK) {
+            S.canonicalize(L);
+            size = S.record_size();
+            if (lane == 0) off = atomicAdd(a.heap_used, (unsigned long long)size);
+            off = __shfl_sync(0xFFFFFFFFu, off, 0);
+            if (off + size > a.heap_cap) st = CUT_DEFER;
+        }
+        if (st == CUT_OK) {
+            IASummary sum;
+            S.emit(L, a.heap + off, sum);
+            if (lane == 0) {
+                a.act_desc[ai] = off | a.desc_bit;
+                a.act_sum[ai] = pack_sum<IASummary>(sum);
+            }
+        } else if (lane == 0) {
+            // capacity, or an exact evaluation out of range: the exact kernel takes it (and reports)
+            a.deferred[atomicAdd(a.n_deferred, 1u)] = ai;
+        }
+        L.sync();
     }
 }
 
@@ -519,6 +698,16 @@ void launch_cut_mi_split(const CutArgs& a, cudaStream_t s) {
     note_launch();
 }
 
+void launch_cut_wait(const CutArgs& a, cudaStream_t s) {
+    if (a.n == 0) return;
+    const unsigned nb = (unsigned)((a.n + 127) / 128);
+    if (a.mi)
+        k_cut_wait<true><<<nb, 128, 0, s>>>(a);
+    else
+        k_cut_wait<false><<<nb, 128, 0, s>>>(a);
+    note_launch();
+}
+
 void launch_cut_prep(const CutArgs& a, cudaStream_t s) {
     if (a.n == 0) return;
     const unsigned nb = (unsigned)((a.n + 127) / 128);
@@ -529,12 +718,37 @@ void launch_cut_prep(const CutArgs& a, cudaStream_t s) {
     note_launch();
 }
 
+void launch_cut_warp(const CutArgs& a, cudaStream_t s) {
+    if (a.n == 0) return;
+    static bool attr = false;
+    const size_t smem = sizeof(IAWarpCutDev) * kCutWarps;
+    if (!attr) {
+        cudaFuncSetAttribute(k_cut_warp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        attr = true;
+    }
+    const int64_t want = (a.n + kCutWarps - 1) / kCutWarps;
+    const int64_t blocks = want < 152 * 64 ? want : 152 * 64;
+    k_cut_warp<<<(unsigned)blocks, 32 * kCutWarps, smem, s>>>(a);
+    note_launch();
+}
+
 void launch_cut_fast(const CutArgs& a, cudaStream_t s, bool mid) {
     if (a.n == 0) return;
     // each thread runs one long serial cut: with few tets, smaller blocks spread them over all SMs
     int bs = 128;
     while (bs > 32 && (a.n + bs - 1) / bs < 4 * 152) bs >>= 1;
     const unsigned nb = (unsigned)((a.n + bs - 1) / bs);
+    // the per-thread state lives in local memory: ask for the largest L1 (no shared memory used)
+    static bool carve = false;
+    if (!carve) {
+        cudaFuncSetAttribute(k_cut_fast<true, true>, cudaFuncAttributePreferredSharedMemoryCarveout, 0);
+        cudaFuncSetAttribute(k_cut_fast<true, false>, cudaFuncAttributePreferredSharedMemoryCarveout, 0);
+        cudaFuncSetAttribute(k_cut_fast<false, true>, cudaFuncAttributePreferredSharedMemoryCarveout, 0);
+        cudaFuncSetAttribute(k_cut_fast<false, false>, cudaFuncAttributePreferredSharedMemoryCarveout, 0);
+        cudaFuncSetAttribute(k_cut_prep<true>, cudaFuncAttributePreferredSharedMemoryCarveout, 0);
+        cudaFuncSetAttribute(k_cut_prep<false>, cudaFuncAttributePreferredSharedMemoryCarveout, 0);
+        carve = true;
+    }
     if (a.mi) {
         if (mid) k_cut_fast<true, true><<<nb, bs, 0, s>>>(a);
         else k_cut_fast<true, false><<<nb, bs, 0, s>>>(a);

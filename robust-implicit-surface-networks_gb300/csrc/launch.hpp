@@ -114,6 +114,7 @@ void launch_filter_scatter(bool mi, const ulonglong2* vmask, const double* fv, i
                            const IASum4* table_sum, FilterOut out, cudaStream_t s);
 
 // ---- stage c (k_cut.cu)
+struct WaitRec;
 struct CutArgs {
     bool mi;
     const uint32_t* list;  // indices into the active arrays
@@ -151,12 +152,29 @@ struct CutArgs {
         uint8_t* table = nullptr;             // the mode's table region (entries follow the 81 patterns)
         uint32_t* table_off = nullptr;
         IASum4* table_sum = nullptr;
+        uint32_t gen = 0;                     // call number: claims of other calls can be taken over
     } cache;
+    // the lookup pass: tets whose key another tet of this call claimed (resolved after the cuts)
+    WaitRec* wait = nullptr;
+    unsigned int* n_wait = nullptr;
+};
+// a tet waiting for the record of its key (secondary lookup), with what its own record needs
+struct WaitRec {
+    uint32_t ai;
+    uint32_t key;
+    uint8_t k, r0, r1, pad;
+    uint8_t rep[8];
 };
 // tets the lookup tables finish without a cut (IA: one or two effective planes found in the table
 // or the secondary cache; MI: three materials found in the cache); the others are appended, in list
 // order per warp, to `deferred` for the cut kernels
 void launch_cut_prep(const CutArgs& a, cudaStream_t s);
+// the waiting tets of the lookup pass, after the cuts have published their keys' records (a key
+// still unpublished sends its tets to the deferred list)
+void launch_cut_wait(const CutArgs& a, cudaStream_t s);
+// implicit arrangement, one warp per tet with its state in shared memory (exact predicates); a tet
+// beyond its capacity goes to the deferred list
+void launch_cut_warp(const CutArgs& a, cudaStream_t s);
 // filtered variants, one thread per tet: `mid` for the heavy bins (four or more active functions,
 // up to 16), the small one otherwise; a tet that outgrows them, or whose record does not fit the
 // heap, goes to the deferred list

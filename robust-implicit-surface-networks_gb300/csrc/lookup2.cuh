@@ -16,9 +16,11 @@
 
 namespace ria {
 
-// exact sign of a*d - b*c, or 2 if the exact evaluation overflowed
+// exact sign of a*d - b*c, or 2 if the exact evaluation overflowed (inputs within key_range: a
+// product is zero only when a factor is, so two zero products decide the sign without the exact path)
 RIA_HD int sign_det2(double a, double b, double c, double d) {
     const double x = a * d, y = b * c;
+    if (x == 0.0 && y == 0.0) return 0;
     const double v = x - y;
     const double bound = 4.0 * kU * (fabs(x) + fabs(y));
     if (v > bound) return 1;

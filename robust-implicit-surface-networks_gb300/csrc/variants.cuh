@@ -3,6 +3,7 @@
 //         exact predicate or more room is deferred.
 //   big:  state in global scratch, exact predicates, room for up to ~10 active functions.
 #pragma once
+#include "cut_ia_warp.cuh"
 #include "cut_mi.cuh"
 
 namespace ria {
@@ -16,4 +17,6 @@ using MICutFast = MICut<32, 24, 160, 48, 48, 256, false>;
 using IACutMid = IACut<128, 256, 64, 1024, false>;
 using MICutMid = MICut<96, 96, 640, 128, 128, 1024, false>;
 using MICutBig = MICut<255, 255, 2048, 255, 512, 4096, true>;
+// warp variant: one warp per tet, state in shared memory, exact predicates (32 cells)
+using IAWarpCutDev = IAWarpCut<64, 128, 640>;
 }  // namespace ria

@@ -5,6 +5,7 @@
 #include "../../robust-implicit-surface-networks_gb300/csrc/cut_mi.cuh"
 #include "../../robust-implicit-surface-networks_gb300/csrc/variants.cuh"
 #include "../../robust-implicit-surface-networks_gb300/csrc/lookup2.cuh"
+#include "../../robust-implicit-surface-networks_gb300/csrc/cut_ia_warp.cuh"
 
 using namespace ria;
 
@@ -20,8 +21,32 @@ static int finish(C* c, int st, uint8_t* buf, int cap, uint16_t* summary) {
     return n;
 }
 
-// big: 0 the small filtered variant, 1 the exact variant, 2 the mid-size filtered variant
+// big: 0 the small filtered variant, 1 the exact variant, 2 the mid-size filtered variant, 3 the
+// warp variant (one lane: its lane-parallel loops run serially)
 extern "C" int hc_ia_cut(int k, const double* planes, int big, uint8_t* buf, int cap, uint16_t* summary) {
+    if (big == 3) {
+        if (k > kWarpMaxK) return -11;
+        auto* c = new IAWarpCutDev();
+        for (int i = 0; i < 4 * k; ++i) c->pl[i] = planes[i];
+        Lanes L;
+        int st = c->run(L, k);
+        int r = 0;
+        if (st != CUT_OK) {
+            r = -10 - st;
+        } else {
+            c->canonicalize(L);
+            r = c->record_size();
+            if (r > cap) {
+                r = -3;
+            } else {
+                IASummary s;
+                c->emit(L, buf, s);
+                std::memcpy(summary, &s, sizeof(s));
+            }
+        }
+        delete c;
+        return r;
+    }
     if (big == 2) {
         auto* c = new IACutMid();
         int r = finish<IACutMid, IASummary>(c, c->run(planes, k), buf, cap, summary);

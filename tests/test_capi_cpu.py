@@ -54,12 +54,15 @@ def hc():
 
 def _agree(hc, oracle, mode, rows):
     ref = oracle.ia_cut(rows) if mode == "ia" else oracle.mi_cut(rows)
-    big, _ = hc.cut(mode, rows, True)
+    big, bsum = hc.cut(mode, rows, True)
     assert big == ref
     fast, _ = hc.cut(mode, rows, False)
     assert isinstance(fast, int) or fast == ref
     mid, _ = hc.cut(mode, rows, "mid")
     assert isinstance(mid, int) or mid == ref
+    if mode == "ia":
+        warp, wsum = hc.cut(mode, rows, "warp")
+        assert warp == ref and np.array_equal(wsum[:4], bsum[:4])
     return isinstance(fast, int)
 
 
@@ -285,3 +288,29 @@ def test_heavy_tets_exact_variant(hc, oracle):
             out, _ = hc.cut("mi", rows, True)
             assert not isinstance(out, int) and out == oracle.mi_cut(rows)
     assert done >= 8
+
+
+def test_warp_variant_heavy_and_degenerate(hc, oracle):
+    """The warp variant (its lane-parallel steps run serially here) on the heavy bins it serves:
+    four to ten planes, random, integer-degenerate and with duplicated planes.  It either reports
+    its capacity or reproduces the oracle's record and summary."""
+    rng = np.random.default_rng(14)
+    done = 0
+    for k in range(4, 11):
+        for trial in range(30):
+            if trial % 3 == 0:
+                rows = rng.normal(size=(k, 4))
+            elif trial % 3 == 1:
+                rows = rng.integers(-2, 3, size=(k, 4)).astype(np.float64)
+            else:
+                base = rng.normal(size=(max(2, k // 2), 4))
+                rows = np.array([base[int(rng.integers(0, len(base)))] * float(rng.choice([1.0, -2.0, 0.5]))
+                                 for _ in range(k)])
+            out, summ = hc.cut("ia", rows, "warp")
+            if isinstance(out, int):
+                assert out == -11  # capacity
+                continue
+            big, bsum = hc.cut("ia", rows, True)
+            assert out == oracle.ia_cut(rows) == big and np.array_equal(summ[:4], bsum[:4])
+            done += 1
+    assert done >= 150
