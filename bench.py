@@ -407,7 +407,7 @@ def main():
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         for _ in range(args.steps):
-            L.ria_lookup_cache_clear()  # no reuse across steps: each step fills its own lookup cache
+            L.ria_lookup_cache_clear()  # no reuse across steps: each starts from the seeded lookup tables
             m = grid(wl.res, wl.funcs)
             tm = m.timings
             dev_ms.append(tm["total"] * 1e3)

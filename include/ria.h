@@ -306,10 +306,12 @@ RIA_API void ria_mesh_free(ria_mesh* mesh);
 RIA_API const char* ria_last_error(void);
 /* Diagnostics: number of kernels this library has launched in this process. */
 RIA_API uint64_t ria_kernel_launches(void);
-/* Empties the current device's secondary-lookup caches (two-plane and three-material records kept
- * by their combinatorial type; results never depend on them).  Callers that must not reuse work
- * across calls (for example a benchmark timing single calls) clear them first.  Must not overlap
- * with running calls on the device. */
+/* Resets the current device's secondary-lookup tables (two-plane and three-material records kept
+ * by their combinatorial type; results never depend on them) to their seeded state: the records
+ * computed once per process from synthetic configurations when the mode's table is built, like the
+ * reference's precomputed tables.  Records added by later calls are dropped, so callers that must
+ * not reuse work across calls (for example a benchmark timing single calls) reset them first.
+ * Must not overlap with running calls on the device. */
 RIA_API ria_status ria_lookup_cache_clear(void);
 RIA_API int ria_device_count(void);
 

@@ -53,6 +53,9 @@ struct DeviceCtx {
     IASum4* table_sum[2] = {nullptr, nullptr};
     unsigned long long* cache_slots[2] = {nullptr, nullptr};
     unsigned long long* cache_cnt[2] = {nullptr, nullptr};  // [0] entries used, [1] template bytes used
+    // the seeded secondary lookup, restored by ria_lookup_cache_clear
+    unsigned long long* seed_slots[2] = {nullptr, nullptr};
+    unsigned long long* seed_cnt[2] = {nullptr, nullptr};
 };
 
 std::mutex g_mu;
@@ -154,6 +157,21 @@ ria_status ensure_table(bool mi, cudaStream_t s, DeviceCtx** out) {
         cudaFree(scratch);
         cudaFree(status);
         if (h) return fail(RIA_EINTERNAL, "lookup table construction failed");
+        // seed the secondary lookup (RIA_NO_LOOKUP_SEED set: start empty, every key claimed by a
+        // call) and keep a copy of the seeded state
+        if (!getenv("RIA_NO_LOOKUP_SEED")) {
+            CutArgs sa{};
+            sa.mi = mi;
+            set_cache(sa, &c, mi);
+            launch_seed_cache(sa, s);
+            RIA_CUDA(cudaGetLastError());
+        }
+        RIA_CUDA(cudaMalloc(&c.seed_slots[m], sizeof(unsigned long long) * kCacheSlots));
+        RIA_CUDA(cudaMalloc(&c.seed_cnt[m], sizeof(unsigned long long) * 2));
+        RIA_CUDA(cudaMemcpyAsync(c.seed_slots[m], c.cache_slots[m], sizeof(unsigned long long) * kCacheSlots,
+                                 cudaMemcpyDeviceToDevice, s));
+        RIA_CUDA(cudaMemcpyAsync(c.seed_cnt[m], c.cache_cnt[m], sizeof(unsigned long long) * 2, cudaMemcpyDeviceToDevice, s));
+        RIA_CUDA(cudaStreamSynchronize(s));
         c.ready[m] = true;
     }
     *out = &c;
@@ -420,6 +438,7 @@ ria_status run_pipeline(const ria_config* cfg, const Inputs& in, cudaStream_t s,
         const bool prep = G_light > 0 && (ca.table || ca.cache.slots);
         uint32_t* rest = prep ? tmp.get<uint32_t>(G_light, &err) : nullptr;
         WaitRec* waitl = prep ? tmp.get<WaitRec>(G_light, &err) : nullptr;
+        uint32_t* owners = prep && !mi ? tmp.get<uint32_t>(G_light, &err) : nullptr;
         if (err != cudaSuccess) return bail(fail(RIA_ENOMEM, "device allocation failed"));
         AuxStream* aux = nullptr;
         if (G_mid > 0 && G_light > 0) {
@@ -436,6 +455,7 @@ ria_status run_pipeline(const ria_config* cfg, const Inputs& in, cudaStream_t s,
                 // a warp per tet for the heaviest (their latency sets the stage's time when they are
                 // few); past a few waves of resident warps a thread per tet has the higher throughput
                 ch.n = G_mid < kWarpCutTets ? G_mid : kWarpCutTets;
+                ch.next = (unsigned int*)(cnt + 13);
                 launch_cut_warp(ch, s);
                 if (G_mid > ch.n) {
                     CutArgs cf = ca;
@@ -456,9 +476,24 @@ ria_status run_pipeline(const ria_config* cfg, const Inputs& in, cudaStream_t s,
                 cp.n_deferred = (unsigned int*)(cnt + 10);
                 cp.wait = waitl;
                 cp.n_wait = (unsigned int*)(cnt + 11);
+                cp.owners = owners;
+                cp.n_owners = (unsigned int*)(cnt + 12);
                 launch_cut_prep(cp, sl);
+                if (owners) {  // the claiming tets: a two-plane cut each, published for the waiting ones
+                    CutArgs co = cl;
+                    co.list = owners;
+                    co.n_dev = cp.n_owners;
+                    launch_cut_fast(co, sl, false);
+                }
                 cl.list = rest;
                 cl.n_dev = cp.n_deferred;
+            }
+            if (!mi) {
+                // the rest is decided on the device: a warp per tet while the list is short
+                cl.route_at = kWarpCutTets;
+                CutArgs cw = cl;
+                cw.next = (unsigned int*)(cnt + 14);
+                launch_cut_warp(cw, sl);
             }
             launch_cut_fast(cl, sl, false);
             if (prep) {
@@ -1611,8 +1646,9 @@ ria_status ria_lookup_cache_clear(void) {
     DeviceCtx& c = g_ctx[dev];
     for (int m = 0; m < 2; ++m) {
         if (!c.ready[m]) continue;
-        RIA_CUDA(cudaMemset(c.cache_slots[m], 0, sizeof(unsigned long long) * kCacheSlots));
-        RIA_CUDA(cudaMemset(c.cache_cnt[m], 0, sizeof(unsigned long long) * 2));
+        RIA_CUDA(cudaMemcpy(c.cache_slots[m], c.seed_slots[m], sizeof(unsigned long long) * kCacheSlots,
+                            cudaMemcpyDeviceToDevice));
+        RIA_CUDA(cudaMemcpy(c.cache_cnt[m], c.seed_cnt[m], sizeof(unsigned long long) * 2, cudaMemcpyDeviceToDevice));
     }
     RIA_CUDA(cudaDeviceSynchronize());
     return RIA_OK;

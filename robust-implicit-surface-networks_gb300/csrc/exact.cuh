@@ -19,9 +19,11 @@
 #if defined(__CUDACC__)
 #define RIA_HD __host__ __device__ __forceinline__
 #define RIA_HDI __host__ __device__
+#define RIA_COLD __host__ __device__ __noinline__  // rarely taken and large: one copy, out of the hot loops
 #else
 #define RIA_HD inline
 #define RIA_HDI inline
+#define RIA_COLD inline
 #endif
 
 namespace ria {
@@ -179,7 +181,7 @@ RIA_HDI bool det_rec(const double* M, int n, int row, unsigned cols, Expn<CAP>& 
 
 // Sign of an exact n x n determinant (n <= 5).  Returns 2 on capacity overflow.
 template <int CAP = 48>
-RIA_HDI int det_sign_exact(const double* M, int n) {
+RIA_COLD int det_sign_exact(const double* M, int n) {
     Expn<CAP> e;
     bool ok = true;
     switch (n) {

@@ -202,6 +202,58 @@ __device__ __forceinline__ void cache_insert(const CutArgs::Cache& c, uint32_t k
     }
 }
 
+// ---- seeding: the secondary lookup is filled once per process, when the mode's table is built,
+// from synthetic configurations (the reference ships its two-plane and three-material tables
+// precomputed): every row set with entries in {-2, ..., 2} (two planes: 5^8 sets) or {-1, 0, 1}
+// (three materials: 3^12 sets), then pseudo-random real rows with some exact zeros.  A new key is
+// claimed, cut by the small filtered variant and published; a key that variant cannot decide stays
+// claimed, and a call takes it over.
+constexpr int64_t kSeedRandom = 1 << 20;
+
+__device__ __forceinline__ double seed_value(uint64_t t, int i) {
+    const uint64_t h = mix64(t * 0x9E3779B97F4A7C15ull + (uint64_t)(i + 1) * 0xD1B54A32D192ED03ull);
+    if ((h & 7) == 0) return 0.0;
+    const double m = 1.0 + (double)((h >> 12) & ((1ull << 52) - 1)) * 2.220446049250313e-16;  // [1, 2)
+    const int e = (int)((h >> 3) & 7) - 4;
+    return ((h >> 6) & 1 ? -m : m) * ldexp(1.0, e);
+}
+
+template <bool MI>
+__global__ void __launch_bounds__(128) k_seed_cache(CutArgs a, int64_t n_int) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n_int + kSeedRandom) return;
+    constexpr int nr = MI ? 12 : 8;
+    double rows[12];
+    if (t < n_int) {
+        int64_t q = t;
+        for (int i = 0; i < nr; ++i) {
+            rows[i] = MI ? (double)(q % 3) - 1.0 : (double)(q % 5) - 2.0;
+            q /= MI ? 3 : 5;
+        }
+    } else {
+        for (int i = 0; i < nr; ++i) rows[i] = seed_value((uint64_t)t, i);
+    }
+    uint32_t key = 0;
+    if (!MI) {
+        uint8_t rep[2];
+        int first;
+        if (ia_group_planes(rows, 2, rep, first) != 2 || !ia_key2(rows, key)) return;
+    } else {
+        if (!mi_distinct3(rows) || !mi_key3(rows, key)) return;
+    }
+    int j = -1;
+    if (cache_claim(a.cache, key, &j) != CLAIM_OWNER) return;
+    typename Traits<MI>::Fast c;
+    if (c.run(rows, MI ? 3 : 2) != CUT_OK) return;
+    c.canonicalize();
+    const int size = c.record_size();
+    uint8_t rec[1024];
+    if (size > (int)sizeof(rec)) return;
+    typename Traits<MI>::Sum sum;
+    c.emit(rec, sum);
+    cache_insert(a.cache, key, rec, size, pack_sum<typename Traits<MI>::Sum>(sum));
+}
+
 // writes a relabelled two-plane record for tet ai (false: the heap is full)
 __device__ __forceinline__ bool ia_emit_template2(const CutArgs& a, uint32_t ai, const uint8_t* tmpl, int k,
                                                   const uint8_t* rep, int r1, int r2) {
@@ -350,8 +402,10 @@ __device__ __forceinline__ void cut_one(const CutArgs& a, int64_t i) {
 // One thread per tet.
 template <bool MI, bool MID>
 __global__ void __launch_bounds__(128) k_cut_fast(CutArgs a) {
+    const int64_t n = a.n_dev ? (a.n < (int64_t)*a.n_dev ? a.n : (int64_t)*a.n_dev) : a.n;
+    if (a.route_at && n <= a.route_at) return;  // the warp kernel takes a short list
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= a.n || (a.n_dev && i >= (int64_t)*a.n_dev)) return;
+    if (i >= n) return;
     cut_one<MI, MID>(a, i);
 }
 
@@ -381,7 +435,7 @@ __global__ void __launch_bounds__(128) k_cut_prep(CutArgs a) {
     const uint32_t ai = a.list[i];
     double planes[4 * kFastMaxK];
     const int k = gather_planes(a, ai, planes, kFastMaxK);
-    bool done = false, wait = false;
+    bool done = false, wait = false, owner = false;
     WaitRec w{};
     if (k <= kFastMaxK) {
         if (!MI) {
@@ -396,6 +450,8 @@ __global__ void __launch_bounds__(128) k_cut_prep(CutArgs a) {
                 const int c = cache_claim(a.cache, key, &j);
                 if (c == CLAIM_PUBLISHED) {
                     done = ia_from_entry(a, ai, j, k, rep, r[0], r[1]);
+                } else if (c == CLAIM_OWNER) {
+                    owner = a.owners != nullptr;
                 } else if (c == CLAIM_WAIT) {
                     wait = true;
                     w.ai = ai;
@@ -415,6 +471,8 @@ __global__ void __launch_bounds__(128) k_cut_prep(CutArgs a) {
                     a.act_desc[ai] = kTableBit | (uint64_t)(kTablePatterns + j);
                     a.act_sum[ai] = a.cache.table_sum[kTablePatterns + j];
                     done = true;
+                } else if (c == CLAIM_OWNER) {
+                    owner = a.owners != nullptr;
                 } else if (c == CLAIM_WAIT) {
                     wait = true;
                     w.ai = ai;
@@ -425,7 +483,8 @@ __global__ void __launch_bounds__(128) k_cut_prep(CutArgs a) {
         }
     }
     if (wait) a.wait[atomicAdd(a.n_wait, 1u)] = w;
-    append_warp(!done && !wait, ai, a.deferred, a.n_deferred);
+    if (a.owners) append_warp(owner, ai, a.owners, a.n_owners);
+    append_warp(!done && !wait && !owner, ai, a.deferred, a.n_deferred);
 }
 
 // The waiting tets: their keys' records are published by now (or the claiming tet's cut could not
@@ -513,8 +572,17 @@ __global__ void __launch_bounds__(32 * kCutWarps) k_cut_warp(CutArgs a) {
     IAWarpCutDev& S = reinterpret_cast<IAWarpCutDev*>(warp_smem)[wib];
     const Lanes L{(int)(threadIdx.x & 31)};
     const int lane = L.lane;
+    const int64_t n = a.n_dev ? (a.n < (int64_t)*a.n_dev ? a.n : (int64_t)*a.n_dev) : a.n;
+    if (a.route_at && n > a.route_at) return;  // the thread kernel takes a long list
     const int64_t warps = (int64_t)gridDim.x * kCutWarps;
-    for (int64_t i = (int64_t)blockIdx.x * kCutWarps + wib; i < a.n; i += warps) {
+    int64_t i = (int64_t)blockIdx.x * kCutWarps + wib;
+    for (;;) {
+        if (a.next) {  // take the next tet in list order: the heaviest first, and no warp idles early
+            unsigned int t = 0;
+            if (lane == 0) t = atomicAdd(a.next, 1u);
+            i = (int64_t)__shfl_sync(0xFFFFFFFFu, t, 0);
+        }
+        if (i >= n) break;
         const uint32_t ai = a.list[i];
         int k;
         if (a.values) {
@@ -561,6 +629,7 @@ __global__ void __launch_bounds__(32 * kCutWarps) k_cut_warp(CutArgs a) {
             a.deferred[atomicAdd(a.n_deferred, 1u)] = ai;
         }
         L.sync();
+        if (!a.next) i += warps;
     }
 }
 
@@ -698,6 +767,16 @@ void launch_cut_mi_split(const CutArgs& a, cudaStream_t s) {
     note_launch();
 }
 
+void launch_seed_cache(const CutArgs& a, cudaStream_t s) {
+    const int64_t n_int = a.mi ? 531441 : 390625;  // 3^12, 5^8
+    const unsigned nb = (unsigned)((n_int + kSeedRandom + 127) / 128);
+    if (a.mi)
+        k_seed_cache<true><<<nb, 128, 0, s>>>(a, n_int);
+    else
+        k_seed_cache<false><<<nb, 128, 0, s>>>(a, n_int);
+    note_launch();
+}
+
 void launch_cut_wait(const CutArgs& a, cudaStream_t s) {
     if (a.n == 0) return;
     const unsigned nb = (unsigned)((a.n + 127) / 128);
@@ -726,8 +805,17 @@ void launch_cut_warp(const CutArgs& a, cudaStream_t s) {
         cudaFuncSetAttribute(k_cut_warp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         attr = true;
     }
+    // resident blocks only; the warps stride over the list
+    static int resident = 0;
+    if (!resident) {
+        int dev = 0, sms = 0, per_sm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cut_warp, 32 * kCutWarps, smem);
+        resident = (sms > 0 ? sms : 152) * (per_sm > 0 ? per_sm : 1);
+    }
     const int64_t want = (a.n + kCutWarps - 1) / kCutWarps;
-    const int64_t blocks = want < 152 * 64 ? want : 152 * 64;
+    const int64_t blocks = want < resident ? want : resident;
     k_cut_warp<<<(unsigned)blocks, 32 * kCutWarps, smem, s>>>(a);
     note_launch();
 }

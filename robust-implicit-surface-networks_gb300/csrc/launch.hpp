@@ -134,6 +134,12 @@ struct CutArgs {
     uint32_t* deferred;          // fast variant: tets handed to the exact variant
     unsigned int* n_deferred;
     const unsigned int* n_dev = nullptr;  // when set, the list holds min(n, *n_dev) tets (a count on the device)
+    // when set, a list of at most route_at tets goes to the warp kernel and a longer one to the
+    // thread kernel (both are launched; the other returns at once)
+    int64_t route_at = 0;
+    unsigned int* next = nullptr;         // warp kernel: zeroed counter from which warps take tets in list order
+    uint32_t* owners = nullptr;           // the lookup pass: tets that claimed their key (else in deferred)
+    unsigned int* n_owners = nullptr;
     uint32_t* status;
     // explicit per-tet rows (the per-tet batch API): rows of tet i are value_off[i]..value_off[i+1]-1
     const double* values = nullptr;
@@ -169,6 +175,8 @@ struct WaitRec {
 // or the secondary cache; MI: three materials found in the cache); the others are appended, in list
 // order per warp, to `deferred` for the cut kernels
 void launch_cut_prep(const CutArgs& a, cudaStream_t s);
+// fill the secondary lookup (a.cache) from synthetic configurations, once per process and mode
+void launch_seed_cache(const CutArgs& a, cudaStream_t s);
 // the waiting tets of the lookup pass, after the cuts have published their keys' records (a key
 // still unpublished sends its tets to the deferred list)
 void launch_cut_wait(const CutArgs& a, cudaStream_t s);

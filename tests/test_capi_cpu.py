@@ -250,16 +250,19 @@ def test_secondary_lookup_keys(hc, oracle):
     (the combinatorial type fixes the canonical record), for generic and degenerate inputs."""
     rng = np.random.default_rng(12)
     seen = {}
-    for it in range(6000):
+    for it in range(8000):
         mode = "ia" if it % 2 == 0 else "mi"
         n = 2 if mode == "ia" else 3
-        kind = (it // 2) % 3
+        kind = (it // 2) % 4
         if kind == 0:
             rows = rng.normal(size=(n, 4))
         elif kind == 1:
             rows = rng.integers(-2, 3, size=(n, 4)).astype(np.float64)
-        else:
+        elif kind == 2:
             rows = rng.integers(-1, 2, size=(n, 4)).astype(np.float64) + rng.normal(size=(n, 4)) * 1e-9
+        else:  # the seeding's random rows: exact zeros among values of mixed magnitudes
+            rows = rng.normal(size=(n, 4)) * np.exp2(rng.integers(-4, 4, size=(n, 4)))
+            rows[rng.random((n, 4)) < 0.125] = 0.0
         k = hc.key(mode, rows)
         assert k == _exact_key(mode, rows)
         rec = oracle.ia_cut(rows) if mode == "ia" else oracle.mi_cut(rows)
