@@ -465,11 +465,11 @@ ria_status run_pipeline(const ria_config* cfg, const Inputs& in, cudaStream_t s,
                 }
             }
         }
+        CutArgs cl = ca;
+        cl.list = gen + G_mid;
+        cl.n = G_light;
         if (G_light > 0) {
             cudaStream_t sl = aux ? aux->s : s;
-            CutArgs cl = ca;
-            cl.list = gen + G_mid;
-            cl.n = G_light;
             if (prep) {
                 CutArgs cp = cl;
                 cp.deferred = rest;
@@ -479,34 +479,40 @@ ria_status run_pipeline(const ria_config* cfg, const Inputs& in, cudaStream_t s,
                 cp.owners = owners;
                 cp.n_owners = (unsigned int*)(cnt + 12);
                 launch_cut_prep(cp, sl);
-                if (owners) {  // the claiming tets: a two-plane cut each, published for the waiting ones
-                    CutArgs co = cl;
-                    co.list = owners;
-                    co.n_dev = cp.n_owners;
-                    launch_cut_fast(co, sl, false);
-                }
                 cl.list = rest;
                 cl.n_dev = cp.n_deferred;
-            }
-            if (!mi) {
-                // the rest is decided on the device: a warp per tet while the list is short
-                cl.route_at = kWarpCutTets;
-                CutArgs cw = cl;
-                cw.next = (unsigned int*)(cnt + 14);
-                launch_cut_warp(cw, sl);
-            }
-            launch_cut_fast(cl, sl, false);
-            if (prep) {
+                // the claiming tets' cuts publish their keys (implicit arrangement: a two-plane cut
+                // each; material interface: among the rest), then the waiting tets take them
+                if (owners) {
+                    CutArgs co = ca;
+                    co.list = owners;
+                    co.n = G_light;
+                    co.n_dev = cp.n_owners;
+                    launch_cut_fast(co, sl, false);
+                } else {
+                    launch_cut_fast(cl, sl, false);
+                }
                 CutArgs cw = ca;
                 cw.n = G_light;
                 cw.wait = waitl;
                 cw.n_wait = (unsigned int*)(cnt + 11);
                 launch_cut_wait(cw, sl);
+            } else if (mi) {
+                launch_cut_fast(cl, sl, false);
             }
         }
         if (aux) {
             cudaEventRecord(aux->join, aux->s);
             cudaStreamWaitEvent(s, aux->join, 0);
+        }
+        if (G_light > 0 && !mi) {
+            // the light bins' cuts after the heavy bins' (both warp kernels are bound by the same
+            // per-SM shared memory): a warp per tet while the list is short, decided on the device
+            cl.route_at = kWarpCutTets;
+            CutArgs cw = cl;
+            cw.next = (unsigned int*)(cnt + 14);
+            launch_cut_warp(cw, s);
+            launch_cut_fast(cl, s, false);
         }
         unsigned long long h = 0;
         cudaMemcpyAsync(&h, cnt + 7, 8, cudaMemcpyDeviceToHost, s);

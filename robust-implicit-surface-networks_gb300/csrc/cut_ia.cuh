@@ -133,11 +133,14 @@ RIA_HD int ia_template_record_size(const uint8_t* tmpl, int k) {
     return 10 + k + 3 * nv + 8 * nf + 2 * nl + 8 * nc;
 }
 
-// Extraction counts of an implicit-arrangement record (records have at most 128 vertices).
-RIA_HD void ia_record_summary(const uint8_t* b, IASummary& sum) {
-    const int k = b[1], nv = rd16h(b + 2), nf = rd16h(b + 4);
-    const uint8_t* rep = b + 10;
-    const uint8_t* faces = rep + k + 3 * nv;
+// Extraction counts of an implicit-arrangement record (vertex ids below 256).  With `rep_of` set,
+// the iso faces are those of a tet with groups rep_of[0 .. k_of) (a relabelled template: its own
+// plane labels above 3 stay above 3, and only the tet faces' iso status follows the tet's groups).
+RIA_HD void ia_record_summary(const uint8_t* b, IASummary& sum, const uint8_t* rep_of = nullptr, int k_of = 0) {
+    const int kb = b[1], nv = rd16h(b + 2), nf = rd16h(b + 4);
+    const uint8_t* rep = rep_of ? rep_of : b + 10;
+    const int k = rep_of ? k_of : kb;
+    const uint8_t* faces = b + 10 + kb + 3 * nv;
     const uint8_t* loops = faces + 8 * nf;
     uint64_t iso[4] = {0, 0, 0, 0};
     int nisof = 0, nloop = 0, nbnd = 0, off = 0;
@@ -165,35 +168,62 @@ RIA_HD void ia_record_summary(const uint8_t* b, IASummary& sum) {
     sum.n_bnd_f = (uint16_t)nbnd;
 }
 
+// Destinations of the template relabels, written front to back: bytes, or (device, 8-byte aligned
+// destination) 8-byte words assembled in a register.
+struct ByteSink {
+    uint8_t* d;
+    RIA_HD void put(uint8_t b) { *d++ = b; }
+    RIA_HD void flush() {}
+};
+struct WordSink {
+    uint64_t* d;
+    uint64_t acc = 0;
+    int n = 0;
+    RIA_HD void put(uint8_t b) {
+        acc |= (uint64_t)b << (8 * n);
+        if (++n == 8) {
+            *d++ = acc;
+            acc = 0;
+            n = 0;
+        }
+    }
+    RIA_HD void flush() {
+        if (n) *d = acc;  // the rest of the last word is padding of the 8-byte allocation
+    }
+};
+
 // The record of a tet whose planes all coincide with one plane i (or with tet faces / zero when
 // eff == 0): the one-plane table entry `tmpl` of plane i's sign pattern with plane label 4 renamed
 // 4+i, the cell sign bit moved accordingly, and the tet's own groups.  Equal to what the generic cut
 // produces, since that cut skips every plane grouped with an earlier one.
-RIA_HD void ia_record_from_template(const uint8_t* tmpl, int k, const uint8_t* rep, int eff, int i,
-                                    uint8_t* dst) {
+template <class Sink>
+RIA_HD void ia_template_relabel1(const uint8_t* tmpl, int k, const uint8_t* rep, int eff, int i, Sink& out) {
     const int nv = rd16h(tmpl + 2), nf = rd16h(tmpl + 4), nc = rd16h(tmpl + 6), nl = rd16h(tmpl + 8);
     const uint8_t lab = (uint8_t)(4 + (eff ? i : 0));
-    for (int t = 0; t < 10; ++t) dst[t] = tmpl[t];
-    dst[1] = (uint8_t)k;
-    for (int j = 0; j < k; ++j) dst[10 + j] = rep[j];
+    out.put(tmpl[0]);
+    out.put((uint8_t)k);
+    for (int t = 2; t < 10; ++t) out.put(tmpl[t]);
+    for (int j = 0; j < k; ++j) out.put(rep[j]);
     const uint8_t* s = tmpl + 11;
-    uint8_t* d = dst + 10 + k;
-    for (int t = 0; t < 3 * nv; ++t) d[t] = s[t] == 4 ? lab : s[t];
+    for (int t = 0; t < 3 * nv; ++t) out.put(s[t] == 4 ? lab : s[t]);
     s += 3 * nv;
-    d += 3 * nv;
     for (int f = 0; f < nf; ++f)
-        for (int t = 0; t < 8; ++t) d[8 * f + t] = (t == 0 && s[8 * f] == 4) ? lab : s[8 * f + t];
+        for (int t = 0; t < 8; ++t) out.put((t == 0 && s[8 * f] == 4) ? lab : s[8 * f + t]);
     s += 8 * nf;
-    d += 8 * nf;
-    for (int t = 0; t < 2 * nl; ++t) d[t] = s[t];
+    for (int t = 0; t < 2 * nl; ++t) out.put(s[t]);
     s += 2 * nl;
-    d += 2 * nl;
     for (int c = 0; c < nc; ++c) {
         uint64_t sig = 0;
         for (int t = 0; t < 8; ++t) sig |= (uint64_t)s[8 * c + t] << (8 * t);
         sig = eff ? ((sig & 16ull) ? (1ull << lab) : 0ull) : 0ull;
-        for (int t = 0; t < 8; ++t) d[8 * c + t] = (uint8_t)((sig >> (8 * t)) & 0xFF);
+        for (int t = 0; t < 8; ++t) out.put((uint8_t)((sig >> (8 * t)) & 0xFF));
     }
+    out.flush();
+}
+
+RIA_HD void ia_record_from_template(const uint8_t* tmpl, int k, const uint8_t* rep, int eff, int i, uint8_t* dst) {
+    ByteSink o{dst};
+    ia_template_relabel1(tmpl, k, rep, eff, i, o);
 }
 
 // The record of a tet whose planes reduce to two groups with representatives r1 < r2 (local
@@ -201,31 +231,35 @@ RIA_HD void ia_record_from_template(const uint8_t* tmpl, int k, const uint8_t* r
 // 5) with 4 renamed 4+r1 and 5 renamed 4+r2, the cell sign bits moved accordingly, and the tet's own
 // groups.  The renaming keeps every order the canonical form sorts by, and the generic cut inserts
 // exactly the representatives, so the result equals the generic cut's record.
-RIA_HD void ia_record_from_template2(const uint8_t* tmpl, int k, const uint8_t* rep, int r1, int r2, uint8_t* dst) {
+template <class Sink>
+RIA_HD void ia_template_relabel2(const uint8_t* tmpl, int k, const uint8_t* rep, int r1, int r2, Sink& out) {
     const int nv = rd16h(tmpl + 2), nf = rd16h(tmpl + 4), nc = rd16h(tmpl + 6), nl = rd16h(tmpl + 8);
     const uint8_t l1 = (uint8_t)(4 + r1), l2 = (uint8_t)(4 + r2);
     auto ren = [&](uint8_t x) -> uint8_t { return x == 4 ? l1 : (x == 5 ? l2 : x); };
-    for (int t = 0; t < 10; ++t) dst[t] = tmpl[t];
-    dst[1] = (uint8_t)k;
-    for (int j = 0; j < k; ++j) dst[10 + j] = rep[j];
+    out.put(tmpl[0]);
+    out.put((uint8_t)k);
+    for (int t = 2; t < 10; ++t) out.put(tmpl[t]);
+    for (int j = 0; j < k; ++j) out.put(rep[j]);
     const uint8_t* s = tmpl + 12;
-    uint8_t* d = dst + 10 + k;
-    for (int t = 0; t < 3 * nv; ++t) d[t] = ren(s[t]);
+    for (int t = 0; t < 3 * nv; ++t) out.put(ren(s[t]));
     s += 3 * nv;
-    d += 3 * nv;
     for (int f = 0; f < nf; ++f)
-        for (int t = 0; t < 8; ++t) d[8 * f + t] = t == 0 ? ren(s[8 * f]) : s[8 * f + t];
+        for (int t = 0; t < 8; ++t) out.put(t == 0 ? ren(s[8 * f]) : s[8 * f + t]);
     s += 8 * nf;
-    d += 8 * nf;
-    for (int t = 0; t < 2 * nl; ++t) d[t] = s[t];
+    for (int t = 0; t < 2 * nl; ++t) out.put(s[t]);
     s += 2 * nl;
-    d += 2 * nl;
     for (int c = 0; c < nc; ++c) {
         uint64_t sig = 0;
         for (int t = 0; t < 8; ++t) sig |= (uint64_t)s[8 * c + t] << (8 * t);
-        const uint64_t out = ((sig >> 4) & 1 ? (1ull << l1) : 0ull) | ((sig >> 5) & 1 ? (1ull << l2) : 0ull);
-        for (int t = 0; t < 8; ++t) d[8 * c + t] = (uint8_t)((out >> (8 * t)) & 0xFF);
+        const uint64_t o = ((sig >> 4) & 1 ? (1ull << l1) : 0ull) | ((sig >> 5) & 1 ? (1ull << l2) : 0ull);
+        for (int t = 0; t < 8; ++t) out.put((uint8_t)((o >> (8 * t)) & 0xFF));
     }
+    out.flush();
+}
+
+RIA_HD void ia_record_from_template2(const uint8_t* tmpl, int k, const uint8_t* rep, int r1, int r2, uint8_t* dst) {
+    ByteSink o{dst};
+    ia_template_relabel2(tmpl, k, rep, r1, r2, o);
 }
 
 template <int MV, int MF, int MC, int ML, bool EXACT>

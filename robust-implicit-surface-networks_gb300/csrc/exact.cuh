@@ -181,7 +181,7 @@ RIA_HDI bool det_rec(const double* M, int n, int row, unsigned cols, Expn<CAP>& 
 
 // Sign of an exact n x n determinant (n <= 5).  Returns 2 on capacity overflow.
 template <int CAP = 48>
-RIA_COLD int det_sign_exact(const double* M, int n) {
+RIA_HDI int det_sign_exact(const double* M, int n) {
     Expn<CAP> e;
     bool ok = true;
     switch (n) {

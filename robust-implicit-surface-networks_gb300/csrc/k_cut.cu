@@ -82,6 +82,12 @@ __device__ __forceinline__ int gather_planes(const CutArgs& a, uint32_t ai, doub
     return k;
 }
 
+// heap space for a record of `size` bytes; allocations are multiples of 8 bytes, so every record
+// starts 8-byte aligned (the template relabels write whole words)
+__device__ __forceinline__ unsigned long long heap_alloc(const CutArgs& a, int size) {
+    return atomicAdd(a.heap_used, (unsigned long long)((size + 7) & ~7));
+}
+
 // returns the record's place in the heap; nullptr when the heap is full (the exact kernel then
 // reports the capacity; the filtered kernels hand the tet to the exact kernel, whose heap is sized
 // by the record bound)
@@ -90,7 +96,7 @@ __device__ __forceinline__ const uint8_t* finish_cut(const CutArgs& a, uint32_t 
                                                      IASum4* sum_out, bool defer_when_full = false) {
     c.canonicalize();
     const int size = c.record_size();
-    unsigned long long off = atomicAdd(a.heap_used, (unsigned long long)size);
+    unsigned long long off = heap_alloc(a, size);
     if (off + size > a.heap_cap) {
         if (!defer_when_full) raise_status(a.status, ST_CAPACITY);
         return nullptr;
@@ -258,12 +264,17 @@ __global__ void __launch_bounds__(128) k_seed_cache(CutArgs a, int64_t n_int) {
 __device__ __forceinline__ bool ia_emit_template2(const CutArgs& a, uint32_t ai, const uint8_t* tmpl, int k,
                                                   const uint8_t* rep, int r1, int r2) {
     const int size = ia_template_record_size(tmpl, k);
-    unsigned long long off = atomicAdd(a.heap_used, (unsigned long long)size);
+    unsigned long long off = heap_alloc(a, size);
     if (off + size > a.heap_cap) return false;
     uint8_t* dst = a.heap + off;
-    ia_record_from_template2(tmpl, k, rep, r1, r2, dst);
+    if (((uintptr_t)dst & 7) == 0) {
+        WordSink o{reinterpret_cast<uint64_t*>(dst)};
+        ia_template_relabel2(tmpl, k, rep, r1, r2, o);
+    } else {
+        ia_record_from_template2(tmpl, k, rep, r1, r2, dst);
+    }
     IASummary s;
-    ia_record_summary(dst, s);
+    ia_record_summary(tmpl, s, rep, k);  // from the template: the relabel keeps every count
     a.act_desc[ai] = off | a.desc_bit;
     a.act_sum[ai] = pack_sum<IASummary>(s);
     return true;
@@ -336,15 +347,20 @@ __device__ __forceinline__ bool ia_try_template(const CutArgs& a, uint32_t ai, c
     const int pattern = eff ? ia_sign_pattern(planes + 4 * first) : kTablePatterns - 1;  // all positive: uncut
     const uint8_t* tmpl = a.table + a.table_off[pattern];
     const int size = ia_template_record_size(tmpl, k);
-    unsigned long long off = atomicAdd(a.heap_used, (unsigned long long)size);
+    unsigned long long off = heap_alloc(a, size);
     if (off + size > a.heap_cap) {
         raise_status(a.status, ST_CAPACITY);
         return true;
     }
     uint8_t* dst = a.heap + off;
-    ia_record_from_template(tmpl, k, rep, eff, first, dst);
+    if (((uintptr_t)dst & 7) == 0) {
+        WordSink o{reinterpret_cast<uint64_t*>(dst)};
+        ia_template_relabel1(tmpl, k, rep, eff, first, o);
+    } else {
+        ia_record_from_template(tmpl, k, rep, eff, first, dst);
+    }
     IASummary s;
-    ia_record_summary(dst, s);
+    ia_record_summary(tmpl, s, rep, k);  // from the template: the relabel keeps every count
     a.act_desc[ai] = off | a.desc_bit;
     a.act_sum[ai] = pack_sum<IASummary>(s);
     return true;
@@ -428,59 +444,98 @@ __device__ __forceinline__ void append_warp(bool mine, uint32_t ai, uint32_t* li
     }
 }
 
+// the rows of a tet with exactly K active functions (K known at compile time: the rows stay in
+// registers)
+template <int K>
+__device__ __forceinline__ void gather_k(const CutArgs& a, uint32_t ai, double* planes) {
+    if (a.values) {
+        const uint32_t r0 = a.value_off[ai];
+#pragma unroll
+        for (int i = 0; i < 4 * K; ++i) planes[i] = a.values[4 * (size_t)r0 + i];
+        return;
+    }
+    uint64_t m = a.act_mask[ai];
+    int64_t v[4];
+    TetSrc ts{a.d_tets, a.g.res};
+    ts.get(a.act_tet[ai], v);
+#pragma unroll
+    for (int i = 0; i < K; ++i) {
+        const int j = __ffsll((long long)m) - 1;
+        m &= m - 1;
+#pragma unroll
+        for (int c = 0; c < 4; ++c) planes[4 * i + c] = a.fv[v[c] * a.F + j];
+    }
+}
+
+// one tet of the lookup pass: done (record written), waiting (w filled), owner, or none of these
+template <bool MI, int K>
+__device__ __forceinline__ void prep_tet(const CutArgs& a, uint32_t ai, const double* planes, int k, bool& done,
+                                         bool& wait, bool& owner, WaitRec& w) {
+    if (!MI) {
+        uint8_t rep[kFastMaxK];
+        bool two = false;
+        done = ia_try_template(a, ai, planes, k, &two, rep);
+        int r[2];
+        double tw[8];
+        uint32_t key = 0;
+        if (!done && two && a.cache.slots && ia_two_group_key(planes, k, rep, r, tw, key)) {
+            int j = -1;
+            const int c = cache_claim(a.cache, key, &j);
+            if (c == CLAIM_PUBLISHED) {
+                done = ia_from_entry(a, ai, j, k, rep, r[0], r[1]);
+            } else if (c == CLAIM_OWNER) {
+                owner = a.owners != nullptr;
+            } else if (c == CLAIM_WAIT) {
+                wait = true;
+                w.ai = ai;
+                w.key = key;
+                w.k = (uint8_t)k;
+                w.r0 = (uint8_t)r[0];
+                w.r1 = (uint8_t)r[1];
+                for (int t = 0; t < k; ++t) w.rep[t] = rep[t];
+            }
+        }
+    } else if (k == 3 && a.cache.slots && mi_distinct3(planes)) {
+        uint32_t key = 0;
+        if (mi_key3(planes, key)) {
+            int j = -1;
+            const int c = cache_claim(a.cache, key, &j);
+            if (c == CLAIM_PUBLISHED) {
+                a.act_desc[ai] = kTableBit | (uint64_t)(kTablePatterns + j);
+                a.act_sum[ai] = a.cache.table_sum[kTablePatterns + j];
+                done = true;
+            } else if (c == CLAIM_OWNER) {
+                owner = a.owners != nullptr;
+            } else if (c == CLAIM_WAIT) {
+                wait = true;
+                w.ai = ai;
+                w.key = key;
+                w.k = 3;
+            }
+        }
+    }
+}
+
 template <bool MI>
 __global__ void __launch_bounds__(128) k_cut_prep(CutArgs a) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.n) return;
     const uint32_t ai = a.list[i];
-    double planes[4 * kFastMaxK];
-    const int k = gather_planes(a, ai, planes, kFastMaxK);
+    const int k = a.values ? (int)(a.value_off[ai + 1] - a.value_off[ai]) : __popcll(a.act_mask[ai]);
     bool done = false, wait = false, owner = false;
     WaitRec w{};
-    if (k <= kFastMaxK) {
-        if (!MI) {
-            uint8_t rep[kFastMaxK];
-            bool two = false;
-            done = ia_try_template(a, ai, planes, k, &two, rep);
-            int r[2];
-            double tw[8];
-            uint32_t key = 0;
-            if (!done && two && a.cache.slots && ia_two_group_key(planes, k, rep, r, tw, key)) {
-                int j = -1;
-                const int c = cache_claim(a.cache, key, &j);
-                if (c == CLAIM_PUBLISHED) {
-                    done = ia_from_entry(a, ai, j, k, rep, r[0], r[1]);
-                } else if (c == CLAIM_OWNER) {
-                    owner = a.owners != nullptr;
-                } else if (c == CLAIM_WAIT) {
-                    wait = true;
-                    w.ai = ai;
-                    w.key = key;
-                    w.k = (uint8_t)k;
-                    w.r0 = (uint8_t)r[0];
-                    w.r1 = (uint8_t)r[1];
-                    for (int t = 0; t < k; ++t) w.rep[t] = rep[t];
-                }
-            }
-        } else if (k == 3 && a.cache.slots && mi_distinct3(planes)) {
-            uint32_t key = 0;
-            if (mi_key3(planes, key)) {
-                int j = -1;
-                const int c = cache_claim(a.cache, key, &j);
-                if (c == CLAIM_PUBLISHED) {
-                    a.act_desc[ai] = kTableBit | (uint64_t)(kTablePatterns + j);
-                    a.act_sum[ai] = a.cache.table_sum[kTablePatterns + j];
-                    done = true;
-                } else if (c == CLAIM_OWNER) {
-                    owner = a.owners != nullptr;
-                } else if (c == CLAIM_WAIT) {
-                    wait = true;
-                    w.ai = ai;
-                    w.key = key;
-                    w.k = 3;
-                }
-            }
-        }
+    if (k == 2) {  // most tets of the light bins: rows in registers
+        double planes[8];
+        gather_k<2>(a, ai, planes);
+        prep_tet<MI, 2>(a, ai, planes, 2, done, wait, owner, w);
+    } else if (k == 3) {
+        double planes[12];
+        gather_k<3>(a, ai, planes);
+        prep_tet<MI, 3>(a, ai, planes, 3, done, wait, owner, w);
+    } else if (k <= kFastMaxK) {
+        double planes[4 * kFastMaxK];
+        gather_planes(a, ai, planes, kFastMaxK);
+        prep_tet<MI, 0>(a, ai, planes, k, done, wait, owner, w);
     }
     if (wait) a.wait[atomicAdd(a.n_wait, 1u)] = w;
     if (a.owners) append_warp(owner, ai, a.owners, a.n_owners);
@@ -613,7 +668,7 @@ __global__ void __launch_bounds__(32 * kCutWarps) k_cut_warp(CutArgs a) {
         if (st == CUT_OK) {
             S.canonicalize(L);
             size = S.record_size();
-            if (lane == 0) off = atomicAdd(a.heap_used, (unsigned long long)size);
+            if (lane == 0) off = heap_alloc(a, size);
             off = __shfl_sync(0xFFFFFFFFu, off, 0);
             if (off + size > a.heap_cap) st = CUT_DEFER;
         }

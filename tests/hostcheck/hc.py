@@ -50,6 +50,7 @@ def ia_template(rows):
     buf = np.zeros(4096, dtype=np.uint8)
     summ = np.zeros(4, dtype=np.uint16)
     n = L.hc_ia_template(rows.shape[0], rows.ctypes.data, buf.ctypes.data, buf.size, summ.ctypes.data)
+    assert n not in (-98, -99), "device writer or template summary differs"
     if n < 0:
         return None
     return bytes(buf[:n]), summ.copy()
@@ -64,6 +65,7 @@ def ia_template2(rows):
     buf = np.zeros(4096, dtype=np.uint8)
     summ = np.zeros(4, dtype=np.uint16)
     n = L.hc_ia_template2(rows.shape[0], rows.ctypes.data, buf.ctypes.data, buf.size, summ.ctypes.data)
+    assert n not in (-98, -99), "device writer or template summary differs"
     if n < 0:
         return None
     return bytes(buf[:n]), summ.copy()

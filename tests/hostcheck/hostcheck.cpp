@@ -121,8 +121,16 @@ extern "C" int hc_ia_template(int k, const double* planes, uint8_t* buf, int cap
     int n = ia_template_record_size(tmpl, k);
     if (n > cap) return -3;
     ia_record_from_template(tmpl, k, rep, eff, first, buf);
-    IASummary s;
+    IASummary s, st;
     ia_record_summary(buf, s);
+    ia_record_summary(tmpl, st, rep, k);  // the device's summary, from the template
+    if (std::memcmp(&s, &st, sizeof(s)) != 0) return -99;
+    {  // the device's word-wise writer
+        uint64_t words[512] = {};
+        WordSink o{words};
+        ia_template_relabel1(tmpl, k, rep, eff, first, o);
+        if (n > (int)sizeof(words) || std::memcmp(words, buf, n) != 0) return -98;
+    }
     std::memcpy(summary, &s, sizeof(s));
     return n;
 }
@@ -152,8 +160,16 @@ extern "C" int hc_ia_template2(int k, const double* planes, uint8_t* buf, int ca
     const int size = ia_template_record_size(rec2, k);
     if (size > cap) return -3;
     ia_record_from_template2(rec2, k, rep, r[0], r[1], buf);
-    IASummary s;
+    IASummary s, st;
     ia_record_summary(buf, s);
+    ia_record_summary(rec2, st, rep, k);  // the device's summary, from the template
+    if (std::memcmp(&s, &st, sizeof(s)) != 0) return -99;
+    {  // the device's word-wise writer
+        uint64_t words[512] = {};
+        WordSink o{words};
+        ia_template_relabel2(rec2, k, rep, r[0], r[1], o);
+        if (size > (int)sizeof(words) || std::memcmp(words, buf, size) != 0) return -98;
+    }
     std::memcpy(summary, &s, sizeof(s));
     return size;
 }
