@@ -62,6 +62,7 @@ struct Lanes {
 
 constexpr int kWarpMaxK = 16;      // active planes of a tet the warp cut takes
 constexpr int kEdgeSlots = 128;    // shared hash of the crossing edges of one insertion
+constexpr int kCapEdges = 16;      // edges of one cap face
 
 template <int MV, int MF, int ML>
 struct IAWarpCut {
@@ -80,20 +81,32 @@ struct IAWarpCut {
     uint8_t loops[2][ML];
     uint64_t csign[MC];
     // per insertion
-    uint32_t eslot[kEdgeSlots];  // crossing edge key + 1 (u | w << 8, u < w); 0 = empty
-    uint8_t evert[kEdgeSlots];
     int8_t fside[MF];
-    uint8_t cwa[MF], cwb[MF];
+    uint8_t cwa[MF], cwb[MF];  // cap edge of the face: the two zero vertices bounding its negative run
     int8_t chas[MF];
-    uint16_t fout[MF];   // loop offset of the face's rebuilt loop(s)
-    uint16_t fnegid[MF];  // id of its negative part
     uint8_t cneg_of[MC];
     uint16_t capoff[MC];  // loop offset of the cap face of a crossed cell
-    // canonical form
-    uint8_t vnew[MV], vorder[MV], live[MV];
-    uint8_t cnew[MC], corder[MC];
-    uint16_t forder[MF], floff[MF];
-    uint32_t fkey[MF];
+    // scratch of one step at a time: new vertices and face rebuild (cd), cap faces (e), canonical
+    // form (can)
+    union {
+        struct {
+            uint32_t eslot[kEdgeSlots];  // crossing edge key + 1 (u | w << 8, u < w); 0 = empty
+            uint8_t evert[kEdgeSlots];
+            uint16_t fout[MF];    // loop offset of the face's rebuilt loop(s)
+            uint16_t fnegid[MF];  // id of its negative part
+        } cd;
+        struct {
+            uint32_t capn[MC];             // cap edges gathered per crossed cell
+            uint8_t capet[MC][kCapEdges];  // edge tail and head, oriented outward for the cell
+            uint8_t capeh[MC][kCapEdges];
+        } e;
+        struct {
+            uint8_t vnew[MV], vorder[MV], live[MV];
+            uint8_t cnew[MC], corder[MC];
+            uint16_t forder[MF], floff[MF];
+            uint32_t fkey[MF];
+        } can;
+    } sc;
     int nv_live, loop_total;
 
     RIA_HD void set_fail(int code) { fail = code; }
@@ -128,8 +141,8 @@ struct IAWarpCut {
         const uint32_t key = (uint32_t)(u < w ? (u | (w << 8)) : (w | (u << 8))) + 1u;
         uint32_t h = (key * 2654435761u) >> 25;
         for (int p = 0; p < kEdgeSlots; ++p) {
-            const uint32_t s = eslot[(h + p) & (kEdgeSlots - 1)];
-            if (s == key) return evert[(h + p) & (kEdgeSlots - 1)];
+            const uint32_t s = sc.cd.eslot[(h + p) & (kEdgeSlots - 1)];
+            if (s == key) return sc.cd.evert[(h + p) & (kEdgeSlots - 1)];
             if (s == 0) return -1;
         }
         return -1;
@@ -232,7 +245,7 @@ struct IAWarpCut {
                 sg[v] = (int8_t)(s == 2 ? 0 : s);
                 if (s == 0) mask[v] |= bit64(q);
             }
-            for (int t = lane; t < kEdgeSlots; t += L.W) eslot[t] = 0;
+            for (int t = lane; t < kEdgeSlots; t += L.W) sc.cd.eslot[t] = 0;
             L.sync();
             if (fail != CUT_OK) return fail;
             // B: crossed cells
@@ -267,7 +280,7 @@ struct IAWarpCut {
                     uint32_t h = (key * 2654435761u) >> 25;
                     bool placed = false;
                     for (int p = 0; p < kEdgeSlots && !placed; ++p) {
-                        uint32_t* slot = &eslot[(h + p) & (kEdgeSlots - 1)];
+                        uint32_t* slot = &sc.cd.eslot[(h + p) & (kEdgeSlots - 1)];
 #if defined(__CUDA_ARCH__)
                         const uint32_t old = atomicCAS(slot, 0u, key);
 #else
@@ -285,14 +298,14 @@ struct IAWarpCut {
             int added = 0;
             for (int base = 0; base < kEdgeSlots; base += L.W) {
                 const int t = base + lane;
-                const uint32_t key = eslot[t];
+                const uint32_t key = sc.cd.eslot[t];
                 const unsigned m = L.ballot(key != 0);
                 if (key) {
                     const int id = nv0 + added + L.below(m);
                     if (id >= MV) {
                         set_fail(CUT_DEFER);
                     } else {
-                        evert[t] = (uint8_t)id;
+                        sc.cd.evert[t] = (uint8_t)id;
                         const int u = (int)((key - 1u) & 0xFF), w = (int)((key - 1u) >> 8);
                         const uint64_t em = mask[u] & mask[w];
                         if (popc64u(em) < 2) {  // an edge lies on two planes; guards the labels below
@@ -362,8 +375,8 @@ struct IAWarpCut {
                 const int off = L.scan(out, tot_out);
                 const unsigned sm = L.ballot(split);
                 if (f < nf0) {
-                    fout[f] = (uint16_t)(nused + off);
-                    fnegid[f] = (uint16_t)(nf0 + nsplit + L.below(sm));
+                    sc.cd.fout[f] = (uint16_t)(nused + off);
+                    sc.cd.fnegid[f] = (uint16_t)(nf0 + nsplit + L.below(sm));
                 }
                 nused += tot_out;
                 nsplit += L.count(sm);
@@ -379,7 +392,7 @@ struct IAWarpCut {
                     set_fail(CUT_FAIL);
                     continue;
                 }
-                int w = fout[f];
+                int w = sc.cd.fout[f];
                 if (fside[f] == 2) {
                     int lp = 0, ln = 0, j0 = -1;
                     for (int j = 0; j < n; ++j) {
@@ -393,7 +406,7 @@ struct IAWarpCut {
                             break;
                         }
                     }
-                    const int g = fnegid[f];
+                    const int g = sc.cd.fnegid[f];
                     fsupp[g] = fsupp[f];
                     fpos[g] = fpos[f];
                     fneg[g] = fneg[f];
@@ -416,6 +429,26 @@ struct IAWarpCut {
             }
             const int nf1 = nf0 + nsplit;
             L.sync();
+            // E0: the cap edges of the crossed cells, gathered per cell (lanes over faces)
+            for (int c = lane; c < nc0; c += L.W) sc.e.capn[c] = 0;
+            L.sync();
+            for (int f = lane; f < nf0; f += L.W) {
+                if (!chas[f]) continue;
+                for (int side = 0; side < 2; ++side) {
+                    const int c = side ? fneg[f] : fpos[f];
+                    if (c == kNoCell || !((strad >> c) & 1)) continue;
+#if defined(__CUDA_ARCH__)
+                    const uint32_t slot = atomicAdd(&sc.e.capn[c], 1u);
+#else
+                    const uint32_t slot = sc.e.capn[c]++;
+#endif
+                    if (slot >= (uint32_t)kCapEdges) continue;
+                    // the face loop runs outward for its negative cell
+                    sc.e.capet[c][slot] = side ? cwa[f] : cwb[f];
+                    sc.e.capeh[c][slot] = side ? cwb[f] : cwa[f];
+                }
+            }
+            L.sync();
             // E1: new cells, cap-face sizes
             int ncells = 0, ncap_used = 0;
             for (int base = 0; base < nc0; base += L.W) {
@@ -427,8 +460,8 @@ struct IAWarpCut {
                     const int id = nc0 + ncells + L.below(m);
                     if (id >= MC) set_fail(CUT_DEFER);
                     cneg_of[c] = (uint8_t)(id < MC ? id : 0);
-                    for (int f = 0; f < nf0; ++f)
-                        if (chas[f] && (fpos[f] == c || fneg[f] == c)) ++nedge;
+                    nedge = (int)sc.e.capn[c];
+                    if (nedge > kCapEdges) set_fail(CUT_DEFER);
                     if (nedge < 3) set_fail(CUT_FAIL);  // an open cap cannot happen with exact signs
                 } else if (c < nc0) {
                     cneg_of[c] = kNoCell;
@@ -449,23 +482,9 @@ struct IAWarpCut {
                 const int g = nf1 + (id - nc0);
                 csign[id] = csign[c];
                 csign[c] |= bit64(q);
-                uint8_t et[64], eh[64];
-                int nedge = 0;
-                for (int f = 0; f < nf0; ++f) {
-                    if (!chas[f] || (fpos[f] != c && fneg[f] != c)) continue;
-                    if (nedge >= 64) {
-                        set_fail(CUT_DEFER);
-                        break;
-                    }
-                    if (fneg[f] == c) {  // loop is outward for c
-                        et[nedge] = cwa[f];
-                        eh[nedge] = cwb[f];
-                    } else {
-                        et[nedge] = cwb[f];
-                        eh[nedge] = cwa[f];
-                    }
-                    ++nedge;
-                }
+                const int nedge = (int)sc.e.capn[c];
+                const uint8_t* et = sc.e.capet[c];
+                const uint8_t* eh = sc.e.capeh[c];
                 int w = capoff[c];
                 fsupp[g] = (uint8_t)q;
                 fpos[g] = (uint8_t)c;
@@ -515,7 +534,7 @@ struct IAWarpCut {
     RIA_HD uint32_t face_key(int f) const {
         uint32_t s0 = 0xFF, s1 = 0xFF, s2 = 0xFF;
         for (int j = 0; j < flen[f]; ++j) {
-            const uint32_t v = vnew[loops[cur][foff[f] + j]];
+            const uint32_t v = sc.can.vnew[loops[cur][foff[f] + j]];
             if (v < s0) {
                 s2 = s1;
                 s1 = s0;
@@ -542,50 +561,50 @@ struct IAWarpCut {
     // face and cell order)
     RIA_HDI void canonicalize(const Lanes& L) {
         const int lane = L.lane;
-        for (int v = lane; v < nv; v += L.W) live[v] = 0;
+        for (int v = lane; v < nv; v += L.W) sc.can.live[v] = 0;
         L.sync();
         for (int f = lane; f < nf; f += L.W)
-            for (int j = 0; j < flen[f]; ++j) live[loops[cur][foff[f] + j]] = 1;
+            for (int j = 0; j < flen[f]; ++j) sc.can.live[loops[cur][foff[f] + j]] = 1;
         L.sync();
         int nl = 0;
-        for (int v = lane; v < nv; v += L.W) nl += live[v];
+        for (int v = lane; v < nv; v += L.W) nl += sc.can.live[v];
         nl = L.add_all(nl);
         for (int v = lane; v < nv; v += L.W) {
-            if (!live[v]) continue;
+            if (!sc.can.live[v]) continue;
             const uint32_t kv = vkey(v);
             int r = 0;
-            for (int u = 0; u < nv; ++u) r += live[u] && (vkey(u) < kv || (vkey(u) == kv && u < v));
-            vnew[v] = (uint8_t)r;
-            vorder[r] = (uint8_t)v;
+            for (int u = 0; u < nv; ++u) r += sc.can.live[u] && (vkey(u) < kv || (vkey(u) == kv && u < v));
+            sc.can.vnew[v] = (uint8_t)r;
+            sc.can.vorder[r] = (uint8_t)v;
         }
         for (int c = lane; c < nc; c += L.W) {
             int r = 0;
             for (int d = 0; d < nc; ++d) r += csign[d] < csign[c] || (csign[d] == csign[c] && d < c);
-            cnew[c] = (uint8_t)r;
-            corder[r] = (uint8_t)c;
+            sc.can.cnew[c] = (uint8_t)r;
+            sc.can.corder[r] = (uint8_t)c;
         }
         L.sync();
         int lt = 0;
         for (int f = lane; f < nf; f += L.W) {
-            fkey[f] = face_key(f);
+            sc.can.fkey[f] = face_key(f);
             lt += flen[f];
         }
         lt = L.add_all(lt);
         L.sync();
         for (int f = lane; f < nf; f += L.W) {
             int r = 0;
-            for (int g = 0; g < nf; ++g) r += fkey[g] < fkey[f] || (fkey[g] == fkey[f] && g < f);  // stable
-            forder[r] = (uint16_t)f;
+            for (int g = 0; g < nf; ++g) r += sc.can.fkey[g] < sc.can.fkey[f] || (sc.can.fkey[g] == sc.can.fkey[f] && g < f);  // stable
+            sc.can.forder[r] = (uint16_t)f;
         }
         L.sync();
         // loop offsets in sorted order
         int acc = 0;
         for (int base = 0; base < nf; base += L.W) {
             const int i = base + lane;
-            const int len = i < nf ? flen[forder[i]] : 0;
+            const int len = i < nf ? flen[sc.can.forder[i]] : 0;
             int tot = 0;
             const int off = L.scan(len, tot);
-            if (i < nf) floff[i] = (uint16_t)(acc + off);
+            if (i < nf) sc.can.floff[i] = (uint16_t)(acc + off);
             acc += tot;
         }
         if (lane == 0) {
@@ -615,17 +634,17 @@ struct IAWarpCut {
         for (int i = lane; i < k; i += L.W) dst[10 + i] = rep[i];
         const int ov = 10 + k, ofc = ov + 3 * nv_live, olp = ofc + 8 * nf, oc = olp + 2 * loop_total;
         for (int i = lane; i < nv_live; i += L.W)
-            for (int t = 0; t < 3; ++t) dst[ov + 3 * i + t] = lab[vorder[i]][t];
-        for (int v = lane; v < nv; v += L.W) live[v] = 0;  // reused: vertex on an iso face
+            for (int t = 0; t < 3; ++t) dst[ov + 3 * i + t] = lab[sc.can.vorder[i]][t];
+        for (int v = lane; v < nv; v += L.W) sc.can.live[v] = 0;  // reused: vertex on an iso face
         L.sync();
         int niso = 0, nloop = 0, nbnd = 0;
         for (int i = lane; i < nf; i += L.W) {
-            const int f = forder[i];
+            const int f = sc.can.forder[i];
             const int o = ofc + 8 * i;
             dst[o] = fsupp[f];
             dst[o + 1] = (uint8_t)(fneg[f] == kNoCell ? 1 : 0);
-            w16(o + 2, cnew[fpos[f]]);
-            w16(o + 4, fneg[f] == kNoCell ? 0xFFFF : cnew[fneg[f]]);
+            w16(o + 2, sc.can.cnew[fpos[f]]);
+            w16(o + 4, fneg[f] == kNoCell ? 0xFFFF : sc.can.cnew[fneg[f]]);
             w16(o + 6, flen[f]);
             const int Lf = flen[f];
             const bool iso = plane_is_iso(fsupp[f]);
@@ -636,15 +655,15 @@ struct IAWarpCut {
             }
             int jm = 0;
             for (int j = 1; j < Lf; ++j)
-                if (vnew[loops[cur][foff[f] + j]] < vnew[loops[cur][foff[f] + jm]]) jm = j;
+                if (sc.can.vnew[loops[cur][foff[f] + j]] < sc.can.vnew[loops[cur][foff[f] + jm]]) jm = j;
             for (int t = 0; t < Lf; ++t) {
                 const int v = loops[cur][foff[f] + (jm + t) % Lf];
-                w16(olp + 2 * (floff[i] + t), vnew[v]);
-                if (iso) live[v] = 1;
+                w16(olp + 2 * (sc.can.floff[i] + t), sc.can.vnew[v]);
+                if (iso) sc.can.live[v] = 1;
             }
         }
         for (int i = lane; i < nc; i += L.W) {
-            const uint64_t s = csign[corder[i]];
+            const uint64_t s = csign[sc.can.corder[i]];
             for (int b = 0; b < 8; ++b) dst[oc + 8 * i + b] = (uint8_t)((s >> (8 * b)) & 0xFF);
         }
         niso = L.add_all(niso);
@@ -652,7 +671,7 @@ struct IAWarpCut {
         nbnd = L.add_all(nbnd);
         L.sync();
         int nisov = 0;
-        for (int v = lane; v < nv; v += L.W) nisov += live[v];
+        for (int v = lane; v < nv; v += L.W) nisov += sc.can.live[v];
         nisov = L.add_all(nisov);
         sum.n_iso_v = (uint16_t)nisov;
         sum.n_iso_f = (uint16_t)niso;
