@@ -1003,22 +1003,40 @@ ria_status ria_sample_functions(const ria_function* funcs, uint32_t n_func, cons
     int dev = 0;
     ria_status st = current_device(&dev);
     if (st != RIA_OK) return st;
-    cudaStream_t s;
-    RIA_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    // Chunks of points on two streams: a chunk's upload, sampling and download overlap those of its
+    // neighbours (the copy engines of both directions and the SMs work at the same time).
+    cudaStream_t s[2];
+    RIA_CUDA(cudaStreamCreateWithFlags(&s[0], cudaStreamNonBlocking));
+    RIA_CUDA(cudaStreamCreateWithFlags(&s[1], cudaStreamNonBlocking));
+    cudaEvent_t ready;
+    RIA_CUDA(cudaEventCreateWithFlags(&ready, cudaEventDisableTiming));
     ria_function* d_funcs = nullptr;
     double *d_pts = nullptr, *d_fv = nullptr;
-    RIA_CUDA(cudaMallocAsync(&d_funcs, sizeof(ria_function) * (n_func ? n_func : 1), s));
-    RIA_CUDA(cudaMallocAsync(&d_pts, sizeof(double) * 3 * (n_pts ? n_pts : 1), s));
-    RIA_CUDA(cudaMallocAsync(&d_fv, sizeof(double) * (n_pts * n_func ? n_pts * n_func : 1), s));
-    RIA_CUDA(cudaMemcpyAsync(d_funcs, funcs, sizeof(ria_function) * n_func, cudaMemcpyHostToDevice, s));
-    RIA_CUDA(cudaMemcpyAsync(d_pts, pts, sizeof(double) * 3 * n_pts, cudaMemcpyHostToDevice, s));
-    launch_sample_points(d_funcs, (int)n_func, d_pts, (int64_t)n_pts, d_fv, nullptr, nullptr, s);
-    RIA_CUDA(cudaMemcpyAsync(func_vals, d_fv, sizeof(double) * n_pts * n_func, cudaMemcpyDeviceToHost, s));
-    cudaFreeAsync(d_funcs, s);
-    cudaFreeAsync(d_pts, s);
-    cudaFreeAsync(d_fv, s);
-    cudaError_t e = cudaStreamSynchronize(s);
-    cudaStreamDestroy(s);
+    RIA_CUDA(cudaMallocAsync(&d_funcs, sizeof(ria_function) * (n_func ? n_func : 1), s[0]));
+    RIA_CUDA(cudaMallocAsync(&d_pts, sizeof(double) * 3 * (n_pts ? n_pts : 1), s[0]));
+    RIA_CUDA(cudaMallocAsync(&d_fv, sizeof(double) * (n_pts * n_func ? n_pts * n_func : 1), s[0]));
+    RIA_CUDA(cudaMemcpyAsync(d_funcs, funcs, sizeof(ria_function) * n_func, cudaMemcpyHostToDevice, s[0]));
+    RIA_CUDA(cudaEventRecord(ready, s[0]));
+    RIA_CUDA(cudaStreamWaitEvent(s[1], ready, 0));
+    const uint64_t chunk = std::max<uint64_t>(1 << 16, (n_pts + 7) / 8);
+    int c = 0;
+    for (uint64_t p0 = 0; p0 < n_pts; p0 += chunk, ++c) {
+        const uint64_t n = std::min(chunk, n_pts - p0);
+        cudaStream_t sc = s[c & 1];
+        RIA_CUDA(cudaMemcpyAsync(d_pts + 3 * p0, pts + 3 * p0, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, sc));
+        launch_sample_points(d_funcs, (int)n_func, d_pts + 3 * p0, (int64_t)n, d_fv + p0 * n_func, nullptr, nullptr, sc);
+        RIA_CUDA(cudaMemcpyAsync(func_vals + p0 * n_func, d_fv + p0 * n_func, sizeof(double) * n * n_func,
+                                 cudaMemcpyDeviceToHost, sc));
+    }
+    RIA_CUDA(cudaEventRecord(ready, s[1]));
+    RIA_CUDA(cudaStreamWaitEvent(s[0], ready, 0));
+    cudaFreeAsync(d_funcs, s[0]);
+    cudaFreeAsync(d_pts, s[0]);
+    cudaFreeAsync(d_fv, s[0]);
+    cudaError_t e = cudaStreamSynchronize(s[0]);
+    cudaEventDestroy(ready);
+    cudaStreamDestroy(s[0]);
+    cudaStreamDestroy(s[1]);
     if (e != cudaSuccess) return fail(RIA_ECUDA, cudaGetErrorString(e));
     return RIA_OK;
 }
