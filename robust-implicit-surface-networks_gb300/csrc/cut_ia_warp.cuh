@@ -111,8 +111,7 @@ struct IAWarpCut {
 
     RIA_HD void set_fail(int code) { fail = code; }
 
-    // out of line: one copy of the cofactor code (the warp cut is bound by instruction fetch)
-    RIA_COLD bool build_cache(int v) {
+    RIA_HD bool build_cache(int v) {
         bool bound[4] = {false, false, false, false};
         const double* rows[3];
         int m = 0;
