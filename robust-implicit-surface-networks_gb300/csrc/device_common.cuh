@@ -213,6 +213,26 @@ __device__ __forceinline__ bool cas128(ulonglong2* addr, uint64_t new_lo, uint64
     return olo == cmp && ohi == cmp;
 }
 
+// Open addressing with 64-bit keys (all bits set = empty), for keys that pack into one word.
+struct HashTab64 {
+    unsigned long long* keys;
+    uint32_t* owner;
+    uint64_t cap_mask;
+};
+
+__device__ __forceinline__ int64_t ht64_insert_min(const HashTab64& h, uint64_t key, uint32_t pos) {
+    uint64_t slot = mix64(key) & h.cap_mask;
+    for (uint64_t probe = 0; probe <= h.cap_mask; ++probe) {
+        const unsigned long long old = atomicCAS(&h.keys[slot], ~0ull, (unsigned long long)key);
+        if (old == ~0ull || old == key) {
+            atomicMin(&h.owner[slot], pos);
+            return (int64_t)slot;
+        }
+        slot = (slot + 1) & h.cap_mask;
+    }
+    return -1;
+}
+
 // Insert (k0, k1) and lower its owner to `pos`; returns the slot or -1 when the table is full.
 __device__ __forceinline__ int64_t ht_insert_min(const HashTab& h, uint64_t k0, uint64_t k1, uint32_t pos) {
     uint64_t slot = mix64(k0 * 0x9E3779B97F4A7C15ull ^ mix64(k1)) & h.cap_mask;

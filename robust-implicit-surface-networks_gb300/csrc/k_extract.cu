@@ -25,6 +25,8 @@ struct ExtractCtx {
     const U4* base;        // per active tet: occurrence bases (vert, face, loop, boundary face)
     uint32_t* corner_owner;
     HashTab he, hf, hb;
+    HashTab64 he64;        // edge keys packed in one word (vertex ids below 2^28, functions below 256)
+    bool edge64;
     uint64_t* vocc;        // per vertex occurrence: type << 62 | payload
     uint64_t* vsrc;        // per vertex occurrence: active index << 8 | local vertex
     uint32_t* vowner;      // per vertex occurrence: owner position
@@ -145,7 +147,11 @@ __global__ void __launch_bounds__(kBs) k_ia_vert_keys(ExtractCtx C) {
             atomicMin(&C.corner_owner[k.sv[0]], pos);
             occ = (OCC_CORNER << 62) | (uint64_t)k.sv[0];
         } else if (k.type == 2) {
-            int64_t s = ht_insert_min(C.he, ((uint64_t)k.sv[0] << 32) | (uint64_t)k.sv[1], (uint64_t)k.fn[0] + 1, pos);
+            int64_t s = C.edge64
+                            ? ht64_insert_min(C.he64, ((uint64_t)k.sv[0] << 36) | ((uint64_t)k.sv[1] << 8) |
+                                                          (uint64_t)k.fn[0], pos)
+                            : ht_insert_min(C.he, ((uint64_t)k.sv[0] << 32) | (uint64_t)k.sv[1], (uint64_t)k.fn[0] + 1,
+                                            pos);
             if (s < 0) raise_status(C.a.status, ST_HASH_FULL);
             occ = (OCC_EDGE << 62) | (uint64_t)(s < 0 ? 0 : s);
         } else if (k.type == 3) {
@@ -171,21 +177,29 @@ __global__ void k_vert_owner(ExtractCtx C, int64_t n) {
     uint32_t own;
     if (ty == OCC_SELF) own = (uint32_t)p;
     else if (ty == OCC_CORNER) own = C.corner_owner[pay];
-    else if (ty == OCC_EDGE) own = C.he.owner[pay];
+    else if (ty == OCC_EDGE) own = C.edge64 ? C.he64.owner[pay] : C.he.owner[pay];
     else own = C.hf.owner[pay];
     C.vowner[p] = own;
     C.vflag[p] = own == (uint32_t)p ? 1u : 0u;
 }
 
-// D4: global vertex ids, vertex records and coordinates of the new vertices
-__global__ void k_vert_emit(ExtractCtx C, int64_t n, int64_t* __restrict__ verts, double* __restrict__ xyz) {
+// D4a: global vertex id of every occurrence; the occurrence of each new vertex, by id
+__global__ void k_vert_gid(ExtractCtx C, int64_t n, uint32_t* __restrict__ gid_src) {
     const int64_t p = (int64_t)blockIdx.x * kBs + threadIdx.x;
     if (p >= n) return;
     const uint32_t own = C.vowner[p];
-    C.occ_gid[p] = C.vgid_new[own];
-    if (own != (uint32_t)p) return;
-    const uint32_t gid = C.vgid_new[p];
-    const uint64_t src = C.vsrc[p];
+    const uint32_t gid = C.vgid_new[own];
+    C.occ_gid[p] = gid;
+    if (own == (uint32_t)p) gid_src[gid] = (uint32_t)p;
+}
+
+// D4b: vertex records and coordinates, one thread per new vertex (no idle lanes in the long path)
+__global__ void k_vert_emit(ExtractCtx C, int64_t n_new, const uint32_t* __restrict__ gid_src,
+                            int64_t* __restrict__ verts, double* __restrict__ xyz) {
+    const int64_t g = (int64_t)blockIdx.x * kBs + threadIdx.x;
+    if (g >= n_new) return;
+    const uint32_t gid = (uint32_t)g;
+    const uint64_t src = C.vsrc[gid_src[g]];
     const int64_t a = (int64_t)(src >> 8);
     const int j = (int)(src & 0xFF);
     IAView r;
@@ -409,7 +423,14 @@ cudaError_t run_extract(const ExtractArgs& a, const IASum4* act_sum, ExtractOut&
     C.corner_owner = pool.get<uint32_t>(a.V);
     const uint64_t cap_e = pow2_at_least((uint64_t)NV), cap_f = pow2_at_least((uint64_t)NV / 2 + 1);
     const uint64_t cap_b = pow2_at_least(2 * (uint64_t)NB + 1);
-    C.he = HashTab{pool.get<ulonglong2>((int64_t)cap_e), pool.get<uint32_t>((int64_t)cap_e), cap_e - 1};
+    C.edge64 = a.V < (1ll << 28) && a.F <= 256;
+    if (C.edge64) {
+        C.he = HashTab{nullptr, nullptr, 0};
+        C.he64 = HashTab64{pool.get<unsigned long long>((int64_t)cap_e), pool.get<uint32_t>((int64_t)cap_e), cap_e - 1};
+    } else {
+        C.he = HashTab{pool.get<ulonglong2>((int64_t)cap_e), pool.get<uint32_t>((int64_t)cap_e), cap_e - 1};
+        C.he64 = HashTab64{nullptr, nullptr, 0};
+    }
     C.hf = HashTab{pool.get<ulonglong2>((int64_t)cap_f), pool.get<uint32_t>((int64_t)cap_f), cap_f - 1};
     C.hb = HashTab{pool.get<ulonglong2>((int64_t)cap_b), pool.get<uint32_t>((int64_t)cap_b), cap_b - 1};
     C.vocc = pool.get<uint64_t>(NV);
@@ -431,8 +452,13 @@ cudaError_t run_extract(const ExtractArgs& a, const IASum4* act_sum, ExtractOut&
     if (pool.err) return pool.err;
     cudaMemsetAsync(C.corner_owner, 0xFF, sizeof(uint32_t) * (size_t)(a.V > 0 ? a.V : 1), s);
     for (HashTab* h : {&C.he, &C.hf, &C.hb}) {
+        if (!h->keys) continue;
         cudaMemsetAsync(h->keys, 0xFF, sizeof(ulonglong2) * (h->cap_mask + 1), s);
         cudaMemsetAsync(h->owner, 0xFF, sizeof(uint32_t) * (h->cap_mask + 1), s);
+    }
+    if (C.edge64) {
+        cudaMemsetAsync(C.he64.keys, 0xFF, sizeof(unsigned long long) * (C.he64.cap_mask + 1), s);
+        cudaMemsetAsync(C.he64.owner, 0xFF, sizeof(uint32_t) * (C.he64.cap_mask + 1), s);
     }
     cudaMemsetAsync(C.fdup, 0, sizeof(uint32_t) * (size_t)(NF > 0 ? NF : 1), s);
     // vertices
@@ -456,8 +482,14 @@ cudaError_t run_extract(const ExtractArgs& a, const IASum4* act_sum, ExtractOut&
     if ((e = cudaMallocAsync((void**)&out.verts, sizeof(int64_t) * 11 * (size_t)(n_verts > 0 ? n_verts : 1), s)) !=
         cudaSuccess)
         return e;
+    uint32_t* gid_src = pool.get<uint32_t>(n_verts);
+    if (pool.err) return pool.err;
     if (NV > 0) {
-        k_vert_emit<<<nblk(NV), kBs, 0, s>>>(C, NV, out.verts, out.xyz);
+        k_vert_gid<<<nblk(NV), kBs, 0, s>>>(C, NV, gid_src);
+        note_launch();
+    }
+    if (n_verts > 0) {
+        k_vert_emit<<<nblk(n_verts), kBs, 0, s>>>(C, n_verts, gid_src, out.verts, out.xyz);
         note_launch();
     }
     // faces
