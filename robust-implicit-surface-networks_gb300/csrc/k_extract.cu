@@ -43,6 +43,11 @@ struct ExtractCtx {
     uint32_t* fntet;
     uint32_t* foff;
     uint32_t* ftoff;
+    // per face occurrence, from the keys pass: loop start in fgids, (active tet, record face), function
+    uint32_t* floop;
+    uint64_t* fsrc;
+    int32_t* ffunc;
+    uint32_t* fgids;  // global vertex ids of every iso face loop, in occurrence order
 };
 
 // iso flags of the local vertices of an IA record (vertex ids below 256)
@@ -276,7 +281,7 @@ __global__ void k_vert_emit(ExtractCtx C, int64_t n_new, const uint32_t* __restr
     for (int c = 0; c < 3; ++c) xyz[3 * (int64_t)gid + c] = out[c];
 }
 
-// D5: keys of the iso faces on the tet boundary
+// D5: keys of the iso faces on the tet boundary; every iso face's global vertex ids staged for D7
 __global__ void __launch_bounds__(kBs) k_ia_face_keys(ExtractCtx C) {
     const int64_t a = (int64_t)blockIdx.x * kBs + threadIdx.x;
     if (a >= C.a.A) return;
@@ -286,35 +291,42 @@ __global__ void __launch_bounds__(kBs) k_ia_face_keys(ExtractCtx C) {
     iso_vertex_flags(r, iso);
     const uint32_t vb = C.base[a].a;
     uint32_t fpos = C.base[a].b;
+    uint32_t lpos = C.base[a].c;
+    const uint64_t mask = C.a.act_mask[a];
     int off = 0;
     for (int f = 0; f < r.nf; ++f) {
         const int L = r.len(f);
         if (r.plane_is_iso(r.supp(f))) {
+            uint32_t* g = C.fgids + lpos;
+            for (int t = 0; t < L; ++t) g[t] = C.occ_gid[vb + iso_rank(iso, r.loopv(off + t))];
             uint64_t occ = OCC_SELF << 62;
             if (r.bnd(f)) {
                 // (smallest, second smallest, largest) global vertex id (src/extract_mesh.h:68-92)
                 int64_t mn = -1, mx = -1;
                 int mpos = 0;
                 for (int t = 0; t < L; ++t) {
-                    int64_t g = C.occ_gid[vb + iso_rank(iso, r.loopv(off + t))];
-                    if (t == 0 || g < mn) {
-                        mn = g;
+                    const int64_t v = g[t];
+                    if (t == 0 || v < mn) {
+                        mn = v;
                         mpos = t;
                     }
-                    if (t == 0 || g > mx) mx = g;
+                    if (t == 0 || v > mx) mx = v;
                 }
                 int64_t second = mx + 1;
-                for (int t = 0; t < L; ++t) {
-                    int64_t g = C.occ_gid[vb + iso_rank(iso, r.loopv(off + t))];
-                    if (t != mpos && g < second) second = g;
-                }
-                int64_t s = ht_insert_min(C.hb, ((uint64_t)mn << 32) | (uint64_t)second, (uint64_t)mx + 1, fpos);
-                if (s < 0) raise_status(C.a.status, ST_HASH_FULL);
-                occ = (OCC_EDGE << 62) | (uint64_t)(s < 0 ? 0 : s);
+                for (int t = 0; t < L; ++t)
+                    if (t != mpos && (int64_t)g[t] < second) second = g[t];
+                int64_t sl = ht_insert_min(C.hb, ((uint64_t)mn << 32) | (uint64_t)second, (uint64_t)mx + 1, fpos);
+                if (sl < 0) raise_status(C.a.status, ST_HASH_FULL);
+                occ = (OCC_EDGE << 62) | (uint64_t)(sl < 0 ? 0 : sl);
             }
+            const int lf = r.plane_func_local(r.supp(f));
             C.focc[fpos] = occ;
             C.flen[fpos] = (uint32_t)L;
+            C.floop[fpos] = lpos;
+            C.fsrc[fpos] = ((uint64_t)a << 16) | (uint64_t)f;
+            C.ffunc[fpos] = lf < 0 ? -1 : local_func(mask, lf);
             ++fpos;
+            lpos += (uint32_t)L;
         }
         off += L;
     }
@@ -340,46 +352,34 @@ __global__ void k_face_sizes(ExtractCtx C, int64_t n) {
     if (isnew && C.fdup[p] > 1) raise_status(C.a.status, ST_NONMANIFOLD);
 }
 
-// D7: face vertex lists, function ids and tet-face lists
-__global__ void __launch_bounds__(kBs) k_ia_face_emit(ExtractCtx C, int64_t* __restrict__ face_offsets,
+// D7: face vertex lists, function ids and tet-face lists, one thread per face occurrence
+__global__ void __launch_bounds__(kBs) k_ia_face_emit(ExtractCtx C, int64_t n, int64_t* __restrict__ face_offsets,
                                                       int64_t* __restrict__ face_verts,
                                                       int64_t* __restrict__ face_tet_offsets,
                                                       int64_t* __restrict__ face_tets, int64_t* __restrict__ face_func) {
-    const int64_t a = (int64_t)blockIdx.x * kBs + threadIdx.x;
-    if (a >= C.a.A) return;
-    IAView r;
-    r.init(C.rs.get(C.a.act_desc[a]));
-    uint64_t iso[4];
-    iso_vertex_flags(r, iso);
-    const uint32_t vb = C.base[a].a;
-    uint32_t fpos = C.base[a].b;
-    const uint64_t mask = C.a.act_mask[a];
-    const int64_t tet = C.a.act_tet[a];
-    int off = 0;
-    for (int f = 0; f < r.nf; ++f) {
-        const int L = r.len(f);
-        if (r.plane_is_iso(r.supp(f))) {
-            const uint32_t own = C.fowner[fpos];
-            if (own == fpos) {
-                const uint32_t gid = C.fgid[fpos];
-                const uint32_t vo = C.foff[fpos];
-                face_offsets[gid] = vo;
-                for (int t = 0; t < L; ++t) face_verts[vo + t] = C.occ_gid[vb + iso_rank(iso, r.loopv(off + t))];
-                const uint32_t to = C.ftoff[fpos];
-                face_tet_offsets[gid] = to;
-                face_tets[2 * (int64_t)to] = tet;
-                face_tets[2 * (int64_t)to + 1] = f;
-                int lf = r.plane_func_local(r.supp(f));
-                face_func[2 * (int64_t)gid] = lf < 0 ? -1 : local_func(mask, lf);
-                face_func[2 * (int64_t)gid + 1] = -1;
-            } else {
-                const uint32_t to = C.ftoff[own] + 1;
-                face_tets[2 * (int64_t)to] = tet;
-                face_tets[2 * (int64_t)to + 1] = f;
-            }
-            ++fpos;
-        }
-        off += L;
+    const int64_t p = (int64_t)blockIdx.x * kBs + threadIdx.x;
+    if (p >= n) return;
+    const uint32_t own = C.fowner[p];
+    const uint64_t src = C.fsrc[p];
+    const int64_t tet = C.a.act_tet[src >> 16];
+    const int64_t f = (int64_t)(src & 0xFFFF);
+    if (own == (uint32_t)p) {
+        const uint32_t gid = C.fgid[p];
+        const uint32_t vo = C.foff[p];
+        const uint32_t L = C.flen[p];
+        const uint32_t* g = C.fgids + C.floop[p];
+        face_offsets[gid] = vo;
+        for (uint32_t t = 0; t < L; ++t) face_verts[vo + t] = g[t];
+        const uint32_t to = C.ftoff[p];
+        face_tet_offsets[gid] = to;
+        face_tets[2 * (int64_t)to] = tet;
+        face_tets[2 * (int64_t)to + 1] = f;
+        face_func[2 * (int64_t)gid] = C.ffunc[p];
+        face_func[2 * (int64_t)gid + 1] = -1;
+    } else {
+        const uint32_t to = C.ftoff[own] + 1;
+        face_tets[2 * (int64_t)to] = tet;
+        face_tets[2 * (int64_t)to + 1] = f;
     }
 }
 
@@ -449,6 +449,10 @@ cudaError_t run_extract(const ExtractArgs& a, const IASum4* act_sum, ExtractOut&
     C.fntet = pool.get<uint32_t>(NF);
     C.foff = pool.get<uint32_t>(NF);
     C.ftoff = pool.get<uint32_t>(NF);
+    C.floop = pool.get<uint32_t>(NF);
+    C.fsrc = pool.get<uint64_t>(NF);
+    C.ffunc = pool.get<int32_t>(NF);
+    C.fgids = pool.get<uint32_t>((int64_t)tot.c);
     if (pool.err) return pool.err;
     cudaMemsetAsync(C.corner_owner, 0xFF, sizeof(uint32_t) * (size_t)(a.V > 0 ? a.V : 1), s);
     for (HashTab* h : {&C.he, &C.hf, &C.hb}) {
@@ -525,12 +529,11 @@ cudaError_t run_extract(const ExtractArgs& a, const IASum4* act_sum, ExtractOut&
         (e = cudaMallocAsync((void**)&out.face_func, sizeof(int64_t) * 2 * (size_t)(n_faces > 0 ? n_faces : 1), s)) !=
             cudaSuccess)
         return e;
-    if (A > 0)
-        {
-            k_ia_face_emit<<<nblk(A), kBs, 0, s>>>(C, out.face_offsets, out.face_verts, out.face_tet_offsets, out.face_tets,
-                                             out.face_func);
-            note_launch();
-        }
+    if (NF > 0) {
+        k_ia_face_emit<<<nblk(NF), kBs, 0, s>>>(C, NF, out.face_offsets, out.face_verts, out.face_tet_offsets,
+                                                out.face_tets, out.face_func);
+        note_launch();
+    }
     {
         k_set_last<<<1, 1, 0, s>>>(out.face_offsets, n_faces, C.fnewlen, C.foff, NF);
         note_launch();
