@@ -445,12 +445,25 @@ struct MICut {
 
     RIA_HDI void pair_faces() {
         uint8_t keep[OF];
+        // vertex-set signature of each face (length, smallest id, id sum): equal polygons have equal
+        // signatures, so only faces with the signature of face i are compared vertex by vertex
+        uint32_t sig[OF];
+        for (int i = 0; i < onf; ++i) {
+            uint32_t mn = 0xFF, sum = 0;
+            for (int t = 0; t < olen[i]; ++t) {
+                const uint32_t v = oloops[ooff[i] + t];
+                mn = v < mn ? v : mn;
+                sum += v;
+            }
+            sig[i] = ((uint32_t)olen[i] << 24) | (mn << 16) | (sum & 0xFFFFu);
+        }
         for (int i = 0; i < onf; ++i) {
             keep[i] = 1;
             if (opos[i] < 4) continue;
             int partner = -1;
             for (int j = 0; j < onf && partner < 0; ++j)
-                if (j != i && opos[j] >= 4 && oneg[j] != oneg[i] && same_polygon(i, j)) partner = j;
+                if (j != i && sig[j] == sig[i] && opos[j] >= 4 && oneg[j] != oneg[i] && same_polygon(i, j))
+                    partner = j;
             if (partner >= 0) {
                 if (oneg[i] > oneg[partner]) {
                     keep[i] = 0;

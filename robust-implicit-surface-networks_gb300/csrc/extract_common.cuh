@@ -96,6 +96,35 @@ inline cudaError_t scan_total(const uint32_t* in, const uint32_t* out, int64_t n
     return e;
 }
 
+// Totals of several exclusive scans (out[n-1] + in[n-1] each), read with one synchronization.
+struct ScanTotals {
+    const uint32_t* in[8];
+    const uint32_t* out[8];
+    int64_t n[8];
+    int count = 0;
+    void add(const uint32_t* i, const uint32_t* o, int64_t len) {
+        in[count] = i;
+        out[count] = o;
+        n[count] = len;
+        ++count;
+    }
+};
+
+static __global__ void k_scan_totals(ScanTotals r, int64_t* __restrict__ dst) {
+    const int i = threadIdx.x;
+    if (i < r.count) dst[i] = r.n[i] ? (int64_t)r.in[i][r.n[i] - 1] + (int64_t)r.out[i][r.n[i] - 1] : 0;
+}
+
+inline cudaError_t read_totals(const ScanTotals& r, int64_t* host, Pool& pool, cudaStream_t s) {
+    int64_t* d = pool.get<int64_t>(8);
+    if (pool.err) return pool.err;
+    k_scan_totals<<<1, 32, 0, s>>>(r, d);
+    note_launch();
+    cudaError_t e = cudaMemcpyAsync(host, d, sizeof(int64_t) * (size_t)r.count, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    return e;
+}
+
 // exclusive scan of per-item U4 counts; returns the totals (synchronizes the stream)
 inline cudaError_t exscan_u4(const U4* in, U4* out, int64_t n, U4* total, Pool& pool, cudaStream_t s) {
     *total = U4{0, 0, 0, 0};

@@ -476,24 +476,12 @@ cudaError_t run_extract(const ExtractArgs& a, const IASum4* act_sum, ExtractOut&
     }
     cudaError_t e = exscan_u32(C.vflag, C.vgid_new, NV, s);
     if (e != cudaSuccess) return e;
-    int64_t n_verts = 0;
-    e = scan_total(C.vflag, C.vgid_new, NV, &n_verts, s);
-    if (e != cudaSuccess) return e;
-    out.n_verts = n_verts;
-    if ((e = cudaMallocAsync((void**)&out.xyz, sizeof(double) * 3 * (size_t)(n_verts > 0 ? n_verts : 1), s)) !=
-        cudaSuccess)
-        return e;
-    if ((e = cudaMallocAsync((void**)&out.verts, sizeof(int64_t) * 11 * (size_t)(n_verts > 0 ? n_verts : 1), s)) !=
-        cudaSuccess)
-        return e;
-    uint32_t* gid_src = pool.get<uint32_t>(n_verts);
+    // the occurrence of each new vertex, by id (sized by the occurrences: the vertex count is read
+    // together with the face counts, in one synchronization)
+    uint32_t* gid_src = pool.get<uint32_t>(NV);
     if (pool.err) return pool.err;
     if (NV > 0) {
         k_vert_gid<<<nblk(NV), kBs, 0, s>>>(C, NV, gid_src);
-        note_launch();
-    }
-    if (n_verts > 0) {
-        k_vert_emit<<<nblk(n_verts), kBs, 0, s>>>(C, n_verts, gid_src, out.verts, out.xyz);
         note_launch();
     }
     // faces
@@ -512,10 +500,25 @@ cudaError_t run_extract(const ExtractArgs& a, const IASum4* act_sum, ExtractOut&
     if ((e = exscan_u32(C.fflag, C.fgid, NF, s)) != cudaSuccess) return e;
     if ((e = exscan_u32(C.fnewlen, C.foff, NF, s)) != cudaSuccess) return e;
     if ((e = exscan_u32(C.fntet, C.ftoff, NF, s)) != cudaSuccess) return e;
-    int64_t n_faces = 0, n_fv = 0, n_ft = 0;
-    if ((e = scan_total(C.fflag, C.fgid, NF, &n_faces, s)) != cudaSuccess) return e;
-    if ((e = scan_total(C.fnewlen, C.foff, NF, &n_fv, s)) != cudaSuccess) return e;
-    if ((e = scan_total(C.fntet, C.ftoff, NF, &n_ft, s)) != cudaSuccess) return e;
+    ScanTotals st;
+    st.add(C.vflag, C.vgid_new, NV);
+    st.add(C.fflag, C.fgid, NF);
+    st.add(C.fnewlen, C.foff, NF);
+    st.add(C.fntet, C.ftoff, NF);
+    int64_t tots[4] = {0, 0, 0, 0};
+    if ((e = read_totals(st, tots, pool, s)) != cudaSuccess) return e;
+    const int64_t n_verts = tots[0], n_faces = tots[1], n_fv = tots[2], n_ft = tots[3];
+    out.n_verts = n_verts;
+    if ((e = cudaMallocAsync((void**)&out.xyz, sizeof(double) * 3 * (size_t)(n_verts > 0 ? n_verts : 1), s)) !=
+        cudaSuccess)
+        return e;
+    if ((e = cudaMallocAsync((void**)&out.verts, sizeof(int64_t) * 11 * (size_t)(n_verts > 0 ? n_verts : 1), s)) !=
+        cudaSuccess)
+        return e;
+    if (n_verts > 0) {
+        k_vert_emit<<<nblk(n_verts), kBs, 0, s>>>(C, n_verts, gid_src, out.verts, out.xyz);
+        note_launch();
+    }
     out.n_faces = n_faces;
     out.n_face_verts = n_fv;
     out.n_face_tets = n_ft;
