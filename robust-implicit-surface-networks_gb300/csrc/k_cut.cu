@@ -568,51 +568,70 @@ __global__ void __launch_bounds__(128) k_cut_wait(CutArgs a) {
 // cells, so the threads clip in parallel and export their cells to shared memory; thread 0 then
 // merges them in material order, canonicalises and emits, exactly as the serial cut does.
 constexpr int kSplitMaxK = 32;
-using SplitCut = MICutMid;
-using SplitCell = MICell<96, 96, 640>;
+// Each lane's clipping state is small and lives in shared memory: kept per thread in local
+// memory, the state of a few active lanes is spread over a warp-interleaved footprint that L1
+// does not hold.  A cell beyond these capacities sends the tet to the exact kernel.
+using SplitClip = MICut<32, 32, 192, 1, 1, 1, false>;
+using SplitCell = MICell<32, 32, 192>;
+struct SplitSmem {
+    double planes[4 * kSplitMaxK];
+    SplitClip clip[kSplitMaxK];
+    SplitCell cells[kSplitMaxK];
+    MIMerge<SplitCell> mg;
+    int8_t cst[kSplitMaxK];  // 0 cell, 1 no cell, 2 defer
+    uint8_t has[kSplitMaxK];
+    int kk;
+};
 
 __global__ void __launch_bounds__(kSplitMaxK) k_cut_mi_split(CutArgs a) {
-    __shared__ double planes[4 * kSplitMaxK];
-    __shared__ SplitCell cells[kSplitMaxK];
-    __shared__ int8_t cst[kSplitMaxK];  // 0 cell, 1 no cell, 2 defer
-    __shared__ int kk;
+    extern __shared__ __align__(16) unsigned char split_smem[];
+    SplitSmem& S = *reinterpret_cast<SplitSmem*>(split_smem);
     const int lane = threadIdx.x;
+    const Lanes L{lane};
+    SplitClip& c = S.clip[lane];
     for (int64_t i = blockIdx.x; i < a.n; i += gridDim.x) {
         const uint32_t ai = a.list[i];
-        if (lane == 0) kk = gather_planes(a, ai, planes, kSplitMaxK);
+        if (lane == 0) S.kk = gather_planes(a, ai, S.planes, kSplitMaxK);
         __syncthreads();
-        const int k = kk;
+        const int k = S.kk;
         if (k > kSplitMaxK) {
             if (lane == 0) a.deferred[atomicAdd(a.n_deferred, 1u)] = ai;
             __syncthreads();
             continue;
         }
-        SplitCut c;
-        int st = c.prepare(planes, k);
-        cst[lane] = 1;
+        int st = c.prepare(S.planes, k);
+        S.cst[lane] = 1;
         if (st == CUT_OK && lane < k && c.has_cell(4 + lane)) {
             bool empty = false;
             st = c.clip(4 + lane, empty);
-            if (st == CUT_OK && !empty) st = c.export_cell(cells[lane]);
-            cst[lane] = st != CUT_OK ? 2 : (empty ? 1 : 0);
+            if (st == CUT_OK && !empty) st = c.export_cell(S.cells[lane]);
+            S.cst[lane] = st != CUT_OK ? 2 : (empty ? 1 : 0);
         } else if (st != CUT_OK) {
-            cst[lane] = 2;
+            S.cst[lane] = 2;
         }
+        S.has[lane] = S.cst[lane] == 0 ? 1 : 0;
         __syncthreads();
-        if (lane == 0) {
-            bool ok = true;
-            for (int j = 0; j < k; ++j) ok = ok && cst[j] != 2;
-            if (ok) ok = c.prepare(planes, k) == CUT_OK;
-            for (int m = 4; m < 4 + k && ok; ++m)
-                if (cst[m - 4] == 0) ok = c.append_cell(m, cells[m - 4]) == CUT_OK;
-            const uint8_t* rec = nullptr;
-            if (ok) {
-                int size = 0;
-                IASum4 sum;
-                rec = finish_cut<SplitCut, MISummary>(a, ai, c, &size, &sum, true);
+        bool ok = true;
+        for (int j = 0; j < k; ++j) ok = ok && S.cst[j] != 2;
+        // the merge across the lanes (cut_mi_merge.cuh)
+        const int merged = ok ? S.mg.run(L, S.cells, S.has, k) : CUT_DEFER;
+        bool done = false;
+        if (merged == CUT_OK) {
+            const int size = S.mg.record_size(k);
+            unsigned long long off = 0;
+            if (lane == 0) off = heap_alloc(a, size);
+            off = __shfl_sync(0xFFFFFFFFu, off, 0);
+            if (off + size <= a.heap_cap) {
+                MISummary sum;
+                S.mg.emit(L, S.cells, k, c.rep, a.heap + off, sum);
+                if (lane == 0) {
+                    a.act_desc[ai] = off | a.desc_bit;
+                    a.act_sum[ai] = pack_sum<MISummary>(sum);
+                }
+                done = true;
             }
-            if (!rec) a.deferred[atomicAdd(a.n_deferred, 1u)] = ai;
         }
+        if (!done && lane == 0) a.deferred[atomicAdd(a.n_deferred, 1u)] = ai;
         __syncthreads();
     }
 }
@@ -817,8 +836,13 @@ size_t cut_big_slot_bytes(bool mi) { return mi ? sizeof(BigSlot<true>) : sizeof(
 
 void launch_cut_mi_split(const CutArgs& a, cudaStream_t s) {
     if (a.n == 0) return;
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(k_cut_mi_split, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SplitSmem));
+        attr = true;
+    }
     const int64_t blocks = a.n < 152 * 32 ? a.n : 152 * 32;
-    k_cut_mi_split<<<(unsigned)blocks, kSplitMaxK, 0, s>>>(a);
+    k_cut_mi_split<<<(unsigned)blocks, kSplitMaxK, sizeof(SplitSmem), s>>>(a);
     note_launch();
 }
 

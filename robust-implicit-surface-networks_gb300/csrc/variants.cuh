@@ -5,6 +5,7 @@
 #pragma once
 #include "cut_ia_warp.cuh"
 #include "cut_mi.cuh"
+#include "cut_mi_merge.cuh"
 
 namespace ria {
 using IACutFast = IACut<32, 48, 16, 192, false>;

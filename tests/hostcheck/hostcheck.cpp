@@ -1,6 +1,7 @@
 // Test-only harness: compiles the device per-tet cut headers for the host so that their logic can be
 // checked against the CPU oracle without a GPU.  Never linked into the product library.
 #include <cstring>
+#include <vector>
 
 #include "../../robust-implicit-surface-networks_gb300/csrc/cut_mi.cuh"
 #include "../../robust-implicit-surface-networks_gb300/csrc/variants.cuh"
@@ -65,7 +66,54 @@ extern "C" int hc_ia_cut(int k, const double* planes, int big, uint8_t* buf, int
     return r;
 }
 
+// big == 3: the split path of the device (one clipper per material, then the lane-parallel merge
+// with one lane)
+static int mi_split(int k, const double* mats, uint8_t* buf, int cap, uint16_t* summary) {
+    using SplitClip = MICut<32, 32, 192, 1, 1, 1, false>;  // the device's compact clipper
+    using SplitCell = MICell<32, 32, 192>;
+    if (k > 32) return -11;
+    std::vector<SplitCell> cells(k);
+    uint8_t has[32] = {};
+    auto* c = new SplitClip();
+    int st = c->prepare(mats, k);
+    for (int m = 0; m < k && st == CUT_OK; ++m) {
+        auto* cm = new SplitClip();
+        st = cm->prepare(mats, k);
+        if (st == CUT_OK && cm->has_cell(4 + m)) {
+            bool empty = false;
+            st = cm->clip(4 + m, empty);
+            if (st == CUT_OK && !empty) {
+                st = cm->export_cell(cells[m]);
+                has[m] = 1;
+            }
+        }
+        delete cm;
+    }
+    int r = -10 - st;
+    if (st == CUT_OK) {
+        auto* mg = new MIMerge<SplitCell>();
+        Lanes L;
+        st = mg->run(L, cells.data(), has, k);
+        if (st != CUT_OK) {
+            r = -10 - st;
+        } else {
+            r = mg->record_size(k);
+            if (r > cap) {
+                r = -3;
+            } else {
+                MISummary s;
+                mg->emit(L, cells.data(), k, c->rep, buf, s);
+                std::memcpy(summary, &s, sizeof(s));
+            }
+        }
+        delete mg;
+    }
+    delete c;
+    return r;
+}
+
 extern "C" int hc_mi_cut(int k, const double* mats, int big, uint8_t* buf, int cap, uint16_t* summary) {
+    if (big == 3) return mi_split(k, mats, buf, cap, summary);
     if (big == 2) {
         auto* c = new MICutMid();
         int r = finish<MICutMid, MISummary>(c, c->run(mats, k), buf, cap, summary);

@@ -63,6 +63,9 @@ def _agree(hc, oracle, mode, rows):
     if mode == "ia":
         warp, wsum = hc.cut(mode, rows, "warp")
         assert warp == ref and np.array_equal(wsum[:4], bsum[:4])
+    else:
+        split, ssum = hc.cut(mode, rows, "warp")  # the material interface's split path
+        assert isinstance(split, int) or (split == ref and np.array_equal(ssum[:5], bsum[:5]))
     return isinstance(fast, int)
 
 
