@@ -23,35 +23,55 @@
 
 namespace ria {
 
-struct Lanes {
+// A group of G lanes of one warp (G = 32: the whole warp; G = 16: either half), lanes numbered
+// from 0 within the group.  Ballots return group-relative masks.
+template <int G>
+struct LanesG {
 #if defined(__CUDA_ARCH__)
-    static constexpr int W = 32;
-    int lane;
-    __device__ __forceinline__ void sync() const { __syncwarp(); }
-    __device__ __forceinline__ unsigned ballot(bool p) const { return __ballot_sync(0xFFFFFFFFu, p); }
-    __device__ __forceinline__ unsigned or_all(unsigned x) const { return __reduce_or_sync(0xFFFFFFFFu, x); }
-    __device__ __forceinline__ int add_all(int x) const { return (int)__reduce_add_sync(0xFFFFFFFFu, (unsigned)x); }
+    static constexpr int W = G;
+    int lane;       // within the group
+    int base;       // first warp lane of the group
+    unsigned mask;  // the group's lanes in the warp
+    __device__ __forceinline__ static LanesG of_thread(int warp_lane) {
+        LanesG g;
+        g.lane = warp_lane & (G - 1);
+        g.base = warp_lane & ~(G - 1);
+        g.mask = G == 32 ? 0xFFFFFFFFu : (((1u << G) - 1u) << g.base);
+        return g;
+    }
+    __device__ __forceinline__ void sync() const { __syncwarp(mask); }
+    __device__ __forceinline__ unsigned ballot(bool p) const {
+        const unsigned b = __ballot_sync(mask, p);
+        return G == 32 ? b : ((b >> base) & ((1u << G) - 1u));
+    }
+    __device__ __forceinline__ unsigned or_all(unsigned x) const { return __reduce_or_sync(mask, x); }
+    __device__ __forceinline__ int add_all(int x) const { return (int)__reduce_add_sync(mask, (unsigned)x); }
     __device__ __forceinline__ int below(unsigned m) const { return __popc(m & ((1u << lane) - 1u)); }
     __device__ __forceinline__ int count(unsigned m) const { return __popc(m); }
+    template <class T>
+    __device__ __forceinline__ T bcast(T x) const { return __shfl_sync(mask, x, 0, G); }
 #else
     static constexpr int W = 1;
     int lane = 0;
+    static LanesG of_thread(int) { return LanesG{}; }
     void sync() const {}
     unsigned ballot(bool p) const { return p ? 1u : 0u; }
     unsigned or_all(unsigned x) const { return x; }
     int add_all(int x) const { return x; }
     int below(unsigned) const { return 0; }
     int count(unsigned m) const { return m ? 1 : 0; }
+    template <class T>
+    T bcast(T x) const { return x; }
 #endif
     // exclusive prefix of `x` over the lanes of one round, plus the round's total
     RIA_HD int scan(int x, int& total) const {
 #if defined(__CUDA_ARCH__)
         int v = x;
-        for (int d = 1; d < 32; d <<= 1) {
-            int y = __shfl_up_sync(0xFFFFFFFFu, v, d);
+        for (int d = 1; d < G; d <<= 1) {
+            int y = __shfl_up_sync(mask, v, d, G);
             if (lane >= d) v += y;
         }
-        total = __shfl_sync(0xFFFFFFFFu, v, 31);
+        total = __shfl_sync(mask, v, G - 1, G);
         return v - x;
 #else
         total = x;
@@ -59,6 +79,7 @@ struct Lanes {
 #endif
     }
 };
+using Lanes = LanesG<32>;
 
 constexpr int kWarpMaxK = 16;      // active planes of a tet the warp cut takes
 constexpr int kEdgeSlots = 128;    // shared hash of the crossing edges of one insertion
@@ -167,7 +188,8 @@ struct IAWarpCut {
     }
 
     // Planes are in pl[0 .. 4k).  Returns CUT_OK, CUT_DEFER (capacity) or CUT_FAIL.
-    RIA_HDI int run(const Lanes& L, int kk) {
+    template <class LT>
+    RIA_HDI int run(const LT& L, int kk) {
         const int lane = L.lane;
         if (lane == 0) {
             k = kk;
@@ -559,7 +581,8 @@ struct IAWarpCut {
     // ranks instead of sorts, ties broken by id as the serial cut's stable insertion sorts do (face
     // ids are the serial cut's: positive parts keep their id, negative parts and cap faces follow in
     // face and cell order)
-    RIA_HDI void canonicalize(const Lanes& L) {
+    template <class LT>
+    RIA_HDI void canonicalize(const LT& L) {
         const int lane = L.lane;
         for (int v = lane; v < nv; v += L.W) sc.can.live[v] = 0;
         L.sync();
@@ -617,7 +640,8 @@ struct IAWarpCut {
     RIA_HD int record_size() const { return 10 + k + 3 * nv_live + 8 * nf + 2 * loop_total + 8 * nc; }
 
     // the canonical record (record_size() bytes) and the extraction summary, written by the lanes
-    RIA_HDI void emit(const Lanes& L, uint8_t* dst, IASummary& sum) {
+    template <class LT>
+    RIA_HDI void emit(const LT& L, uint8_t* dst, IASummary& sum) {
         const int lane = L.lane;
         auto w16 = [&](int o, int v) {
             dst[o] = (uint8_t)(v & 0xFF);

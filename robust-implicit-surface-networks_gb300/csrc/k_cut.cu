@@ -587,7 +587,7 @@ __global__ void __launch_bounds__(kSplitMaxK) k_cut_mi_split(CutArgs a) {
     extern __shared__ __align__(16) unsigned char split_smem[];
     SplitSmem& S = *reinterpret_cast<SplitSmem*>(split_smem);
     const int lane = threadIdx.x;
-    const Lanes L{lane};
+    const Lanes L = Lanes::of_thread(lane);
     SplitClip& c = S.clip[lane];
     for (int64_t i = blockIdx.x; i < a.n; i += gridDim.x) {
         const uint32_t ai = a.list[i];
@@ -640,21 +640,23 @@ __global__ void __launch_bounds__(kSplitMaxK) k_cut_mi_split(CutArgs a) {
 // the implicit arrangement.  A tet beyond the warp variant's capacity goes to the deferred list.
 constexpr int kCutWarps = 4;  // warps per block
 
+template <int G>
 __global__ void __launch_bounds__(32 * kCutWarps) k_cut_warp(CutArgs a) {
+    constexpr int kGroups = 32 * kCutWarps / G;  // groups (one tet each) per block
     extern __shared__ __align__(16) unsigned char warp_smem[];
-    const int wib = threadIdx.x >> 5;
-    IAWarpCutDev& S = reinterpret_cast<IAWarpCutDev*>(warp_smem)[wib];
-    const Lanes L{(int)(threadIdx.x & 31)};
+    const int gib = threadIdx.x / G;
+    IAWarpCutDev& S = reinterpret_cast<IAWarpCutDev*>(warp_smem)[gib];
+    const LanesG<G> L = LanesG<G>::of_thread((int)(threadIdx.x & 31));
     const int lane = L.lane;
     const int64_t n = a.n_dev ? (a.n < (int64_t)*a.n_dev ? a.n : (int64_t)*a.n_dev) : a.n;
     if (a.route_at && n > a.route_at) return;  // the thread kernel takes a long list
-    const int64_t warps = (int64_t)gridDim.x * kCutWarps;
-    int64_t i = (int64_t)blockIdx.x * kCutWarps + wib;
+    const int64_t groups = (int64_t)gridDim.x * kGroups;
+    int64_t i = (int64_t)blockIdx.x * kGroups + gib;
     for (;;) {
-        if (a.next) {  // take the next tet in list order: the heaviest first, and no warp idles early
+        if (a.next) {  // take the next tet in list order: the heaviest first, and no group idles early
             unsigned int t = 0;
             if (lane == 0) t = atomicAdd(a.next, 1u);
-            i = (int64_t)__shfl_sync(0xFFFFFFFFu, t, 0);
+            i = (int64_t)L.bcast(t);
         }
         if (i >= n) break;
         const uint32_t ai = a.list[i];
@@ -663,7 +665,7 @@ __global__ void __launch_bounds__(32 * kCutWarps) k_cut_warp(CutArgs a) {
             const uint32_t r0 = a.value_off[ai];
             k = (int)(a.value_off[ai + 1] - r0);
             if (k <= kWarpMaxK)
-                for (int x = lane; x < 4 * k; x += 32) S.pl[x] = a.values[4 * (size_t)r0 + x];
+                for (int x = lane; x < 4 * k; x += G) S.pl[x] = a.values[4 * (size_t)r0 + x];
         } else {
             const uint64_t m = a.act_mask[ai];
             k = __popcll(m);
@@ -671,7 +673,7 @@ __global__ void __launch_bounds__(32 * kCutWarps) k_cut_warp(CutArgs a) {
                 int64_t v[4];
                 TetSrc ts{a.d_tets, a.g.res};
                 ts.get(a.act_tet[ai], v);
-                for (int x = lane; x < 4 * k; x += 32) {
+                for (int x = lane; x < 4 * k; x += G) {
                     // plane x/4 is the (x/4)-th active function, at corner x%4
                     uint64_t mm = m;
                     for (int p = 0; p < (x >> 2); ++p) mm &= mm - 1;
@@ -688,7 +690,7 @@ __global__ void __launch_bounds__(32 * kCutWarps) k_cut_warp(CutArgs a) {
             S.canonicalize(L);
             size = S.record_size();
             if (lane == 0) off = heap_alloc(a, size);
-            off = __shfl_sync(0xFFFFFFFFu, off, 0);
+            off = L.bcast(off);
             if (off + size > a.heap_cap) st = CUT_DEFER;
         }
         if (st == CUT_OK) {
@@ -703,7 +705,7 @@ __global__ void __launch_bounds__(32 * kCutWarps) k_cut_warp(CutArgs a) {
             a.deferred[atomicAdd(a.n_deferred, 1u)] = ai;
         }
         L.sync();
-        if (!a.next) i += warps;
+        if (!a.next) i += groups;
     }
 }
 
@@ -876,27 +878,35 @@ void launch_cut_prep(const CutArgs& a, cudaStream_t s) {
     note_launch();
 }
 
-void launch_cut_warp(const CutArgs& a, cudaStream_t s) {
-    if (a.n == 0) return;
+template <int G>
+void launch_warp_groups(const CutArgs& a, cudaStream_t s) {
+    constexpr int kGroups = 32 * kCutWarps / G;
     static bool attr = false;
-    const size_t smem = sizeof(IAWarpCutDev) * kCutWarps;
+    const size_t smem = sizeof(IAWarpCutDev) * kGroups;
     if (!attr) {
-        cudaFuncSetAttribute(k_cut_warp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaFuncSetAttribute(k_cut_warp<G>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         attr = true;
     }
-    // resident blocks only; the warps stride over the list
+    // resident blocks only; the groups take tets from the list
     static int resident = 0;
     if (!resident) {
         int dev = 0, sms = 0, per_sm = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cut_warp, 32 * kCutWarps, smem);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cut_warp<G>, 32 * kCutWarps, smem);
         resident = (sms > 0 ? sms : 152) * (per_sm > 0 ? per_sm : 1);
     }
-    const int64_t want = (a.n + kCutWarps - 1) / kCutWarps;
+    const int64_t want = (a.n + kGroups - 1) / kGroups;
     const int64_t blocks = want < resident ? want : resident;
-    k_cut_warp<<<(unsigned)blocks, 32 * kCutWarps, smem, s>>>(a);
+    k_cut_warp<G><<<(unsigned)blocks, 32 * kCutWarps, smem, s>>>(a);
     note_launch();
+}
+
+// Whole warps: half-warp groups (two tets per warp) measured slower on the large config, as the
+// two halves' data-dependent phases diverge.
+void launch_cut_warp(const CutArgs& a, cudaStream_t s) {
+    if (a.n == 0) return;
+    launch_warp_groups<32>(a, s);
 }
 
 void launch_cut_fast(const CutArgs& a, cudaStream_t s, bool mid) {
