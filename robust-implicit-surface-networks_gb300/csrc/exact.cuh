@@ -19,11 +19,9 @@
 #if defined(__CUDACC__)
 #define RIA_HD __host__ __device__ __forceinline__
 #define RIA_HDI __host__ __device__
-#define RIA_COLD __host__ __device__ __noinline__  // rarely taken and large: one copy, out of the hot loops
 #else
 #define RIA_HD inline
 #define RIA_HDI inline
-#define RIA_COLD inline
 #endif
 
 namespace ria {
