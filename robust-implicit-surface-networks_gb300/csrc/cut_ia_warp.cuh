@@ -107,14 +107,12 @@ struct IAWarpCut {
     int8_t chas[MF];
     uint8_t cneg_of[MC];
     uint16_t capoff[MC];  // loop offset of the cap face of a crossed cell
-    // scratch of one step at a time: new vertices and face rebuild (cd), cap faces (e), canonical
+    // scratch of one step at a time: crossing edges (cd), cap faces (e), canonical
     // form (can)
     union {
         struct {
             uint32_t eslot[kEdgeSlots];  // crossing edge key + 1 (u | w << 8, u < w); 0 = empty
             uint8_t evert[kEdgeSlots];
-            uint16_t fout[MF];    // loop offset of the face's rebuilt loop(s)
-            uint16_t fnegid[MF];  // id of its negative part
         } cd;
         struct {
             uint32_t capn[MC];             // cap edges gathered per crossed cell
@@ -347,15 +345,16 @@ struct IAWarpCut {
             }
             L.sync();
             if (fail != CUT_OK) return fail;
-            // D1: sizes of the rebuilt loops, split flags and cap edges
+            // D: every face rebuilt in one pass: its loop with the new vertices, its split, its cap
+            // edge, then (after the round's scans give offsets and ids) its loop(s) written
             int nsplit = 0, nused = 0;
             for (int base = 0; base < nf0; base += L.W) {
                 const int f = base + lane;
-                int out = 0;
+                int out = 0, n = -1, j0 = -1, lp = 0, ln = 0;
                 bool split = false;
+                uint8_t full[MV + 8];
                 if (f < nf0) {
-                    uint8_t full[MV + 8];
-                    const int n = full_loop(f, full, MV + 8);
+                    n = full_loop(f, full, MV + 8);
                     if (n < 0) {
                         set_fail(CUT_DEFER);
                     } else {
@@ -363,9 +362,10 @@ struct IAWarpCut {
                         for (int j = 0; j < n; ++j) {
                             hp = hp || sg[full[j]] > 0;
                             hn = hn || sg[full[j]] < 0;
+                            lp += sg[full[j]] >= 0;
+                            ln += sg[full[j]] <= 0;
                         }
                         chas[f] = 0;
-                        int j0 = -1;
                         for (int j = 0; j < n; ++j) {
                             const int prev = full[j == 0 ? n - 1 : j - 1];
                             if (sg[full[j]] < 0 && sg[prev] >= 0) {
@@ -386,7 +386,7 @@ struct IAWarpCut {
                         if (hp && hn) {
                             split = true;
                             fside[f] = 2;
-                            for (int j = 0; j < n; ++j) out += (sg[full[j]] >= 0) + (sg[full[j]] <= 0);
+                            out = lp + ln;
                         } else {
                             fside[f] = hp ? 1 : -1;
                             out = n;
@@ -396,59 +396,38 @@ struct IAWarpCut {
                 int tot_out = 0;
                 const int off = L.scan(out, tot_out);
                 const unsigned sm = L.ballot(split);
-                if (f < nf0) {
-                    sc.cd.fout[f] = (uint16_t)(nused + off);
-                    sc.cd.fnegid[f] = (uint16_t)(nf0 + nsplit + L.below(sm));
+                const bool fits = nused + tot_out <= ML && nf0 + nsplit + L.count(sm) <= MF;
+                if (!fits) set_fail(CUT_DEFER);
+                if (fits && f < nf0 && n >= 0) {
+                    int w = nused + off;
+                    if (split) {
+                        // positive part keeps id f, negative part becomes face nf0 + rank; it starts at wa
+                        const int g = nf0 + nsplit + L.below(sm);
+                        fsupp[g] = fsupp[f];
+                        fpos[g] = fpos[f];
+                        fneg[g] = fneg[f];
+                        foff[f] = (uint16_t)w;
+                        flen[f] = (uint16_t)lp;
+                        for (int j = 0; j < n; ++j)
+                            if (sg[full[j]] >= 0) loops[nb][w++] = full[j];
+                        foff[g] = (uint16_t)w;
+                        flen[g] = (uint16_t)ln;
+                        const int jstart = (j0 - 1 + n) % n;
+                        for (int t = 0; t < n; ++t) {
+                            const int v = full[(jstart + t) % n];
+                            if (sg[v] <= 0) loops[nb][w++] = (uint8_t)v;
+                        }
+                    } else {
+                        foff[f] = (uint16_t)w;
+                        flen[f] = (uint16_t)n;
+                        for (int j = 0; j < n; ++j) loops[nb][w++] = full[j];
+                    }
                 }
                 nused += tot_out;
                 nsplit += L.count(sm);
             }
-            if (nf0 + nsplit > MF || nused > ML) set_fail(CUT_DEFER);
             L.sync();
             if (fail != CUT_OK) return fail;
-            // D2: write the rebuilt loops
-            for (int f = lane; f < nf0; f += L.W) {
-                uint8_t full[MV + 8];
-                const int n = full_loop(f, full, MV + 8);
-                if (n < 0) {
-                    set_fail(CUT_FAIL);
-                    continue;
-                }
-                int w = sc.cd.fout[f];
-                if (fside[f] == 2) {
-                    int lp = 0, ln = 0, j0 = -1;
-                    for (int j = 0; j < n; ++j) {
-                        lp += sg[full[j]] >= 0;
-                        ln += sg[full[j]] <= 0;
-                    }
-                    for (int j = 0; j < n; ++j) {
-                        const int prev = full[j == 0 ? n - 1 : j - 1];
-                        if (sg[full[j]] < 0 && sg[prev] >= 0) {
-                            j0 = j;
-                            break;
-                        }
-                    }
-                    const int g = sc.cd.fnegid[f];
-                    fsupp[g] = fsupp[f];
-                    fpos[g] = fpos[f];
-                    fneg[g] = fneg[f];
-                    foff[f] = (uint16_t)w;
-                    flen[f] = (uint16_t)lp;
-                    for (int j = 0; j < n; ++j)
-                        if (sg[full[j]] >= 0) loops[nb][w++] = full[j];
-                    foff[g] = (uint16_t)w;
-                    flen[g] = (uint16_t)ln;
-                    const int jstart = (j0 - 1 + n) % n;
-                    for (int t = 0; t < n; ++t) {
-                        const int v = full[(jstart + t) % n];
-                        if (sg[v] <= 0) loops[nb][w++] = (uint8_t)v;
-                    }
-                } else {
-                    foff[f] = (uint16_t)w;
-                    flen[f] = (uint16_t)n;
-                    for (int j = 0; j < n; ++j) loops[nb][w++] = full[j];
-                }
-            }
             const int nf1 = nf0 + nsplit;
             L.sync();
             // E0: the cap edges of the crossed cells, gathered per cell (lanes over faces)
