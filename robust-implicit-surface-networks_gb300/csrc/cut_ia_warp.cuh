@@ -268,34 +268,19 @@ struct IAWarpCut {
             for (int t = lane; t < kEdgeSlots; t += L.W) sc.cd.eslot[t] = 0;
             L.sync();
             if (fail != CUT_OK) return fail;
-            // B: crossed cells
+            // B and C in one pass over the faces: the cells the plane crosses (OR-reductions of the
+            // faces' side masks) and the crossing edges, into the shared hash (a crossing edge only
+            // exists when some face has both signs, so a plane that crosses no cell inserts none)
             unsigned cp = 0, cn = 0;
             for (int f = lane; f < nf0; f += L.W) {
                 bool hp = false, hn = false;
-                for (int j = 0; j < flen[f]; ++j) {
-                    const int s = sg[loops[cur][foff[f] + j]];
-                    hp = hp || s > 0;
-                    hn = hn || s < 0;
-                }
-                const unsigned cells = (1u << fpos[f]) | (fneg[f] != kNoCell ? (1u << fneg[f]) : 0u);
-                if (hp) cp |= cells;
-                if (hn) cn |= cells;
-            }
-            cp = L.or_all(cp);
-            cn = L.or_all(cn);
-            const unsigned strad = cp & cn;
-            for (int c = lane; c < nc0; c += L.W)
-                if (!((strad >> c) & 1) && ((cp >> c) & 1)) csign[c] |= bit64(q);
-            if (!strad) {
-                L.sync();
-                continue;
-            }
-            // C: crossing edges into the shared hash
-            for (int f = lane; f < nf0; f += L.W) {
                 const int Lf = flen[f];
                 for (int j = 0; j < Lf; ++j) {
                     const int u = loops[cur][foff[f] + j], w = loops[cur][foff[f] + (j + 1 == Lf ? 0 : j + 1)];
-                    if (sg[u] * sg[w] >= 0) continue;
+                    const int su = sg[u];
+                    hp = hp || su > 0;
+                    hn = hn || su < 0;
+                    if (su * sg[w] >= 0) continue;
                     const uint32_t key = (uint32_t)(u < w ? (u | (w << 8)) : (w | (u << 8))) + 1u;
                     uint32_t h = (key * 2654435761u) >> 25;
                     bool placed = false;
@@ -311,8 +296,17 @@ struct IAWarpCut {
                     }
                     if (!placed) set_fail(CUT_DEFER);
                 }
+                const unsigned cells = (1u << fpos[f]) | (fneg[f] != kNoCell ? (1u << fneg[f]) : 0u);
+                if (hp) cp |= cells;
+                if (hn) cn |= cells;
             }
+            cp = L.or_all(cp);
+            cn = L.or_all(cn);
+            const unsigned strad = cp & cn;
+            for (int c = lane; c < nc0; c += L.W)
+                if (!((strad >> c) & 1) && ((cp >> c) & 1)) csign[c] |= bit64(q);
             L.sync();
+            if (!strad) continue;
             if (fail != CUT_OK) return fail;
             // new vertices, numbered by slot
             int added = 0;
@@ -571,11 +565,13 @@ struct IAWarpCut {
         int nl = 0;
         for (int v = lane; v < nv; v += L.W) nl += sc.can.live[v];
         nl = L.add_all(nl);
+        for (int v = lane; v < nv; v += L.W) sc.can.fkey[v] = sc.can.live[v] ? vkey(v) : 0xFFFFFFFFu;  // vertex keys first
+        L.sync();
         for (int v = lane; v < nv; v += L.W) {
             if (!sc.can.live[v]) continue;
-            const uint32_t kv = vkey(v);
+            const uint32_t kv = sc.can.fkey[v];
             int r = 0;
-            for (int u = 0; u < nv; ++u) r += sc.can.live[u] && (vkey(u) < kv || (vkey(u) == kv && u < v));
+            for (int u = 0; u < nv; ++u) r += sc.can.fkey[u] < kv || (sc.can.fkey[u] == kv && u < v);
             sc.can.vnew[v] = (uint8_t)r;
             sc.can.vorder[r] = (uint8_t)v;
         }
