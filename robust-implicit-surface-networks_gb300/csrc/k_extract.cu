@@ -48,6 +48,7 @@ struct ExtractCtx {
     uint64_t* fsrc;
     int32_t* ffunc;
     uint32_t* fgids;  // global vertex ids of every iso face loop, in occurrence order
+    uint64_t* iso0;   // per active tet: iso flags of its first 64 record vertices, from the vertex pass
 };
 
 // iso flags of the local vertices of an IA record (vertex ids below 256)
@@ -143,6 +144,7 @@ __global__ void __launch_bounds__(kBs) k_ia_vert_keys(ExtractCtx C) {
     const uint64_t mask = C.a.act_mask[a];
     uint64_t iso[4];
     iso_vertex_flags(r, iso);
+    C.iso0[a] = iso[0];
     uint32_t pos = C.base[a].a;
     for (int j = 0; j < r.nv; ++j) {
         if (!((iso[j >> 6] >> (j & 63)) & 1)) continue;
@@ -287,8 +289,11 @@ __global__ void __launch_bounds__(kBs) k_ia_face_keys(ExtractCtx C) {
     if (a >= C.a.A) return;
     IAView r;
     r.init(C.rs.get(C.a.act_desc[a]));
-    uint64_t iso[4];
-    iso_vertex_flags(r, iso);
+    uint64_t iso[4] = {0, 0, 0, 0};
+    if (r.nv <= 64)
+        iso[0] = C.iso0[a];  // computed by the vertex pass
+    else
+        iso_vertex_flags(r, iso);
     const uint32_t vb = C.base[a].a;
     uint32_t fpos = C.base[a].b;
     uint32_t lpos = C.base[a].c;
@@ -453,6 +458,7 @@ cudaError_t run_extract(const ExtractArgs& a, const IASum4* act_sum, ExtractOut&
     C.fsrc = pool.get<uint64_t>(NF);
     C.ffunc = pool.get<int32_t>(NF);
     C.fgids = pool.get<uint32_t>((int64_t)tot.c);
+    C.iso0 = pool.get<uint64_t>(A);
     if (pool.err) return pool.err;
     cudaMemsetAsync(C.corner_owner, 0xFF, sizeof(uint32_t) * (size_t)(a.V > 0 ? a.V : 1), s);
     for (HashTab* h : {&C.he, &C.hf, &C.hb}) {
