@@ -331,10 +331,11 @@ ria_status run_pipeline(const ria_config* cfg, const Inputs& in, cudaStream_t s,
         ria_function* d_funcs = tmp.get<ria_function>(in.F, &err);
         coords = tmp.get<double>(3 * N, &err);
         double* tab = tmp.get<double>(6 * N * in.F, &err);
+        double* xy = tmp.get<double>(N * N * in.F, &err);
         if (err != cudaSuccess) return bail(fail(RIA_ENOMEM, "device allocation failed"));
         cudaMemcpyAsync(d_funcs, in.funcs, sizeof(ria_function) * in.F, cudaMemcpyHostToDevice, s);
         launch_grid_coords(in.g, coords, s);
-        launch_sample_grid(mi, d_funcs, in.F, in.g, coords, tab, d_fv, vmask, cnt + 1, s);
+        launch_sample_grid(mi, d_funcs, in.F, in.g, coords, tab, xy, d_fv, vmask, cnt + 1, s);
         fv = d_fv;
         M->fv = d_fv;
     } else {

@@ -87,26 +87,31 @@ __device__ __forceinline__ void axis_parts(const ria_function& f, int a, double 
     }
 }
 
-__device__ __forceinline__ double combine_parts(const ria_function& f, const double w0[3], const double w1[3]) {
+// Every formula starts with the sum of its x and y terms: w0 (plane, spheres) or w1 (cylinder,
+// torus).  On a grid it is tabulated per (x, y) column; `s` is that first sum.
+__device__ __forceinline__ bool first_sum_of_w1(int type) { return type == RIA_FUNC_CYLINDER || type == RIA_FUNC_TORUS; }
+
+__device__ __forceinline__ double combine_from_sum(const ria_function& f, double s, const double w0[3],
+                                                   const double w1[3]) {
     double v;
     switch (f.type) {
         case RIA_FUNC_PLANE:
-            v = (w0[0] + w0[1]) + w0[2];
+            v = s + w0[2];
             break;
         case RIA_FUNC_SPHERE:
-            v = f.p[3] - sqrt((w0[0] + w0[1]) + w0[2]);
+            v = f.p[3] - sqrt(s + w0[2]);
             break;
         case RIA_FUNC_SPHERE_SQUARED:
-            v = f.p[3] * f.p[3] - ((w0[0] + w0[1]) + w0[2]);
+            v = f.p[3] * f.p[3] - (s + w0[2]);
             break;
         case RIA_FUNC_CYLINDER: {
-            double t = (w1[0] + w1[1]) + w1[2];
+            double t = s + w1[2];
             double wx = w0[0] - t * f.p[3], wy = w0[1] - t * f.p[4], wz = w0[2] - t * f.p[5];
             v = f.p[6] - sqrt((wx * wx + wy * wy) + wz * wz);
             break;
         }
         case RIA_FUNC_TORUS: {
-            double h = (w1[0] + w1[1]) + w1[2];
+            double h = s + w1[2];
             double wx = w0[0] - h * f.p[3], wy = w0[1] - h * f.p[4], wz = w0[2] - h * f.p[5];
             double rho = sqrt((wx * wx + wy * wy) + wz * wz);
             double a = rho - f.p[6];
@@ -117,6 +122,11 @@ __device__ __forceinline__ double combine_parts(const ria_function& f, const dou
             v = 0.0;
     }
     return f.flipped ? -v : v;
+}
+
+__device__ __forceinline__ double combine_parts(const ria_function& f, const double w0[3], const double w1[3]) {
+    const double s = first_sum_of_w1(f.type) ? w1[0] + w1[1] : w0[0] + w0[1];
+    return combine_from_sum(f, s, w0, w1);
 }
 
 // grid coordinates per axis (src/io.cpp:104-106): coords[a * N + n]
@@ -139,13 +149,26 @@ __global__ void k_axis_tables(const ria_function* __restrict__ funcs, int F, con
     tab[(fa * 2 + 1) * N + n] = w1;
 }
 
+// first sums per (x, y) column: xy[(f * N + i) * N + j] (one FP64 addition per column and function
+// instead of one per vertex; the same operands, so the same bits)
+__global__ void k_xy_tables(const ria_function* __restrict__ funcs, int F, const double* __restrict__ tab, int N,
+                            double* __restrict__ xy) {
+    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (int64_t)F * N * N) return;
+    const int j = (int)(idx % N), i = (int)((idx / N) % N), f = (int)(idx / ((int64_t)N * N));
+    const double* t = tab + (size_t)f * 6 * N;
+    const int w = first_sum_of_w1(funcs[f].type) ? 1 : 0;
+    xy[idx] = t[w * N + i] + t[(2 + w) * N + j];
+}
+
 constexpr int kSampleBlock = 128;
 
 // One thread per vertex, a loop over the functions (uniform across the warp); the block's rows are
 // staged in shared memory and stored row by row, so the V x F stores stay coalesced.
 template <bool MI, bool GRID>
 __global__ void __launch_bounds__(kSampleBlock) k_sample(const ria_function* __restrict__ funcs, int F,
-                                                         const double* __restrict__ tab, int N,
+                                                         const double* __restrict__ tab,
+                                                         const double* __restrict__ xy, int N,
                                                          const double* __restrict__ pts, int64_t V,
                                                          double* __restrict__ fv, ulonglong2* __restrict__ vmask,
                                                          unsigned long long* __restrict__ n_zero) {
@@ -173,16 +196,18 @@ __global__ void __launch_bounds__(kSampleBlock) k_sample(const ria_function* __r
     for (int f = 0; f < F; ++f) {
         const ria_function& fn = funcs[f];
         double w0[3], w1[3];
+        double val;
         if (GRID) {
             const double* t = tab + (size_t)f * 6 * N;
             for (int a = 0; a < 3; ++a) {
                 w0[a] = t[(2 * a) * N + ix[a]];
                 w1[a] = t[(2 * a + 1) * N + ix[a]];
             }
+            val = combine_from_sum(fn, xy[((size_t)f * N + ix[0]) * N + ix[1]], w0, w1);
         } else {
             for (int a = 0; a < 3; ++a) axis_parts(fn, a, x[a], w0[a], w1[a]);
+            val = combine_parts(fn, w0, w1);
         }
-        const double val = combine_parts(fn, w0, w1);
         tile[threadIdx.x * stride + f] = val;
         if (!MI) {
             if (val > 0.0) m0 |= bit64(f);
@@ -565,19 +590,23 @@ void launch_grid_coords(const GridDesc& g, double* coords, cudaStream_t s) {
 }
 
 void launch_sample_grid(bool mi, const ria_function* d_funcs, int F, const GridDesc& g, const double* coords,
-                        double* tab, double* fv, ulonglong2* vmask, unsigned long long* n_zero, cudaStream_t s) {
+                        double* tab, double* xy, double* fv, ulonglong2* vmask, unsigned long long* n_zero,
+                        cudaStream_t s) {
     const int N = (int)g.res + 1;
     const int64_t V = (int64_t)N * N * N;
     k_axis_tables<<<(F * 3 * N + 127) / 128, 128, 0, s>>>(d_funcs, F, coords, N, tab);
+    note_launch();
+    const int64_t nxy = (int64_t)F * N * N;
+    k_xy_tables<<<(unsigned)((nxy + 127) / 128), 128, 0, s>>>(d_funcs, F, tab, N, xy);
     note_launch();
     const unsigned blocks = (unsigned)((V + kSampleBlock - 1) / kSampleBlock);
     const size_t smem = sizeof(double) * kSampleBlock * (F + 1);
     if (mi) {
         set_sample_smem<true, true>(smem);
-        k_sample<true, true><<<blocks, kSampleBlock, smem, s>>>(d_funcs, F, tab, N, nullptr, V, fv, vmask, n_zero);
+        k_sample<true, true><<<blocks, kSampleBlock, smem, s>>>(d_funcs, F, tab, xy, N, nullptr, V, fv, vmask, n_zero);
     } else {
         set_sample_smem<false, true>(smem);
-        k_sample<false, true><<<blocks, kSampleBlock, smem, s>>>(d_funcs, F, tab, N, nullptr, V, fv, vmask, n_zero);
+        k_sample<false, true><<<blocks, kSampleBlock, smem, s>>>(d_funcs, F, tab, xy, N, nullptr, V, fv, vmask, n_zero);
     }
     note_launch();
 }
@@ -588,7 +617,7 @@ void launch_sample_points(const ria_function* d_funcs, int F, const double* pts,
     const unsigned blocks = (unsigned)((V + kSampleBlock - 1) / kSampleBlock);
     const size_t smem = sizeof(double) * kSampleBlock * (F + 1);
     set_sample_smem<false, false>(smem);
-    k_sample<false, false><<<blocks, kSampleBlock, smem, s>>>(d_funcs, F, nullptr, 0, pts, V, fv, vmask, n_zero);
+    k_sample<false, false><<<blocks, kSampleBlock, smem, s>>>(d_funcs, F, nullptr, nullptr, 0, pts, V, fv, vmask, n_zero);
     note_launch();
 }
 

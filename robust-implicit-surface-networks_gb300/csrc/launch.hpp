@@ -25,8 +25,10 @@ struct GridDesc {
 void launch_grid_coords(const GridDesc& g, double* coords, cudaStream_t s);
 // grid sampling fused with the per-vertex masks: IA -> (pos, neg) masks; MI -> (argmax mask, 0).
 // tab: scratch of 6 * F * (res+1) doubles for the per-axis terms.
+// tab: 6 N F per-axis terms; xy: N N F first sums per (x, y) column (scratch)
 void launch_sample_grid(bool mi, const ria_function* d_funcs, int F, const GridDesc& g, const double* coords,
-                        double* tab, double* fv, ulonglong2* vmask, unsigned long long* n_zero, cudaStream_t s);
+                        double* tab, double* xy, double* fv, ulonglong2* vmask, unsigned long long* n_zero,
+                        cudaStream_t s);
 // sampling at explicit points (vmask / n_zero may be null)
 void launch_sample_points(const ria_function* d_funcs, int F, const double* pts, int64_t V, double* fv,
                           ulonglong2* vmask, unsigned long long* n_zero, cudaStream_t s);
