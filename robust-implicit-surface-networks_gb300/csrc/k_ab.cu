@@ -574,10 +574,11 @@ __global__ void k_batch_active_stats(const int64_t* __restrict__ tet_base, int n
 
 template <bool MI, bool GRID>
 void set_sample_smem(size_t smem) {
-    static bool done = false;
-    if (!done && smem > 48 * 1024) {
-        cudaFuncSetAttribute(k_sample<MI, GRID>, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024);
-        done = true;
+    if (smem > 48 * 1024) {  // once per process (thread-safe static initialisation)
+        static const bool done =
+            cudaFuncSetAttribute(k_sample<MI, GRID>, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024) ==
+            cudaSuccess;
+        (void)done;
     }
 }
 
@@ -643,11 +644,18 @@ void launch_batch_sample(bool mi, const BatchProblem* probs, int n, const uint32
                          unsigned long long* n_zero, unsigned long long* n_zero_p, cudaStream_t s) {
     if (n_blocks == 0) return;
     const size_t smem = sizeof(double) * kBatchSampleBlock * (Fmax + 1);
-    static bool attr[2] = {false, false};
-    if (!attr[mi] && smem > 48 * 1024) {
-        if (mi) cudaFuncSetAttribute(k_batch_sample<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024);
-        else cudaFuncSetAttribute(k_batch_sample<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024);
-        attr[mi] = true;
+    if (smem > 48 * 1024) {  // once per process and mode (thread-safe static initialisation)
+        if (mi) {
+            static const bool done =
+                cudaFuncSetAttribute(k_batch_sample<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024) ==
+                cudaSuccess;
+            (void)done;
+        } else {
+            static const bool done =
+                cudaFuncSetAttribute(k_batch_sample<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024) ==
+                cudaSuccess;
+            (void)done;
+        }
     }
     if (mi)
         k_batch_sample<true><<<n_blocks, kBatchSampleBlock, smem, s>>>(probs, n, blk_off, funcs, Fmax, pts, fv, vmask,

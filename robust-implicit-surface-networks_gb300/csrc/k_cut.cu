@@ -838,11 +838,10 @@ size_t cut_big_slot_bytes(bool mi) { return mi ? sizeof(BigSlot<true>) : sizeof(
 
 void launch_cut_mi_split(const CutArgs& a, cudaStream_t s) {
     if (a.n == 0) return;
-    static bool attr = false;
-    if (!attr) {
-        cudaFuncSetAttribute(k_cut_mi_split, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SplitSmem));
-        attr = true;
-    }
+    static const bool attr =  // once per process (thread-safe static initialisation)
+        cudaFuncSetAttribute(k_cut_mi_split, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SplitSmem)) ==
+        cudaSuccess;
+    (void)attr;
     const int64_t blocks = a.n < 152 * 32 ? a.n : 152 * 32;
     k_cut_mi_split<<<(unsigned)blocks, kSplitMaxK, sizeof(SplitSmem), s>>>(a);
     note_launch();
@@ -881,21 +880,17 @@ void launch_cut_prep(const CutArgs& a, cudaStream_t s) {
 template <int G>
 void launch_warp_groups(const CutArgs& a, cudaStream_t s) {
     constexpr int kGroups = 32 * kCutWarps / G;
-    static bool attr = false;
-    const size_t smem = sizeof(IAWarpCutDev) * kGroups;
-    if (!attr) {
+    constexpr size_t smem = sizeof(IAWarpCutDev) * kGroups;
+    // the shared-memory size, then the resident blocks on the device: once per process
+    // (thread-safe static initialisation); the groups take tets from the list
+    static const int resident = [] {
         cudaFuncSetAttribute(k_cut_warp<G>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        attr = true;
-    }
-    // resident blocks only; the groups take tets from the list
-    static int resident = 0;
-    if (!resident) {
         int dev = 0, sms = 0, per_sm = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cut_warp<G>, 32 * kCutWarps, smem);
-        resident = (sms > 0 ? sms : 152) * (per_sm > 0 ? per_sm : 1);
-    }
+        return (sms > 0 ? sms : 152) * (per_sm > 0 ? per_sm : 1);
+    }();
     const int64_t want = (a.n + kGroups - 1) / kGroups;
     const int64_t blocks = want < resident ? want : resident;
     k_cut_warp<G><<<(unsigned)blocks, 32 * kCutWarps, smem, s>>>(a);
@@ -916,16 +911,16 @@ void launch_cut_fast(const CutArgs& a, cudaStream_t s, bool mid) {
     while (bs > 32 && (a.n + bs - 1) / bs < 4 * 152) bs >>= 1;
     const unsigned nb = (unsigned)((a.n + bs - 1) / bs);
     // the per-thread state lives in local memory: ask for the largest L1 (no shared memory used)
-    static bool carve = false;
-    if (!carve) {
+    static const bool carve = [] {  // once per process (thread-safe static initialisation)
         cudaFuncSetAttribute(k_cut_fast<true, true>, cudaFuncAttributePreferredSharedMemoryCarveout, 0);
         cudaFuncSetAttribute(k_cut_fast<true, false>, cudaFuncAttributePreferredSharedMemoryCarveout, 0);
         cudaFuncSetAttribute(k_cut_fast<false, true>, cudaFuncAttributePreferredSharedMemoryCarveout, 0);
         cudaFuncSetAttribute(k_cut_fast<false, false>, cudaFuncAttributePreferredSharedMemoryCarveout, 0);
         cudaFuncSetAttribute(k_cut_prep<true>, cudaFuncAttributePreferredSharedMemoryCarveout, 0);
         cudaFuncSetAttribute(k_cut_prep<false>, cudaFuncAttributePreferredSharedMemoryCarveout, 0);
-        carve = true;
-    }
+        return true;
+    }();
+    (void)carve;
     if (a.mi) {
         if (mid) k_cut_fast<true, true><<<nb, bs, 0, s>>>(a);
         else k_cut_fast<true, false><<<nb, bs, 0, s>>>(a);
@@ -938,12 +933,10 @@ void launch_cut_fast(const CutArgs& a, cudaStream_t s, bool mid) {
 
 template <bool MI>
 void launch_big(const CutArgs& a, cudaStream_t s) {
-    static bool attr = false;
     const size_t smem = sizeof(BigSlot<MI>);
-    if (!attr) {
-        cudaFuncSetAttribute(k_cut_big<MI>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        attr = true;
-    }
+    static const bool attr =  // once per process (thread-safe static initialisation)
+        cudaFuncSetAttribute(k_cut_big<MI>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) == cudaSuccess;
+    (void)attr;
     const int64_t blocks = a.n < 152 * 8 ? a.n : 152 * 8;
     k_cut_big<MI><<<(unsigned)blocks, 32, smem, s>>>(a);
     note_launch();
