@@ -563,10 +563,10 @@ __global__ void __launch_bounds__(128) k_cut_wait(CutArgs a) {
     if (!done) a.deferred[atomicAdd(a.n_deferred, 1u)] = w.ai;
 }
 
-// Material interface with many materials: one block per tet, one thread per material.  A material's
+// Material interface with many materials: one warp per tet, one lane per material.  A material's
 // cell is the tet clipped by its half-spaces against every other material, independent of the other
-// cells, so the threads clip in parallel and export their cells to shared memory; thread 0 then
-// merges them in material order, canonicalises and emits, exactly as the serial cut does.
+// cells, so the lanes clip in parallel and export their cells to shared memory; the lanes then merge
+// them (MIMerge, cut_mi_merge.cuh) into the bytes the serial cut emits.
 constexpr int kSplitMaxK = 32;
 // Each lane's clipping state is small and lives in shared memory: kept per thread in local
 // memory, the state of a few active lanes is spread over a warp-interleaved footprint that L1
