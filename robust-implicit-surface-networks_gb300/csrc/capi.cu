@@ -430,11 +430,12 @@ ria_status run_pipeline(const ria_config* cfg, const Inputs& in, cudaStream_t s,
         if (cfg->use_lookup && cfg->use_secondary_lookup) set_cache(ca, ctx, mi);
         // The general-case list is heaviest first.  Its heavy bins (four or more active functions)
         // are a few long cuts, its light bins many short lookups and cuts: the two parts run at the
-        // same time on two streams.  Heavy: the small variant (implicit arrangement), or one block
-        // per tet clipping the materials' cells in parallel (material interface).  Light: the
-        // lookup pass, then the small variant over the tets it did not finish.  The tets the small
-        // variant cannot finish go to the mid-size variant, and what that cannot finish to the
-        // exact variant.
+        // same time on two streams.  Heavy: a warp per tet (implicit arrangement: the warp cut, the
+        // small variant past kWarpCutTets; material interface: the lanes clip the materials' cells
+        // in parallel and merge them).  Light: the lookup pass, the claiming tets' cuts and the
+        // waiting tets; after the join, the tets the lookup pass left (implicit arrangement).  The
+        // tets these variants cannot finish go to the mid-size variant, and what that cannot
+        // finish to the exact variant.
         const int64_t G_light = G - G_mid;
         const bool prep = G_light > 0 && (ca.table || ca.cache.slots);
         uint32_t* rest = prep ? tmp.get<uint32_t>(G_light, &err) : nullptr;
