@@ -320,3 +320,32 @@ def test_warp_variant_heavy_and_degenerate(hc, oracle):
             assert out == oracle.ia_cut(rows) == big and np.array_equal(summ[:4], bsum[:4])
             done += 1
     assert done >= 150
+
+
+def test_split_variant_heavy_and_degenerate(hc, oracle):
+    """The material interface's warp variant (per-lane clips, then the lane-parallel merge; its
+    lane-parallel steps run serially here) on the heavy bins it serves: four to 32 materials, random,
+    integer-degenerate (ties and dominated materials) and with duplicated materials.  It either
+    defers the tet or reproduces the oracle's record and the exact variant's summary.  Exact ties
+    defer (its predicates are filtered), and so do cells beyond its capacities, which random tets
+    with twelve or more materials reach; up to eight materials every tie-free tet completes."""
+    rng = np.random.default_rng(15)
+    done = 0
+    for k in (4, 5, 6, 8, 12, 16, 24, 32):
+        for trial in range(12):
+            if trial % 3 == 0:
+                rows = rng.normal(size=(k, 4)) * 0.3
+            elif trial % 3 == 1:
+                rows = rng.integers(-2, 3, size=(k, 4)).astype(np.float64)
+            else:
+                base = rng.normal(size=(max(2, k // 2), 4)) * 0.3
+                rows = np.array([base[int(rng.integers(0, len(base)))] for _ in range(k)])
+            out, summ = hc.cut("mi", rows, "warp")
+            if isinstance(out, int):
+                assert out == -11  # deferred
+                assert k > 8 or trial % 3 == 1
+                continue
+            big, bsum = hc.cut("mi", rows, True)
+            assert out == oracle.mi_cut(rows) == big and np.array_equal(summ[:5], bsum[:5])
+            done += 1
+    assert done >= 50
