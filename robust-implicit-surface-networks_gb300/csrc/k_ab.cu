@@ -17,6 +17,7 @@
 
 #include "device_common.cuh"
 #include "launch.hpp"
+#include "sqrt_rn.cuh"
 
 namespace ria {
 
@@ -25,6 +26,15 @@ namespace {
 constexpr int kTileV = 32;
 constexpr int kBlock = 256;
 
+// the sign of a value from its bits, off the FP64 pipe: 1 positive, -1 negative, 0 for zeros and
+// NaN (the outcomes of v > 0 and v < 0)
+__device__ __forceinline__ int value_sign(double v) {
+    const long long b = __double_as_longlong(v);
+    const unsigned long long mag = (unsigned long long)b & 0x7FFFFFFFFFFFFFFFull;
+    if (mag == 0 || mag > 0x7FF0000000000000ull) return 0;
+    return b < 0 ? -1 : 1;
+}
+
 // masks of one vertex row held in shared memory
 template <bool MI>
 __device__ __forceinline__ ulonglong2 row_masks(const double* row, int F, int& nzero) {
@@ -32,9 +42,9 @@ __device__ __forceinline__ ulonglong2 row_masks(const double* row, int F, int& n
     if (!MI) {
         uint64_t pos = 0, neg = 0;
         for (int f = 0; f < F; ++f) {
-            double x = row[f];
-            if (x > 0.0) pos |= bit64(f);
-            else if (x < 0.0) neg |= bit64(f);
+            const int sg = value_sign(row[f]);
+            if (sg > 0) pos |= bit64(f);
+            else if (sg < 0) neg |= bit64(f);
         }
         nzero = F - __popcll(pos) - __popcll(neg);
         m.x = pos;
@@ -88,7 +98,8 @@ __device__ __forceinline__ void axis_parts(const ria_function& f, int a, double 
 }
 
 // Every formula starts with the sum of its x and y terms: w0 (plane, spheres) or w1 (cylinder,
-// torus).  On a grid it is tabulated per (x, y) column; `s` is that first sum.
+// torus).  On a grid it is tabulated per (x, y) column; `s` is that first sum.  Square roots go
+// through sqrt_rn (correctly rounded like sqrt, on the integer and FP32 pipes).
 __device__ __forceinline__ bool first_sum_of_w1(int type) { return type == RIA_FUNC_CYLINDER || type == RIA_FUNC_TORUS; }
 
 __device__ __forceinline__ double combine_from_sum(const ria_function& f, double s, const double w0[3],
@@ -99,7 +110,7 @@ __device__ __forceinline__ double combine_from_sum(const ria_function& f, double
             v = s + w0[2];
             break;
         case RIA_FUNC_SPHERE:
-            v = f.p[3] - sqrt(s + w0[2]);
+            v = f.p[3] - sqrt_rn(s + w0[2]);
             break;
         case RIA_FUNC_SPHERE_SQUARED:
             v = f.p[3] * f.p[3] - (s + w0[2]);
@@ -107,15 +118,15 @@ __device__ __forceinline__ double combine_from_sum(const ria_function& f, double
         case RIA_FUNC_CYLINDER: {
             double t = s + w1[2];
             double wx = w0[0] - t * f.p[3], wy = w0[1] - t * f.p[4], wz = w0[2] - t * f.p[5];
-            v = f.p[6] - sqrt((wx * wx + wy * wy) + wz * wz);
+            v = f.p[6] - sqrt_rn((wx * wx + wy * wy) + wz * wz);
             break;
         }
         case RIA_FUNC_TORUS: {
             double h = s + w1[2];
             double wx = w0[0] - h * f.p[3], wy = w0[1] - h * f.p[4], wz = w0[2] - h * f.p[5];
-            double rho = sqrt((wx * wx + wy * wy) + wz * wz);
+            double rho = sqrt_rn((wx * wx + wy * wy) + wz * wz);
             double a = rho - f.p[6];
-            v = f.p[7] - sqrt(a * a + h * h);
+            v = f.p[7] - sqrt_rn(a * a + h * h);
             break;
         }
         default:
@@ -210,8 +221,9 @@ __global__ void __launch_bounds__(kSampleBlock) k_sample(const ria_function* __r
         }
         tile[threadIdx.x * stride + f] = val;
         if (!MI) {
-            if (val > 0.0) m0 |= bit64(f);
-            else if (val < 0.0) m1 |= bit64(f);
+            const int sg = value_sign(val);
+            if (sg > 0) m0 |= bit64(f);
+            else if (sg < 0) m1 |= bit64(f);
         } else {
             if (f == 0 || val > mx) {
                 mx = val;
@@ -489,8 +501,9 @@ __global__ void __launch_bounds__(kBatchSampleBlock)
         }
         tile[threadIdx.x * stride + f] = val;
         if (!MI) {
-            if (val > 0.0) m0 |= bit64(f);
-            else if (val < 0.0) m1 |= bit64(f);
+            const int sg = value_sign(val);
+            if (sg > 0) m0 |= bit64(f);
+            else if (sg < 0) m1 |= bit64(f);
         } else {
             if (f == 0 || val > mx) {
                 mx = val;

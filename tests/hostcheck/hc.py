@@ -20,6 +20,7 @@ def lib():
         L.hc_det_sign.argtypes = [ctypes.c_void_p, ctypes.c_int]
         for f in (L.hc_ia_key2, L.hc_mi_key3, L.hc_ia_key3):
             f.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+        L.hc_sqrt_rn.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int]
         _lib = L
     return _lib
 
@@ -77,3 +78,10 @@ def key(mode, rows):
     out = np.zeros(1, dtype=np.uint64 if mode == "ia3" else np.uint32)
     f = {"ia": lib().hc_ia_key2, "mi": lib().hc_mi_key3, "ia3": lib().hc_ia_key3}[mode]
     return int(out[0]) if f(rows.ctypes.data, out.ctypes.data) else None
+
+
+def sqrt_rn(values, perturb=0):
+    values = np.ascontiguousarray(values, dtype=np.float64)
+    out = np.empty_like(values)
+    lib().hc_sqrt_rn(values.ctypes.data, out.ctypes.data, values.size, perturb)
+    return out

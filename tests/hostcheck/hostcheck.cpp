@@ -7,6 +7,7 @@
 #include "../../robust-implicit-surface-networks_gb300/csrc/variants.cuh"
 #include "../../robust-implicit-surface-networks_gb300/csrc/lookup2.cuh"
 #include "../../robust-implicit-surface-networks_gb300/csrc/cut_ia_warp.cuh"
+#include "../../robust-implicit-surface-networks_gb300/csrc/sqrt_rn.cuh"
 
 using namespace ria;
 
@@ -228,4 +229,19 @@ extern "C" int hc_sizes(int* out) {
     out[2] = (int)sizeof(MICutFast);
     out[3] = (int)sizeof(MICutBig);
     return 0;
+}
+
+// the sampler's square root; perturb != 0 moves its seed by perturb * 2^-20 (relative), beyond the
+// FP32 estimate's error, to show the margin of the two Newton steps
+extern "C" void hc_sqrt_rn(const double* in, double* out, int64_t n, int perturb) {
+    for (int64_t i = 0; i < n; ++i) {
+        uint64_t x;
+        int e;
+        if (perturb == 0 || !sqrt_split(in[i], x, e)) {
+            out[i] = sqrt_rn(in[i]);
+            continue;
+        }
+        const uint64_t r0 = sqrt_seed(x);
+        out[i] = sqrt_rn_finish(x, e, (uint64_t)((int64_t)r0 + perturb * (int64_t)(r0 >> 20)));
+    }
 }

@@ -349,3 +349,32 @@ def test_split_variant_heavy_and_degenerate(hc, oracle):
             assert out == oracle.mi_cut(rows) == big and np.array_equal(summ[:5], bsum[:5])
             done += 1
     assert done >= 50
+
+
+def test_sampler_square_root_is_correctly_rounded(hc):
+    """The sampler's integer square root (sqrt_rn.cuh) against the C library's correctly rounded
+    sqrt, bit for bit: random bit patterns over the whole double range (negative, subnormal,
+    infinite and NaN inputs included), mantissas at both ends of every binade tested, perfect
+    squares and their neighbours.  The same inputs with the seed moved by 2^-20 (relative), about
+    four times the FP32 reciprocal square root's documented error, must still round correctly."""
+    rng = np.random.default_rng(16)
+    vals = [rng.integers(0, 2**64 - 1, size=400_000, dtype=np.uint64).view(np.float64),
+            rng.integers(0, 2**63, size=400_000, dtype=np.uint64).view(np.float64),
+            rng.uniform(0, 10, size=400_000) ** rng.uniform(-3, 3, size=400_000)]
+    for e in (1, 1023 - 52, 1022, 1023, 1024, 2045, 2046):
+        base = np.uint64(e) << np.uint64(52)
+        steps = np.arange(20_000, dtype=np.uint64)
+        vals.append((base + steps).view(np.float64))
+        vals.append((base + (np.uint64(1) << np.uint64(52)) - np.uint64(1) - steps).view(np.float64))
+    k = rng.integers(1, 2**26, size=200_000).astype(np.float64)
+    sq = k * k
+    vals += [sq, np.nextafter(sq, 0), np.nextafter(sq, np.inf)]
+    vals.append(np.array([0.0, -0.0, np.inf, -np.inf, np.nan, 5e-324, 2.2250738585072014e-308,
+                          1.7976931348623157e308, 0.25, 1.0, 2.0, 4.0]))
+    v = np.concatenate(vals)
+    with np.errstate(invalid="ignore"):
+        ref = np.sqrt(v)
+    for perturb in (0, -1, 1):
+        out = hc.sqrt_rn(v, perturb)
+        same = (out.view(np.uint64) == ref.view(np.uint64)) | (np.isnan(out) & np.isnan(ref))
+        assert same.all(), (perturb, v[~same][:4])

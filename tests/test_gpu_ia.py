@@ -58,6 +58,24 @@ def test_sampling_bit_exact(pkg, fns, oracle, lib):
     assert np.array_equal(pkg.sample_functions(funcs, pts), oracle.sample(funcs, pts))
 
 
+def test_sampling_square_roots_wide_range(pkg, fns, oracle, lib):
+    """The device's integer square root over the whole exponent range: points from 1e-170 to 1e170
+    (subnormal and infinite sums of squares included) through the spheres, cylinder and torus,
+    bit for bit against the oracle's C library sqrt."""
+    rng = np.random.default_rng(17)
+    specs = [
+        {"type": "sphere", "center": [0.0, 0.0, 0.0], "radius": 1.0},
+        {"type": "sphere", "center": [1e-3, -2e-3, 5e-4], "radius": 0.5},
+        {"type": "cylinder", "axis_point": [0.0, 0.0, 0.0], "axis_vector": [0.3, -0.4, 0.5], "radius": 0.3},
+        {"type": "torus", "center": [0.0, 0.0, 0.0], "axis_vector": [0.0, 0.0, 1.0], "major_radius": 0.5,
+         "minor_radius": 0.1},
+    ]
+    funcs = fns.make_functions(specs)
+    pts = rng.uniform(-1, 1, size=(400000, 3)) * 10.0 ** rng.uniform(-170, 170, size=(400000, 1))
+    got, want = pkg.sample_functions(funcs, pts), oracle.sample(funcs, pts)
+    assert np.array_equal(got, want, equal_nan=True)
+
+
 @pytest.mark.parametrize("use_lookup", [True, False])
 def test_grid_small_workload(pkg, fns, oracle, lib, use_lookup):
     wl = fns.workload_ia_small()
