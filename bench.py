@@ -16,7 +16,9 @@ mesh (points, vertex records, faces) back; host<->device copies are inside its t
 
 --config batch runs the batched form: 4096 independent grids (vertices per axis uniform in 9..33,
 2..24 functions of mixed kinds; about 2.3x10^8 tets) through ria_grid_batch, one pass of every stage
-over all of them, and beside it the plain drop-in called once per grid (`per_problem_plain`).
+over all of them, and beside it the plain drop-in called once per grid (`per_problem_plain`).  Its
+CPU baseline, and its --impl reference arm, run the CPU restatement over the first 256 grids with one
+grid per process on every host core (the grids are independent).
 
 --impl reference times the CPU restatement of the reference path (oracle/) on this host's cores on a
 bounded slab of the same workload (the reference itself depends on absent third-party libraries and
@@ -116,6 +118,72 @@ def workload(name, res=None):
     raise SystemExit(f"unknown config {name}")
 
 
+def _oracle_worker_init():
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import pyoracle
+
+    pyoracle.lib()
+    importlib.import_module(PKG + ".functions")
+
+
+def _oracle_worker_ready(_):
+    time.sleep(0.05)
+    return os.getpid()
+
+
+def _oracle_problem(job):
+    """One grid of the batch through the CPU restatement, stages a-d (a worker of cpu_batch)."""
+    import pyoracle
+
+    res, funcs, mode = job
+    fns = importlib.import_module(PKG + ".functions")
+    pts, tets = fns.generate_tet_mesh(res)
+    fv = pyoracle.sample(funcs, pts)
+    pyoracle.run(mode, pts, tets, fv)
+    return len(tets)
+
+
+def cpu_batch(probs, mode, n_problems=256, repeats=1):
+    """The CPU restatement over the first n_problems grids of the batch, one process per host core
+    (the grids are independent, so they spread over the cores without any exchange).  Returns
+    per-repeat tets/s, the cores used and a description of the sample."""
+    import multiprocessing as mp
+
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import pyoracle
+
+    pyoracle.build()
+    cores = os.cpu_count() or 1
+    jobs = [(r, f, mode) for r, f in probs[:n_problems]]
+    rates, n = [], 0
+    with mp.get_context("spawn").Pool(cores, initializer=_oracle_worker_init) as pool:
+        pool.map(_oracle_worker_ready, range(2 * cores), chunksize=1)  # every worker started
+        for _ in range(repeats):
+            t0 = time.perf_counter()
+            n = sum(pool.map(_oracle_problem, jobs, chunksize=1))
+            rates.append(n / (time.perf_counter() - t0))
+    desc = (f"the first {len(jobs)} of {len(probs)} grids ({n} tets), stages a-d of the CPU restatement "
+            f"(oracle/), one grid per process on {cores} cores")
+    return rates, n, cores, desc
+
+
+def run_reference_batch(args, world):
+    """The batched workload's CPU arm: every step is the bounded sample of cpu_batch."""
+    fns = importlib.import_module(PKG + ".functions")
+    wl = fns.workload_batch(n=args.batch_n)
+    rates, n, cores, desc = cpu_batch(wl.problems, "ia", repeats=args.warmup + args.steps)
+    per = statistics.median(rates[args.warmup:])
+    line = {
+        "impl": "reference", "metric": METRIC, "value": per, "unit": "tets/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": n / per * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+        "config": {"workload": wl.name, "tets": wl.n_tets, "problems": len(wl.problems), "sample": desc},
+        "cpu_baseline": {"value": per, "unit": "tets/s", "cores": cores, "kind": "port", "sample": desc},
+        "e2e": {"value": per, "unit": "tets/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
 def run_batch(args, world, local):
     """The batched form against the plain drop-in called per problem."""
     import numpy as np
@@ -190,6 +258,9 @@ def run_batch(args, world, local):
                      "frac": None, "peak_kind": peak_kind, "traffic": None},
         "clocks": clk.summary(),
     }
+    if not args.no_cpu_baseline:
+        rates, _, cores, desc = cpu_batch(probs, "ia")
+        line["cpu_baseline"] = {"value": rates[0], "unit": "tets/s", "cores": cores, "kind": "port", "sample": desc}
     print(json.dumps(line))
 
 
@@ -366,8 +437,11 @@ def main():
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if args.config in ("batch", "serve"):
         if args.impl == "reference":
-            print(json.dumps({"impl": "reference", "unavailable": "the batched and served forms have no CPU "
-                              "reference arm; run --impl reference on the other configs"}))
+            if rank == 0 and args.config == "batch":
+                run_reference_batch(args, world)
+            elif rank == 0:
+                print(json.dumps({"impl": "reference", "unavailable": "the served form has no CPU reference "
+                                  "arm; run --impl reference on the other configs"}))
         elif rank == 0:
             (run_batch if args.config == "batch" else run_serve)(args, world, local)
         return
