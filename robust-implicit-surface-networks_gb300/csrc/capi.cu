@@ -59,7 +59,8 @@ struct DeviceCtx {
 };
 
 std::mutex g_mu;
-std::vector<DeviceCtx> g_ctx;
+// a deque: growing it for a new device keeps the contexts that running calls hold in place
+std::deque<DeviceCtx> g_ctx;
 
 constexpr int64_t kFastRecordBytes = 1024;  // heap bytes per tet of the small filtered variant
 constexpr int64_t kMidRecordBytes = 4096;   // per tet of the mid variant (fuller records go to the exact kernel)
