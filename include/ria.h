@@ -264,7 +264,8 @@ RIA_API ria_status ria_server_wait(ria_server* server, uint64_t ticket, double t
 /* CSG requests: the face labels of ria_mesh_csg (host_dst may be NULL to ask for the count). */
 RIA_API uint64_t ria_server_labels(ria_server* server, uint64_t ticket, uint8_t* host_dst);
 RIA_API void ria_server_release(ria_server* server, uint64_t ticket);
-/* Stops the workers after their current batch and frees every result. */
+/* Stops the workers after their current batch and frees every result.  Requests not yet started are
+ * dropped.  No other thread may be inside a ria_server_* call on this server while it is destroyed. */
 RIA_API void ria_server_destroy(ria_server* server);
 
 /* Stage a alone: func_vals[n_pts][n_func] = funcs evaluated at pts (host buffers). */
