@@ -29,7 +29,7 @@ APPS = ["impl_arrangement", "material_interface", "csg"]
 CXX = os.environ.get("CXX", "g++")
 # -ffp-contract=off: the grid coordinates and unit axis vectors round as written (aarch64 g++
 # contracts a*b+c into fma by default)
-HOST_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off"]
+HOST_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-pthread"]
 
 
 def nvcc() -> str:
@@ -91,7 +91,7 @@ def build(verbose: bool = False) -> str:
         _run([[cc, *ARCH, "-shared", *objs, "-o", LIB]], "link", verbose)
         relinked = True
     if relinked or _host_stale(HOST_LIB, host_objs):
-        _run([[CXX, "-shared", *host_objs, "-L" + OUT_DIR, "-lria", "-Wl,-rpath,$ORIGIN", "-o", HOST_LIB]],
+        _run([[CXX, "-shared", "-pthread", *host_objs, "-L" + OUT_DIR, "-lria", "-Wl,-rpath,$ORIGIN", "-o", HOST_LIB]],
              "link", verbose)
         relinked = True
     apps = []

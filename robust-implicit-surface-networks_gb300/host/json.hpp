@@ -5,6 +5,7 @@
 #include <cctype>
 #include <charconv>
 #include <cstdint>
+#include <cstring>
 #include <map>
 #include <memory>
 #include <stdexcept>
@@ -177,40 +178,85 @@ class JsonParser {
 //   d1..dn "." dn+1..dk   if 0 < n <= 15
 //   "0." 0..0 d1..dk      if -4 < n <= 0
 //   d1 "." d2..dk "e" +-XX   otherwise (exponent n-1, at least two digits; no "." when k = 1)
-// and "null" for a NaN or an infinity.
-inline std::string json_double(double x) {
-    if (x != x || x - x != 0.0) return "null";
-    char buf[64];
-    auto r = std::to_chars(buf, buf + sizeof(buf), x, std::chars_format::scientific);
-    std::string s(buf, r.ptr), out;
-    size_t i = 0;
-    if (s[0] == '-') {
-        out.push_back('-');
-        i = 1;
+// and "null" for a NaN or an infinity.  Writes into `out` (room for kJsonDoubleMax characters) and
+// returns the end.
+constexpr int kJsonDoubleMax = 32;
+
+inline char* json_double_to(char* out, double x) {
+    if (x != x || x - x != 0.0) {
+        std::memcpy(out, "null", 4);
+        return out + 4;
     }
-    size_t e = s.find('e');
-    std::string digits;
-    for (size_t j = i; j < e; ++j)
-        if (s[j] != '.') digits.push_back(s[j]);
-    const int n = std::stoi(s.substr(e + 1)) + 1;
-    const int k = (int)digits.size();
-    if (digits == "0") return out + "0.0";
-    if (k <= n && n <= 15) {
-        out += digits + std::string((size_t)(n - k), '0') + ".0";
+    char sci[40];
+    const char* end = std::to_chars(sci, sci + sizeof(sci), x, std::chars_format::scientific).ptr;
+    const char* p = sci;
+    if (*p == '-') {
+        *out++ = '-';
+        ++p;
+    }
+    char digits[24];
+    int k = 0;
+    for (; *p != 'e'; ++p)
+        if (*p != '.') digits[k++] = *p;
+    ++p;
+    const bool eneg = *p == '-';
+    if (*p == '-' || *p == '+') ++p;
+    int e10 = 0;
+    for (; p < end; ++p) e10 = e10 * 10 + (*p - '0');
+    const int n = (eneg ? -e10 : e10) + 1;
+    auto put = [&](const char* src, int len) {
+        std::memcpy(out, src, (size_t)len);
+        out += len;
+    };
+    if (k == 1 && digits[0] == '0') {
+        put("0.0", 3);
+    } else if (k <= n && n <= 15) {
+        put(digits, k);
+        for (int i = k; i < n; ++i) *out++ = '0';
+        put(".0", 2);
     } else if (0 < n && n <= 15) {
-        out += digits.substr(0, (size_t)n) + "." + digits.substr((size_t)n);
+        put(digits, n);
+        *out++ = '.';
+        put(digits + n, k - n);
     } else if (-4 < n && n <= 0) {
-        out += "0." + std::string((size_t)(-n), '0') + digits;
+        put("0.", 2);
+        for (int i = 0; i < -n; ++i) *out++ = '0';
+        put(digits, k);
     } else {
-        out += digits.substr(0, 1);
-        if (k > 1) out += "." + digits.substr(1);
+        *out++ = digits[0];
+        if (k > 1) {
+            *out++ = '.';
+            put(digits + 1, k - 1);
+        }
         const int ex = n - 1;
-        out += ex < 0 ? "e-" : "e+";
+        *out++ = 'e';
+        *out++ = ex < 0 ? '-' : '+';
         const int a = ex < 0 ? -ex : ex;
-        if (a < 10) out.push_back('0');
-        out += std::to_string(a);
+        if (a < 10) *out++ = '0';
+        out = std::to_chars(out, out + 4, a).ptr;
     }
     return out;
 }
+
+inline std::string json_double(double x) {
+    char buf[kJsonDoubleMax];
+    return std::string(buf, json_double_to(buf, x));
+}
+
+// JSON text under construction: numbers formatted in place, without stream state or temporaries
+struct JsonBuf {
+    std::string s;
+    void c(char ch) { s.push_back(ch); }
+    void str(const char* p) { s.append(p); }
+    void str(const std::string& p) { s.append(p); }
+    void u(uint64_t v) {
+        char b[24];
+        s.append(b, std::to_chars(b, b + sizeof(b), v).ptr);
+    }
+    void d(double x) {
+        char b[kJsonDoubleMax];
+        s.append(b, json_double_to(b, x));
+    }
+};
 
 }  // namespace ria_host

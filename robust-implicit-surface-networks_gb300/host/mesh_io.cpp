@@ -1,11 +1,15 @@
 // CPU half of the host layer: configuration, tet-mesh and function-file readers, the tet grid,
 // mesh connectivity (edges, patches, chains) and the JSON writers.  Needs no GPU.
+#include <algorithm>
+#include <atomic>
 #include <cmath>
+#include <cstdio>
 #include <fstream>
 #include <iostream>
 #include <map>
 #include <queue>
 #include <sstream>
+#include <thread>
 
 #include "json.hpp"
 #include "ria_host.hpp"
@@ -40,83 +44,147 @@ std::array<double, 3> unit(const Json& a) {
 }
 
 template <class V>
-void put_list(std::ostringstream& o, const V& v) {
-    o << '[';
-    for (size_t i = 0; i < v.size(); ++i) o << (i ? "," : "") << v[i];
-    o << ']';
+void put_list(JsonBuf& o, const V& v) {
+    o.c('[');
+    for (size_t i = 0; i < v.size(); ++i) {
+        if (i) o.c(',');
+        o.u(v[i]);
+    }
+    o.c(']');
 }
 
-void put_lists(std::ostringstream& o, const std::vector<std::vector<size_t>>& v) {
-    if (v.empty()) {
-        o << "null";
-        return;
+// A JSON document written in order from pieces.  The large arrays (points, faces, edges) are
+// formatted in chunks by several threads, each chunk its own piece.
+struct JsonDoc {
+    std::vector<std::string> parts;
+    JsonBuf cur;
+
+    void flush() {
+        if (!cur.s.empty()) parts.push_back(std::move(cur.s));
+        cur.s = std::string();
     }
-    o << '[';
-    for (size_t i = 0; i < v.size(); ++i) {
-        if (i) o << ',';
-        put_list(o, v[i]);
+    // "null" when n is 0, else [item0,item1,...]; emit(buf, i) writes item i and may run on any thread
+    template <class Emit>
+    void array(size_t n, const Emit& emit) {
+        if (n == 0) {
+            cur.str("null");
+            return;
+        }
+        cur.c('[');
+        constexpr size_t kChunk = 1 << 15;
+        const unsigned hw = std::thread::hardware_concurrency();
+        const size_t threads = std::min<size_t>(hw ? hw : 1, 32);
+        if (threads < 2 || n < 2 * kChunk) {
+            for (size_t i = 0; i < n; ++i) {
+                if (i) cur.c(',');
+                emit(cur, i);
+            }
+        } else {
+            flush();
+            const size_t chunks = std::min(n / kChunk, 4 * threads);
+            std::vector<std::string> out(chunks);
+            std::atomic<size_t> next{0};
+            auto work = [&] {
+                for (size_t c; (c = next.fetch_add(1)) < chunks;) {
+                    JsonBuf b;
+                    const size_t lo = n * c / chunks, hi = n * (c + 1) / chunks;
+                    for (size_t i = lo; i < hi; ++i) {
+                        if (i) b.c(',');
+                        emit(b, i);
+                    }
+                    out[c] = std::move(b.s);
+                }
+            };
+            std::vector<std::thread> pool;
+            for (size_t t = 1; t < std::min(threads, chunks); ++t) pool.emplace_back(work);
+            work();
+            for (auto& t : pool) t.join();
+            for (auto& piece : out) parts.push_back(std::move(piece));
+        }
+        cur.c(']');
     }
-    o << ']';
+    bool write(const std::string& filename) {
+        flush();
+        FILE* f = std::fopen(filename.c_str(), "wb");
+        if (!f) return false;
+        bool ok = true;
+        for (const auto& piece : parts) ok = ok && std::fwrite(piece.data(), 1, piece.size(), f) == piece.size();
+        return std::fclose(f) == 0 && ok;
+    }
+};
+
+void put_lists(JsonDoc& o, const std::vector<std::vector<size_t>>& v) {
+    o.array(v.size(), [&](JsonBuf& b, size_t i) { put_list(b, v[i]); });
+}
+
+void put_corners(JsonDoc& o, const std::vector<std::vector<size_t>>& nm_edges_of_vert) {
+    std::vector<size_t> corners;
+    for (size_t i = 0; i < nm_edges_of_vert.size(); ++i)
+        if (nm_edges_of_vert[i].size() > 2 || nm_edges_of_vert[i].size() == 1) corners.push_back(i);
+    if (corners.empty())
+        o.cur.str("null");
+    else
+        put_list(o.cur, corners);
+}
+
+void put_edges(JsonDoc& o, const std::vector<Edge>& edges) {
+    o.array(edges.size(), [&](JsonBuf& b, size_t i) {
+        b.c('[');
+        b.u(edges[i].v1);
+        b.c(',');
+        b.u(edges[i].v2);
+        b.c(']');
+    });
+}
+
+void put_faces(JsonDoc& o, const std::vector<PolygonFace>& faces) {
+    o.array(faces.size(), [&](JsonBuf& b, size_t i) { put_list(b, faces[i].vert_indices); });
+}
+
+void put_points(JsonDoc& o, const std::vector<std::array<double, 3>>& pts) {
+    o.array(pts.size(), [&](JsonBuf& b, size_t i) {
+        b.c('[');
+        b.d(pts[i][0]);
+        b.c(',');
+        b.d(pts[i][1]);
+        b.c(',');
+        b.d(pts[i][2]);
+        b.c(']');
+    });
 }
 
 // the keys of the reference's mesh.json, in its library's (sorted) key order; a list the reference
 // never appends to stays null, as there
-void write_mesh_json(const std::string& filename, const std::vector<std::array<double, 3>>& pts,
+bool write_mesh_json(const std::string& filename, const std::vector<std::array<double, 3>>& pts,
                      const std::vector<PolygonFace>& faces, const std::vector<std::vector<size_t>>& patches,
                      const std::string& patches_label, const std::vector<Edge>& edges,
                      const std::vector<std::vector<size_t>>& chains,
                      const std::vector<std::vector<size_t>>& nm_edges_of_vert,
                      const std::vector<std::vector<size_t>>& shells, const std::vector<std::vector<size_t>>& cells,
                      const std::string& cells_label) {
-    std::ostringstream o;
-    o << "{\"cells\":";
+    JsonDoc o;
+    o.cur.str("{\"cells\":");
     put_lists(o, cells);
-    o << ",\"cells_label\":" << cells_label << ",\"chains\":";
+    o.cur.str(",\"cells_label\":");
+    o.cur.str(cells_label);
+    o.cur.str(",\"chains\":");
     put_lists(o, chains);
-    std::vector<size_t> corners;
-    for (size_t i = 0; i < nm_edges_of_vert.size(); ++i)
-        if (nm_edges_of_vert[i].size() > 2 || nm_edges_of_vert[i].size() == 1) corners.push_back(i);
-    o << ",\"corners\":";
-    if (corners.empty())
-        o << "null";
-    else
-        put_list(o, corners);
-    o << ",\"edges\":";
-    if (edges.empty()) {
-        o << "null";
-    } else {
-        o << '[';
-        for (size_t i = 0; i < edges.size(); ++i) o << (i ? "," : "") << '[' << edges[i].v1 << ',' << edges[i].v2 << ']';
-        o << ']';
-    }
-    o << ",\"faces\":";
-    if (faces.empty()) {
-        o << "null";
-    } else {
-        o << '[';
-        for (size_t i = 0; i < faces.size(); ++i) {
-            if (i) o << ',';
-            put_list(o, faces[i].vert_indices);
-        }
-        o << ']';
-    }
-    o << ",\"patches\":";
+    o.cur.str(",\"corners\":");
+    put_corners(o, nm_edges_of_vert);
+    o.cur.str(",\"edges\":");
+    put_edges(o, edges);
+    o.cur.str(",\"faces\":");
+    put_faces(o, faces);
+    o.cur.str(",\"patches\":");
     put_lists(o, patches);
-    o << ",\"patches_label\":" << patches_label << ",\"points\":";
-    if (pts.empty()) {
-        o << "null";
-    } else {
-        o << '[';
-        for (size_t i = 0; i < pts.size(); ++i)
-            o << (i ? "," : "") << '[' << json_double(pts[i][0]) << ',' << json_double(pts[i][1]) << ','
-              << json_double(pts[i][2]) << ']';
-        o << ']';
-    }
-    o << ",\"shells\":";
+    o.cur.str(",\"patches_label\":");
+    o.cur.str(patches_label);
+    o.cur.str(",\"points\":");
+    put_points(o, pts);
+    o.cur.str(",\"shells\":");
     put_lists(o, shells);
-    o << "}\n";
-    std::ofstream f(filename);
-    f << o.str();
+    o.cur.str("}\n");
+    return o.write(filename);
 }
 
 }  // namespace
@@ -245,10 +313,61 @@ bool load_functions(const std::string& filename, std::vector<ria_function>& func
     return true;
 }
 
+// src/mesh_connectivity.cpp:10-56: edges numbered by first occurrence in face order, each with its
+// (face, local edge) occurrences in that order.  An edge is found among the edges already seen at
+// its smaller vertex: those lists are laid out by vertex (counted in a first pass) and stay short,
+// and vertices numbered in face order keep the accesses local.  Ids past 32 bits take an ordered map.
 void compute_mesh_edges(const std::vector<PolygonFace>& mesh_faces, std::vector<std::vector<size_t>>& edges_of_face,
                         std::vector<Edge>& mesh_edges) {
-    std::map<std::pair<size_t, size_t>, size_t> edge_id;
+    size_t n_occ = 0, vmax = 0;
+    for (const auto& f : mesh_faces) {
+        n_occ += f.vert_indices.size();
+        for (size_t v : f.vert_indices) vmax = v > vmax ? v : vmax;
+    }
     edges_of_face.assign(mesh_faces.size(), {});
+    mesh_edges.reserve(mesh_edges.size() + n_occ / 2 + 16);  // interior edges are shared by two faces
+    auto add = [&](size_t i, size_t j, size_t v1, size_t v2, size_t id) {
+        if (id == mesh_edges.size()) {
+            mesh_edges.push_back(Edge{v1, v2, {}});
+            mesh_edges.back().face_edge_indices.reserve(2);
+        }
+        mesh_edges[id].face_edge_indices.emplace_back(i, j);
+        edges_of_face[i][j] = id;
+    };
+    if (vmax < 0xFFFFFFFFull && mesh_edges.size() + n_occ < 0xFFFFFFFFull) {
+        // first[v]..first[v+1]: room for every occurrence whose smaller vertex is v
+        std::vector<uint32_t> first(vmax + 2, 0), used(vmax + 1, 0);
+        for (const auto& f : mesh_faces) {
+            const auto& vs = f.vert_indices;
+            for (size_t j = 0; j < vs.size(); ++j) {
+                const size_t a = vs[j], b = vs[(j + 1) % vs.size()];
+                ++first[(a < b ? a : b) + 1];
+            }
+        }
+        for (size_t v = 0; v <= vmax; ++v) first[v + 1] += first[v];
+        std::vector<uint64_t> seen(n_occ);  // (larger vertex << 32) | edge id
+        for (size_t i = 0; i < mesh_faces.size(); ++i) {
+            const auto& vs = mesh_faces[i].vert_indices;
+            const size_t n = vs.size();
+            edges_of_face[i].resize(n);
+            for (size_t j = 0; j < n; ++j) {
+                size_t v1 = vs[j], v2 = vs[(j + 1) % n];
+                if (v1 > v2) std::swap(v1, v2);
+                uint64_t* list = seen.data() + first[v1];
+                const uint32_t m = used[v1];
+                size_t id = mesh_edges.size();
+                for (uint32_t t = 0; t < m; ++t)
+                    if ((list[t] >> 32) == v2) {
+                        id = (size_t)(list[t] & 0xFFFFFFFFull);
+                        break;
+                    }
+                if (id == mesh_edges.size()) list[used[v1]++] = ((uint64_t)v2 << 32) | (uint64_t)id;
+                add(i, j, v1, v2, id);
+            }
+        }
+        return;
+    }
+    std::map<std::pair<size_t, size_t>, size_t> edge_id;
     for (size_t i = 0; i < mesh_faces.size(); ++i) {
         const auto& vs = mesh_faces[i].vert_indices;
         const size_t n = vs.size();
@@ -257,11 +376,7 @@ void compute_mesh_edges(const std::vector<PolygonFace>& mesh_faces, std::vector<
             size_t v1 = vs[j], v2 = vs[(j + 1) % n];
             if (v1 > v2) std::swap(v1, v2);
             auto ins = edge_id.emplace(std::make_pair(v1, v2), mesh_edges.size());
-            if (ins.second) {
-                mesh_edges.push_back(Edge{v1, v2, {}});
-            }
-            mesh_edges[ins.first->second].face_edge_indices.emplace_back(i, j);
-            edges_of_face[i][j] = ins.first->second;
+            add(i, j, v1, v2, ins.first->second);
         }
     }
 }
@@ -330,26 +445,28 @@ bool save_result(const std::string& filename, const std::vector<std::array<doubl
                  const std::vector<std::vector<size_t>>& non_manifold_edges_of_vert,
                  const std::vector<std::vector<size_t>>& shells, const std::vector<std::vector<size_t>>& cells,
                  const std::vector<std::vector<bool>>& cell_function_label) {
-    std::ostringstream pl;
-    pl << '[';
+    JsonBuf pl;
+    pl.c('[');
     put_list(pl, patch_function_label);
-    pl << ']';
-    std::ostringstream cl;
+    pl.c(']');
+    JsonBuf cl;
     if (cell_function_label.empty()) {
-        cl << "null";
+        cl.str("null");
     } else {
-        cl << '[';
+        cl.c('[');
         for (size_t i = 0; i < cell_function_label.size(); ++i) {
-            cl << (i ? "," : "") << '[';
-            for (size_t j = 0; j < cell_function_label[i].size(); ++j)
-                cl << (j ? "," : "") << (cell_function_label[i][j] ? "true" : "false");
-            cl << ']';
+            if (i) cl.c(',');
+            cl.c('[');
+            for (size_t j = 0; j < cell_function_label[i].size(); ++j) {
+                if (j) cl.c(',');
+                cl.str(cell_function_label[i][j] ? "true" : "false");
+            }
+            cl.c(']');
         }
-        cl << ']';
+        cl.c(']');
     }
-    write_mesh_json(filename, mesh_pts, mesh_faces, patches, pl.str(), edges, chains, non_manifold_edges_of_vert, shells,
-                    cells, cl.str());
-    return true;
+    return write_mesh_json(filename, mesh_pts, mesh_faces, patches, pl.s, edges, chains, non_manifold_edges_of_vert,
+                           shells, cells, cl.s);
 }
 
 bool save_result_MI(const std::string& filename, const std::vector<std::array<double, 3>>& mesh_pts,
@@ -359,18 +476,23 @@ bool save_result_MI(const std::string& filename, const std::vector<std::array<do
                     const std::vector<std::vector<size_t>>& non_manifold_edges_of_vert,
                     const std::vector<std::vector<size_t>>& shells, const std::vector<std::vector<size_t>>& cells,
                     const std::vector<size_t>& cell_function_label) {
-    std::ostringstream pl;
-    pl << "[[";
-    for (size_t i = 0; i < patch_function_label.size(); ++i)
-        pl << (i ? "," : "") << '[' << patch_function_label[i].first << ',' << patch_function_label[i].second << ']';
-    pl << "]]";
-    std::ostringstream cl;
-    cl << '[';
+    JsonBuf pl;
+    pl.str("[[");
+    for (size_t i = 0; i < patch_function_label.size(); ++i) {
+        if (i) pl.c(',');
+        pl.c('[');
+        pl.u(patch_function_label[i].first);
+        pl.c(',');
+        pl.u(patch_function_label[i].second);
+        pl.c(']');
+    }
+    pl.str("]]");
+    JsonBuf cl;
+    cl.c('[');
     put_list(cl, cell_function_label);
-    cl << ']';
-    write_mesh_json(filename, mesh_pts, mesh_faces, patches, pl.str(), edges, chains, non_manifold_edges_of_vert, shells,
-                    cells, cl.str());
-    return true;
+    cl.c(']');
+    return write_mesh_json(filename, mesh_pts, mesh_faces, patches, pl.s, edges, chains, non_manifold_edges_of_vert,
+                           shells, cells, cl.s);
 }
 
 bool save_timings(const std::string& filename, const std::vector<std::string>& labels, const std::vector<double>& t) {
@@ -407,54 +529,26 @@ bool save_result_CSG(const std::string& filename, const std::vector<std::array<d
                      const std::vector<std::vector<size_t>>& chains,
                      const std::vector<std::vector<size_t>>& nm_edges_of_vert) {
     // src/io.cpp:314-372: no shells, cells or cell labels
-    std::ostringstream o;
-    o << "{\"chains\":";
+    JsonDoc o;
+    o.cur.str("{\"chains\":");
     put_lists(o, chains);
-    std::vector<size_t> corners;
-    for (size_t i = 0; i < nm_edges_of_vert.size(); ++i)
-        if (nm_edges_of_vert[i].size() > 2 || nm_edges_of_vert[i].size() == 1) corners.push_back(i);
-    o << ",\"corners\":";
-    if (corners.empty())
-        o << "null";
-    else
-        put_list(o, corners);
-    o << ",\"edges\":";
-    if (edges.empty()) {
-        o << "null";
-    } else {
-        o << '[';
-        for (size_t i = 0; i < edges.size(); ++i) o << (i ? "," : "") << '[' << edges[i].v1 << ',' << edges[i].v2 << ']';
-        o << ']';
-    }
-    o << ",\"faces\":";
-    if (faces.empty()) {
-        o << "null";
-    } else {
-        o << '[';
-        for (size_t i = 0; i < faces.size(); ++i) {
-            if (i) o << ',';
-            put_list(o, faces[i].vert_indices);
-        }
-        o << ']';
-    }
-    o << ",\"patches\":";
+    o.cur.str(",\"corners\":");
+    put_corners(o, nm_edges_of_vert);
+    o.cur.str(",\"edges\":");
+    put_edges(o, edges);
+    o.cur.str(",\"faces\":");
+    put_faces(o, faces);
+    o.cur.str(",\"patches\":");
     put_lists(o, patches);
-    o << ",\"patches_label\":[[";
-    for (size_t i = 0; i < patch_sign_label.size(); ++i) o << (i ? "," : "") << (patch_sign_label[i] ? "true" : "false");
-    o << "]],\"points\":";
-    if (pts.empty()) {
-        o << "null";
-    } else {
-        o << '[';
-        for (size_t i = 0; i < pts.size(); ++i)
-            o << (i ? "," : "") << '[' << json_double(pts[i][0]) << ',' << json_double(pts[i][1]) << ','
-              << json_double(pts[i][2]) << ']';
-        o << ']';
+    o.cur.str(",\"patches_label\":[[");
+    for (size_t i = 0; i < patch_sign_label.size(); ++i) {
+        if (i) o.cur.c(',');
+        o.cur.str(patch_sign_label[i] ? "true" : "false");
     }
-    o << "}\n";
-    std::ofstream f(filename);
-    f << o.str();
-    return true;
+    o.cur.str("]],\"points\":");
+    put_points(o, pts);
+    o.cur.str("}\n");
+    return o.write(filename);
 }
 
 bool load_csg_tree(const std::string& filename, std::vector<CsgUnit>& tree) {

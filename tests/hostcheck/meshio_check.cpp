@@ -107,7 +107,12 @@ int main(int argc, char** argv) {
                     nm[edges[i].v2].push_back(i);
                 }
             compute_chains(edges, nm, chains);
-            if (mi) {
+            if (!strcmp(argv[2], "csg")) {
+                // CSG writer: patch i labelled inside when i % 3 == 0
+                std::vector<bool> signs(patches.size());
+                for (size_t i = 0; i < signs.size(); ++i) signs[i] = i % 3 == 0;
+                if (!save_result_CSG(argv[4], pts, faces, patches, signs, edges, chains, nm)) return 4;
+            } else if (mi) {
                 std::vector<size_t> cell_label;
                 save_result_MI(argv[4], pts, faces, patches, labels, edges, chains, nm, shells, cells, cell_label);
             } else {

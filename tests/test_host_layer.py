@@ -165,6 +165,44 @@ def test_mesh_json_writer_degenerate(check, fns, oracle, tmp_path):
     assert out.read_text() == meshjson.dump(exp) + "\n"
 
 
+def test_mesh_json_writer_large_parallel(check, fns, oracle, tmp_path):
+    """A mesh large enough that points, faces and edges are formatted in parallel chunks (over 65,536
+    of each): the same bytes as the serial restatement, and the same edges, patches and chains as
+    the oracle's connectivity."""
+    wl = fns.workload_ia_degenerate(res=48)
+    pts, tets = fns.generate_tet_mesh(wl.res)
+    fv = oracle.sample(wl.funcs, pts, threads=4)
+    ref = oracle.run("ia", pts, tets, fv, threads=4, connectivity=True)
+    assert len(ref["xyz"]) > 65536 and len(ref["face_offsets"]) - 1 > 65536
+    inp = tmp_path / "in.bin"
+    meshjson.write_mesh_input(inp, ref)
+    out = tmp_path / "mesh.json"
+    _run("mesh", "ia", inp, out)
+    exp = meshjson.expected_mesh_json(ref, "ia")
+    assert len(exp["edges"]) > 65536
+    assert out.read_text() == meshjson.dump(exp) + "\n"
+
+
+@pytest.mark.parametrize("res", [12, 48])
+def test_csg_writer(check, fns, oracle, tmp_path, res):
+    """save_result_CSG (src/io.cpp:314-372): the IA document's shared lists without shells and cells,
+    patch labels as booleans; at res 48 its large arrays take the parallel path."""
+    wl = fns.workload_ia_degenerate(res=res)
+    pts, tets = fns.generate_tet_mesh(wl.res)
+    fv = oracle.sample(wl.funcs, pts, threads=4)
+    ref = oracle.run("ia", pts, tets, fv, threads=4, connectivity=True)
+    inp = tmp_path / "in.bin"
+    meshjson.write_mesh_input(inp, ref)
+    out = tmp_path / "mesh.json"
+    _run("mesh", "csg", inp, out)
+    ia = meshjson.expected_mesh_json(ref, "ia")
+    n_patches = len(ia["patches"] or [])
+    exp = {k: ia[k] for k in ("chains", "corners", "edges", "faces", "patches")}
+    exp["patches_label"] = [[i % 3 == 0 for i in range(n_patches)]]
+    exp["points"] = ia["points"]
+    assert out.read_text() == meshjson.dump(exp) + "\n"
+
+
 def test_mesh_json_writer_empty(check, tmp_path):
     inp = tmp_path / "in.bin"
     with open(inp, "wb") as f:
@@ -175,3 +213,11 @@ def test_mesh_json_writer_empty(check, tmp_path):
                                '"faces":null,"patches":null,"patches_label":[[]],"points":null,"shells":null}\n')
     _run("mesh", "mi", inp, out)
     assert '"patches_label":[[]]' in out.read_text() and '"cells_label":[[]]' in out.read_text()
+
+
+def test_writer_reports_unwritable_path(check, tmp_path):
+    inp = tmp_path / "in.bin"
+    with open(inp, "wb") as f:
+        f.write(struct.pack("<q", 0) + struct.pack("<qq", 1, 0) + struct.pack("<q", 0) + struct.pack("<q", 0))
+    r = subprocess.run([CHECK, "mesh", "csg", str(inp), str(tmp_path / "missing" / "mesh.json")], capture_output=True)
+    assert r.returncode == 4
