@@ -31,7 +31,8 @@ void fetch_faces(const DeviceMesh& dm, std::vector<PolygonFace>& faces) {
     auto to = dm.i64(RIA_MESH_FACE_TET_OFFSETS), tf = dm.i64(RIA_MESH_FACE_TETS), fn = dm.i64(RIA_MESH_FACE_FUNC);
     faces.assign(fo.empty() ? 0 : fo.size() - 1, PolygonFace());
     for (size_t f = 0; f < faces.size(); ++f) {
-        for (int64_t i = fo[f]; i < fo[f + 1]; ++i) faces[f].vert_indices.push_back((size_t)fv[i]);
+        faces[f].vert_indices.assign(fv.begin() + fo[f], fv.begin() + fo[f + 1]);
+        faces[f].tet_face_indices.reserve((size_t)(to[f + 1] - to[f]));
         for (int64_t t = to[f]; t < to[f + 1]; ++t) faces[f].tet_face_indices.emplace_back(tf[2 * t], tf[2 * t + 1]);
         faces[f].func_index = {none_or(fn[2 * f]), none_or(fn[2 * f + 1])};
     }
