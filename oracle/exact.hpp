@@ -11,6 +11,7 @@
 // Only tests/, the smoke check and bench.py's CPU baseline use this code.
 #pragma once
 #include <cmath>
+#include <cstdlib>
 #include <cstdint>
 #include <vector>
 
@@ -181,6 +182,7 @@ struct VCache {
 // Build the cache from explicit rows over free corners.  `rows` holds m rows of 4 corner values;
 // for MI the trailing 1 column is appended here.
 inline void vcache_build(VCache& c, bool mi, int s, const int* S, int m, const double* const* rows) {
+    if (s < 1 || s > 4 || m < 0 || m > 4) std::abort();  // a vertex of a tet: at most 4 corners and rows
     c.mi = mi;
     c.s = s;
     c.m = m;
