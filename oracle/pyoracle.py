@@ -13,7 +13,8 @@ import subprocess
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "_build", "libria_oracle.so")
+# RIA_ORACLE_LIB: another build of the same sources (the sanitizer build of `make sanitize`)
+LIB_PATH = os.environ.get("RIA_ORACLE_LIB") or os.path.join(HERE, "_build", "libria_oracle.so")
 
 _lib = None
 

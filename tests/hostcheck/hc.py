@@ -6,7 +6,8 @@ import subprocess
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB = os.path.join(HERE, "_build", "libhostcheck.so")
+# RIA_HOSTCHECK_LIB: another build of the same sources (the sanitizer build of `make sanitize`)
+LIB = os.environ.get("RIA_HOSTCHECK_LIB") or os.path.join(HERE, "_build", "libhostcheck.so")
 _lib = None
 
 

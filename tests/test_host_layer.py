@@ -11,7 +11,8 @@ import pytest
 import meshjson
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-CHECK = os.path.join(HERE, "hostcheck", "_build", "meshio_check")
+# RIA_MESHIO_CHECK: another build of the same sources (the sanitizer builds of `make sanitize`)
+CHECK = os.environ.get("RIA_MESHIO_CHECK") or os.path.join(HERE, "hostcheck", "_build", "meshio_check")
 
 
 @pytest.fixture(scope="module")
