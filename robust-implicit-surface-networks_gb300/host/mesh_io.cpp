@@ -2,6 +2,7 @@
 // mesh connectivity (edges, patches, chains) and the JSON writers.  Needs no GPU.
 #include <algorithm>
 #include <atomic>
+#include <charconv>
 #include <cmath>
 #include <cstdio>
 #include <fstream>
@@ -19,11 +20,14 @@ namespace ria_host {
 namespace {
 
 std::string read_file(const std::string& path) {
-    std::ifstream f(path);
+    std::ifstream f(path, std::ios::binary);
     if (!f) throw std::runtime_error("cannot open " + path);
-    std::stringstream ss;
-    ss << f.rdbuf();
-    return ss.str();
+    f.seekg(0, std::ios::end);
+    const std::streamoff n = f.tellg();
+    f.seekg(0, std::ios::beg);
+    std::string s(n > 0 ? (size_t)n : 0, '\0');
+    if (n > 0 && !f.read(&s[0], n)) throw std::runtime_error("cannot read " + path);
+    return s;
 }
 
 std::string dir_of(const std::string& path) {
@@ -41,6 +45,66 @@ std::array<double, 3> unit(const Json& a) {
     double n = std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
     if (n == 0.0) throw std::runtime_error("zero axis vector");
     return {v[0] / n, v[1] / n, v[2] / n};
+}
+
+// The tet-mesh file [[[x, y, z], ...], [[v0, v1, v2, v3], ...]] read straight into the outputs:
+// numbers by from_chars, no document tree.  Returns false at anything else (another layout,
+// malformed text), which the general parser then reads or reports.
+bool read_tet_mesh_fast(const std::string& text, std::vector<std::array<double, 3>>& pts,
+                        std::vector<std::array<size_t, 4>>& tets) {
+    const char* p = text.data();
+    const char* const end = p + text.size();
+    auto ws = [&] {
+        while (p < end && (*p == ' ' || *p == '\n' || *p == '\r' || *p == '\t')) ++p;
+    };
+    auto lit = [&](char c) {
+        ws();
+        if (p >= end || *p != c) return false;
+        ++p;
+        return true;
+    };
+    auto num = [&](double& v) {
+        ws();
+        const char* q = p;
+        while (q < end && ((*q >= '0' && *q <= '9') || *q == '-' || *q == '+' || *q == '.' || *q == 'e' || *q == 'E'))
+            ++q;
+        if (q == p || std::from_chars(p, q, v).ptr != q) return false;
+        p = q;
+        return true;
+    };
+    // a list of rows of `width` numbers; `put(row)` stores one
+    auto rows = [&](int width, auto&& put) {
+        if (!lit('[')) return false;
+        ws();
+        if (p < end && *p == ']') {
+            ++p;
+            return true;
+        }
+        for (;;) {
+            double row[4];
+            if (!lit('[')) return false;
+            for (int k = 0; k < width; ++k)
+                if ((k && !lit(',')) || !num(row[k])) return false;
+            if (!lit(']')) return false;
+            put(row);
+            if (lit(',')) continue;
+            return lit(']');
+        }
+    };
+    std::vector<std::array<double, 3>> P;
+    std::vector<std::array<size_t, 4>> T;
+    P.reserve(text.size() / 64);
+    T.reserve(text.size() / 64);
+    const bool ok = lit('[') && rows(3, [&](const double* r) { P.push_back({r[0], r[1], r[2]}); }) && lit(',') &&
+                    rows(4, [&](const double* r) {
+                        T.push_back({(size_t)r[0], (size_t)r[1], (size_t)r[2], (size_t)r[3]});
+                    }) &&
+                    lit(']');
+    ws();
+    if (!ok || p != end) return false;
+    pts.swap(P);
+    tets.swap(T);
+    return true;
 }
 
 template <class V>
@@ -220,7 +284,9 @@ bool load_tet_mesh(const std::string& filename, std::vector<std::array<double, 3
         std::cout << "tet mesh file not exist!" << std::endl;
         return false;
     }
-    Json d = JsonParser(read_file(filename)).parse();
+    const std::string text = read_file(filename);
+    if (read_tet_mesh_fast(text, pts, tets)) return true;
+    Json d = JsonParser(text).parse();
     pts.resize(d[0].size());
     for (size_t j = 0; j < pts.size(); ++j)
         for (int k = 0; k < 3; ++k) pts[j][k] = d[0][j][k].as_double();

@@ -47,6 +47,31 @@ def test_tet_mesh_reader(check, tmp_path):
     assert np.array_equal(p2, pts) and np.array_equal(t2, tets)
 
 
+@pytest.mark.parametrize("layout", ["compact", "indented", "extra_values", "float_indices"])
+def test_tet_mesh_reader_layouts(check, fns, tmp_path, layout):
+    """The streaming reader (compact or indented text) and the general parser it falls back to
+    (rows with extra values, indices written as floats) give the same mesh."""
+    pts, tets = fns.generate_tet_mesh(6, (-0.3, 0.1, -2.5), (1.7, 0.45, 3.0))
+    P, T = pts.tolist(), tets.tolist()
+    if layout == "extra_values":
+        P = [p + [9.0] for p in P]
+    if layout == "float_indices":
+        T = [[float(v) for v in t] for t in T]
+    f = tmp_path / "m.json"
+    f.write_text(json.dumps([P, T], indent=2 if layout == "indented" else None))
+    out = tmp_path / "m.bin"
+    _run("tetmesh", f, out)
+    p2, t2 = meshjson.read_grid(out)
+    assert np.array_equal(p2, pts) and np.array_equal(t2, tets)
+
+
+def test_tet_mesh_reader_rejects_truncated_file(check, tmp_path):
+    f = tmp_path / "m.json"
+    f.write_text("[[[0.0, 0.0, 0.0], [1.0, 0.0, 0.0]], [[0, 1, 0")
+    r = subprocess.run([CHECK, "tetmesh", str(f), str(tmp_path / "m.bin")], capture_output=True, text=True)
+    assert r.returncode == 3 and "JSON parse error" in r.stderr
+
+
 def test_function_reader_matches(check, fns, tmp_path):
     files = sorted(os.listdir(os.path.join(HERE, "golden", "functions")))
     specs = [json.load(open(os.path.join(HERE, "golden", "functions", n))) for n in files]
