@@ -378,3 +378,39 @@ def test_sampler_square_root_is_correctly_rounded(hc):
         out = hc.sqrt_rn(v, perturb)
         same = (out.view(np.uint64) == ref.view(np.uint64)) | (np.isnan(out) & np.isnan(ref))
         assert same.all(), (perturb, v[~same][:4])
+
+
+def _stress_fixtures(per_noise=1):
+    """The near-degenerate robustness sets (tests/golden/stress): the first instances of every noise
+    level of both modes."""
+    import json
+    import os
+
+    d = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "stress")
+    seen, out = {}, []
+    for e in json.load(open(os.path.join(d, "manifest.json"))):
+        key = (e["mode"], e["noise"])
+        if seen.get(key, 0) < per_noise:
+            seen[key] = seen.get(key, 0) + 1
+            out.append((e, json.load(open(os.path.join(d, e["file"])))))
+    return out
+
+
+def test_device_cut_logic_on_stress_sets(hc, oracle, fns):
+    """Active tets of the robustness sets (four spheres, or spheres and a zero function, whose
+    centres differ by 1e-7 to 1e-6, on a 99^3-cube grid): every variant of the device cut either
+    defers or reproduces the oracle's record."""
+    rng = np.random.default_rng(18)
+    for e, specs in _stress_fixtures():
+        funcs = fns.make_functions(specs)
+        pts, tets = fns.generate_tet_mesh(e["resolution"])
+        fv = oracle.sample(funcs, pts, threads=4)
+        r = oracle.run(e["mode"], pts, tets, fv, threads=4)
+        si, fit = r["start_index"], r["func_in_tet"]
+        active = np.flatnonzero(np.diff(si) > 0)
+        for t in rng.choice(active, size=min(120, len(active)), replace=False):
+            rows = fv[tets[t]][:, fit[si[t]:si[t + 1]]].T.copy()
+            ref = bytes(r["rec_bytes"][r["rec_offsets"][t]:r["rec_offsets"][t + 1]])
+            _agree(hc, oracle, e["mode"], rows)
+            got, _ = hc.cut(e["mode"], rows, True)
+            assert got == ref, (e["file"], int(t))
