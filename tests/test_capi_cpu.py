@@ -414,3 +414,29 @@ def test_device_cut_logic_on_stress_sets(hc, oracle, fns):
             _agree(hc, oracle, e["mode"], rows)
             got, _ = hc.cut(e["mode"], rows, True)
             assert got == ref, (e["file"], int(t))
+
+
+def test_device_cut_logic_on_paper_examples(hc, oracle, fns):
+    """The reference's paper examples (tests/golden/examples): inverse-CSG models of planes,
+    cylinders and tori, and 18 spheres in both modes, on their 99^3-cube grids.  Up to 40 active
+    tets of every active-function count, through every variant of the device cut."""
+    import json
+    import os
+
+    d = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "examples")
+    rng = np.random.default_rng(19)
+    for e in json.load(open(os.path.join(d, "manifest.json"))):
+        funcs = fns.make_functions(json.load(open(os.path.join(d, e["file"]))))
+        pts, tets = fns.generate_tet_mesh(e["resolution"], *e["bbox"])
+        fv = oracle.sample(funcs, pts, threads=4)
+        r = oracle.run(e["mode"], pts, tets, fv, threads=4)
+        si, fit = r["start_index"], r["func_in_tet"]
+        k = np.diff(si)
+        for kk in np.unique(k[k > 0]):
+            pick = np.flatnonzero(k == kk)
+            for t in rng.choice(pick, size=min(40, len(pick)), replace=False):
+                rows = fv[tets[t]][:, fit[si[t]:si[t + 1]]].T.copy()
+                ref = bytes(r["rec_bytes"][r["rec_offsets"][t]:r["rec_offsets"][t + 1]])
+                _agree(hc, oracle, e["mode"], rows)
+                got, _ = hc.cut(e["mode"], rows, True)
+                assert got == ref, (e["file"], int(t))
