@@ -8,7 +8,6 @@
 #include <fstream>
 #include <iostream>
 #include <map>
-#include <queue>
 #include <sstream>
 #include <thread>
 
@@ -455,21 +454,19 @@ void compute_patches(const std::vector<std::vector<size_t>>& edges_of_face, cons
         if (visited[i]) continue;
         patches.emplace_back();
         auto& patch = patches.back();
-        std::queue<size_t> Q;
-        Q.push(i);
         patch.push_back(i);
         visited[i] = 1;
         patch_label.push_back(mesh_faces[i].func_index);
-        while (!Q.empty()) {
-            size_t f = Q.front();
-            Q.pop();
+        // breadth-first: the patch lists faces in the order they are reached, which is the order
+        // they are expanded, so it serves as the queue
+        for (size_t q = 0; q < patch.size(); ++q) {
+            const size_t f = patch[q];
             for (size_t e : edges_of_face[f]) {
                 const auto& fe = mesh_edges[e].face_edge_indices;
                 if (fe.size() != 2) continue;
                 size_t o = fe[0].first == f ? fe[1].first : fe[0].first;
                 if (!visited[o]) {
                     visited[o] = 1;
-                    Q.push(o);
                     patch.push_back(o);
                 }
             }
@@ -484,19 +481,15 @@ void compute_chains(const std::vector<Edge>& mesh_edges, const std::vector<std::
         if (visited[i] || mesh_edges[i].face_edge_indices.size() <= 2) continue;
         chains.emplace_back();
         auto& chain = chains.back();
-        std::queue<size_t> Q;
-        Q.push(i);
         chain.push_back(i);
         visited[i] = 1;
-        while (!Q.empty()) {
-            size_t e = Q.front();
-            Q.pop();
+        for (size_t q = 0; q < chain.size(); ++q) {  // breadth-first, the chain as the queue
+            const size_t e = chain[q];
             for (size_t v : {mesh_edges[e].v1, mesh_edges[e].v2}) {
                 if (nm_edges_of_vert[v].size() != 2) continue;
                 size_t o = nm_edges_of_vert[v][0] == e ? nm_edges_of_vert[v][1] : nm_edges_of_vert[v][0];
                 if (!visited[o]) {
                     visited[o] = 1;
-                    Q.push(o);
                     chain.push_back(o);
                 }
             }
