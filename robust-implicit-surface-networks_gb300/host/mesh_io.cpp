@@ -250,6 +250,108 @@ bool write_mesh_json(const std::string& filename, const std::vector<std::array<d
     return o.write(filename);
 }
 
+size_t host_threads() {
+    const unsigned hw = std::thread::hardware_concurrency();
+    return std::min<size_t>(hw ? hw : 1, 32);
+}
+
+// f(lo, hi) over [0, n) in contiguous chunks of at least `grain`, on up to host_threads() threads
+template <class F>
+void parallel_ranges(size_t n, size_t grain, const F& f) {
+    const size_t chunks = std::min(host_threads() * 4, (n + grain - 1) / grain);
+    if (chunks <= 1) {
+        if (n) f(size_t(0), n);
+        return;
+    }
+    std::atomic<size_t> next{0};
+    auto work = [&] {
+        for (size_t c; (c = next.fetch_add(1)) < chunks;) f(n * c / chunks, n * (c + 1) / chunks);
+    };
+    std::vector<std::thread> pool;
+    for (size_t t = 1; t < std::min(host_threads(), chunks); ++t) pool.emplace_back(work);
+    work();
+    for (auto& t : pool) t.join();
+}
+
+// compute_mesh_edges for large meshes, on several threads, with the same result: the occurrences
+// (face, local edge) are bucketed by their smaller vertex in occurrence order; within a bucket each
+// occurrence finds the first one of its larger vertex; the first occurrences are numbered by one
+// scan in occurrence order; each edge's occurrences, all in one bucket, are listed in that order.
+void compute_mesh_edges_parallel(const std::vector<PolygonFace>& mesh_faces,
+                                 std::vector<std::vector<size_t>>& edges_of_face, std::vector<Edge>& mesh_edges,
+                                 size_t vmax) {
+    const size_t F = mesh_faces.size();
+    std::vector<size_t> foff(F + 1, 0);
+    for (size_t i = 0; i < F; ++i) foff[i + 1] = foff[i] + mesh_faces[i].vert_indices.size();
+    const size_t n_occ = foff[F];
+    std::vector<uint32_t> lo(n_occ), hi(n_occ), face(n_occ);
+    parallel_ranges(F, 4096, [&](size_t a, size_t b) {
+        for (size_t i = a; i < b; ++i) {
+            const auto& vs = mesh_faces[i].vert_indices;
+            const size_t n = vs.size();
+            for (size_t j = 0; j < n; ++j) {
+                const size_t v1 = vs[j], v2 = vs[(j + 1) % n];
+                lo[foff[i] + j] = (uint32_t)(v1 < v2 ? v1 : v2);
+                hi[foff[i] + j] = (uint32_t)(v1 < v2 ? v2 : v1);
+                face[foff[i] + j] = (uint32_t)i;
+            }
+        }
+    });
+    // buckets by smaller vertex, occurrences in increasing order within each
+    std::vector<uint32_t> boff(vmax + 2, 0);
+    for (size_t o = 0; o < n_occ; ++o) ++boff[lo[o] + 1];
+    for (size_t v = 0; v <= vmax; ++v) boff[v + 1] += boff[v];
+    std::vector<uint32_t> bucket(n_occ);
+    {
+        std::vector<uint32_t> fill(boff.begin(), boff.end() - 1);
+        for (size_t o = 0; o < n_occ; ++o) bucket[fill[lo[o]]++] = (uint32_t)o;
+    }
+    // first occurrence of every occurrence's edge, and how many occurrences each first one heads
+    std::vector<uint32_t> first(n_occ), count(n_occ, 0);
+    parallel_ranges(vmax + 1, 4096, [&](size_t a, size_t b) {
+        for (size_t v = a; v < b; ++v)
+            for (uint32_t x = boff[v]; x < boff[v + 1]; ++x) {
+                const uint32_t o = bucket[x];
+                uint32_t f = o;
+                for (uint32_t y = boff[v]; y < x; ++y)
+                    if (hi[bucket[y]] == hi[o]) {
+                        f = first[bucket[y]];
+                        break;
+                    }
+                first[o] = f;
+                ++count[f];
+            }
+    });
+    // edge ids of the first occurrences, in occurrence order
+    const size_t base = mesh_edges.size();
+    std::vector<uint32_t> eid(n_occ);
+    size_t n_edges = 0;
+    for (size_t o = 0; o < n_occ; ++o)
+        if (first[o] == o) eid[o] = (uint32_t)n_edges++;
+    mesh_edges.resize(base + n_edges);
+    parallel_ranges(vmax + 1, 4096, [&](size_t a, size_t b) {
+        for (size_t v = a; v < b; ++v)
+            for (uint32_t x = boff[v]; x < boff[v + 1]; ++x) {
+                const uint32_t o = bucket[x];
+                Edge& e = mesh_edges[base + eid[first[o]]];
+                if (first[o] == o) {
+                    e.v1 = lo[o];
+                    e.v2 = hi[o];
+                    e.face_edge_indices.reserve(count[o]);
+                }
+                e.face_edge_indices.emplace_back(face[o], o - foff[face[o]]);
+            }
+    });
+    edges_of_face.assign(F, {});
+    parallel_ranges(F, 4096, [&](size_t a, size_t b) {
+        for (size_t i = a; i < b; ++i) {
+            auto& ef = edges_of_face[i];
+            ef.resize(foff[i + 1] - foff[i]);
+            for (size_t j = 0; j < ef.size(); ++j) ef[j] = base + eid[first[foff[i] + j]];
+        }
+    });
+}
+
 }  // namespace
 
 Config parse_config_file(const std::string& filename) {
@@ -388,6 +490,10 @@ void compute_mesh_edges(const std::vector<PolygonFace>& mesh_faces, std::vector<
     for (const auto& f : mesh_faces) {
         n_occ += f.vert_indices.size();
         for (size_t v : f.vert_indices) vmax = v > vmax ? v : vmax;
+    }
+    if (vmax < 0xFFFFFFFFull && n_occ >= (1u << 16) && n_occ < 0xFFFFFFFFull && host_threads() > 1) {
+        compute_mesh_edges_parallel(mesh_faces, edges_of_face, mesh_edges, vmax);
+        return;
     }
     edges_of_face.assign(mesh_faces.size(), {});
     mesh_edges.reserve(mesh_edges.size() + n_occ / 2 + 16);  // interior edges are shared by two faces
