@@ -8,6 +8,7 @@
 #include <fstream>
 #include <iostream>
 #include <map>
+#include <mutex>
 #include <sstream>
 #include <thread>
 
@@ -106,6 +107,29 @@ bool read_tet_mesh_fast(const std::string& text, std::vector<std::array<double, 
     return true;
 }
 
+size_t host_threads() {
+    const unsigned hw = std::thread::hardware_concurrency();
+    return std::min<size_t>(hw ? hw : 1, 32);
+}
+
+// f(lo, hi) over [0, n) in contiguous chunks of at least `grain`, on up to host_threads() threads
+template <class F>
+void parallel_ranges(size_t n, size_t grain, const F& f) {
+    const size_t chunks = std::min(host_threads() * 4, (n + grain - 1) / grain);
+    if (chunks <= 1) {
+        if (n) f(size_t(0), n);
+        return;
+    }
+    std::atomic<size_t> next{0};
+    auto work = [&] {
+        for (size_t c; (c = next.fetch_add(1)) < chunks;) f(n * c / chunks, n * (c + 1) / chunks);
+    };
+    std::vector<std::thread> pool;
+    for (size_t t = 1; t < std::min(host_threads(), chunks); ++t) pool.emplace_back(work);
+    work();
+    for (auto& t : pool) t.join();
+}
+
 template <class V>
 void put_list(JsonBuf& o, const V& v) {
     o.c('[');
@@ -135,34 +159,30 @@ struct JsonDoc {
         }
         cur.c('[');
         constexpr size_t kChunk = 1 << 15;
-        const unsigned hw = std::thread::hardware_concurrency();
-        const size_t threads = std::min<size_t>(hw ? hw : 1, 32);
-        if (threads < 2 || n < 2 * kChunk) {
+        if (host_threads() < 2 || n < 2 * kChunk) {
             for (size_t i = 0; i < n; ++i) {
                 if (i) cur.c(',');
                 emit(cur, i);
             }
         } else {
             flush();
-            const size_t chunks = std::min(n / kChunk, 4 * threads);
-            std::vector<std::string> out(chunks);
-            std::atomic<size_t> next{0};
-            auto work = [&] {
-                for (size_t c; (c = next.fetch_add(1)) < chunks;) {
-                    JsonBuf b;
-                    const size_t lo = n * c / chunks, hi = n * (c + 1) / chunks;
-                    for (size_t i = lo; i < hi; ++i) {
-                        if (i) b.c(',');
-                        emit(b, i);
-                    }
-                    out[c] = std::move(b.s);
+            // one piece per range, kept in range order
+            std::vector<std::pair<size_t, std::string>> out;
+            std::mutex mu;
+            parallel_ranges(n, kChunk, [&](size_t lo, size_t hi) {
+                JsonBuf b;
+                for (size_t i = lo; i < hi; ++i) {
+                    if (i) b.c(',');
+                    emit(b, i);
                 }
-            };
-            std::vector<std::thread> pool;
-            for (size_t t = 1; t < std::min(threads, chunks); ++t) pool.emplace_back(work);
-            work();
-            for (auto& t : pool) t.join();
-            for (auto& piece : out) parts.push_back(std::move(piece));
+                std::lock_guard<std::mutex> lk(mu);
+                out.emplace_back(lo, std::move(b.s));
+            });
+            std::sort(out.begin(), out.end(),
+                      [](const std::pair<size_t, std::string>& a, const std::pair<size_t, std::string>& b) {
+                          return a.first < b.first;
+                      });
+            for (auto& piece : out) parts.push_back(std::move(piece.second));
         }
         cur.c(']');
     }
@@ -248,29 +268,6 @@ bool write_mesh_json(const std::string& filename, const std::vector<std::array<d
     put_lists(o, shells);
     o.cur.str("}\n");
     return o.write(filename);
-}
-
-size_t host_threads() {
-    const unsigned hw = std::thread::hardware_concurrency();
-    return std::min<size_t>(hw ? hw : 1, 32);
-}
-
-// f(lo, hi) over [0, n) in contiguous chunks of at least `grain`, on up to host_threads() threads
-template <class F>
-void parallel_ranges(size_t n, size_t grain, const F& f) {
-    const size_t chunks = std::min(host_threads() * 4, (n + grain - 1) / grain);
-    if (chunks <= 1) {
-        if (n) f(size_t(0), n);
-        return;
-    }
-    std::atomic<size_t> next{0};
-    auto work = [&] {
-        for (size_t c; (c = next.fetch_add(1)) < chunks;) f(n * c / chunks, n * (c + 1) / chunks);
-    };
-    std::vector<std::thread> pool;
-    for (size_t t = 1; t < std::min(host_threads(), chunks); ++t) pool.emplace_back(work);
-    work();
-    for (auto& t : pool) t.join();
 }
 
 // compute_mesh_edges for large meshes, on several threads, with the same result: the occurrences
