@@ -112,7 +112,8 @@ size_t host_threads() {
     return std::min<size_t>(hw ? hw : 1, 32);
 }
 
-// f(lo, hi) over [0, n) in contiguous chunks of at least `grain`, on up to host_threads() threads
+// f(lo, hi) over [0, n) in contiguous chunks (at most ceil(n / grain) of them, and at most four per
+// thread), on up to host_threads() threads
 template <class F>
 void parallel_ranges(size_t n, size_t grain, const F& f) {
     const size_t chunks = std::min(host_threads() * 4, (n + grain - 1) / grain);
