@@ -167,6 +167,18 @@ def cpu_batch(probs, mode, n_problems=256, repeats=1):
     return rates, n, cores, desc
 
 
+def max_over_ranks(x, dist, device):
+    """The largest x over the ranks of the process group (x itself without one).  Every rank calls
+    it at the same point: it is a collective."""
+    if dist is None:
+        return x
+    import torch
+
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def run_reference_batch(args, world):
     """The batched workload's CPU arm: every step is the bounded sample of cpu_batch."""
     fns = importlib.import_module(PKG + ".functions")
@@ -489,13 +501,11 @@ def main():
                 stage[k].append(tm[k] * 1e3)
             m.close()
         torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
         wall = time.perf_counter() - t0
     launches = int(L.ria_kernel_launches()) - launches0
-    ms = statistics.mean(dev_ms)
-    if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(statistics.mean(dev_ms), dist, "cuda")
     value = world * wl.n_tets / (ms * 1e-3)
 
     # ---- end to end through the host-buffer entry points, host buffers in pinned memory
@@ -532,7 +542,7 @@ def main():
             e2e_times.append(dt)
         h2d = pts_h.nbytes + wl.funcs.nbytes + pts_h.nbytes + tets_h.nbytes + fv.nbytes
         d2h = fv.nbytes + sum(o.nbytes for o in outs)
-    e2e = world * wl.n_tets / statistics.median(e2e_times) if e2e_times else None
+    e2e = world * wl.n_tets / max_over_ranks(statistics.median(e2e_times), dist, "cuda") if e2e_times else None
 
     if rank != 0:
         if dist:
