@@ -88,7 +88,7 @@ def build(verbose: bool = False) -> str:
     objs = [os.path.join(OUT_DIR, s.replace(".cu", ".o")) for s in SOURCES]
     relinked = False
     if any(j[0] == cc for j in jobs) or not os.path.exists(LIB):
-        _run([[cc, *ARCH, "-shared", *objs, "-o", LIB]], "link", verbose)
+        _run([[cc, *ARCH, "-shared", *objs, "-ldl", "-o", LIB]], "link", verbose)  # -ldl: NVTX loads its tool
         relinked = True
     if relinked or _host_stale(HOST_LIB, host_objs):
         _run([[CXX, "-shared", "-pthread", *host_objs, "-L" + OUT_DIR, "-lria", "-Wl,-rpath,$ORIGIN", "-o", HOST_LIB]],

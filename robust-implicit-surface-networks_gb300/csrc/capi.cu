@@ -5,6 +5,7 @@
 // table) -> fast per-tet cut -> exact cut of the deferred tets -> extraction.  Device memory comes
 // from the stream-ordered allocator and is returned to its pool when the mesh is freed.
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <cub/cub.cuh>
 #include <algorithm>
@@ -68,6 +69,23 @@ constexpr int64_t kMidThreshold = 4 * 152 * 5;  // deferred tets the exact kerne
 constexpr int64_t kBigRecordBytes = 28672;  // bound of a record of the exact variants
 constexpr int64_t kBigSlots = 152 * 64;     // concurrent exact-variant threads
 constexpr int64_t kWarpCutTets = 152 * 20 * 8;  // heaviest tets cut a warp each (about 8 waves of resident warps)
+
+// One NVTX range per pipeline stage ("ria a sample", "ria b filter", "ria c cut", "ria d extract"),
+// so that a profiler can select one stage's kernels (ncu --nvtx --nvtx-include "ria c cut/"); the
+// calls do nothing without a tool attached.  A range still open when the call returns is closed.
+struct StageRanges {
+    bool open = false;
+    void next(const char* name) {
+        end();
+        nvtxRangePushA(name);
+        open = true;
+    }
+    void end() {
+        if (open) nvtxRangePop();
+        open = false;
+    }
+    ~StageRanges() { end(); }
+};
 
 // A second stream per host thread and device, for work that overlaps the caller's stream inside one
 // call; created on first use and kept for the life of the thread's process, like the tables.
@@ -305,6 +323,8 @@ ria_status run_pipeline(const ria_config* cfg, const Inputs& in, cudaStream_t s,
         ria_mesh_free(M);
         return r;
     };
+    StageRanges ranges;
+    ranges.next("ria a sample");
     cudaEventRecord(ev[0], s);
 
     // counters: 0 status, 1 n_zero, 2..4 k histogram, 5 heap used, 6 big heap used, 7 deferred by the small
@@ -344,6 +364,7 @@ ria_status run_pipeline(const ria_config* cfg, const Inputs& in, cudaStream_t s,
         if (!in.d_vmask) launch_vertex_masks(mi, fv, in.V, in.F, vmask, cnt + 1, s);
     }
     cudaEventRecord(ev[1], s);
+    ranges.next("ria b filter");
 
     // ---- stage b
     const int64_t nb = filter_num_blocks(in.T);
@@ -381,6 +402,7 @@ ria_status run_pipeline(const ria_config* cfg, const Inputs& in, cudaStream_t s,
         launch_filter_scatter(mi, vmask, fv, in.F, in.d_tets, in.g, in.T, use_table, blk_off, ctx->table_sum[mi], fo, s);
     }
     cudaEventRecord(ev[2], s);
+    ranges.next("ria c cut");
 
     // ---- stage c
     CutArgs ca{};
@@ -552,6 +574,7 @@ ria_status run_pipeline(const ria_config* cfg, const Inputs& in, cudaStream_t s,
         }
     }
     cudaEventRecord(ev[3], s);
+    ranges.next("ria d extract");
 
     // ---- stage d
     if (!cfg->robust_test) {
@@ -583,6 +606,7 @@ ria_status run_pipeline(const ria_config* cfg, const Inputs& in, cudaStream_t s,
         if (e != cudaSuccess) return bail(fail(RIA_ECUDA, std::string("extract: ") + cudaGetErrorString(e)));
     }
     cudaEventRecord(ev[4], s);
+    ranges.end();
 
     unsigned long long h[16];
     cudaMemcpyAsync(h, cnt, sizeof(h), cudaMemcpyDeviceToHost, s);
