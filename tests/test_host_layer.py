@@ -65,6 +65,45 @@ def test_tet_mesh_reader_layouts(check, fns, tmp_path, layout):
     assert np.array_equal(p2, pts) and np.array_equal(t2, tets)
 
 
+def test_tet_mesh_reader_fuzzed_formatting(check, tmp_path):
+    """Random whitespace between tokens and varied number spellings (exponents, signs, integers for
+    coordinates): the reader agrees with Python's JSON parser on the same text."""
+    rng = np.random.default_rng(20)
+    ws = [" ", "\n", "\t", "\r\n", "  ", ""]
+
+    def sp():
+        return "".join(rng.choice(ws) for _ in range(int(rng.integers(0, 3))))
+
+    def num(x, integer=False):
+        if integer:
+            return str(int(x))
+        form = int(rng.integers(0, 4))
+        if form == 0:
+            return repr(float(x))
+        if form == 1:
+            return "%.17e" % x
+        if form == 2:
+            return ("%.17E" % x).replace("E+", "E")
+        return str(int(round(x)))
+
+    for trial in range(30):
+        n_p, n_t = int(rng.integers(0, 40)), int(rng.integers(0, 60))
+        pts = rng.normal(size=(n_p, 3)) * 10.0 ** rng.uniform(-8, 8, size=(n_p, 1))
+        tets = rng.integers(0, max(n_p, 1), size=(n_t, 4))
+        rows_p = [sp() + "[" + ",".join(sp() + num(v) + sp() for v in p) + "]" + sp() for p in pts]
+        rows_t = [sp() + "[" + ",".join(sp() + num(v, True) + sp() for v in t) + "]" + sp() for t in tets]
+        text = sp() + "[" + sp() + "[" + ",".join(rows_p) + "]" + sp() + "," + sp() + "[" + ",".join(rows_t) + "]" \
+            + sp() + "]" + sp()
+        f = tmp_path / ("m%d.json" % trial)
+        f.write_text(text)
+        out = tmp_path / ("m%d.bin" % trial)
+        _run("tetmesh", f, out)
+        p2, t2 = meshjson.read_grid(out)
+        P, T = json.loads(text)
+        assert np.array_equal(p2, np.array(P, dtype=np.float64).reshape(-1, 3)), trial
+        assert np.array_equal(t2, np.array(T, dtype=np.int64).reshape(-1, 4)), trial
+
+
 def test_tet_mesh_reader_rejects_truncated_file(check, tmp_path):
     f = tmp_path / "m.json"
     f.write_text("[[[0.0, 0.0, 0.0], [1.0, 0.0, 0.0]], [[0, 1, 0")
