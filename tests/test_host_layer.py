@@ -191,6 +191,27 @@ def test_double_format_writer(check, tmp_path):
     assert '"points":' + pts + "," in text
 
 
+def test_double_format_writer_random(check, tmp_path):
+    """Random finite doubles over the whole exponent range, and values around the notation
+    boundaries (1e-5, 1e-4, 1e15, 1e16) and integers: the writer prints the restatement's text."""
+    rng = np.random.default_rng(21)
+    bits = rng.integers(0, 2**64 - 1, size=210000, dtype=np.uint64).view(np.float64)  # > 65,536 rows: parallel chunks
+    xs = [bits[np.isfinite(bits)]]
+    for b in (1e-5, 1e-4, 1e15, 1e16):
+        xs.append(b * rng.uniform(0.5, 2.0, size=3000) * rng.choice([-1.0, 1.0], size=3000))
+    xs.append(rng.integers(-10**17, 10**17, size=3000).astype(np.float64))
+    xs.append(np.round(rng.uniform(-1e6, 1e6, size=3000), int(rng.integers(0, 8))))
+    x = np.concatenate(xs)
+    x = np.concatenate([x, np.zeros(-len(x) % 3)])
+    ref = {"xyz": x, "face_offsets": np.zeros(1, np.int64), "face_verts": np.zeros(0, np.int64),
+           "face_func": np.zeros(0, np.int64)}
+    inp = tmp_path / "in.bin"
+    meshjson.write_mesh_input(inp, ref)
+    out = tmp_path / "mesh.json"
+    _run("mesh", "ia", inp, out)
+    assert '"points":' + meshjson.dump(x.reshape(-1, 3).tolist()) + "," in out.read_text()
+
+
 def _oracle_mesh(fns, oracle, mode, name=None, res=16, wl=None):
     if wl is None:
         spec = json.load(open(os.path.join(HERE, "golden", "functions", name + ".json")))
