@@ -14,9 +14,11 @@
 //     records per call (RIA_ECAPACITY beyond);
 //   * the first call on a device looks up the array's device address there (cudaGetSymbolAddress);
 //     make that first call before any stream capture;
-//   * all calls share the array: the counters are cleared at the start of each call, the rest keeps
-//     the previous call's contents; calls that overlap on the GPU (different streams, or different
-//     host threads) race on it and must be serialized by the caller;
+//   * all calls share the array: the counters and the call's record descriptors are cleared at the
+//     start of each call, the rest keeps the previous call's contents; the per-tet cuts' status is
+//     checked before any record is sized or copied, so a failed call writes no records; calls that
+//     overlap on the GPU (different streams, or different host threads) race on it and must be
+//     serialized by the caller;
 //   * nothing in this path calls cudaMalloc, cudaFree or an allocating library routine.  The
 //     one-plane lookup table (allocated on first use by the other entry points) is not used here;
 //     the result is the same.
@@ -99,16 +101,19 @@ __global__ void __launch_bounds__(1024) k_na_offsets(unsigned char* scr, int64_t
     }
 }
 
+// one warp per tet: the lanes copy consecutive bytes, so a heavy tet's record (tens of KB) is copied
+// 32 bytes per step and both sides are accessed in contiguous runs
 __global__ void k_na_copy(unsigned char* scr, int64_t n, const uint64_t* __restrict__ off, uint8_t* __restrict__ dst,
                           uint64_t capacity) {
-    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
     if (i >= n || off[n] > capacity) return;
     const uint64_t d = ((const uint64_t*)(scr + kOffDesc))[i];
     RecSrc rs{scr + kOffHeap, scr + kOffHeap, nullptr, nullptr};
     const uint8_t* src = rs.get(d);
     const uint64_t o = off[i];
     const uint32_t len = (uint32_t)(off[i + 1] - o);
-    for (uint32_t b = 0; b < len; ++b) dst[o + b] = src[b];
+    for (uint32_t b = lane; b < len; b += 32) dst[o + b] = src[b];
 }
 
 std::mutex g_na_mu;
@@ -152,7 +157,10 @@ int run_batch_noalloc(const double* d_values, const uint32_t* d_value_offsets, u
     const int64_t n = (int64_t)n_tets;
     unsigned long long* cnt = (unsigned long long*)(scr + kOffCnt);
     uint32_t* status = (uint32_t*)cnt;
-    if (cudaMemsetAsync(cnt, 0, 8 * 8, s) != cudaSuccess) {
+    // the descriptors are cleared too: a tet whose cut fails writes none, and no later kernel may
+    // read an offset left by an earlier call
+    if (cudaMemsetAsync(cnt, 0, 8 * 8, s) != cudaSuccess ||
+        (n_tets > 0 && cudaMemsetAsync(scr + kOffDesc, 0, 8 * n_tets, s) != cudaSuccess)) {
         *msg = "CUDA error";
         return RIA_ECUDA;
     }
@@ -199,6 +207,25 @@ int run_batch_noalloc(const double* d_values, const uint32_t* d_value_offsets, u
         // both variants append to the one record heap
         launch_cut_big(cb, s);
     }
+    // every record must exist before the sizes are read: a failed cut leaves its descriptor unset
+    if (cudaMemcpyAsync(h, cnt, sizeof(h), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess) {
+        *msg = "CUDA error";
+        return RIA_ECUDA;
+    }
+    if ((uint32_t)h[0] & ST_INTERNAL) {
+        *msg = "per-tet cut: internal consistency check failed";
+        return RIA_EINTERNAL;
+    }
+    if ((uint32_t)h[0] & ST_EXACT) {
+        *msg = "an exact predicate exceeded its expansion capacity";
+        return RIA_EDEGENERATE;
+    }
+    if ((uint32_t)h[0] & ST_CAPACITY) {
+        *msg = "the records exceed the 8 MiB record space of the no-allocation path, or a tet exceeds the "
+               "per-tet capacity";
+        return RIA_ECAPACITY;
+    }
     if (n > 0) {
         k_na_sizes<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(scr, n);
         note_launch();
@@ -206,7 +233,7 @@ int run_batch_noalloc(const double* d_values, const uint32_t* d_value_offsets, u
     k_na_offsets<<<1, 1024, 0, s>>>(scr, n, d_record_offsets, capacity);
     note_launch();
     if (n > 0) {
-        k_na_copy<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(scr, n, d_record_offsets, d_records, capacity);
+        k_na_copy<<<(unsigned)((n * 32 + 127) / 128), 128, 0, s>>>(scr, n, d_record_offsets, d_records, capacity);
         note_launch();
     }
     if (cudaMemcpyAsync(h, cnt, sizeof(h), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
@@ -220,7 +247,7 @@ int run_batch_noalloc(const double* d_values, const uint32_t* d_value_offsets, u
         return RIA_EINTERNAL;
     }
     if (st & ST_CAPACITY) {
-        *msg = "record buffer too small, or a tet exceeds the per-tet or per-call scratch capacity";
+        *msg = "record buffer too small";
         return RIA_ECAPACITY;
     }
     return RIA_OK;
