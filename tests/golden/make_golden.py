@@ -5,9 +5,11 @@ Reads, as data:
     the function file, the tet mesh, and the REQUIREd patch count, chain count, corner count and
     patch_function_label list);
   * the function lists examples/tests/*.json and the tet mesh examples/tests/mesh.json.
-Writes kat.json, functions/*.json and mesh_8sphere.npz next to this script.
+  * the CSG known answers of the same file (the lambda over cell labels, written here as a CSG tree;
+    the REQUIREd patch, chain and corner counts and the patch_sign_label list).
+Writes kat.json, csg_kat.json, functions/*.json and mesh_8sphere.npz next to this script.
 
-Usage: python tests/golden/make_golden.py [reference_root]
+Usage: python tests/golden/make_golden.py REFERENCE_ROOT
 Nothing else reads the reference checkout; the tests only read the files written here.
 """
 import json
@@ -52,6 +54,13 @@ def parse_kats(src: str):
         m = re.search(r"REQUIRE\(corners_count == (\d+)\)", line)
         if m:
             cur["corners"] = int(m.group(1))
+        m = re.search(r"return \((.*)\);", line)
+        if m and "cells_label" in line:
+            cur["lambda"] = m.group(1).strip()
+        m = re.search(r"gt_sign_label = \{(.*)\};", line)
+        if m:
+            body = m.group(1).strip()
+            cur["sign_label"] = [bool(int(x)) for x in body.split(",")] if body else []
         m = re.search(r"patch_gt = \{(.*)\};", line)
         if m:
             body = m.group(1).strip()
@@ -60,28 +69,101 @@ def parse_kats(src: str):
                 cur["patch_label"] = [[int(a), int(b)] for a, b in pairs]
             else:
                 cur["patch_label"] = [int(x) for x in body.split(",")] if body else []
-    out = []
+    out, csg = [], []
     for c in cases:
         tc = c["test_case"]
         if tc.startswith("implicit arrangement"):
             c["mode"] = "ia"
         elif tc.startswith("material interface on known"):
             c["mode"] = "mi"
+        elif tc.startswith("CSG on known"):
+            c["mode"] = "csg"
+            c["positive_inside"] = True
+            c["tree"] = lambda_to_tree(c["lambda"])
+            csg.append(c)
+            continue
         else:
-            continue  # CSG needs arrangement cells; the failing example is not a known answer
+            continue  # the failing example is not a known answer
         out.append(c)
-    return out
+    return out, csg
+
+
+def lambda_to_tree(text: str):
+    """The reference test's CSG lambda body (cells_label[i], !, &&, || and parentheses) as the units
+    of a CSG tree file (app/csg.cpp:15-52): [op, a, b] with op 0 Intersection, 1 Union, 2 Negation;
+    an element e > 0 is unit e (1-based), e < 0 is function -e-1; unit 1 is the root."""
+    toks = re.findall(r"cells_label\[\d+\]|&&|\|\||!|\(|\)", text)
+    if "".join(toks) != re.sub(r"\s+", "", text):
+        raise ValueError("unsupported lambda: " + text)
+    pos = 0
+
+    def peek():
+        return toks[pos] if pos < len(toks) else None
+
+    def take():
+        nonlocal pos
+        pos += 1
+        return toks[pos - 1]
+
+    # expression tree first: ("f", j) | ("!", x) | ("&&"/"||", x, y)
+    def expr():
+        x = term()
+        while peek() == "||":
+            take()
+            x = ("||", x, term())
+        return x
+
+    def term():
+        x = factor()
+        while peek() == "&&":
+            take()
+            x = ("&&", x, factor())
+        return x
+
+    def factor():
+        t = take()
+        if t == "!":
+            return ("!", factor())
+        if t == "(":
+            x = expr()
+            if take() != ")":
+                raise ValueError("unbalanced parentheses: " + text)
+            return x
+        return ("f", int(re.search(r"\d+", t).group(0)))
+
+    root = expr()
+    if pos != len(toks):
+        raise ValueError("trailing tokens: " + text)
+    if root[0] == "f":
+        root = ("||", root, root)
+    units = []
+
+    def emit(node):
+        if node[0] == "f":
+            return -node[1] - 1
+        idx = len(units)
+        units.append(None)
+        if node[0] == "!":
+            units[idx] = [2, emit(node[1]), 0]
+        else:
+            units[idx] = [0 if node[0] == "&&" else 1, emit(node[1]), emit(node[2])]
+        return idx + 1
+
+    emit(root)
+    return units
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) < 2:
+        raise SystemExit("usage: python %s REFERENCE_ROOT" % sys.argv[0])
+    ref = sys.argv[1]
     src_path = os.path.join(ref, "tests", "test_implicit_networks.cpp")
     with open(src_path) as f:
-        kats = parse_kats(f.read())
-    for k in kats:
+        kats, csg = parse_kats(f.read())
+    for k in kats + csg:
         k["source"] = "tests/test_implicit_networks.cpp:%d" % k["line"]
     os.makedirs(os.path.join(HERE, "functions"), exist_ok=True)
-    for name in sorted({k["functions"] for k in kats}):
+    for name in sorted({k["functions"] for k in kats + csg}):
         shutil.copyfile(os.path.join(ref, "examples", "tests", name + ".json"),
                         os.path.join(HERE, "functions", name + ".json"))
     with open(os.path.join(ref, "examples", "tests", "mesh.json")) as f:
@@ -90,7 +172,9 @@ def main():
                         pts=np.asarray(mesh[0], dtype=np.float64), tets=np.asarray(mesh[1], dtype=np.int64))
     with open(os.path.join(HERE, "kat.json"), "w") as f:
         json.dump(kats, f, indent=1)
-    print("wrote %d known-answer cases" % len(kats))
+    with open(os.path.join(HERE, "csg_kat.json"), "w") as f:
+        json.dump(csg, f, indent=1)
+    print("wrote %d known-answer cases and %d CSG known-answer cases" % (len(kats), len(csg)))
 
 
 if __name__ == "__main__":

@@ -135,32 +135,98 @@ def test_cli_known_answers(built, tmp_path, kat):
     assert mesh["patches_label"] == [kat["patch_label"]]
 
 
-def test_cli_csg(built, pkg, fns, oracle, tmp_path):
-    """app/csg.cpp through the C++ host layer: the kept patches are those whose faces separate the
-    CSG shape's inside from its outside (device labels), with chains and corners pruned to them."""
-    specs = [{"type": "sphere", "center": [0.1, 0.0, 0.05], "radius": 0.55},
-             {"type": "cylinder", "axis_point": [0.0, 0.1, 0.0], "axis_vector": [0.2, 1.0, 0.1], "radius": 0.3},
-             {"type": "sphere", "center": [-0.3, 0.2, -0.1], "radius": 0.4}]
-    (tmp_path / "fn.json").write_text(json.dumps(specs))
-    tree = [{"type": "Union", "elements": [2, -3]}, {"type": "Intersection", "elements": [-1, 3]},
-            {"type": "Negation", "elements": [-2, 0]}]  # (f0 - f1) | f2
-    (tmp_path / "tree.json").write_text(json.dumps(tree))
+_OPS = {0: "Intersection", 1: "Union", 2: "Negation"}
+
+
+def _run_csg_cli(tmp_path, res, tree):
+    """app/csg.cpp's command line on a grid of `res` cubes with the functions in tmp_path/fn.json
+    and `tree` (units [op, a, b]) as its --tree file; returns mesh.json."""
+    (tmp_path / "tree.json").write_text(json.dumps([{"type": _OPS[op], "elements": [a, b]} for op, a, b in tree]))
     os.makedirs(tmp_path / "out", exist_ok=True)
-    res = 20
     (tmp_path / "config.json").write_text(json.dumps({"gridResolution": res, "gridBbox": [[-1, -1, -1], [1, 1, 1]],
                                                        "funcFile": "fn.json", "outputDir": "out"}))
     r = subprocess.run([os.path.join(BIN, "csg"), str(tmp_path / "config.json"), "--tree", str(tmp_path / "tree.json")],
                        capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stdout + r.stderr
-    text = open(tmp_path / "out" / "mesh.json").read()
-    got = json.loads(text)
+    got = json.loads(open(tmp_path / "out" / "mesh.json").read())
     assert list(got) == ["chains", "corners", "edges", "faces", "patches", "patches_label", "points"]
+    return got
+
+
+def _csg_expected(oracle, pts, tets, fv, tree):
+    """The oracle's arrangement, patches and chains, each patch labelled by point evaluation of the
+    tree (independent of the library's labels), pruned as src/csg.cpp:55-116 does."""
+    import csgcheck
+
+    ref = oracle.run("ia", pts, tets, fv, threads=os.cpu_count() or 1, connectivity=True)
+    full = meshjson.expected_mesh_json(ref, "ia")
+    full = {k: (v if v is not None else []) for k, v in full.items()}
+    fo, fvs = ref["face_offsets"], ref["face_verts"]
+    first_tet = ref["face_tets"][ref["face_tet_offsets"][:-1], 0]
+    label = lambda f: csgcheck.face_label(f, ref["xyz"], fo, fvs, first_tet, ref["face_func"], pts, tets, fv, tree)
+    labels = csgcheck.patch_labels(full["patches"], label)
+    kept, sign, chains, corners = csgcheck.prune(full["patches"], labels, full["faces"], len(ref["xyz"]),
+                                                 full["chains"] or [], ref["edges"].tolist(), ref["nm_degree"])
+    return full, kept, sign, chains, corners
+
+
+def _corners_after_prune(mesh):
+    """The reference test's corners_count from mesh.json: vertices with more than two non-manifold
+    edges, once the vertices counted at most twice in the kept patches' faces lost theirs."""
+    import csgcheck
+
+    faces = mesh["faces"] or []
+    nm = csgcheck.nm_degree_from_faces(faces, len(mesh["points"] or []))
+    if len(nm) == 0:
+        return 0
+    count = np.zeros(len(nm), dtype=np.int64)
+    for p in mesh["patches"] or []:
+        for f in p:
+            for v in faces[f]:
+                count[v] += 1
+    nm[count <= 2] = 0
+    return int((nm > 2).sum())
+
+
+def test_cli_csg(built, fns, oracle, tmp_path):
+    """app/csg.cpp through the C++ host layer: the kept patches, their sign labels and the kept
+    chains equal the oracle's, labelled by point evaluation of the tree on both sides of a face."""
+    specs = [{"type": "sphere", "center": [0.1, 0.0, 0.05], "radius": 0.55},
+             {"type": "cylinder", "axis_point": [0.0, 0.1, 0.0], "axis_vector": [0.2, 1.0, 0.1], "radius": 0.3},
+             {"type": "sphere", "center": [-0.3, 0.2, -0.1], "radius": 0.4}]
+    (tmp_path / "fn.json").write_text(json.dumps(specs))
+    tree = [(1, 2, -3), (0, -1, 3), (2, -2, 0)]  # (f0 - f1) | f2
+    res = 20
+    got = _run_csg_cli(tmp_path, res, tree)
     funcs = fns.make_functions(specs)
     pts, tets = fns.generate_tet_mesh(res)
-    ref = oracle.run("ia", pts, tets, oracle.sample(funcs, pts), connectivity=True)
-    full = meshjson.expected_mesh_json(ref, "ia")
-    labels = pkg.grid_implicit_arrangement(res, funcs).csg([(1, 2, -3), (0, -1, 3), (2, -2, 0)])
-    kept = [p for p in full["patches"] if labels[p[0]] != 0]
-    assert got["patches"] == kept and len(kept) > 0
-    assert got["patches_label"] == [[bool(labels[p[0]] == 1) for p in kept]]
+    full, kept, sign, chains, corners = _csg_expected(oracle, pts, tets, oracle.sample(funcs, pts), tree)
+    assert len(kept) > 0
+    assert got["patches"] == kept
+    assert got["patches_label"] == [sign]
+    assert (got["chains"] or []) == chains
+    assert _corners_after_prune(got) == corners
     assert got["faces"] == full["faces"] and got["edges"] == full["edges"]
+
+
+with open(os.path.join(GOLDEN, "csg_kat.json")) as _f:
+    CSG_KATS = json.load(_f)
+
+
+@pytest.mark.parametrize("kat", CSG_KATS, ids=[k["functions"] for k in CSG_KATS])
+def test_cli_csg_known_answers(built, fns, oracle, tmp_path, kat):
+    """The reference's CSG known answers (tests/test_implicit_networks.cpp:814-1034) through the csg
+    program (ria_host::csg, positive_inside = true) at 101^3 cubes: patch, chain and corner counts
+    and the ordered patch_sign_label list; the kept patches and chains also equal the oracle's."""
+    shutil.copy(os.path.join(GOLDEN, "functions", kat["functions"] + ".json"), tmp_path / "fn.json")
+    got = _run_csg_cli(tmp_path, 101, kat["tree"])
+    patches, chains = got["patches"] or [], got["chains"] or []
+    assert len(patches) == kat["patches"]
+    assert len(chains) == kat["chains"]
+    assert _corners_after_prune(got) == kat["corners"]
+    assert got["patches_label"] == [kat["sign_label"]]
+    funcs = fns.load_functions(os.path.join(GOLDEN, "functions", kat["functions"] + ".json"))
+    pts, tets = fns.generate_tet_mesh(101)
+    fv = oracle.sample(funcs, pts, threads=os.cpu_count() or 1)
+    _, kept, sign, kchains, corners = _csg_expected(oracle, pts, tets, fv, kat["tree"])
+    assert patches == kept and chains == kchains and corners == kat["corners"]
