@@ -85,7 +85,9 @@ typedef struct ria_config {
     int32_t use_topo_ray_shooting; /* accepted for the downstream stages; unused here */
     int32_t robust_test;           /* -R: cut every tet in both plane orders and compare the
                                       vertex/face/cell counts (src/implicit_arrangement.cpp:137-243);
-                                      the call then returns without a mesh */
+                                      the mesh then holds only the statistics, with the tets of each
+                                      failure type counted (RIA_STAT_ROBUST_*), and the call returns
+                                      RIA_EINTERNAL when any tet failed */
     int32_t keep_records;          /* keep the per-tet records (RIA_MESH_REC_*) */
 } ria_config;
 
@@ -147,8 +149,12 @@ enum {
     RIA_STAT_NUM_VERTS = 7,      /* num_iso_verts / num_MI_verts */
     RIA_STAT_NUM_FACES = 8,      /* num_iso_faces / num_MI_faces */
     RIA_STAT_NUM_DEFERRED = 9,   /* tets cut by the exact (slow) variant */
-    RIA_STAT_ROBUST_FAILURES = 10,/* robust_test: tets whose two plane orders disagree */
-    RIA_NUM_STATS = 11
+    RIA_STAT_ROBUST_FAILURES = 10,/* robust_test, type 1: tets cut in both plane orders whose vertex, face
+                                     or cell counts differ ("inconsistency") */
+    RIA_STAT_ROBUST_TYPE2 = 11,  /* robust_test, type 2: tets whose cut fails in the given order */
+    RIA_STAT_ROBUST_TYPE3 = 12,  /* robust_test, type 3: tets whose cut succeeds in the given order and
+                                     fails in the reversed order */
+    RIA_NUM_STATS = 13
 };
 enum {
     RIA_TIME_SAMPLE = 0,   /* stage a (grid entry points) or upload */
@@ -209,8 +215,8 @@ RIA_API ria_status ria_grid_batch(const ria_config* cfg, int32_t material_interf
 /* Number of problems of a batch mesh (0 for a mesh of any other entry point). */
 RIA_API uint32_t ria_batch_size(const ria_mesh* mesh);
 /* One problem's part of a field, with vertex, tet, mesh-vertex and offset values relative to the
- * problem.  RIA_MESH_STATS are the problem's own counts (RIA_STAT_NUM_DEFERRED and
- * RIA_STAT_ROBUST_FAILURES are 0); RIA_MESH_TIMINGS are the batch's. */
+ * problem.  RIA_MESH_STATS are the problem's own counts (RIA_STAT_NUM_DEFERRED and the
+ * RIA_STAT_ROBUST_* counts are 0); RIA_MESH_TIMINGS are the batch's. */
 RIA_API uint64_t ria_batch_count(const ria_mesh* mesh, uint32_t problem, ria_mesh_field field);
 RIA_API ria_status ria_batch_copy(const ria_mesh* mesh, uint32_t problem, ria_mesh_field field, void* host_dst);
 
@@ -315,6 +321,11 @@ RIA_API uint64_t ria_kernel_launches(void);
  * Must not overlap with running calls on the device. */
 RIA_API ria_status ria_lookup_cache_clear(void);
 RIA_API int ria_device_count(void);
+/* Diagnostics, no counterpart in the reference: FP64 operations per second on the current device,
+ * measured with a probe kernel that keeps every SM's FP64 pipe busy (op 0: fused multiply-add, 1: add,
+ * 2: multiply; each instruction counts as one operation, so the FP64 FLOP/s peak is twice the
+ * multiply-add rate).  It is the denominator of the FP64 fractions of the sampling and cut stages. */
+RIA_API ria_status ria_measure_fp64_rate(int32_t op, double* ops_per_s);
 
 #ifdef __cplusplus
 }

@@ -20,7 +20,8 @@ RIA_OK, RIA_EINVAL, RIA_ENOMEM, RIA_ECAPACITY, RIA_EDEGENERATE, RIA_ETIMEOUT, RI
  FIELD_TIMINGS, FIELD_FUNC_VALS) = range(14)
 
 STAT_NAMES = ["num_pts", "num_tets", "num_degenerate_vertex", "num_intersecting_tet", "num_a_func", "num_b_func",
-              "num_more_func", "num_verts", "num_faces", "num_deferred", "robust_failures"]
+              "num_more_func", "num_verts", "num_faces", "num_deferred", "robust_failures", "robust_type2",
+              "robust_type3"]
 TIMING_NAMES = ["sample", "filter", "cut", "extract", "total"]
 
 
@@ -129,6 +130,8 @@ def load():
     L.ria_device_count.argtypes = []
     L.ria_lookup_cache_clear.restype = i32
     L.ria_lookup_cache_clear.argtypes = []
+    L.ria_measure_fp64_rate.restype = i32
+    L.ria_measure_fp64_rate.argtypes = [i32, ctypes.POINTER(ctypes.c_double)]
     L.ria_kernel_launches.restype = u64
     L.ria_kernel_launches.argtypes = []
     _lib = L

@@ -142,8 +142,7 @@ def _run_host(name, pts, tets, func_vals, **kw):
     h = ctypes.c_void_p()
     st = getattr(L, name)(ctypes.byref(cfg), pts.ctypes.data, pts.shape[0], tets.ctypes.data, tets.shape[0],
                           fv.ctypes.data, fv.shape[1], ctypes.byref(h))
-    _lib.check(st)
-    return Mesh(h)
+    return _mesh_or_raise(st, h, kw)
 
 
 def implicit_arrangement(pts, tets, func_vals, **kw) -> Mesh:
@@ -163,6 +162,14 @@ def _run_grid(name, res, funcs, bbox_min=(-1.0, -1.0, -1.0), bbox_max=(1.0, 1.0,
     h = ctypes.c_void_p()
     st = getattr(L, name)(ctypes.byref(cfg), int(res), bmin.ctypes.data, bmax.ctypes.data, funcs.ctypes.data,
                           len(funcs), ctypes.byref(h))
+    return _mesh_or_raise(st, h, kw)
+
+
+def _mesh_or_raise(st, h, kw):
+    """The mesh of a call; a robust test whose tets failed (RIA_EINTERNAL with a mesh) still returns
+    it, since its statistics count the failing tets of each type."""
+    if st == _lib.RIA_EINTERNAL and kw.get("robust_test") and h.value:
+        return Mesh(h)
     _lib.check(st)
     return Mesh(h)
 

@@ -328,7 +328,7 @@ ria_status run_pipeline(const ria_config* cfg, const Inputs& in, cudaStream_t s,
     cudaEventRecord(ev[0], s);
 
     // counters: 0 status, 1 n_zero, 2..4 k histogram, 5 heap used, 6 big heap used, 7 deferred by the small
-    // variant, 8 robust failures, 9 deferred by the mid variant
+    // variant, 8 unused, 9 deferred by the mid variant, 10..12 robust-test tets of types 1, 2 and 3
     unsigned long long* cnt = tmp.get<unsigned long long>(16, &err);
     uint32_t* status = (uint32_t*)cnt;
     if (err != cudaSuccess) return bail(fail(RIA_ENOMEM, "device allocation failed"));
@@ -427,7 +427,7 @@ ria_status run_pipeline(const ria_config* cfg, const Inputs& in, cudaStream_t s,
         cudaMemcpyAsync(ident, h.data(), 4 * A, cudaMemcpyHostToDevice, s);
         ca.list = ident;
         ca.n = A;
-        launch_robust(ca, scratch, kBigSlots, cnt + 8, s);
+        launch_robust(ca, scratch, kBigSlots, cnt + 10, s);
         cudaStreamSynchronize(s);
     } else if (G > 0) {
         // one heap for both filtered variants: the small records of every tet plus room for the mid
@@ -624,7 +624,9 @@ ria_status run_pipeline(const ria_config* cfg, const Inputs& in, cudaStream_t s,
     M->stats[RIA_STAT_NUM_VERTS] = M->ex.n_verts;
     M->stats[RIA_STAT_NUM_FACES] = M->ex.n_faces;
     M->stats[RIA_STAT_NUM_DEFERRED] = n_def;
-    M->stats[RIA_STAT_ROBUST_FAILURES] = (int64_t)h[8];
+    M->stats[RIA_STAT_ROBUST_FAILURES] = (int64_t)h[10];
+    M->stats[RIA_STAT_ROBUST_TYPE2] = (int64_t)h[11];
+    M->stats[RIA_STAT_ROBUST_TYPE3] = (int64_t)h[12];
     float ms_[4];
     for (int i = 0; i < 4; ++i) cudaEventElapsedTime(&ms_[i], ev[i], ev[i + 1]);
     for (int i = 0; i < 4; ++i) M->timings[i] = ms_[i] * 1e-3;
@@ -634,8 +636,10 @@ ria_status run_pipeline(const ria_config* cfg, const Inputs& in, cudaStream_t s,
     destroy_events();
     tmp.release();
     *out = M;
-    if (cfg->robust_test && h[8] > 0) {
-        g_err = "robust test: results differ between the two plane orders";
+    if (cfg->robust_test && (h[10] | h[11] | h[12])) {
+        // the reference reports the first of these that occurred (src/implicit_arrangement.cpp:329-343)
+        g_err = h[11] ? "type 2 failure (crash in the normal order)."
+                      : (h[12] ? "type 3 failure (crash in the reverse order)." : "type 1 failure (inconsistency).");
         return RIA_EINTERNAL;
     }
     return RIA_OK;
@@ -1702,6 +1706,71 @@ ria_status ria_lookup_cache_clear(void) {
         RIA_CUDA(cudaMemcpy(c.cache_cnt[m], c.seed_cnt[m], sizeof(unsigned long long) * 2, cudaMemcpyDeviceToDevice));
     }
     RIA_CUDA(cudaDeviceSynchronize());
+    return RIA_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+// FP64 issue-rate probe: every thread runs 8 independent chains of `iters` operations of one kind
+// (OP 0 fused multiply-add, 1 add, 2 multiply), enough independent work to keep the FP64 pipe of
+// every SM busy; the sums are stored so that nothing is optimised away.
+template <int OP>
+__global__ void __launch_bounds__(256) k_fp64_probe(double* __restrict__ out, int iters, double a, double b) {
+    double x[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) x[i] = 1.0 + 1e-9 * (double)(threadIdx.x + 7 * i);
+    for (int it = 0; it < iters; ++it) {
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+            if (OP == 0) x[i] = fma(x[i], a, b);
+            else if (OP == 1) x[i] = x[i] + b;
+            else x[i] = x[i] * a;
+        }
+    }
+    double sum = 0.0;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) sum += x[i];
+    out[(size_t)blockIdx.x * blockDim.x + threadIdx.x] = sum;
+}
+
+}  // namespace
+
+extern "C" {
+
+ria_status ria_measure_fp64_rate(int32_t op, double* ops_per_s) {
+    if (!ops_per_s || op < 0 || op > 2) return fail(RIA_EINVAL, "op must be 0 (fma), 1 (add) or 2 (mul)");
+    int dev = 0;
+    ria_status st = current_device(&dev);
+    if (st != RIA_OK) return st;
+    int sms = 0;
+    RIA_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const int blocks = sms * 8, threads = 256, iters = 4096;
+    double* out = nullptr;
+    RIA_CUDA(cudaMalloc(&out, sizeof(double) * blocks * threads));
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    float best = 0.0f;
+    for (int rep = 0; rep < 6; ++rep) {  // the first launch warms up, the best of the rest counts
+        cudaEventRecord(e0);
+        if (op == 0) k_fp64_probe<0><<<blocks, threads>>>(out, iters, 0.999999999, 1e-12);
+        else if (op == 1) k_fp64_probe<1><<<blocks, threads>>>(out, iters, 0.999999999, 1e-12);
+        else k_fp64_probe<2><<<blocks, threads>>>(out, iters, 0.999999999, 1e-12);
+        note_launch();
+        cudaEventRecord(e1);
+        cudaEventSynchronize(e1);
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (rep > 0 && (best == 0.0f || ms < best)) best = ms;
+    }
+    cudaError_t e = cudaGetLastError();
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(out);
+    if (e != cudaSuccess) return fail(RIA_ECUDA, cudaGetErrorString(e));
+    *ops_per_s = (double)blocks * threads * 8.0 * iters / (best * 1e-3);
     return RIA_OK;
 }
 

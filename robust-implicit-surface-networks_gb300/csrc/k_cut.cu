@@ -15,6 +15,7 @@
 #include "device_common.cuh"
 #include "launch.hpp"
 #include "lookup2.cuh"
+#include "robust.cuh"
 
 namespace ria {
 
@@ -770,8 +771,9 @@ __global__ void k_build_table(uint8_t* table, uint32_t* table_off, IASum4* table
 }
 
 // The reference's robustness mode (src/implicit_arrangement.cpp:137-243,
-// src/material_interface.cpp:174-287): cut each tet with its rows in the given order and in the
-// reversed order, and count the tets whose vertex, face or cell counts differ.
+// src/material_interface.cpp:174-287): every listed tet through robust_tet (robust.cuh) with the
+// exact variant; n_fail[0..2] count the tets of type 1 (counts differ), type 2 (the cut fails in the
+// given order) and type 3 (it fails in the reversed order).
 template <bool MI>
 __global__ void __launch_bounds__(64) k_robust(CutArgs a, BigSlot<MI>* scratch, int64_t slots,
                                                unsigned long long* n_fail) {
@@ -785,33 +787,9 @@ __global__ void __launch_bounds__(64) k_robust(CutArgs a, BigSlot<MI>* scratch, 
             raise_status(a.status, ST_CAPACITY);
             continue;
         }
-        for (int r = 0; r < k; ++r)
-            for (int c = 0; c < 4; ++c) S.planes[4 * (2 * k - 1 - r) + c] = S.planes[4 * r + c];
-        int counts[2][3];
-        bool ok = true;
-        for (int pass = 0; pass < 2 && ok; ++pass) {
-            int st = S.cut.run(S.planes + (pass ? 4 * k : 0), k);
-            if (st != CUT_OK) {
-                ok = false;
-                break;
-            }
-            S.cut.canonicalize();
-            if constexpr (MI) {
-                counts[pass][0] = S.cut.onv;
-                counts[pass][1] = S.cut.onf;
-                counts[pass][2] = S.cut.onc;
-            } else {
-                counts[pass][0] = S.cut.nv_live;
-                counts[pass][1] = S.cut.nf;
-                counts[pass][2] = S.cut.nc;
-            }
-        }
-        if (!ok) {
-            raise_status(a.status, ST_CAPACITY);
-            continue;
-        }
-        if (counts[0][0] != counts[1][0] || counts[0][1] != counts[1][1] || counts[0][2] != counts[1][2])
-            atomicAdd(n_fail, 1ull);
+        const int r = robust_tet(S.cut, S.planes, k);
+        if (r == ROBUST_CAPACITY) raise_status(a.status, ST_CAPACITY);
+        else if (r != ROBUST_OK) atomicAdd(n_fail + (r - ROBUST_TYPE1), 1ull);
     }
 }
 

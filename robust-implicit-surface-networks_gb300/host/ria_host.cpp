@@ -72,8 +72,18 @@ bool run_pipeline(bool mi, bool robust_test, bool use_lookup, bool use_secondary
             std::cout << ria_last_error() << std::endl;
             return false;
         }
-        std::cout << (s[RIA_STAT_ROBUST_FAILURES] ? "type 1 failure (inconsistency)." : "success.") << std::endl;
-        return s[RIA_STAT_ROBUST_FAILURES] == 0 && st == RIA_OK;
+        // the reference's messages, in its order of precedence (src/implicit_arrangement.cpp:329-343)
+        if (s[RIA_STAT_ROBUST_TYPE2])
+            std::cout << "type 2 failure (crash in the normal order)." << std::endl;
+        else if (s[RIA_STAT_ROBUST_TYPE3])
+            std::cout << "type 3 failure (crash in the reverse order)." << std::endl;
+        else if (s[RIA_STAT_ROBUST_FAILURES])
+            std::cout << "type 1 failure (inconsistency)." << std::endl;
+        else if (st == RIA_OK)
+            std::cout << "success." << std::endl;
+        else
+            std::cout << ria_last_error() << std::endl;
+        return st == RIA_OK;
     }
     if (st != RIA_OK) {
         std::cout << ria_last_error() << std::endl;

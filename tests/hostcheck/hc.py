@@ -86,3 +86,12 @@ def sqrt_rn(values, perturb=0):
     out = np.empty_like(values)
     lib().hc_sqrt_rn(values.ctypes.data, out.ctypes.data, values.size, perturb)
     return out
+
+
+def robust(mode, rows, forge=0):
+    """The device's robust-test outcome of one tet (0 ok, 1 counts differ, 2 the given order fails, 3 the
+    reversed order fails); forge 1..3 plants that outcome in the cut wrapper of the harness."""
+    rows = np.ascontiguousarray(rows, dtype=np.float64).reshape(-1, 4)
+    L = lib()
+    L.hc_robust.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_int]
+    return L.hc_robust(1 if mode == "mi" else 0, rows.shape[0], rows.ctypes.data, forge)

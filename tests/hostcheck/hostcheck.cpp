@@ -8,6 +8,7 @@
 #include "../../robust-implicit-surface-networks_gb300/csrc/lookup2.cuh"
 #include "../../robust-implicit-surface-networks_gb300/csrc/cut_ia_warp.cuh"
 #include "../../robust-implicit-surface-networks_gb300/csrc/sqrt_rn.cuh"
+#include "../../robust-implicit-surface-networks_gb300/csrc/robust.cuh"
 
 using namespace ria;
 
@@ -244,4 +245,43 @@ extern "C" void hc_sqrt_rn(const double* in, double* out, int64_t n, int perturb
         const uint64_t r0 = sqrt_seed(x);
         out[i] = sqrt_rn_finish(x, e, (uint64_t)((int64_t)r0 + perturb * (int64_t)(r0 >> 20)));
     }
+}
+
+// ---- robust test (robust.cuh): the device's per-tet classification with a cut wrapper that can forge
+// a failure of the first or second cut, or a different face count of the second, so that the test can
+// check that every outcome is reported.  forge: 0 none, 1 count mismatch, 2 first cut fails, 3 second
+// cut fails.
+namespace ria {
+template <class Base>
+struct ForgeCut : Base {
+    int forge = 0, calls = 0;
+    int run(const double* rows, int k) {
+        ++calls;
+        if ((forge == 2 && calls == 1) || (forge == 3 && calls == 2)) return CUT_FAIL;
+        return Base::run(rows, k);
+    }
+};
+template <class Base>
+void cut_counts(const ForgeCut<Base>& c, int out[3]) {
+    cut_counts(static_cast<const Base&>(c), out);
+    if (c.forge == 1 && c.calls == 2) out[1] += 1;
+}
+}  // namespace ria
+
+extern "C" int hc_robust(int mi, int k, const double* rows, int forge) {
+    std::vector<double> buf(8 * (size_t)(k > 0 ? k : 1));
+    for (int i = 0; i < 4 * k; ++i) buf[i] = rows[i];
+    int r;
+    if (mi) {
+        auto* c = new ForgeCut<MICutBig>();
+        c->forge = forge;
+        r = robust_tet(*c, buf.data(), k);
+        delete c;
+    } else {
+        auto* c = new ForgeCut<IACutBig>();
+        c->forge = forge;
+        r = robust_tet(*c, buf.data(), k);
+        delete c;
+    }
+    return r;
 }

@@ -440,3 +440,18 @@ def test_device_cut_logic_on_paper_examples(hc, oracle, fns):
                 _agree(hc, oracle, e["mode"], rows)
                 got, _ = hc.cut(e["mode"], rows, True)
                 assert got == ref, (e["file"], int(t))
+
+
+def test_robust_test_classification(hc):
+    """The robust test's per-tet outcome (robust.cuh, src/implicit_arrangement.cpp:137-243): exact cuts
+    agree in both plane orders; a forged count mismatch is type 1, a forged failure of the cut in the
+    given order type 2, of the reversed order type 3, in both modes."""
+    rng = np.random.default_rng(77)
+    for mode in ("ia", "mi"):
+        for trial in range(40):
+            k = int(rng.integers(2 if mode == "mi" else 1, 7))
+            rows = rng.normal(size=(k, 4)) if trial % 2 else rng.integers(-2, 3, size=(k, 4)).astype(np.float64)
+            assert hc.robust(mode, rows) == 0
+            assert hc.robust(mode, rows, forge=1) == 1
+            assert hc.robust(mode, rows, forge=2) == 2
+            assert hc.robust(mode, rows, forge=3) == 3

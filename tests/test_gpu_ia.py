@@ -102,7 +102,7 @@ def test_known_answer_fixtures(pkg, fns, oracle, lib, name):
     mesh = pkg.grid_implicit_arrangement(101, funcs)
     pts, tets = fns.generate_tet_mesh(101)
     fv = oracle.sample(funcs, pts, threads=os.cpu_count() or 1)
-    assert_mesh_equal(mesh, oracle.run("ia", pts, tets, fv, threads=os.cpu_count() or 1), records=False)
+    assert_mesh_equal(mesh, oracle.run("ia", pts, tets, fv, threads=os.cpu_count() or 1))
 
 
 @pytest.mark.parametrize("res", [24, 128])
@@ -113,7 +113,7 @@ def test_degenerate_workload(pkg, fns, oracle, lib, res):
     pts, tets = fns.generate_tet_mesh(wl.res)
     fv = oracle.sample(wl.funcs, pts, threads=os.cpu_count() or 1)
     assert np.array_equal(mesh["func_vals"].reshape(fv.shape), fv)
-    assert_mesh_equal(mesh, oracle.run("ia", pts, tets, fv, threads=os.cpu_count() or 1), records=res < 100)
+    assert_mesh_equal(mesh, oracle.run("ia", pts, tets, fv, threads=os.cpu_count() or 1))
 
 
 def test_batch_api_records(pkg, oracle, lib):
@@ -131,9 +131,15 @@ def test_batch_api_records(pkg, oracle, lib):
 
 
 def test_robust_mode(pkg, fns, lib):
-    wl = fns.workload_ia_small(res=16)
+    """-R on a grid (src/implicit_arrangement.cpp:137-243): no tet of any failure type, and the
+    per-count statistics of the tets the robust pass cut equal the normal pass's."""
+    wl = fns.workload_ia_degenerate(res=24)
     mesh = pkg.grid_implicit_arrangement(wl.res, wl.funcs, robust_test=True)
-    assert mesh.stats["robust_failures"] == 0
+    st = mesh.stats
+    assert st["robust_failures"] == 0 and st["robust_type2"] == 0 and st["robust_type3"] == 0
+    ref = pkg.grid_implicit_arrangement(wl.res, wl.funcs).stats
+    for k in ("num_intersecting_tet", "num_a_func", "num_b_func", "num_more_func", "num_degenerate_vertex"):
+        assert st[k] == ref[k], k
 
 
 def test_repeatable(pkg, fns, lib):

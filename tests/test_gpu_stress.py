@@ -41,3 +41,22 @@ def test_stress_set_every_stage(pkg, fns, oracle, lib, case):
     fv = oracle.sample(funcs, pts, threads=os.cpu_count() or 1)
     assert np.array_equal(mesh["func_vals"].reshape(fv.shape), fv)
     assert_mesh_equal(mesh, oracle.run(case["mode"], pts, tets, fv, threads=os.cpu_count() or 1))
+
+
+def _all_cases():
+    return json.load(open(os.path.join(STRESS, "manifest.json")))
+
+
+@pytest.mark.parametrize("case", _all_cases(), ids=lambda e: e["file"][:-5])
+def test_stress_set_robust_mode(pkg, fns, lib, case):
+    """-R on every instance of the robustness sets, the inputs the reference's robustness test was
+    made for (src/implicit_arrangement.cpp:137-243, src/material_interface.cpp:174-287): every active
+    tet is cut in both row orders with exact predicates, and no tet fails in either order or differs
+    in its vertex, face or cell counts."""
+    funcs = fns.make_functions(json.load(open(os.path.join(STRESS, case["file"]))))
+    res = case["resolution"]
+    bmin, bmax = case["bbox"]
+    grid = pkg.grid_implicit_arrangement if case["mode"] == "ia" else pkg.grid_material_interface
+    st = grid(res, funcs, bbox_min=bmin, bbox_max=bmax, robust_test=True).stats
+    assert st["num_intersecting_tet"] > 0
+    assert (st["robust_failures"], st["robust_type2"], st["robust_type3"]) == (0, 0, 0)
