@@ -132,7 +132,10 @@ __device__ __forceinline__ double combine_from_sum(const ria_function& f, double
         default:
             v = 0.0;
     }
-    return f.flipped ? -v : v;
+    // negation flips the sign bit (IEEE 754 negate, exact for every value, NaN included); done on the
+    // integer pipe, since the FP64 pipe bounds this kernel
+    const long long flip = f.flipped ? (long long)0x8000000000000000ull : 0ll;
+    return __longlong_as_double(__double_as_longlong(v) ^ flip);
 }
 
 __device__ __forceinline__ double combine_parts(const ria_function& f, const double w0[3], const double w1[3]) {

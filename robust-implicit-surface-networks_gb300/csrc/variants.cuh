@@ -1,7 +1,8 @@
 // Capacities of the per-tet cut variants.
 //   fast: one thread per tet, state in local memory, filter-only predicates; a tet that needs an
 //         exact predicate or more room is deferred.
-//   big:  state in global scratch, exact predicates, room for up to ~10 active functions.
+//   big:  one tet per block with its state in shared memory, exact predicates, the full range of the
+//         8-bit vertex and cell ids (about 13 planes in general position).
 #pragma once
 #include "cut_ia_warp.cuh"
 #include "cut_mi.cuh"

@@ -8,7 +8,7 @@ Reads, as data, the function files and configs of
 Writes examples/<name>.json (the function list) and examples/manifest.json (mode, grid resolution,
 box and lookup switches of each).
 
-Usage: python tests/golden/make_examples.py [reference_root]
+Usage: python tests/golden/make_examples.py REFERENCE_ROOT
 Nothing else reads the reference checkout; the tests only read the files written here.
 """
 import json
@@ -30,7 +30,9 @@ def entry(src_dir, name, mode, out_dir):
 
 
 def main():
-    root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) < 2:
+        raise SystemExit("usage: python %s REFERENCE_ROOT" % sys.argv[0])
+    root = sys.argv[1]
     ex = os.path.join(root, "examples")
     out_dir = os.path.join(HERE, "examples")
     os.makedirs(out_dir, exist_ok=True)

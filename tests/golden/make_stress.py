@@ -7,7 +7,7 @@ the first `per_level` instances of every noise level (by instance number) and wr
 stress/<mode>_<noise>_<id>.json (the function list) and stress/manifest.json (mode, noise, instance,
 grid resolution and box of each).
 
-Usage: python tests/golden/make_stress.py [reference_root] [per_level]
+Usage: python tests/golden/make_stress.py REFERENCE_ROOT [per_level]
 Nothing else reads the reference checkout; the tests only read the files written here.
 """
 import json
@@ -18,7 +18,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 
 
 def main():
-    root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) < 2:
+        raise SystemExit("usage: python %s REFERENCE_ROOT" % sys.argv[0])
+    root = sys.argv[1]
     per_level = int(sys.argv[2]) if len(sys.argv) > 2 else 3
     base = os.path.join(root, "examples", "Table2_Fig11")
     out_dir = os.path.join(HERE, "stress")

@@ -41,7 +41,7 @@ def test_known_answer_grids(pkg, fns, oracle, lib, name):
     mesh = pkg.grid_material_interface(101, funcs)
     pts, tets = fns.generate_tet_mesh(101)
     fv = oracle.sample(funcs, pts, threads=os.cpu_count() or 1)
-    assert_mesh_equal(mesh, oracle.run("mi", pts, tets, fv, threads=os.cpu_count() or 1), records=False)
+    assert_mesh_equal(mesh, oracle.run("mi", pts, tets, fv, threads=os.cpu_count() or 1))
 
 
 def test_degenerate_ties(pkg, fns, oracle, lib):
