@@ -132,8 +132,33 @@ typedef enum ria_mesh_field {
     RIA_MESH_REC_BYTES = 10,      /* uint8 [...] */
     RIA_MESH_STATS = 11,          /* int64 [RIA_NUM_STATS] */
     RIA_MESH_TIMINGS = 12,        /* double [RIA_NUM_TIMINGS]: seconds of each device stage */
-    RIA_MESH_FUNC_VALS = 13       /* double [n_pts][n_func]: the values the mesh was computed from (device
+    RIA_MESH_FUNC_VALS = 13,      /* double [n_pts][n_func]: the values the mesh was computed from (device
                                      entry points: read from the caller's buffer, which must still exist) */
+    /* Local-to-global maps, the outputs of the reference's extraction variants used when
+     * useTopoRayShooting is off (src/extract_mesh.cpp:268-566 and 988-1443, called at
+     * src/implicit_arrangement.cpp:370-385).  Computed on the device on first request; not available
+     * for a batch mesh.  Local vertex and face ids are those of the per-tet records (RIA_MESH_REC_*). */
+    RIA_MESH_TET_VERT_OFFSETS = 14,/* int64 [n_tets + 1] (global_vId_start_index_of_tet) */
+    RIA_MESH_TET_VERTS = 15,      /* int64 [...] per record vertex: its mesh vertex, or -v-1 for tet vertex v
+                                     (a record vertex on a tet corner; global_vId_of_tet_vert) */
+    RIA_MESH_TET_FACE_OFFSETS = 16,/* int64 [n_tets + 1] (iso_fId_start_index_of_tet / MI_fId_...) */
+    RIA_MESH_TET_FACES = 17,      /* int64 [...] per record face: its mesh face, or -1 (iso_fId_of_tet_face /
+                                     MI_fId_of_tet_face: an interface face on the tet boundary is set in both
+                                     tets that share it) */
+    /* Mesh connectivity, the host stages that follow extraction in the reference
+     * (src/mesh_connectivity.cpp:10-242, called at src/implicit_arrangement.cpp:410-440), computed on the
+     * device on first request with the reference's numbering; not available for a batch mesh. */
+    RIA_MESH_EDGES = 18,          /* int64 [n_edges][2]: v1 < v2, numbered by first occurrence in face order
+                                     (compute_mesh_edges) */
+    RIA_MESH_EDGE_FACE_OFFSETS = 19,/* int64 [n_edges + 1] */
+    RIA_MESH_EDGE_FACES = 20,     /* int64 [...][2]: (face, local edge) occurrences (Edge::face_edge_indices) */
+    RIA_MESH_FACE_EDGES = 21,     /* int64 [n_face_verts]: the edge of each face corner (edges_of_face; offsets
+                                     are RIA_MESH_FACE_OFFSETS) */
+    RIA_MESH_PATCH_OFFSETS = 22,  /* int64 [n_patches + 1] (compute_patches) */
+    RIA_MESH_PATCH_FACES = 23,    /* int64 [n_faces]: each patch's faces in the reference's breadth-first order */
+    RIA_MESH_PATCH_LABELS = 24,   /* int64 [n_patches][2]: func_index of each patch's first face (IA: first only) */
+    RIA_MESH_CHAIN_OFFSETS = 25,  /* int64 [n_chains + 1] (compute_chains) */
+    RIA_MESH_CHAIN_EDGES = 26     /* int64 [...]: non-manifold edges of each chain, in breadth-first order */
 } ria_mesh_field;
 
 /* RIA_MESH_STATS entries, named as in the reference's stats.json
@@ -273,6 +298,32 @@ RIA_API void ria_server_release(ria_server* server, uint64_t ticket);
 /* Stops the workers after their current batch and frees every result.  Requests not yet started are
  * dropped.  No other thread may be inside a ria_server_* call on this server while it is destroyed. */
 RIA_API void ria_server_destroy(ria_server* server);
+
+/* ---- tuning of the per-tet cut ---------------------------------------------------------------------
+ * The routing and launch shapes of stage c, per device.  The general-case tets come from the filter in
+ * bins of equal active-function count, heaviest first; the heavy bins and the light bins' leftovers are
+ * cut a warp per tet up to warp_route tets, the rest a thread per tet.  No counterpart in the
+ * reference (its cut is serial). */
+typedef struct ria_tuning {
+    int64_t warp_route;         /* general-case tets cut a warp each (the bin of the warp kernel) */
+    int32_t warp_blocks_per_sm; /* resident blocks of the warp kernel per SM (0: its occupancy limit) */
+    int32_t fast_block;         /* threads per block of the thread-per-tet kernel: 32, 64 or 128 (0: chosen
+                                   from the tet count) */
+    int64_t mid_threshold;      /* deferred tets above which the mid-size variant runs before the exact one */
+    int32_t cut_graph;          /* capture stage c's launches (both streams) as one CUDA graph: 0 never,
+                                   1 batched grids (the default), 2 every call */
+} ria_tuning;
+/* The current device's tuning record. */
+RIA_API ria_status ria_get_tuning(ria_tuning* tuning);
+RIA_API ria_status ria_set_tuning(const ria_tuning* tuning);
+/* Project-written autotuner: runs ria_grid_batch on `problems` (a sample of the caller's batches) with
+ * each candidate of a small grid of tuning records (warp_route x warp_blocks_per_sm x fast_block x
+ * cut_graph), `reps` times each with the secondary lookup reset to its seeded state, and installs the
+ * record with the smallest median device time on the current device.  best_s / default_s (may be
+ * NULL): that time, and the time of the record in place when the call started. */
+RIA_API ria_status ria_autotune(const ria_config* cfg, int32_t material_interface, const ria_grid_problem* problems,
+                                uint32_t n_problems, uint32_t reps, ria_tuning* best, double* best_s,
+                                double* default_s);
 
 /* Stage a alone: func_vals[n_pts][n_func] = funcs evaluated at pts (host buffers). */
 RIA_API ria_status ria_sample_functions(const ria_function* funcs, uint32_t n_func, const double* pts, uint64_t n_pts,

@@ -8,6 +8,7 @@
 //   per-tet cut     cut.cpp (replaces the absent simplicial_arrangement library)
 //   IA extraction   src/extract_mesh.cpp:10-265     (extract_iso_mesh)
 //   MI extraction   src/extract_mesh.cpp:569-986    (extract_MI_mesh)
+//   local-to-global maps of the extraction variants  src/extract_mesh.cpp:268-566, 988-1443
 //   vertex xyz      src/extract_mesh.cpp:1446-1637, src/extract_mesh.h:111-159
 //   edges/patches/chains  src/mesh_connectivity.cpp:10-242 (only to pin the oracle against the
 //                   reference's known-answer tests)
@@ -23,6 +24,7 @@
 #include <cstring>
 #include <map>
 #include <queue>
+#include <climits>
 #include <set>
 #include <string>
 #include <thread>
@@ -123,8 +125,13 @@ struct Mesh {
     std::vector<int64_t> verts;  // N x 11: tet, local, simplex_size, sv[4], funcs[4]
     std::vector<double> xyz;
     std::vector<int64_t> face_offsets{0}, face_verts, face_tet_offsets{0}, face_tets, face_func;
+    // local-to-global maps of the extraction variants (src/extract_mesh.cpp:268-566, 988-1443):
+    // per record vertex its mesh vertex or -v-1, per record face its mesh face or -1; CRS over the tets
+    std::vector<int64_t> tet_vert_offsets{0}, tet_verts, tet_face_offsets{0}, tet_faces;
     // downstream (KAT pinning)
     std::vector<int64_t> edges, patch_offsets{0}, patch_faces, patch_label, chain_offsets{0}, chain_edges;
+    // each edge's occurrences (face, local edge) in face order, and each face corner's edge
+    std::vector<int64_t> edge_face_offsets{0}, edge_faces, face_edges;
     std::vector<int64_t> nm_degree;  // per vertex: number of incident non-manifold edges
     std::vector<int64_t> stats;
     std::vector<double> timings;
@@ -275,7 +282,11 @@ void extract_iso(int64_t T, const int64_t* tets, Mesh& M) {
         return nverts++;
     };
     for (int64_t i = 0; i < T; ++i) {
-        if (M.rec_offsets[i + 1] == M.rec_offsets[i]) continue;
+        if (M.rec_offsets[i + 1] == M.rec_offsets[i]) {
+            M.tet_vert_offsets.push_back((int64_t)M.tet_verts.size());
+            M.tet_face_offsets.push_back((int64_t)M.tet_faces.size());
+            continue;
+        }
         IAView r = ia_view(M.rec_bytes.data() + M.rec_offsets[i]);
         int64_t start = M.start_index[i];
         const int64_t* tet = tets + 4 * i;
@@ -383,6 +394,32 @@ void extract_iso(int64_t T, const int64_t* tets, Mesh& M) {
                 }
             }
         }
+        // vertex map: a vertex on no iso face is a tet corner (its three labels are tet faces), and an
+        // iso vertex on a tet vertex is named by that vertex too (src/extract_mesh.cpp:384-403, 514-519)
+        for (int j = 0; j < r.nv; ++j) {
+            const uint8_t* lab = r.vlab + 3 * j;
+            int nb = 0;
+            bool used[4] = {false, false, false, false};
+            for (int t = 0; t < 3; ++t)
+                if (lab[t] <= 3) {
+                    used[lab[t]] = true;
+                    ++nb;
+                }
+            if (!is_iso_vert[j] || nb == 3) {
+                if (nb != 3) {  // impossible for a vertex on no iso face: marked for the tests to see
+                    M.tet_verts.push_back(INT64_MIN);
+                    continue;
+                }
+                int c0 = 0;
+                while (used[c0]) ++c0;
+                M.tet_verts.push_back(-tet[c0] - 1);
+            } else {
+                M.tet_verts.push_back(iso_vid[j]);
+            }
+        }
+        M.tet_vert_offsets.push_back((int64_t)M.tet_verts.size());
+        const size_t fmap0 = M.tet_faces.size();
+        M.tet_faces.resize(fmap0 + r.nf, kNone);
         int off = 0;
         std::vector<int64_t> fvs;
         for (int f = 0; f < r.nf; ++f) {
@@ -395,14 +432,17 @@ void extract_iso(int64_t T, const int64_t* tets, Mesh& M) {
                     compute_iso_face_key(fvs, key);
                     auto it = face_on_tetFace.find(key);
                     if (it == face_on_tetFace.end()) {
+                        M.tet_faces[fmap0 + f] = (int64_t)face_vlists.size();
                         face_on_tetFace.emplace(key, (int64_t)face_vlists.size());
                         face_vlists.push_back(fvs);
                         tet_face_lists.push_back({{i, f}});
                         face_func.push_back(plane_func(r.face_supp(f)));
                     } else {
+                        M.tet_faces[fmap0 + f] = it->second;
                         tet_face_lists[it->second].push_back({i, f});
                     }
                 } else {
+                    M.tet_faces[fmap0 + f] = (int64_t)face_vlists.size();
                     face_vlists.push_back(fvs);
                     tet_face_lists.push_back({{i, f}});
                     face_func.push_back(plane_func(r.face_supp(f)));
@@ -410,6 +450,7 @@ void extract_iso(int64_t T, const int64_t* tets, Mesh& M) {
             }
             off += len;
         }
+        M.tet_face_offsets.push_back((int64_t)M.tet_faces.size());
     }
     for (size_t f = 0; f < face_vlists.size(); ++f) {
         for (auto v : face_vlists[f]) M.face_verts.push_back(v);
@@ -446,8 +487,14 @@ void extract_mi(int64_t T, const int64_t* tets, Mesh& M) {
     };
     std::vector<char> is_mi_vert;
     std::vector<int64_t> mvid;
+    // first record face of each boundary key, as a position in tet_faces (src/extract_mesh.cpp:1420-1431)
+    std::unordered_map<std::array<int64_t, 3>, int64_t, KeyHash> tet_face_of_bndry_face;
     for (int64_t i = 0; i < T; ++i) {
-        if (M.rec_offsets[i + 1] == M.rec_offsets[i]) continue;
+        if (M.rec_offsets[i + 1] == M.rec_offsets[i]) {
+            M.tet_vert_offsets.push_back((int64_t)M.tet_verts.size());
+            M.tet_face_offsets.push_back((int64_t)M.tet_faces.size());
+            continue;
+        }
         MIView r = mi_view(M.rec_bytes.data() + M.rec_offsets[i]);
         int64_t start = M.start_index[i];
         const int64_t* tet = tets + 4 * i;
@@ -543,6 +590,17 @@ void extract_mi(int64_t T, const int64_t* tets, Mesh& M) {
                 }
             }
         }
+        // vertex map (src/extract_mesh.cpp:1112-1128, 1240-1259): tet vertices, and interface vertices
+        // on a tet vertex, as -v-1
+        for (int j = 0; j < r.nv; ++j) {
+            if (!is_mi_vert[j] || (mvid[j] >= 0 && simplex_size[mvid[j]] == 1))
+                M.tet_verts.push_back(mvid[j] >= 0 ? -sv0[mvid[j]] - 1 : mvid[j]);
+            else
+                M.tet_verts.push_back(mvid[j]);
+        }
+        M.tet_vert_offsets.push_back((int64_t)M.tet_verts.size());
+        const size_t fmap0 = M.tet_faces.size();
+        M.tet_faces.resize(fmap0 + r.nf, kNone);
         int off = 0;
         std::vector<int64_t> fvs, bfv, mats_here;
         for (int f = 0; f < r.nf; ++f) {
@@ -553,6 +611,7 @@ void extract_mi(int64_t T, const int64_t* tets, Mesh& M) {
             if (pos > 3) {
                 fvs.clear();
                 for (int t = 0; t < len; ++t) fvs.push_back(mvid[rd16(loop + 2 * t)]);
+                M.tet_faces[fmap0 + f] = (int64_t)face_vlists.size();
                 face_vlists.push_back(fvs);
                 face_tf.push_back({i, f});
                 face_func.push_back({M.func_in_tet[pos - 4 + start], M.func_in_tet[neg - 4 + start]});
@@ -568,6 +627,7 @@ void extract_mi(int64_t T, const int64_t* tets, Mesh& M) {
             }
             std::array<int64_t, 3> key;
             compute_iso_face_key(bfv, key);
+            const int64_t first_occ = tet_face_of_bndry_face.emplace(key, (int64_t)(fmap0 + f)).first->second;
             int64_t m = kNone;
             mats_here.clear();
             if (unique) {
@@ -654,11 +714,14 @@ void extract_mi(int64_t T, const int64_t* tets, Mesh& M) {
                     }
                 }
                 int64_t m_here = (m != kNone) ? m : mats_here.front();
+                M.tet_faces[fmap0 + f] = (int64_t)face_vlists.size();
+                M.tet_faces[first_occ] = (int64_t)face_vlists.size();
                 face_vlists.push_back(fvs);
                 face_tf.push_back({i, f});
                 face_func.push_back({std::max(m_here, m_other), std::min(m_here, m_other)});
             }
         }
+        M.tet_face_offsets.push_back((int64_t)M.tet_faces.size());
     }
     for (size_t f = 0; f < face_vlists.size(); ++f) {
         for (auto v : face_vlists[f]) M.face_verts.push_back(v);
@@ -770,6 +833,14 @@ void connectivity(Mesh& M, bool mi) {
             face_edges[f].push_back(ins.first->second);
         }
     }
+    for (auto& occ : efaces) {
+        for (auto& fj : occ) {
+            M.edge_faces.push_back(fj.first);
+            M.edge_faces.push_back(fj.second);
+        }
+        M.edge_face_offsets.push_back((int64_t)M.edge_faces.size() / 2);
+    }
+    for (auto& fe : face_edges) M.face_edges.insert(M.face_edges.end(), fe.begin(), fe.end());
     std::vector<char> seen(nf, 0);
     for (int64_t i = 0; i < nf; ++i) {
         if (seen[i]) continue;
@@ -1070,6 +1141,13 @@ int64_t oracle_len(void* h, const char* name) {
     if (n == "nm_degree") return (int64_t)M->nm_degree.size();
     if (n == "stats") return (int64_t)M->stats.size();
     if (n == "timings") return (int64_t)M->timings.size();
+    if (n == "face_edges") return (int64_t)M->face_edges.size();
+    if (n == "edge_faces") return (int64_t)M->edge_faces.size();
+    if (n == "edge_face_offsets") return (int64_t)M->edge_face_offsets.size();
+    if (n == "tet_faces") return (int64_t)M->tet_faces.size();
+    if (n == "tet_face_offsets") return (int64_t)M->tet_face_offsets.size();
+    if (n == "tet_verts") return (int64_t)M->tet_verts.size();
+    if (n == "tet_vert_offsets") return (int64_t)M->tet_vert_offsets.size();
     return -1;
 }
 
@@ -1100,6 +1178,13 @@ int oracle_copy(void* h, const char* name, void* dst) {
     if (n == "nm_degree") return cp(M->nm_degree);
     if (n == "stats") return cp(M->stats);
     if (n == "timings") return cp(M->timings);
+    if (n == "face_edges") return cp(M->face_edges);
+    if (n == "edge_faces") return cp(M->edge_faces);
+    if (n == "edge_face_offsets") return cp(M->edge_face_offsets);
+    if (n == "tet_faces") return cp(M->tet_faces);
+    if (n == "tet_face_offsets") return cp(M->tet_face_offsets);
+    if (n == "tet_verts") return cp(M->tet_verts);
+    if (n == "tet_vert_offsets") return cp(M->tet_vert_offsets);
     return -1;
 }
 

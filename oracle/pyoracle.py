@@ -95,6 +95,8 @@ _ARRAYS = {
     "face_tet_offsets": np.int64, "face_tets": np.int64, "face_func": np.int64, "edges": np.int64,
     "patch_offsets": np.int64, "patch_faces": np.int64, "patch_label": np.int64, "chain_offsets": np.int64,
     "chain_edges": np.int64, "nm_degree": np.int64, "stats": np.int64, "timings": np.float64,
+    "edge_face_offsets": np.int64, "edge_faces": np.int64, "face_edges": np.int64,
+    "tet_vert_offsets": np.int64, "tet_verts": np.int64, "tet_face_offsets": np.int64, "tet_faces": np.int64,
 }
 
 STAT_NAMES = ["num_pts", "num_tets", "num_degenerate_vertex", "num_intersecting_tet", "num_a_func",

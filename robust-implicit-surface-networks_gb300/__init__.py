@@ -9,7 +9,7 @@ from . import functions  # noqa: F401
 from ._lib import RiaError, declared_functions, load  # noqa: F401
 from .api import (BatchMesh, Mesh, Server, compute_arrangement_batch, grid_batch, compute_material_interface_batch, device_count,  # noqa: F401
                   grid_implicit_arrangement, grid_material_interface, implicit_arrangement, material_interface,
-                  sample_functions)
+                  sample_functions, get_tuning, set_tuning, autotune)
 
 
 def build(verbose: bool = False) -> str:

@@ -17,7 +17,9 @@ RIA_OK, RIA_EINVAL, RIA_ENOMEM, RIA_ECAPACITY, RIA_EDEGENERATE, RIA_ETIMEOUT, RI
 
 (FIELD_POINTS, FIELD_VERTS, FIELD_FACE_OFFSETS, FIELD_FACE_VERTS, FIELD_FACE_TET_OFFSETS, FIELD_FACE_TETS,
  FIELD_FACE_FUNC, FIELD_FUNC_IN_TET, FIELD_START_INDEX, FIELD_REC_OFFSETS, FIELD_REC_BYTES, FIELD_STATS,
- FIELD_TIMINGS, FIELD_FUNC_VALS) = range(14)
+ FIELD_TIMINGS, FIELD_FUNC_VALS, FIELD_TET_VERT_OFFSETS, FIELD_TET_VERTS, FIELD_TET_FACE_OFFSETS,
+ FIELD_TET_FACES, FIELD_EDGES, FIELD_EDGE_FACE_OFFSETS, FIELD_EDGE_FACES, FIELD_FACE_EDGES, FIELD_PATCH_OFFSETS,
+ FIELD_PATCH_FACES, FIELD_PATCH_LABELS, FIELD_CHAIN_OFFSETS, FIELD_CHAIN_EDGES) = range(27)
 
 STAT_NAMES = ["num_pts", "num_tets", "num_degenerate_vertex", "num_intersecting_tet", "num_a_func", "num_b_func",
               "num_more_func", "num_verts", "num_faces", "num_deferred", "robust_failures", "robust_type2",
@@ -44,6 +46,12 @@ class Request(ctypes.Structure):
 
 
 REQ_IA, REQ_MI, REQ_CSG = 0, 1, 2
+
+
+class Tuning(ctypes.Structure):
+    """ria_tuning of include/ria.h."""
+    _fields_ = [("warp_route", ctypes.c_int64), ("warp_blocks_per_sm", ctypes.c_int32), ("fast_block", ctypes.c_int32),
+                ("mid_threshold", ctypes.c_int64), ("cut_graph", ctypes.c_int32)]
 
 
 class Config(ctypes.Structure):
@@ -130,6 +138,13 @@ def load():
     L.ria_device_count.argtypes = []
     L.ria_lookup_cache_clear.restype = i32
     L.ria_lookup_cache_clear.argtypes = []
+    L.ria_get_tuning.restype = i32
+    L.ria_get_tuning.argtypes = [ctypes.POINTER(Tuning)]
+    L.ria_set_tuning.restype = i32
+    L.ria_set_tuning.argtypes = [ctypes.POINTER(Tuning)]
+    L.ria_autotune.restype = i32
+    L.ria_autotune.argtypes = [cfgp, i32, vp, u32, u32, ctypes.POINTER(Tuning), ctypes.POINTER(ctypes.c_double),
+                               ctypes.POINTER(ctypes.c_double)]
     L.ria_measure_fp64_rate.restype = i32
     L.ria_measure_fp64_rate.argtypes = [i32, ctypes.POINTER(ctypes.c_double)]
     L.ria_kernel_launches.restype = u64

@@ -33,6 +33,21 @@ class Mesh:
         "rec_offsets": (_lib.FIELD_REC_OFFSETS, np.int64, None),
         "rec_bytes": (_lib.FIELD_REC_BYTES, np.uint8, None),
         "func_vals": (_lib.FIELD_FUNC_VALS, np.float64, None),
+        # local-to-global maps (the reference's extraction variants for useTopoRayShooting = false)
+        "tet_vert_offsets": (_lib.FIELD_TET_VERT_OFFSETS, np.int64, None),
+        "tet_verts": (_lib.FIELD_TET_VERTS, np.int64, None),
+        "tet_face_offsets": (_lib.FIELD_TET_FACE_OFFSETS, np.int64, None),
+        "tet_faces": (_lib.FIELD_TET_FACES, np.int64, None),
+        # mesh connectivity (compute_mesh_edges / compute_patches / compute_chains)
+        "edges": (_lib.FIELD_EDGES, np.int64, (-1, 2)),
+        "edge_face_offsets": (_lib.FIELD_EDGE_FACE_OFFSETS, np.int64, None),
+        "edge_faces": (_lib.FIELD_EDGE_FACES, np.int64, (-1, 2)),
+        "face_edges": (_lib.FIELD_FACE_EDGES, np.int64, None),
+        "patch_offsets": (_lib.FIELD_PATCH_OFFSETS, np.int64, None),
+        "patch_faces": (_lib.FIELD_PATCH_FACES, np.int64, None),
+        "patch_label": (_lib.FIELD_PATCH_LABELS, np.int64, (-1, 2)),
+        "chain_offsets": (_lib.FIELD_CHAIN_OFFSETS, np.int64, None),
+        "chain_edges": (_lib.FIELD_CHAIN_EDGES, np.int64, None),
     }
 
     def __init__(self, handle):
@@ -50,10 +65,10 @@ class Mesh:
     def _copy(self, field, dtype):
         L = _lib.load()
         n = int(L.ria_mesh_count(self._h, field))
-        out = np.zeros(n, dtype=dtype)
-        if n:
-            _lib.check(L.ria_mesh_copy(self._h, field, out.ctypes.data))
-        return out
+        out = np.zeros(max(n, 1), dtype=dtype)
+        # copied even when empty: a field built on first request reports its error here
+        _lib.check(L.ria_mesh_copy(self._h, field, out.ctypes.data))
+        return out[:n]
 
     def copy_into(self, name, out):
         """Copy a field into a caller buffer (e.g. pinned host memory); returns the filled view."""
@@ -232,11 +247,8 @@ class _ProblemView:
         return out
 
 
-def grid_batch(problems, mode="ia", **kw) -> BatchMesh:
-    """Solve many grid problems in one pass of every stage.  problems: iterable of
-    (res, funcs) or (res, funcs, bbox_min, bbox_max)."""
-    L = _lib.load()
-    problems = list(problems)
+def _problem_array(problems):
+    """ria_grid_problem array of (res, funcs[, bbox_min, bbox_max]) tuples, and the arrays it points to."""
     arr = (_lib.GridProblem * len(problems))()
     keep = []
     for i, pr in enumerate(problems):
@@ -250,10 +262,47 @@ def grid_batch(problems, mode="ia", **kw) -> BatchMesh:
             arr[i].bbox_min[a] = float(bmin[a])
             arr[i].bbox_max[a] = float(bmax[a])
         arr[i].funcs = funcs.ctypes.data
+    return arr, keep
+
+
+def grid_batch(problems, mode="ia", **kw) -> BatchMesh:
+    """Solve many grid problems in one pass of every stage.  problems: iterable of
+    (res, funcs) or (res, funcs, bbox_min, bbox_max)."""
+    L = _lib.load()
+    problems = list(problems)
+    arr, keep = _problem_array(problems)
     cfg = _config(**kw)
     h = ctypes.c_void_p()
     _lib.check(L.ria_grid_batch(ctypes.byref(cfg), 1 if mode == "mi" else 0, arr, len(problems), ctypes.byref(h)))
     return BatchMesh(h)
+
+
+_TUNING_KEYS = ("warp_route", "warp_blocks_per_sm", "fast_block", "mid_threshold", "cut_graph")
+
+
+def get_tuning() -> dict:
+    """The current device's tuning record of the per-tet cut (ria_tuning)."""
+    t = _lib.Tuning()
+    _lib.check(_lib.load().ria_get_tuning(ctypes.byref(t)))
+    return {k: getattr(t, k) for k in _TUNING_KEYS}
+
+
+def set_tuning(tuning: dict) -> None:
+    t = _lib.Tuning(*[int(tuning[k]) for k in _TUNING_KEYS])
+    _lib.check(_lib.load().ria_set_tuning(ctypes.byref(t)))
+
+
+def autotune(problems, mode="ia", reps=2, **kw):
+    """The project's autotuner (ria_autotune) on a sample of batched problems: installs the fastest
+    tuning record on the current device; returns (record, its median seconds, the previous record's)."""
+    problems = list(problems)
+    arr, keep = _problem_array(problems)
+    cfg = _config(**kw)
+    t = _lib.Tuning()
+    best, dflt = ctypes.c_double(), ctypes.c_double()
+    _lib.check(_lib.load().ria_autotune(ctypes.byref(cfg), 1 if mode == "mi" else 0, arr, len(problems), int(reps),
+                                        ctypes.byref(t), ctypes.byref(best), ctypes.byref(dflt)))
+    return {k: getattr(t, k) for k in _TUNING_KEYS}, best.value, dflt.value
 
 
 class _Borrowed:

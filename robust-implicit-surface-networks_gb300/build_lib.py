@@ -19,7 +19,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libria.so")
-SOURCES = ["k_ab.cu", "k_cut.cu", "k_extract.cu", "k_extract_mi.cu", "k_noalloc.cu", "capi.cu"]
+SOURCES = ["k_ab.cu", "k_cut.cu", "k_extract.cu", "k_extract_mi.cu", "k_noalloc.cu", "k_tetmaps.cu", "k_connect.cu", "capi.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-fmad=false", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden"]
 HOST = os.path.join(HERE, "host")

@@ -47,6 +47,11 @@ ria_status fail(ria_status s, const std::string& msg) {
         if (e_ != cudaSuccess) return fail(RIA_ECUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
     } while (0)
 
+// the tuning record's defaults (ria_tuning; ria_autotune replaces them per device): 24,320 tets cut
+// a warp each, the warp kernel at its occupancy limit, the thread kernel's block from the tet count,
+// the mid-size variant past 3,040 deferred tets, the cut stage captured as a graph for batched grids
+constexpr ria_tuning kDefaultTuning = {152 * 20 * 8, 0, 0, 4 * 152 * 5, 1};
+
 struct DeviceCtx {
     bool ready[2] = {false, false};
     uint8_t* table[2] = {nullptr, nullptr};      // 81 patterns, then the secondary-lookup templates
@@ -57,6 +62,7 @@ struct DeviceCtx {
     // the seeded secondary lookup, restored by ria_lookup_cache_clear
     unsigned long long* seed_slots[2] = {nullptr, nullptr};
     unsigned long long* seed_cnt[2] = {nullptr, nullptr};
+    ria_tuning tune = kDefaultTuning;  // routing and launch shapes of the cut (ria_set_tuning / ria_autotune)
 };
 
 std::mutex g_mu;
@@ -109,6 +115,35 @@ cudaError_t aux_stream(AuxStream** out) {
     *out = &a;
     return cudaSuccess;
 }
+
+// A stream capture of the cut stage's launches: ended, instantiated and launched by finish(); the
+// graph is released after the stream has run it (the destructor waits for the stream).
+struct CutGraph {
+    bool capturing = false;
+    cudaGraph_t g = nullptr;
+    cudaGraphExec_t x = nullptr;
+    cudaStream_t s = nullptr;
+    cudaError_t finish(cudaStream_t st) {
+        capturing = false;
+        s = st;
+        cudaError_t e = cudaStreamEndCapture(st, &g);
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&x, g, 0);
+        if (e == cudaSuccess) e = cudaGraphLaunch(x, st);
+        return e;
+    }
+    ~CutGraph() {
+        if (capturing) {  // a failure between the capture's start and end: close the capture
+            cudaGraph_t dummy = nullptr;
+            cudaStreamEndCapture(s ? s : nullptr, &dummy);
+            if (dummy) cudaGraphDestroy(dummy);
+        }
+        if (x || g) {
+            if (s) cudaStreamSynchronize(s);
+            if (x) cudaGraphExecDestroy(x);
+            if (g) cudaGraphDestroy(g);
+        }
+    }
+};
 
 ria_status current_device(int* dev) {
     int n = 0;
@@ -217,6 +252,7 @@ struct Inputs {
     const ria_function* funcs = nullptr;  // functions sampled on the grid (host array)
     ulonglong2* d_vmask = nullptr;      // vertex masks computed with the values (batched grids)
     bool trusted_tets = false;          // tets generated here: no range check
+    bool batch = false;                 // a batch of grids (ria_grid_batch)
 };
 
 // one problem of a batched-grid mesh
@@ -274,6 +310,15 @@ struct ria_mesh {
     int64_t* start_index = nullptr;
     int64_t* func_in_tet = nullptr;
     int64_t n_fit = 0;
+    bool have_conn = false;  // edges, patches and chains (RIA_MESH_EDGE* ... CHAIN*), built on first request
+    ConnOut conn;
+    bool have_maps = false;  // local-to-global maps (RIA_MESH_TET_*), built on first request
+    int64_t* tet_vert_offsets = nullptr;
+    int64_t* tet_verts = nullptr;
+    int64_t n_tet_verts = 0;
+    int64_t* tet_face_offsets = nullptr;
+    int64_t* tet_faces = nullptr;
+    int64_t n_tet_faces = 0;
     int64_t stats[RIA_NUM_STATS] = {0};
     double timings[RIA_NUM_TIMINGS] = {0};
     std::vector<BatchInfo> batch;  // batched grids: per-problem ranges (empty otherwise)
@@ -328,11 +373,12 @@ ria_status run_pipeline(const ria_config* cfg, const Inputs& in, cudaStream_t s,
     cudaEventRecord(ev[0], s);
 
     // counters: 0 status, 1 n_zero, 2..4 k histogram, 5 heap used, 6 big heap used, 7 deferred by the small
-    // variant, 8 unused, 9 deferred by the mid variant, 10..12 robust-test tets of types 1, 2 and 3
-    unsigned long long* cnt = tmp.get<unsigned long long>(16, &err);
+    // variant, 8 unused, 9 deferred by the mid variant, 10..14 the cut routing's counters, 16..18
+    // robust-test tets of types 1, 2 and 3
+    unsigned long long* cnt = tmp.get<unsigned long long>(20, &err);
     uint32_t* status = (uint32_t*)cnt;
     if (err != cudaSuccess) return bail(fail(RIA_ENOMEM, "device allocation failed"));
-    cudaMemsetAsync(cnt, 0, sizeof(unsigned long long) * 16, s);
+    cudaMemsetAsync(cnt, 0, sizeof(unsigned long long) * 20, s);
     if (in.d_tets && !in.trusted_tets) {
         // every kernel below indexes through the tets: check them before any of them runs
         launch_check_tets(in.d_tets, in.T, in.V, status, s);
@@ -427,7 +473,7 @@ ria_status run_pipeline(const ria_config* cfg, const Inputs& in, cudaStream_t s,
         cudaMemcpyAsync(ident, h.data(), 4 * A, cudaMemcpyHostToDevice, s);
         ca.list = ident;
         ca.n = A;
-        launch_robust(ca, scratch, kBigSlots, cnt + 10, s);
+        launch_robust(ca, scratch, kBigSlots, cnt + 16, s);
         cudaStreamSynchronize(s);
     } else if (G > 0) {
         // one heap for both filtered variants: the small records of every tet plus room for the mid
@@ -451,6 +497,9 @@ ria_status run_pipeline(const ria_config* cfg, const Inputs& in, cudaStream_t s,
             ca.table_off = ctx->table_off[0];
         }
         if (cfg->use_lookup && cfg->use_secondary_lookup) set_cache(ca, ctx, mi);
+        const ria_tuning tune = ctx->tune;
+        ca.warp_blocks_per_sm = tune.warp_blocks_per_sm;
+        ca.fast_block = tune.fast_block;
         // The general-case list is heaviest first.  Its heavy bins (four or more active functions)
         // are a few long cuts, its light bins many short lookups and cuts: the two parts run at the
         // same time on two streams.  Heavy: a warp per tet (implicit arrangement: the warp cut, the
@@ -466,8 +515,18 @@ ria_status run_pipeline(const ria_config* cfg, const Inputs& in, cudaStream_t s,
         uint32_t* owners = prep && !mi ? tmp.get<uint32_t>(G_light, &err) : nullptr;
         if (err != cudaSuccess) return bail(fail(RIA_ENOMEM, "device allocation failed"));
         AuxStream* aux = nullptr;
-        if (G_mid > 0 && G_light > 0) {
-            if (aux_stream(&aux) != cudaSuccess) return bail(fail(RIA_ECUDA, "stream creation failed"));
+        if (G_mid > 0 && G_light > 0 && aux_stream(&aux) != cudaSuccess)
+            return bail(fail(RIA_ECUDA, "stream creation failed"));
+        // the launches from here to the join take their sizes from the device only, so they are
+        // captured as one CUDA graph (both streams, with the fork and the join) and launched at once
+        CutGraph graph;
+        const bool capture = (tune.cut_graph == 2 || (tune.cut_graph == 1 && in.batch)) && s != nullptr &&
+                             s != cudaStreamLegacy && s != cudaStreamPerThread;
+        if (capture && cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed) != cudaSuccess)
+            return bail(fail(RIA_ECUDA, "stream capture failed"));
+        graph.capturing = capture;
+        graph.s = s;
+        if (aux) {
             cudaEventRecord(aux->fork, s);
             cudaStreamWaitEvent(aux->s, aux->fork, 0);
         }
@@ -479,7 +538,7 @@ ria_status run_pipeline(const ria_config* cfg, const Inputs& in, cudaStream_t s,
             } else {
                 // a warp per tet for the heaviest (their latency sets the stage's time when they are
                 // few); past a few waves of resident warps a thread per tet has the higher throughput
-                ch.n = G_mid < kWarpCutTets ? G_mid : kWarpCutTets;
+                ch.n = G_mid < tune.warp_route ? G_mid : tune.warp_route;
                 ch.next = (unsigned int*)(cnt + 13);
                 launch_cut_warp(ch, s);
                 if (G_mid > ch.n) {
@@ -533,12 +592,13 @@ ria_status run_pipeline(const ria_config* cfg, const Inputs& in, cudaStream_t s,
         if (G_light > 0 && !mi) {
             // the light bins' cuts after the heavy bins' (both warp kernels are bound by the same
             // per-SM shared memory): a warp per tet while the list is short, decided on the device
-            cl.route_at = kWarpCutTets;
+            cl.route_at = tune.warp_route;
             CutArgs cw = cl;
             cw.next = (unsigned int*)(cnt + 14);
             launch_cut_warp(cw, s);
             launch_cut_fast(cl, s, false);
         }
+        if (graph.capturing && graph.finish(s) != cudaSuccess) return bail(fail(RIA_ECUDA, "cut graph launch failed"));
         unsigned long long h = 0;
         cudaMemcpyAsync(&h, cnt + 7, 8, cudaMemcpyDeviceToHost, s);
         if (cudaStreamSynchronize(s) != cudaSuccess) return bail(fail(RIA_ECUDA, cudaGetErrorString(cudaGetLastError())));
@@ -547,7 +607,7 @@ ria_status run_pipeline(const ria_config* cfg, const Inputs& in, cudaStream_t s,
         // block, the shortest per-tet time); many: the mid-size variant first (one tet per thread,
         // every SM full), the exact kernel for what remains
         n_def = n_def1;
-        if (n_def1 > kMidThreshold) {
+        if (n_def1 > tune.mid_threshold) {
             CutArgs cm = ca;
             cm.list = deferred;
             cm.n = n_def1;
@@ -559,7 +619,7 @@ ria_status run_pipeline(const ria_config* cfg, const Inputs& in, cudaStream_t s,
                 return bail(fail(RIA_ECUDA, cudaGetErrorString(cudaGetLastError())));
             n_def = (int64_t)(h & 0xFFFFFFFFull);
         }
-        uint32_t* big_list = n_def1 > kMidThreshold ? deferred2 : deferred;
+        uint32_t* big_list = n_def1 > tune.mid_threshold ? deferred2 : deferred;
         if (n_def > 0) {
             M->heap_big = M->keep.get<uint8_t>(n_def * kBigRecordBytes, &err);
             if (err != cudaSuccess) return bail(fail(RIA_ENOMEM, "device allocation failed"));
@@ -608,7 +668,7 @@ ria_status run_pipeline(const ria_config* cfg, const Inputs& in, cudaStream_t s,
     cudaEventRecord(ev[4], s);
     ranges.end();
 
-    unsigned long long h[16];
+    unsigned long long h[20];
     cudaMemcpyAsync(h, cnt, sizeof(h), cudaMemcpyDeviceToHost, s);
     cudaError_t se = cudaStreamSynchronize(s);
     if (se != cudaSuccess) return bail(fail(RIA_ECUDA, cudaGetErrorString(se)));
@@ -624,9 +684,9 @@ ria_status run_pipeline(const ria_config* cfg, const Inputs& in, cudaStream_t s,
     M->stats[RIA_STAT_NUM_VERTS] = M->ex.n_verts;
     M->stats[RIA_STAT_NUM_FACES] = M->ex.n_faces;
     M->stats[RIA_STAT_NUM_DEFERRED] = n_def;
-    M->stats[RIA_STAT_ROBUST_FAILURES] = (int64_t)h[10];
-    M->stats[RIA_STAT_ROBUST_TYPE2] = (int64_t)h[11];
-    M->stats[RIA_STAT_ROBUST_TYPE3] = (int64_t)h[12];
+    M->stats[RIA_STAT_ROBUST_FAILURES] = (int64_t)h[16];
+    M->stats[RIA_STAT_ROBUST_TYPE2] = (int64_t)h[17];
+    M->stats[RIA_STAT_ROBUST_TYPE3] = (int64_t)h[18];
     float ms_[4];
     for (int i = 0; i < 4; ++i) cudaEventElapsedTime(&ms_[i], ev[i], ev[i + 1]);
     for (int i = 0; i < 4; ++i) M->timings[i] = ms_[i] * 1e-3;
@@ -636,10 +696,10 @@ ria_status run_pipeline(const ria_config* cfg, const Inputs& in, cudaStream_t s,
     destroy_events();
     tmp.release();
     *out = M;
-    if (cfg->robust_test && (h[10] | h[11] | h[12])) {
+    if (cfg->robust_test && (h[16] | h[17] | h[18])) {
         // the reference reports the first of these that occurred (src/implicit_arrangement.cpp:329-343)
-        g_err = h[11] ? "type 2 failure (crash in the normal order)."
-                      : (h[12] ? "type 3 failure (crash in the reverse order)." : "type 1 failure (inconsistency).");
+        g_err = h[17] ? "type 2 failure (crash in the normal order)."
+                      : (h[18] ? "type 3 failure (crash in the reverse order)." : "type 1 failure (inconsistency).");
         return RIA_EINTERNAL;
     }
     return RIA_OK;
@@ -801,6 +861,7 @@ ria_status grid_batch_run(bool mi, const ria_config* cfg, const ria_grid_problem
     in.d_fv = d_fv;
     in.d_vmask = d_vmask;
     in.trusted_tets = true;
+    in.batch = true;
     st = run_pipeline(cfg, in, s, true, out);
     if (st != RIA_OK) {
         cudaEventDestroy(e0);
@@ -1359,6 +1420,38 @@ static ria_status ensure_gathered(ria_mesh* m, ria_mesh_field f) {
         m->keep.v.push_back(m->func_in_tet);
         m->have_fit = true;
     }
+    if (f >= RIA_MESH_EDGES && f <= RIA_MESH_CHAIN_EDGES && !m->have_conn) {
+        if (!m->batch.empty()) return fail(RIA_EINVAL, "edges, patches and chains are not available for a batch");
+        ConnArgs ca{m->ex.n_faces, m->ex.n_face_verts, m->ex.n_verts, m->ex.face_offsets, m->ex.face_verts,
+                    m->ex.face_func};
+        cudaError_t e = build_connectivity(ca, m->conn, m->s);
+        for (void* p : {(void*)m->conn.edges, (void*)m->conn.edge_face_offsets, (void*)m->conn.edge_faces,
+                        (void*)m->conn.face_edges, (void*)m->conn.patch_offsets, (void*)m->conn.patch_faces,
+                        (void*)m->conn.patch_labels, (void*)m->conn.chain_offsets, (void*)m->conn.chain_edges})
+            if (p) m->keep.v.push_back(p);
+        if (e == cudaErrorUnknown) return fail(RIA_EINTERNAL, "mesh connectivity: internal consistency check failed");
+        if (e != cudaSuccess) return fail(RIA_ECUDA, cudaGetErrorString(e));
+        m->have_conn = true;
+    }
+    if ((f == RIA_MESH_TET_VERT_OFFSETS || f == RIA_MESH_TET_VERTS || f == RIA_MESH_TET_FACE_OFFSETS ||
+         f == RIA_MESH_TET_FACES) &&
+        !m->have_maps) {
+        if (!m->batch.empty()) return fail(RIA_EINVAL, "the local-to-global maps are not available for a batch");
+        cudaError_t err = cudaSuccess;
+        m->tet_vert_offsets = m->keep.get<int64_t>(m->T + 1, &err);
+        m->tet_face_offsets = m->keep.get<int64_t>(m->T + 1, &err);
+        if (err != cudaSuccess) return fail(RIA_ENOMEM, "device allocation failed");
+        TetMapArgs ta{m->mi, m->A, m->T, m->act_tet, m->act_desc, m->act_mask, m->heap, m->heap_big, m->table,
+                      m->table_off, m->d_tets, m->res, m->ex.verts, m->ex.n_verts, m->ex.face_tet_offsets,
+                      m->ex.face_tets, m->ex.n_faces};
+        cudaError_t e = gather_tet_maps(ta, m->tet_vert_offsets, m->tet_face_offsets, &m->tet_verts, &m->n_tet_verts,
+                                        &m->tet_faces, &m->n_tet_faces, m->s);
+        if (m->tet_verts) m->keep.v.push_back(m->tet_verts);
+        if (m->tet_faces) m->keep.v.push_back(m->tet_faces);
+        if (e == cudaErrorUnknown) return fail(RIA_EINTERNAL, "local-to-global maps: records and mesh disagree");
+        if (e != cudaSuccess) return fail(RIA_ECUDA, cudaGetErrorString(e));
+        m->have_maps = true;
+    }
     return RIA_OK;
 }
 
@@ -1384,6 +1477,37 @@ uint64_t ria_mesh_count(const ria_mesh* mc, ria_mesh_field f) {
         case RIA_MESH_STATS: return RIA_NUM_STATS;
         case RIA_MESH_TIMINGS: return RIA_NUM_TIMINGS;
         case RIA_MESH_FUNC_VALS: return m->fv ? (uint64_t)m->V * m->F : 0;
+        case RIA_MESH_TET_VERT_OFFSETS:
+        case RIA_MESH_TET_FACE_OFFSETS: return (uint64_t)m->T + 1;
+        case RIA_MESH_TET_VERTS:
+            if (ensure_gathered(m, f) != RIA_OK) return 0;
+            return (uint64_t)m->n_tet_verts;
+        case RIA_MESH_TET_FACES:
+            if (ensure_gathered(m, f) != RIA_OK) return 0;
+            return (uint64_t)m->n_tet_faces;
+        case RIA_MESH_EDGES:
+        case RIA_MESH_EDGE_FACE_OFFSETS:
+        case RIA_MESH_EDGE_FACES:
+        case RIA_MESH_FACE_EDGES:
+        case RIA_MESH_PATCH_OFFSETS:
+        case RIA_MESH_PATCH_FACES:
+        case RIA_MESH_PATCH_LABELS:
+        case RIA_MESH_CHAIN_OFFSETS:
+        case RIA_MESH_CHAIN_EDGES: {
+            if (ensure_gathered(m, f) != RIA_OK) return 0;
+            const ConnOut& c = m->conn;
+            switch (f) {
+                case RIA_MESH_EDGES: return 2 * (uint64_t)c.n_edges;
+                case RIA_MESH_EDGE_FACE_OFFSETS: return (uint64_t)c.n_edges + 1;
+                case RIA_MESH_EDGE_FACES: return 2 * (uint64_t)m->ex.n_face_verts;
+                case RIA_MESH_FACE_EDGES: return (uint64_t)m->ex.n_face_verts;
+                case RIA_MESH_PATCH_OFFSETS: return (uint64_t)c.n_patches + 1;
+                case RIA_MESH_PATCH_FACES: return (uint64_t)m->ex.n_faces;
+                case RIA_MESH_PATCH_LABELS: return 2 * (uint64_t)c.n_patches;
+                case RIA_MESH_CHAIN_OFFSETS: return (uint64_t)c.n_chains + 1;
+                default: return (uint64_t)c.n_nm_edges;
+            }
+        }
     }
     return 0;
 }
@@ -1410,6 +1534,19 @@ ria_status ria_mesh_copy(const ria_mesh* mc, ria_mesh_field f, void* dst) {
         case RIA_MESH_STATS: std::memcpy(dst, m->stats, sizeof(m->stats)); return RIA_OK;
         case RIA_MESH_TIMINGS: std::memcpy(dst, m->timings, sizeof(m->timings)); return RIA_OK;
         case RIA_MESH_FUNC_VALS: src = m->fv; bytes = m->fv ? 8 * (size_t)m->V * m->F : 0; break;
+        case RIA_MESH_TET_VERT_OFFSETS: src = m->tet_vert_offsets; bytes = 8 * (size_t)(m->T + 1); break;
+        case RIA_MESH_TET_VERTS: src = m->tet_verts; bytes = 8 * (size_t)m->n_tet_verts; break;
+        case RIA_MESH_TET_FACE_OFFSETS: src = m->tet_face_offsets; bytes = 8 * (size_t)(m->T + 1); break;
+        case RIA_MESH_TET_FACES: src = m->tet_faces; bytes = 8 * (size_t)m->n_tet_faces; break;
+        case RIA_MESH_EDGES: src = m->conn.edges; bytes = 16 * (size_t)m->conn.n_edges; break;
+        case RIA_MESH_EDGE_FACE_OFFSETS: src = m->conn.edge_face_offsets; bytes = 8 * (size_t)(m->conn.n_edges + 1); break;
+        case RIA_MESH_EDGE_FACES: src = m->conn.edge_faces; bytes = 16 * (size_t)m->ex.n_face_verts; break;
+        case RIA_MESH_FACE_EDGES: src = m->conn.face_edges; bytes = 8 * (size_t)m->ex.n_face_verts; break;
+        case RIA_MESH_PATCH_OFFSETS: src = m->conn.patch_offsets; bytes = 8 * (size_t)(m->conn.n_patches + 1); break;
+        case RIA_MESH_PATCH_FACES: src = m->conn.patch_faces; bytes = 8 * (size_t)m->ex.n_faces; break;
+        case RIA_MESH_PATCH_LABELS: src = m->conn.patch_labels; bytes = 16 * (size_t)m->conn.n_patches; break;
+        case RIA_MESH_CHAIN_OFFSETS: src = m->conn.chain_offsets; bytes = 8 * (size_t)(m->conn.n_chains + 1); break;
+        case RIA_MESH_CHAIN_EDGES: src = m->conn.chain_edges; bytes = 8 * (size_t)m->conn.n_nm_edges; break;
         default: return fail(RIA_EINVAL, "unknown field");
     }
     if (bytes == 0) return RIA_OK;
@@ -1691,6 +1828,83 @@ void ria_server_destroy(ria_server* sv) {
 const char* ria_last_error(void) { return g_err.c_str(); }
 
 uint64_t ria_kernel_launches(void) { return g_launches.load(); }
+
+ria_status ria_get_tuning(ria_tuning* t) {
+    if (!t) return fail(RIA_EINVAL, "null argument");
+    int dev = 0;
+    ria_status st = current_device(&dev);
+    if (st != RIA_OK) return st;
+    std::lock_guard<std::mutex> lk(g_mu);
+    *t = (int)g_ctx.size() > dev ? g_ctx[dev].tune : kDefaultTuning;
+    return RIA_OK;
+}
+
+ria_status ria_set_tuning(const ria_tuning* t) {
+    if (!t || t->warp_route < 0 || t->warp_blocks_per_sm < 0 || t->mid_threshold < 0 || t->cut_graph < 0 ||
+        t->cut_graph > 2 || !(t->fast_block == 0 || t->fast_block == 32 || t->fast_block == 64 || t->fast_block == 128))
+        return fail(RIA_EINVAL, "tuning out of range");
+    int dev = 0;
+    ria_status st = current_device(&dev);
+    if (st != RIA_OK) return st;
+    std::lock_guard<std::mutex> lk(g_mu);
+    if ((int)g_ctx.size() <= dev) g_ctx.resize(dev + 1);
+    g_ctx[dev].tune = *t;
+    return RIA_OK;
+}
+
+ria_status ria_autotune(const ria_config* cfg, int32_t material_interface, const ria_grid_problem* problems,
+                        uint32_t n, uint32_t reps, ria_tuning* best, double* best_s, double* default_s) {
+    if (!cfg || !problems || n == 0) return fail(RIA_EINVAL, "null argument or no problems");
+    if (reps == 0) reps = 1;
+    ria_tuning start;
+    ria_status st = ria_get_tuning(&start);
+    if (st != RIA_OK) return st;
+    // median device time of the batch under one tuning record (secondary lookup reset before each run,
+    // so no run reuses another's records)
+    auto measure = [&](const ria_tuning& t, double* out) -> ria_status {
+        ria_status r = ria_set_tuning(&t);
+        if (r != RIA_OK) return r;
+        std::vector<double> v;
+        for (uint32_t k = 0; k < reps; ++k) {
+            if ((r = ria_lookup_cache_clear()) != RIA_OK) return r;
+            ria_mesh* m = nullptr;
+            if ((r = ria_grid_batch(cfg, material_interface, problems, n, &m)) != RIA_OK) return r;
+            v.push_back(m->timings[RIA_TIME_TOTAL]);
+            ria_mesh_free(m);
+        }
+        std::sort(v.begin(), v.end());
+        *out = v[v.size() / 2];
+        return RIA_OK;
+    };
+    double t0 = 0.0;
+    if ((st = measure(start, &t0)) != RIA_OK) return st;
+    ria_tuning bt = start;
+    double bs = t0;
+    const int64_t routes[] = {152 * 8 * 5, 152 * 8 * 10, 152 * 8 * 20, 152 * 8 * 40};
+    const int32_t blocks[] = {0, 4, 2};
+    const int32_t fast[] = {0, 64};
+    const int32_t graph[] = {1, 0};
+    for (int64_t r : routes)
+        for (int32_t b : blocks)
+            for (int32_t f : fast)
+                for (int32_t g : graph) {
+                    ria_tuning t{r, b, f, start.mid_threshold, g};
+                    double x = 0.0;
+                    if ((st = measure(t, &x)) != RIA_OK) {
+                        ria_set_tuning(&start);
+                        return st;
+                    }
+                    if (x < bs) {
+                        bs = x;
+                        bt = t;
+                    }
+                }
+    if ((st = ria_set_tuning(&bt)) != RIA_OK) return st;
+    if (best) *best = bt;
+    if (best_s) *best_s = bs;
+    if (default_s) *default_s = t0;
+    return RIA_OK;
+}
 
 ria_status ria_lookup_cache_clear(void) {
     int dev = 0;

@@ -28,12 +28,192 @@ __device__ __forceinline__ int local_func(uint64_t mask, int j) {  // j-th set b
     return __ffsll((long long)mask) - 1;
 }
 
+// ---- per-vertex keys of the records: the reference's dedup keys (implicit arrangement
+// src/extract_mesh.cpp:94-230, material interface :654-819)
+
+// iso flags of the local vertices of an IA record (vertex ids below 256)
+__device__ __forceinline__ void iso_vertex_flags(const IAView& r, uint64_t iso[4]) {
+    iso[0] = iso[1] = iso[2] = iso[3] = 0;
+    int off = 0;
+    for (int f = 0; f < r.nf; ++f) {
+        int L = r.len(f);
+        if (r.plane_is_iso(r.supp(f)))
+            for (int t = 0; t < L; ++t) {
+                int v = r.loopv(off + t);
+                iso[v >> 6] |= 1ull << (v & 63);
+            }
+        off += L;
+    }
+}
+
+__device__ __forceinline__ int iso_rank(const uint64_t iso[4], int v) {
+    int n = 0;
+    for (int w = 0; w < (v >> 6); ++w) n += __popcll(iso[w]);
+    return n + __popcll(iso[v >> 6] & ((1ull << (v & 63)) - 1));
+}
+
+struct VertKey {
+    int type;       // 1 corner, 2 edge, 3 face, 4 interior (simplex size)
+    int64_t sv[4];  // simplex vertex ids
+    int fn[3];      // global function ids
+};
+
+__device__ __forceinline__ VertKey ia_vertex_key(const IAView& r, int j, const int64_t tv[4], uint64_t mask) {
+    VertKey k;
+    const uint8_t* lab = r.vlab + 3 * j;
+    int nb = 0, bnd[3];
+    int ni = 0;
+    k.fn[0] = k.fn[1] = k.fn[2] = -1;
+    for (int t = 0; t < 3; ++t) {
+        if (lab[t] > 3)
+            k.fn[ni++] = local_func(mask, lab[t] - 4);
+        else
+            bnd[nb++] = lab[t];
+    }
+    for (int c = 0; c < 4; ++c) k.sv[c] = -1;
+    switch (nb) {
+        case 3: {
+            int c0 = 0;
+            for (int c = 0; c < 4; ++c)
+                if (c != bnd[0] && c != bnd[1] && c != bnd[2]) c0 = c;
+            k.type = 1;
+            k.sv[0] = tv[c0];
+            break;
+        }
+        case 2: {
+            int n = 0;
+            for (int c = 0; c < 4; ++c)
+                if (c != bnd[0] && c != bnd[1]) k.sv[n++] = tv[c];
+            if (k.sv[0] > k.sv[1]) {
+                int64_t x = k.sv[0];
+                k.sv[0] = k.sv[1];
+                k.sv[1] = x;
+            }
+            k.type = 2;
+            break;
+        }
+        case 1: {
+            int n = 0;
+            for (int c = 0; c < 4; ++c)
+                if (c != bnd[0]) k.sv[n++] = tv[c];
+            for (int x = 1; x < 3; ++x)
+                for (int y = x; y > 0 && k.sv[y - 1] > k.sv[y]; --y) {
+                    int64_t s = k.sv[y];
+                    k.sv[y] = k.sv[y - 1];
+                    k.sv[y - 1] = s;
+                }
+            k.type = 3;
+            break;
+        }
+        default:
+            for (int c = 0; c < 4; ++c) k.sv[c] = tv[c];
+            k.type = 4;
+    }
+    return k;
+}
+
+struct MIKey {
+    int type;  // 1 corner, 2 edge, 3 face, 4 interior, 0 not on an interface
+    int64_t sv[4];
+    int mats[4];
+};
+
+__device__ __forceinline__ int corner_of(const uint8_t* lab, int nb) {
+    for (int c = 0; c < 4; ++c) {
+        bool used = false;
+        for (int t = 0; t < nb; ++t) used = used || lab[t] == c;
+        if (!used) return c;
+    }
+    return 0;
+}
+
+__device__ __forceinline__ MIKey mi_vertex_key(const MIView& r, int j, const int64_t tv[4], uint64_t mask) {
+    MIKey k;
+    const uint8_t* lab = r.vlab + 4 * j;
+    int nb = 0, nm = 0;
+    uint8_t bnd[4];
+    for (int t = 0; t < 4; ++t) {
+        k.sv[t] = -1;
+        k.mats[t] = -1;
+    }
+    int ms[4];
+    for (int t = 0; t < 4; ++t) {
+        if (lab[t] > 3)
+            ms[nm++] = local_func(mask, lab[t] - 4);
+        else
+            bnd[nb++] = lab[t];
+    }
+    switch (nb) {
+        case 3:
+            k.type = 1;
+            k.sv[0] = tv[corner_of(bnd, 3)];
+            break;
+        case 2: {
+            int n = 0;
+            for (int c = 0; c < 4; ++c)
+                if (c != bnd[0] && c != bnd[1]) k.sv[n++] = tv[c];
+            if (k.sv[0] > k.sv[1]) {
+                int64_t x = k.sv[0];
+                k.sv[0] = k.sv[1];
+                k.sv[1] = x;
+            }
+            k.mats[0] = ms[0] < ms[1] ? ms[0] : ms[1];
+            k.mats[1] = ms[0] < ms[1] ? ms[1] : ms[0];
+            k.type = 2;
+            break;
+        }
+        case 1: {
+            int n = 0;
+            for (int c = 0; c < 4; ++c)
+                if (c != bnd[0]) k.sv[n++] = tv[c];
+            for (int x = 1; x < 3; ++x)
+                for (int y = x; y > 0 && k.sv[y - 1] > k.sv[y]; --y) {
+                    int64_t s = k.sv[y];
+                    k.sv[y] = k.sv[y - 1];
+                    k.sv[y - 1] = s;
+                }
+            for (int x = 0; x < 3; ++x) k.mats[x] = ms[x];
+            for (int x = 1; x < 3; ++x)
+                for (int y = x; y > 0 && k.mats[y - 1] > k.mats[y]; --y) {
+                    int s = k.mats[y];
+                    k.mats[y] = k.mats[y - 1];
+                    k.mats[y - 1] = s;
+                }
+            k.type = 3;
+            break;
+        }
+        default:
+            for (int c = 0; c < 4; ++c) {
+                k.sv[c] = tv[c];
+                k.mats[c] = ms[c];
+            }
+            k.type = 4;
+    }
+    return k;
+}
+
 // per-active-tet extraction counts widened for the scans
 static __global__ void k_base_in(int64_t A, const IASum4* __restrict__ sum, U4* __restrict__ out) {
     int64_t a = (int64_t)blockIdx.x * kBs + threadIdx.x;
     if (a >= A) return;
     IASum4 s = sum[a];
     out[a] = U4{s.a, s.b, s.c, s.d};
+}
+
+// per-tet offsets from per-active-tet offsets: off[t] = exclusive total before tet t
+static __global__ void k_expand_offsets(int64_t T, int64_t A, const uint32_t* __restrict__ act_tet,
+                                 const uint32_t* __restrict__ aoff, const uint32_t* __restrict__ asz,
+                                 int64_t* __restrict__ toff) {
+    const int64_t t = (int64_t)blockIdx.x * kBs + threadIdx.x;
+    if (t > T) return;
+    // number of active tets before t (binary search in the sorted act_tet)
+    int64_t lo = 0, hi = A;
+    while (lo < hi) {
+        int64_t mid = (lo + hi) >> 1;
+        if ((int64_t)act_tet[mid] < t) lo = mid + 1;
+        else hi = mid;
+    }
+    toff[t] = lo == 0 ? 0 : (int64_t)aoff[lo - 1] + (int64_t)asz[lo - 1];
 }
 
 // p[idx] = a[n-1] + b[n-1] (the total of an exclusive scan), or 0 when n == 0

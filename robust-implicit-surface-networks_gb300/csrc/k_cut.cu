@@ -861,14 +861,16 @@ void launch_warp_groups(const CutArgs& a, cudaStream_t s) {
     constexpr size_t smem = sizeof(IAWarpCutDev) * kGroups;
     // the shared-memory size, then the resident blocks on the device: once per process
     // (thread-safe static initialisation); the groups take tets from the list
-    static const int resident = [] {
+    static const int2 occ = [] {  // (SMs, resident blocks per SM)
         cudaFuncSetAttribute(k_cut_warp<G>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         int dev = 0, sms = 0, per_sm = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cut_warp<G>, 32 * kCutWarps, smem);
-        return (sms > 0 ? sms : 152) * (per_sm > 0 ? per_sm : 1);
+        return make_int2(sms > 0 ? sms : 152, per_sm > 0 ? per_sm : 1);
     }();
+    const int per_sm = a.warp_blocks_per_sm > 0 && a.warp_blocks_per_sm < occ.y ? a.warp_blocks_per_sm : occ.y;
+    const int64_t resident = (int64_t)occ.x * per_sm;
     const int64_t want = (a.n + kGroups - 1) / kGroups;
     const int64_t blocks = want < resident ? want : resident;
     k_cut_warp<G><<<(unsigned)blocks, 32 * kCutWarps, smem, s>>>(a);
@@ -886,7 +888,10 @@ void launch_cut_fast(const CutArgs& a, cudaStream_t s, bool mid) {
     if (a.n == 0) return;
     // each thread runs one long serial cut: with few tets, smaller blocks spread them over all SMs
     int bs = 128;
-    while (bs > 32 && (a.n + bs - 1) / bs < 4 * 152) bs >>= 1;
+    if (a.fast_block >= 32 && a.fast_block <= 128 && (a.fast_block & 31) == 0)  // __launch_bounds__(128)
+        bs = a.fast_block;
+    else
+        while (bs > 32 && (a.n + bs - 1) / bs < 4 * 152) bs >>= 1;
     const unsigned nb = (unsigned)((a.n + bs - 1) / bs);
     // the per-thread state lives in local memory: ask for the largest L1 (no shared memory used)
     static const bool carve = [] {  // once per process (thread-safe static initialisation)

@@ -51,127 +51,129 @@ struct ExtractCtx {
     uint64_t* iso0;   // per active tet: iso flags of its first 64 record vertices, from the vertex pass
 };
 
-// iso flags of the local vertices of an IA record (vertex ids below 256)
-__device__ __forceinline__ void iso_vertex_flags(const IAView& r, uint64_t iso[4]) {
-    iso[0] = iso[1] = iso[2] = iso[3] = 0;
-    int off = 0;
-    for (int f = 0; f < r.nf; ++f) {
-        int L = r.len(f);
-        if (r.plane_is_iso(r.supp(f)))
-            for (int t = 0; t < L; ++t) {
-                int v = r.loopv(off + t);
-                iso[v >> 6] |= 1ull << (v & 63);
-            }
-        off += L;
-    }
+// D2: keys of the iso vertices.  A warp takes 32 consecutive active tets, whose iso-vertex
+// occurrences are consecutive positions; every round, each lane takes one occurrence (its tet found
+// by a search over the lanes' counts, its local vertex as the r-th iso flag).  Lanes of a round with
+// equal keys are grouped (__match_any_sync), and only the group's lowest lane, which holds the
+// group's smallest position, inserts the key and lowers the owner; the others take its slot.  So
+// every lane works on every round, and each key reaches the global tables about once per warp.
+__device__ __forceinline__ int nth_set_bit(uint64_t x, int n) {
+    for (int k = 0; k < n; ++k) x &= x - 1;
+    return __ffsll((long long)x) - 1;
 }
 
-__device__ __forceinline__ int iso_rank(const uint64_t iso[4], int v) {
-    int n = 0;
-    for (int w = 0; w < (v >> 6); ++w) n += __popcll(iso[w]);
-    return n + __popcll(iso[v >> 6] & ((1ull << (v & 63)) - 1));
+__device__ __forceinline__ uint64_t shfl64(uint64_t v, int src) {
+    const uint32_t lo = __shfl_sync(0xFFFFFFFFu, (uint32_t)v, src);
+    const uint32_t hi = __shfl_sync(0xFFFFFFFFu, (uint32_t)(v >> 32), src);
+    return ((uint64_t)hi << 32) | lo;
 }
 
-struct VertKey {
-    int type;       // 1 corner, 2 edge, 3 face, 4 interior (simplex size)
-    int64_t sv[4];  // simplex vertex ids
-    int fn[3];      // global function ids
-};
-
-__device__ __forceinline__ VertKey ia_vertex_key(const IAView& r, int j, const int64_t tv[4], uint64_t mask) {
-    VertKey k;
-    const uint8_t* lab = r.vlab + 3 * j;
-    int nb = 0, bnd[3];
-    int ni = 0;
-    k.fn[0] = k.fn[1] = k.fn[2] = -1;
-    for (int t = 0; t < 3; ++t) {
-        if (lab[t] > 3)
-            k.fn[ni++] = local_func(mask, lab[t] - 4);
-        else
-            bnd[nb++] = lab[t];
-    }
-    for (int c = 0; c < 4; ++c) k.sv[c] = -1;
-    switch (nb) {
-        case 3: {
-            int c0 = 0;
-            for (int c = 0; c < 4; ++c)
-                if (c != bnd[0] && c != bnd[1] && c != bnd[2]) c0 = c;
-            k.type = 1;
-            k.sv[0] = tv[c0];
-            break;
-        }
-        case 2: {
-            int n = 0;
-            for (int c = 0; c < 4; ++c)
-                if (c != bnd[0] && c != bnd[1]) k.sv[n++] = tv[c];
-            if (k.sv[0] > k.sv[1]) {
-                int64_t x = k.sv[0];
-                k.sv[0] = k.sv[1];
-                k.sv[1] = x;
-            }
-            k.type = 2;
-            break;
-        }
-        case 1: {
-            int n = 0;
-            for (int c = 0; c < 4; ++c)
-                if (c != bnd[0]) k.sv[n++] = tv[c];
-            for (int x = 1; x < 3; ++x)
-                for (int y = x; y > 0 && k.sv[y - 1] > k.sv[y]; --y) {
-                    int64_t s = k.sv[y];
-                    k.sv[y] = k.sv[y - 1];
-                    k.sv[y - 1] = s;
-                }
-            k.type = 3;
-            break;
-        }
-        default:
-            for (int c = 0; c < 4; ++c) k.sv[c] = tv[c];
-            k.type = 4;
-    }
-    return k;
-}
-
-// D2: keys of the iso vertices
 __global__ void __launch_bounds__(kBs) k_ia_vert_keys(ExtractCtx C) {
     const int64_t a = (int64_t)blockIdx.x * kBs + threadIdx.x;
-    if (a >= C.a.A) return;
-    IAView r;
-    r.init(C.rs.get(C.a.act_desc[a]));
-    int64_t tv[4];
-    TetSrc ts{C.a.d_tets, C.a.g.res};
-    ts.get(C.a.act_tet[a], tv);
-    const uint64_t mask = C.a.act_mask[a];
-    uint64_t iso[4];
-    iso_vertex_flags(r, iso);
-    C.iso0[a] = iso[0];
-    uint32_t pos = C.base[a].a;
-    for (int j = 0; j < r.nv; ++j) {
-        if (!((iso[j >> 6] >> (j & 63)) & 1)) continue;
-        VertKey k = ia_vertex_key(r, j, tv, mask);
-        uint64_t occ;
-        if (k.type == 1) {
-            atomicMin(&C.corner_owner[k.sv[0]], pos);
-            occ = (OCC_CORNER << 62) | (uint64_t)k.sv[0];
-        } else if (k.type == 2) {
-            int64_t s = C.edge64
-                            ? ht64_insert_min(C.he64, ((uint64_t)k.sv[0] << 36) | ((uint64_t)k.sv[1] << 8) |
-                                                          (uint64_t)k.fn[0], pos)
-                            : ht_insert_min(C.he, ((uint64_t)k.sv[0] << 32) | (uint64_t)k.sv[1], (uint64_t)k.fn[0] + 1,
-                                            pos);
-            if (s < 0) raise_status(C.a.status, ST_HASH_FULL);
-            occ = (OCC_EDGE << 62) | (uint64_t)(s < 0 ? 0 : s);
-        } else if (k.type == 3) {
-            int64_t s = ht_insert_min(C.hf, ((uint64_t)k.sv[0] << 32) | (uint64_t)k.sv[1],
-                                      ((uint64_t)k.sv[2] << 32) | ((uint64_t)k.fn[0] << 16) | (uint64_t)k.fn[1], pos);
-            if (s < 0) raise_status(C.a.status, ST_HASH_FULL);
-            occ = (OCC_FACE << 62) | (uint64_t)(s < 0 ? 0 : s);
-        } else {
-            occ = OCC_SELF << 62;
+    const int lane = threadIdx.x & 31;
+    const bool valid = a < C.a.A;
+    const uint8_t* rec = nullptr;
+    int64_t tv[4] = {0, 0, 0, 0};
+    uint64_t mask = 0;
+    uint64_t iso[4] = {0, 0, 0, 0};
+    int n = 0;
+    uint32_t pos0 = 0;
+    if (valid) {
+        rec = C.rs.get(C.a.act_desc[a]);
+        IAView r;
+        r.init(rec);
+        TetSrc ts{C.a.d_tets, C.a.g.res};
+        ts.get(C.a.act_tet[a], tv);
+        mask = C.a.act_mask[a];
+        iso_vertex_flags(r, iso);
+        C.iso0[a] = iso[0];
+        n = __popcll(iso[0]) + __popcll(iso[1]) + __popcll(iso[2]) + __popcll(iso[3]);
+        pos0 = C.base[a].a;
+    }
+    int incl = n;
+    for (int o = 1; o < 32; o <<= 1) {
+        const int v = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+        if (lane >= o) incl += v;
+    }
+    const int total = __shfl_sync(0xFFFFFFFFu, incl, 31);
+    const uint32_t wpos = __shfl_sync(0xFFFFFFFFu, pos0, 0);  // lane 0's tet opens the warp's positions
+    const int64_t a0 = a - lane;
+    for (int base = 0; base < total; base += 32) {
+        const int i = base + lane;
+        const bool has = i < total;
+        // owner lane: the number of lanes whose inclusive count is at most i
+        int owner = 0;
+        for (int step = 16; step > 0; step >>= 1) {
+            const int v = __shfl_sync(0xFFFFFFFFu, incl, owner + step - 1);
+            if (has && v <= i) owner += step;
         }
-        C.vocc[pos] = occ;
-        C.vsrc[pos] = ((uint64_t)a << 8) | (uint64_t)j;
-        ++pos;
+        const int excl = __shfl_sync(0xFFFFFFFFu, incl - n, owner);
+        const uint64_t rp = shfl64((uint64_t)rec, owner);
+        int64_t otv[4];
+        for (int c = 0; c < 4; ++c) otv[c] = (int64_t)shfl64((uint64_t)tv[c], owner);
+        const uint64_t omask = shfl64(mask, owner);
+        uint64_t oiso[4];
+        for (int w = 0; w < 4; ++w) oiso[w] = shfl64(iso[w], owner);
+        int type = 0, j = 0;
+        VertKey k;
+        uint64_t k0 = (uint64_t)lane, k1 = ~0ull;  // lanes without a keyed occurrence match no one
+        if (has) {
+            int rr = i - excl;
+            for (int w = 0; w < 4; ++w) {
+                const int c = __popcll(oiso[w]);
+                if (rr < c) {
+                    j = 64 * w + nth_set_bit(oiso[w], rr);
+                    break;
+                }
+                rr -= c;
+            }
+            IAView r;
+            r.init((const uint8_t*)rp);
+            k = ia_vertex_key(r, j, otv, omask);
+            type = k.type;
+            if (type == 1) {
+                k0 = (uint64_t)k.sv[0];
+                k1 = 1;
+            } else if (type == 2) {
+                k0 = ((uint64_t)k.sv[0] << 32) | (uint64_t)k.sv[1];
+                k1 = ((uint64_t)k.fn[0] << 8) | 2;
+            } else if (type == 3) {
+                k0 = ((uint64_t)k.sv[0] << 32) | (uint64_t)k.sv[1];
+                k1 = ((uint64_t)k.sv[2] << 32) | ((uint64_t)k.fn[0] << 16) | ((uint64_t)k.fn[1] << 4) | 3;
+            } else {
+                k0 = (uint64_t)lane;  // inside the tet: always new
+                k1 = ~0ull;
+            }
+        }
+        const unsigned grp = __match_any_sync(0xFFFFFFFFu, k0) & __match_any_sync(0xFFFFFFFFu, k1);
+        const int leader = __ffs(grp) - 1;
+        const uint32_t pos = wpos + (uint32_t)i;
+        int64_t slot = 0;
+        if (has && leader == lane) {
+            if (type == 1) {
+                atomicMin(&C.corner_owner[k.sv[0]], pos);
+            } else if (type == 2) {
+                slot = C.edge64 ? ht64_insert_min(C.he64, ((uint64_t)k.sv[0] << 36) | ((uint64_t)k.sv[1] << 8) |
+                                                              (uint64_t)k.fn[0], pos)
+                                : ht_insert_min(C.he, ((uint64_t)k.sv[0] << 32) | (uint64_t)k.sv[1],
+                                                (uint64_t)k.fn[0] + 1, pos);
+                if (slot < 0) raise_status(C.a.status, ST_HASH_FULL);
+            } else if (type == 3) {
+                slot = ht_insert_min(C.hf, ((uint64_t)k.sv[0] << 32) | (uint64_t)k.sv[1],
+                                     ((uint64_t)k.sv[2] << 32) | ((uint64_t)k.fn[0] << 16) | (uint64_t)k.fn[1], pos);
+                if (slot < 0) raise_status(C.a.status, ST_HASH_FULL);
+            }
+        }
+        slot = (int64_t)shfl64((uint64_t)slot, leader);
+        if (has) {
+            uint64_t occ;
+            if (type == 1) occ = (OCC_CORNER << 62) | (uint64_t)k.sv[0];
+            else if (type == 2) occ = (OCC_EDGE << 62) | (uint64_t)(slot < 0 ? 0 : slot);
+            else if (type == 3) occ = (OCC_FACE << 62) | (uint64_t)(slot < 0 ? 0 : slot);
+            else occ = OCC_SELF << 62;
+            C.vocc[pos] = occ;
+            C.vsrc[pos] = ((uint64_t)(a0 + owner) << 8) | (uint64_t)j;
+        }
     }
 }
 
@@ -682,22 +684,6 @@ __global__ void k_rec_copy(bool mi, int64_t A, const uint64_t* __restrict__ desc
     const uint8_t* b = rs.get(desc[a]);
     const int n = mi ? mi_record_size(b) : ia_record_size(b);
     for (int i = 0; i < n; ++i) dst[off[a] + i] = b[i];
-}
-
-// per-tet offsets from per-active-tet offsets: off[t] = exclusive total before tet t
-__global__ void k_expand_offsets(int64_t T, int64_t A, const uint32_t* __restrict__ act_tet,
-                                 const uint32_t* __restrict__ aoff, const uint32_t* __restrict__ asz,
-                                 int64_t* __restrict__ toff) {
-    const int64_t t = (int64_t)blockIdx.x * kBs + threadIdx.x;
-    if (t > T) return;
-    // number of active tets before t (binary search in the sorted act_tet)
-    int64_t lo = 0, hi = A;
-    while (lo < hi) {
-        int64_t mid = (lo + hi) >> 1;
-        if ((int64_t)act_tet[mid] < t) lo = mid + 1;
-        else hi = mid;
-    }
-    toff[t] = lo == 0 ? 0 : (int64_t)aoff[lo - 1] + (int64_t)asz[lo - 1];
 }
 
 __global__ void k_popc(int64_t A, const uint64_t* __restrict__ mask, uint32_t* __restrict__ k) {

@@ -50,85 +50,6 @@ struct MICtx {
     uint32_t* any_emit;
 };
 
-struct MIKey {
-    int type;  // 1 corner, 2 edge, 3 face, 4 interior, 0 not on an interface
-    int64_t sv[4];
-    int mats[4];
-};
-
-__device__ __forceinline__ int corner_of(const uint8_t* lab, int nb) {
-    for (int c = 0; c < 4; ++c) {
-        bool used = false;
-        for (int t = 0; t < nb; ++t) used = used || lab[t] == c;
-        if (!used) return c;
-    }
-    return 0;
-}
-
-__device__ __forceinline__ MIKey mi_vertex_key(const MIView& r, int j, const int64_t tv[4], uint64_t mask) {
-    MIKey k;
-    const uint8_t* lab = r.vlab + 4 * j;
-    int nb = 0, nm = 0;
-    uint8_t bnd[4];
-    for (int t = 0; t < 4; ++t) {
-        k.sv[t] = -1;
-        k.mats[t] = -1;
-    }
-    int ms[4];
-    for (int t = 0; t < 4; ++t) {
-        if (lab[t] > 3)
-            ms[nm++] = local_func(mask, lab[t] - 4);
-        else
-            bnd[nb++] = lab[t];
-    }
-    switch (nb) {
-        case 3:
-            k.type = 1;
-            k.sv[0] = tv[corner_of(bnd, 3)];
-            break;
-        case 2: {
-            int n = 0;
-            for (int c = 0; c < 4; ++c)
-                if (c != bnd[0] && c != bnd[1]) k.sv[n++] = tv[c];
-            if (k.sv[0] > k.sv[1]) {
-                int64_t x = k.sv[0];
-                k.sv[0] = k.sv[1];
-                k.sv[1] = x;
-            }
-            k.mats[0] = ms[0] < ms[1] ? ms[0] : ms[1];
-            k.mats[1] = ms[0] < ms[1] ? ms[1] : ms[0];
-            k.type = 2;
-            break;
-        }
-        case 1: {
-            int n = 0;
-            for (int c = 0; c < 4; ++c)
-                if (c != bnd[0]) k.sv[n++] = tv[c];
-            for (int x = 1; x < 3; ++x)
-                for (int y = x; y > 0 && k.sv[y - 1] > k.sv[y]; --y) {
-                    int64_t s = k.sv[y];
-                    k.sv[y] = k.sv[y - 1];
-                    k.sv[y - 1] = s;
-                }
-            for (int x = 0; x < 3; ++x) k.mats[x] = ms[x];
-            for (int x = 1; x < 3; ++x)
-                for (int y = x; y > 0 && k.mats[y - 1] > k.mats[y]; --y) {
-                    int s = k.mats[y];
-                    k.mats[y] = k.mats[y - 1];
-                    k.mats[y - 1] = s;
-                }
-            k.type = 3;
-            break;
-        }
-        default:
-            for (int c = 0; c < 4; ++c) {
-                k.sv[c] = tv[c];
-                k.mats[c] = ms[c];
-            }
-            k.type = 4;
-    }
-    return k;
-}
 
 // flags of the local vertices on an interface face (vertex ids below 256)
 __device__ __forceinline__ void mi_vertex_flags(const MIView& r, uint64_t f[4]) {

@@ -140,6 +140,10 @@ struct CutArgs {
     // thread kernel (both are launched; the other returns at once)
     int64_t route_at = 0;
     unsigned int* next = nullptr;         // warp kernel: zeroed counter from which warps take tets in list order
+    // launch shapes chosen by the tuning record (ria_tuning): resident blocks of the warp kernel per
+    // SM (0: the occupancy limit) and threads per block of the thread kernel (0: from the tet count)
+    int warp_blocks_per_sm = 0;
+    int fast_block = 0;
     uint32_t* owners = nullptr;           // the lookup pass: tets that claimed their key (else in deferred)
     unsigned int* n_owners = nullptr;
     uint32_t* status;
@@ -248,6 +252,55 @@ cudaError_t run_extract(const ExtractArgs& a, const IASum4* act_sum, ExtractOut&
 // message on failure; allocates nothing
 int run_batch_noalloc(const double* d_values, const uint32_t* d_value_offsets, uint64_t n_tets, uint8_t* d_records,
                       uint64_t capacity, uint64_t* d_record_offsets, cudaStream_t s, const char** msg);
+
+// local-to-global maps of a finished mesh (k_tetmaps.cu, RIA_MESH_TET_*): per record vertex its mesh
+// vertex or -v-1, per record face its mesh face or -1, each a CRS over the tets
+struct TetMapArgs {
+    bool mi;
+    int64_t A, T;
+    const uint32_t* act_tet;
+    const uint64_t* act_desc;
+    const uint64_t* act_mask;
+    const uint8_t* heap;
+    const uint8_t* heap_big;
+    const uint8_t* table;
+    const uint32_t* table_off;
+    const int64_t* d_tets;  // explicit tets, or nullptr for the grid of `res` cubes
+    int64_t res;
+    const int64_t* verts;   // mesh vertex records [n_verts][11]
+    int64_t n_verts;
+    const int64_t* face_tet_offsets;
+    const int64_t* face_tets;
+    int64_t n_faces;
+};
+// d_vert_offsets / d_face_offsets: [T + 1]; the maps are allocated with cudaMallocAsync on `s`;
+// cudaErrorUnknown when the records and the mesh disagree
+cudaError_t gather_tet_maps(const TetMapArgs& m, int64_t* d_vert_offsets, int64_t* d_face_offsets,
+                            int64_t** d_tet_verts, int64_t* n_tet_verts, int64_t** d_tet_faces, int64_t* n_tet_faces,
+                            cudaStream_t s);
+
+// mesh connectivity (k_connect.cu): the reference's compute_mesh_edges, compute_patches and
+// compute_chains over a finished mesh (RIA_MESH_EDGE*, RIA_MESH_PATCH*, RIA_MESH_CHAIN*)
+struct ConnArgs {
+    int64_t n_faces, n_face_verts, n_verts;
+    const int64_t* face_offsets;
+    const int64_t* face_verts;
+    const int64_t* face_func;  // [n_faces][2]
+};
+struct ConnOut {
+    int64_t n_edges = 0, n_patches = 0, n_chains = 0, n_nm_edges = 0;
+    int64_t* edges = nullptr;              // [n_edges][2]
+    int64_t* edge_face_offsets = nullptr;  // [n_edges + 1]
+    int64_t* edge_faces = nullptr;         // [n_face_verts][2]: (face, local edge)
+    int64_t* face_edges = nullptr;         // [n_face_verts]: edges_of_face, by face_offsets
+    int64_t* patch_offsets = nullptr;      // [n_patches + 1]
+    int64_t* patch_faces = nullptr;        // [n_faces]
+    int64_t* patch_labels = nullptr;       // [n_patches][2]: func_index of the patch's first face
+    int64_t* chain_offsets = nullptr;      // [n_chains + 1]
+    int64_t* chain_edges = nullptr;        // [n_nm_edges]
+};
+// allocates the outputs with cudaMallocAsync on `s`; cudaErrorUnknown on an internal inconsistency
+cudaError_t build_connectivity(const ConnArgs& a, ConnOut& out, cudaStream_t s);
 
 // records in tet order (for RIA_MESH_REC_*)
 cudaError_t gather_records(bool mi, int64_t A, int64_t T, const uint32_t* act_tet, const uint64_t* act_desc,

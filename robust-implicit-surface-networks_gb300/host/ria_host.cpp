@@ -118,23 +118,45 @@ bool run_pipeline(bool mi, bool robust_test, bool use_lookup, bool use_secondary
     }
     timing_labels.emplace_back("device to host");
     timings.push_back(t1 - t0 - tm[RIA_TIME_TOTAL]);
-    // host stages
+    // edges, patches and chains (src/mesh_connectivity.cpp:10-242): computed on the device with the
+    // reference's numbering and orders, then laid out in the reference's containers
     double h0 = now();
-    std::vector<std::vector<size_t>> edges_of_face;
-    compute_mesh_edges(faces, edges_of_face, edges);
+    auto eo = dm.i64(RIA_MESH_EDGE_FACE_OFFSETS);  // the first request builds all three on the device
+    if (eo.empty()) {  // n_edges + 1 entries when it succeeded
+        std::cout << ria_last_error() << std::endl;
+        return false;
+    }
+    auto ev = dm.i64(RIA_MESH_EDGES), ef = dm.i64(RIA_MESH_EDGE_FACES);
+    edges.assign(ev.size() / 2, Edge());
+    parallel_ranges(edges.size(), 1 << 15, [&](size_t lo, size_t hi) {
+        for (size_t e = lo; e < hi; ++e) {
+            edges[e].v1 = (size_t)ev[2 * e];
+            edges[e].v2 = (size_t)ev[2 * e + 1];
+            auto& fe = edges[e].face_edge_indices;
+            fe.reserve((size_t)(eo[e + 1] - eo[e]));
+            for (int64_t o = eo[e]; o < eo[e + 1]; ++o) fe.emplace_back((size_t)ef[2 * o], (size_t)ef[2 * o + 1]);
+        }
+    });
     double h1 = now();
     timing_labels.emplace_back(mi ? "MIEdge-face connectivity" : "isoEdge-face connectivity");
     timings.push_back(h1 - h0);
     stats_labels.emplace_back(mi ? "num_MI_edges" : "num_iso_edges");
     stats.push_back(edges.size());
-    std::vector<std::pair<size_t, size_t>> labels;
-    compute_patches(edges_of_face, edges, faces, patches, labels);
+    auto lists = [](const std::vector<int64_t>& off, const std::vector<int64_t>& val,
+                    std::vector<std::vector<size_t>>& out) {
+        out.assign(off.empty() ? 0 : off.size() - 1, {});
+        parallel_ranges(out.size(), 1 << 12, [&](size_t lo, size_t hi) {
+            for (size_t i = lo; i < hi; ++i) out[i].assign(val.begin() + off[i], val.begin() + off[i + 1]);
+        });
+    };
+    lists(dm.i64(RIA_MESH_PATCH_OFFSETS), dm.i64(RIA_MESH_PATCH_FACES), patches);
+    auto pl = dm.i64(RIA_MESH_PATCH_LABELS);
     patch_function_label.clear();
-    for (auto& l : labels) {
+    for (size_t p = 0; p < patches.size(); ++p) {
         if constexpr (std::is_same<Label, size_t>::value)
-            patch_function_label.push_back(l.first);
+            patch_function_label.push_back(none_or(pl[2 * p]));
         else
-            patch_function_label.push_back(l);
+            patch_function_label.push_back({none_or(pl[2 * p]), none_or(pl[2 * p + 1])});
     }
     double h2 = now();
     timing_labels.emplace_back("patches");
@@ -143,11 +165,11 @@ bool run_pipeline(bool mi, bool robust_test, bool use_lookup, bool use_secondary
     stats.push_back(patches.size());
     nm_edges_of_vert.assign(out_pts.size(), {});
     for (size_t i = 0; i < edges.size(); ++i)
-        if (edges[i].face_edge_indices.size() > 2) {
+        if (eo[i + 1] - eo[i] > 2) {
             nm_edges_of_vert[edges[i].v1].push_back(i);
             nm_edges_of_vert[edges[i].v2].push_back(i);
         }
-    compute_chains(edges, nm_edges_of_vert, chains);
+    lists(dm.i64(RIA_MESH_CHAIN_OFFSETS), dm.i64(RIA_MESH_CHAIN_EDGES), chains);
     timing_labels.emplace_back("chains");
     timings.push_back(now() - h2);
     stats_labels.emplace_back("num_chains");

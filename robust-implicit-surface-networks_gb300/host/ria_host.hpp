@@ -11,17 +11,46 @@
 // sign propagation are not part of this build: `shells`, `arrangement_cells` and
 // `cell_function_label` come back empty.
 #pragma once
+#include <algorithm>
 #include <array>
+#include <atomic>
 #include <cstddef>
 #include <functional>
 #include <limits>
 #include <string>
+#include <thread>
 #include <utility>
 #include <vector>
 
 #include "../../include/ria.h"
 
 namespace ria_host {
+
+// Host threads for the parallel host stages, and a parallel loop over contiguous ranges.
+inline size_t host_threads() {
+    const unsigned hw = std::thread::hardware_concurrency();
+    return std::min<size_t>(hw ? hw : 1, 32);
+}
+
+// f(lo, hi) over [0, n) in contiguous chunks (at most ceil(n / grain) of them, and at most four per
+// thread), on up to host_threads() threads
+template <class F>
+void parallel_ranges(size_t n, size_t grain, const F& f) {
+    const size_t chunks = std::min(host_threads() * 4, (n + grain - 1) / grain);
+    if (chunks <= 1) {
+        if (n) f(size_t(0), n);
+        return;
+    }
+    std::atomic<size_t> next{0};
+    auto work = [&] {
+        for (size_t c; (c = next.fetch_add(1)) < chunks;) f(n * c / chunks, n * (c + 1) / chunks);
+    };
+    std::vector<std::thread> pool;
+    for (size_t t = 1; t < std::min(host_threads(), chunks); ++t) pool.emplace_back(work);
+    work();
+    for (auto& t : pool) t.join();
+}
+
 
 constexpr size_t Mesh_None = std::numeric_limits<size_t>::max();
 

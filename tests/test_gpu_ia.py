@@ -17,10 +17,17 @@ pytestmark = pytest.mark.gpu
 XYZ_RTOL = 1e-12
 
 
-def assert_mesh_equal(mesh, ref, records=True):
+def assert_mesh_equal(mesh, ref, records=True, maps=True):
+    """Every field of a device mesh against the oracle's; `maps`: also the local-to-global maps of the
+    extraction variants (src/extract_mesh.cpp:268-566, 988-1443)."""
     for k in ("verts", "face_offsets", "face_verts", "face_tet_offsets", "face_tets", "face_func"):
         a, b = mesh[k], ref[k]
         assert a.shape == b.shape and np.array_equal(a, b), k
+    if maps:
+        assert not (ref["tet_verts"] == np.iinfo(np.int64).min).any(), "oracle: vertex on no face is not a corner"
+        for k in ("tet_vert_offsets", "tet_verts", "tet_face_offsets", "tet_faces"):
+            a, b = mesh[k], ref[k]
+            assert a.shape == b.shape and np.array_equal(a, b), k
     x, y = mesh["xyz"], ref["xyz"]
     assert x.shape == y.shape
     assert np.all(np.abs(x - y) <= XYZ_RTOL * np.maximum(1.0, np.abs(y)))
@@ -30,6 +37,7 @@ def assert_mesh_equal(mesh, ref, records=True):
         assert np.array_equal(mesh["rec_offsets"], ref["rec_offsets"])
         assert np.array_equal(mesh["rec_bytes"], ref["rec_bytes"])
     st = mesh.stats
+    assert st["robust_failures"] == st["robust_type2"] == st["robust_type3"] == 0
     rs = ref["stats_named"]
     for k in ("num_pts", "num_tets", "num_degenerate_vertex", "num_intersecting_tet", "num_a_func", "num_b_func",
               "num_more_func", "num_verts", "num_faces"):
