@@ -42,6 +42,11 @@ PKG = "robust-implicit-surface-networks_gb300"
 
 METRIC = "tets/s (arrangement+extract) on 1 GB300"
 
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one k_sample launch on the large
+# degenerate workload, from one ncu capture of that launch
+SAMPLE_TRAFFIC_WORKLOAD = "ia-degenerate-32func-res128"
+SAMPLE_TRAFFIC = 4809728 + 521974528
+
 
 def _peaks():
     try:
@@ -364,9 +369,11 @@ def run_serve(args, world, local):
     print(json.dumps(line))
 
 
-def algorithmic_bytes(wl, st, n_fit, n_rec):
-    """Bytes each stage must move at least (per-unit figures in the design doc); n_fit = sum of active
-    functions over the active tets, n_rec = record bytes."""
+def algorithmic_bytes(wl, st, n_fit, n_rec, n_face_verts, n_face_tets):
+    """Bytes each stage must move at least: n_fit = sum of active functions over the active tets,
+    n_rec = record bytes; the extraction reads the active lists and every record once and writes the
+    points, the vertex records (11 int64) and the face lists (vertex ids, offsets, (tet, face) pairs,
+    function pairs)."""
     V, T, F = wl.n_verts, wl.n_tets, len(wl.funcs)
     A = st["num_intersecting_tet"]
     nv, nf = st["num_verts"], st["num_faces"]
@@ -374,52 +381,88 @@ def algorithmic_bytes(wl, st, n_fit, n_rec):
         "sample": 8 * V * F + 16 * V,           # values written + per-vertex masks written
         "filter": 16 * V + 28 * A,              # masks read once + active-tet lists written
         "cut": 32 * n_fit + n_rec,              # corner values read + records written
-        "extract": 20 * A + 24 * nv + 88 * nv + 8 * 4 * nf,  # lists read + points, vertex records, faces
+        "extract": 20 * A + n_rec + 24 * nv + 88 * nv + 8 * n_face_verts + 16 * nf + 16 * n_face_tets + 16 * nf,
     }
 
 
-def cpu_slab(wl, seconds_target=12.0):
-    """A contiguous slab of cube layers of the workload grid (re-indexed): the bounded CPU sample."""
+# FP64 operations per grid vertex of each function kind in the sampler (include/ria.h formulas, with
+# the first sum of every formula tabulated per (x, y) column): additions, multiplications
+SAMPLE_FP64_OPS = {1: (1, 0), 2: (2, 0), 3: (2, 1), 4: (7, 6), 5: (9, 8), 0: (0, 0)}
+
+
+def sample_fp64_ops(wl):
+    """FP64 additions and multiplications the sampling formulas need over the grid (algorithmic)."""
+    per_vertex = sum(sum(SAMPLE_FP64_OPS[int(t)]) for t in wl.funcs["type"])
+    return per_vertex * wl.n_verts
+
+
+def fp64_rate(L):
+    """Measured FP64 add/mul and fused multiply-add rates of this GPU (ria_measure_fp64_rate)."""
+    import ctypes
+
+    out = {}
+    for op, name in ((0, "fma"), (1, "add")):
+        r = ctypes.c_double()
+        out[name] = r.value if L.ria_measure_fp64_rate(op, ctypes.byref(r)) == 0 else None
+    return out
+
+
+def cpu_slabs(wl, parts=3):
+    """The workload grid cut into `parts` contiguous x-slabs of cube layers (each re-indexed as a grid
+    of its own); together they hold every tet of the grid once."""
     fns = importlib.import_module(PKG + ".functions")
     res = wl.res
     n = res + 1
-    layers = max(1, min(res, int(round(res * seconds_target / 60.0))))
-    i0 = (res - layers) // 2
-    xs, ys, zs = fns.grid_coords(res, wl.bbox_min, wl.bbox_max)
-    import numpy as np
-
     pts_all, tets_all = fns.generate_tet_mesh(res, wl.bbox_min, wl.bbox_max)
     per_layer = 5 * res * res
-    tets = tets_all[i0 * per_layer:(i0 + layers) * per_layer] - i0 * n * n
-    pts = pts_all[i0 * n * n:(i0 + layers + 1) * n * n]
-    return pts, tets, f"{layers} of {res} cube layers ({len(tets)} tets), x-slab starting at layer {i0}"
+    out = []
+    for p in range(parts):
+        i0, i1 = res * p // parts, res * (p + 1) // parts
+        tets = tets_all[i0 * per_layer:i1 * per_layer] - i0 * n * n
+        pts = pts_all[i0 * n * n:(i1 + 1) * n * n]
+        out.append((pts, tets, i0, i1))
+    return out
 
 
-def run_reference(args, wl, world):
+def cpu_whole_grid(wl, threads, parts=3):
+    """Stages a-d of the CPU restatement over the whole workload grid, in x-slabs: (tets/s over the
+    grid, per-slab tets/s, description)."""
     sys.path.insert(0, os.path.join(REPO, "oracle"))
     import pyoracle
 
     pyoracle.build()
-    cores = os.cpu_count() or 1
-    pts, tets, desc = cpu_slab(wl)
-    times = []
-    for it in range(args.warmup + args.steps):
+    total_t, total_n, rates = 0.0, 0, []
+    for pts, tets, i0, i1 in cpu_slabs(wl, parts):
         t0 = time.perf_counter()
-        fv = pyoracle.sample(wl.funcs, pts, threads=cores)
-        pyoracle.run(wl.mode, pts, tets, fv, threads=cores)
+        fv = pyoracle.sample(wl.funcs, pts, threads=threads)
+        pyoracle.run(wl.mode, pts, tets, fv, threads=threads)
         dt = time.perf_counter() - t0
+        total_t += dt
+        total_n += len(tets)
+        rates.append(len(tets) / dt)
+    desc = (f"the whole grid ({total_n} tets) in {parts} x-slabs of cube layers; stages a-d of the CPU "
+            f"restatement (oracle/)")
+    return total_n / total_t, rates, desc
+
+
+def run_reference(args, wl, world):
+    """The CPU restatement over the whole workload, every host thread for stages a-c (the extraction is
+    serial, as in the reference); each step is one pass over the grid."""
+    cores = os.cpu_count() or 1
+    vals = []
+    for it in range(args.warmup + args.steps):
+        v, _, desc = cpu_whole_grid(wl, cores)
         if it >= args.warmup:
-            times.append(dt)
-    per = statistics.median(times)
-    value = len(tets) / per
+            vals.append(v)
+    value = statistics.median(vals)
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "tets/s", "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": per * 1e3, "higher_is_better": True, "scaling": "weak",
+        "warmup": args.warmup, "ms_per_step": wl.n_tets / value * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
         "config": {"workload": wl.name, "tets": wl.n_tets, "functions": len(wl.funcs), "sample": desc},
         "cpu_baseline": {"value": value, "unit": "tets/s", "cores": cores, "kind": "port",
-                         "sample": desc + "; stages a-d of the CPU restatement (oracle/), stages a-c threaded, "
-                                          "extraction single-threaded as in the reference"},
+                         "sample": desc + ", stages a-c on every host thread, extraction single-threaded as in "
+                                          "the reference; median of the steps"},
         "e2e": {"value": value, "unit": "tets/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -552,11 +595,22 @@ def main():
     peak, peak_kind = _peaks()
     m = grid(wl.res, wl.funcs)  # counts for the byte model (untimed)
     n_fit, n_rec = len(m["func_in_tet"]), len(m["rec_bytes"])
+    n_fvert = int(L.ria_mesh_count(m._h, pkg.Mesh._FIELDS["face_verts"][0]))
+    n_ftet = int(L.ria_mesh_count(m._h, pkg.Mesh._FIELDS["face_tets"][0])) // 2
     m.close()
-    ab = algorithmic_bytes(wl, st, n_fit, n_rec)
+    ab = algorithmic_bytes(wl, st, n_fit, n_rec, n_fvert, n_ftet)
     stage_ms = {k: statistics.mean(v) for k, v in stage.items()}
-    dom = max(stage_ms, key=stage_ms.get)
+    rates = fp64_rate(L)
+    # the dominant kernel is the sampler (the largest share of the launch list); it is bound by the
+    # FP64 pipe, so its FP64 fraction is reported beside its HBM fraction
+    dom = "sample"
     achieved = ab[dom] / (stage_ms[dom] * 1e-3) / 1e9
+    ops = sample_fp64_ops(wl) if wl.mode in ("ia", "mi") else None
+    fp64 = {"kernel": "k_sample", "ops_per_launch": ops,
+            "achieved": ops / (stage_ms[dom] * 1e-3) / 1e9 if ops else None,
+            "peak": rates["add"] / 1e9 if rates.get("add") else None, "unit": "G FP64 add/mul per s",
+            "peak_kind": "measured (ria_measure_fp64_rate, this run)"}
+    fp64["frac"] = fp64["achieved"] / fp64["peak"] if fp64["achieved"] and fp64["peak"] else None
     line = {
         "metric": METRIC, "value": value, "unit": "tets/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
@@ -569,24 +623,21 @@ def main():
         "wall_ms_per_step": wall / args.steps * 1e3,
         "e2e": {"value": e2e, "unit": "tets/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
         "gpu_launches": launches,
-        "roofline": {"bound": "hbm", "kernel_stage": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "peak_kind": peak_kind, "traffic": None,
+        "roofline": {"bound": "hbm", "kernel": "k_sample", "kernel_stage": dom, "achieved": achieved, "peak": peak,
+                     "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
+                     "algorithmic_bytes": ab[dom], "traffic": SAMPLE_TRAFFIC if wl.name == SAMPLE_TRAFFIC_WORKLOAD else None,
+                     "fp64": fp64,
                      "stage_frac": {k: ab[k] / (stage_ms[k] * 1e-3) / 1e9 / peak for k in stage_ms},
-                     "note": "the cut is latency-bound and sampling FP64-bound (profiles/): HBM fractions are low"},
+                     "stage_algorithmic_bytes": ab,
+                     "note": "sampling is bound by the FP64 pipe (fp64.frac); the cut and the extraction are "
+                             "latency-bound (see the ncu summaries): their HBM fractions are low"},
         "clocks": clk.summary(),
     }
     if not args.no_cpu_baseline:
-        sys.path.insert(0, os.path.join(REPO, "oracle"))
-        import pyoracle
-
-        pyoracle.build()
-        cpts, ctets, desc = cpu_slab(wl)
-        t0 = time.perf_counter()
-        cfv = pyoracle.sample(wl.funcs, cpts, threads=1)
-        pyoracle.run(wl.mode, cpts, ctets, cfv, threads=1)
-        dt = time.perf_counter() - t0
-        line["cpu_baseline"] = {"value": len(ctets) / dt, "unit": "tets/s", "cores": 1, "kind": "port",
-                                "sample": desc + "; stages a-d of the CPU restatement (oracle/), one thread"}
+        v, per_slab, desc = cpu_whole_grid(wl, 1)
+        line["cpu_baseline"] = {"value": v, "unit": "tets/s", "cores": 1, "kind": "port",
+                                "sample": desc + ", one thread; tets/s per slab " +
+                                          ", ".join("%.3g" % r for r in per_slab)}
     print(json.dumps(line))
     if dist:
         dist.destroy_process_group()

@@ -29,6 +29,8 @@ def test_reference_arm_grid_config():
     d = _bench("--impl", "reference", "--config", "ia-small", "--steps", "2", "--warmup", "3")
     _check_reference_line(d, 2, 3)
     assert d["config"]["workload"].startswith("ia-")
+    # the whole workload, not a sample of it
+    assert "the whole grid (%d tets)" % d["config"]["tets"] in d["config"]["sample"]
 
 
 def test_reference_arm_batch_all_cores():
