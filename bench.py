@@ -213,6 +213,14 @@ def run_batch(args, world, local):
     L = pkg.load()
     wl = fns.workload_batch(n=args.batch_n)
     probs = wl.problems
+    # the project's autotuner on a sample of the batch (the first 256 grids) chooses the cut's bins,
+    # launch shapes and graph capture for this device before anything is timed
+    tuned = None
+    if not args.no_tune:
+        t0 = time.perf_counter()
+        rec, best_s, dflt_s = pkg.autotune(probs[:256], reps=2)
+        tuned = {"record": rec, "sample_problems": min(256, len(probs)), "sample_best_ms": best_s * 1e3,
+                 "sample_default_ms": dflt_s * 1e3, "tuner_wall_s": time.perf_counter() - t0}
     for _ in range(args.warmup):
         pkg.grid_batch(probs).close()
     launches0 = int(L.ria_kernel_launches())
@@ -269,6 +277,7 @@ def run_batch(args, world, local):
         "e2e": {"value": wl.n_tets / statistics.median(e2e_t) if e2e_t else None, "unit": "tets/s",
                 "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
         "gpu_launches": launches,
+        "tuning": tuned if tuned else {"record": pkg.get_tuning()},
         "per_problem_plain": {"tets_per_s_wall": wl.n_tets / plain_wall, "wall_s": plain_wall,
                               "device_s": plain_dev, "batch_speedup_wall": plain_wall / (wall / args.steps)},
         "roofline": {"bound": "hbm", "kernel_stage": "total", "achieved": None, "peak": peak, "unit": "GB/s",
@@ -483,6 +492,7 @@ def main():
     ap.add_argument("--res", type=int, default=None, help="grid resolution override (small profiling cases)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer end-to-end leg (profiling runs)")
+    ap.add_argument("--no-tune", action="store_true", help="--config batch: keep the current tuning record")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -9,6 +9,7 @@
 
 #include <cub/cub.cuh>
 #include <algorithm>
+#include <initializer_list>
 #include <atomic>
 #include <chrono>
 #include <cstring>
@@ -50,7 +51,15 @@ ria_status fail(ria_status s, const std::string& msg) {
 // the tuning record's defaults (ria_tuning; ria_autotune replaces them per device): 24,320 tets cut
 // a warp each, the warp kernel at its occupancy limit, the thread kernel's block from the tet count,
 // the mid-size variant past 3,040 deferred tets, the cut stage captured as a graph for batched grids
-constexpr ria_tuning kDefaultTuning = {152 * 20 * 8, 0, 0, 4 * 152 * 5, 1};
+constexpr ria_tuning kDefaultTuning = {152 * 20 * 8, 0, 0, 4 * 152 * 5, 1, 0};
+
+// the first light bin of the general-case list (bins hold tets of equal active count, heaviest first)
+int first_light_bin(bool mi, int heavy_min_k) {
+    if (heavy_min_k <= 0) return kFirstSmallBin(mi);
+    const int kk = heavy_min_k - 1 - (mi ? 1 : 0);  // the heaviest light count, as the bins count it
+    const int b = kGenBins - (kk < kGenBins ? kk : kGenBins);
+    return b < 1 ? 1 : (b > kGenBins ? kGenBins : b);
+}
 
 struct DeviceCtx {
     bool ready[2] = {false, false};
@@ -430,7 +439,8 @@ ria_status run_pipeline(const ria_config* cfg, const Inputs& in, cudaStream_t s,
         cudaMemcpyAsync(&h[0], blk_off + nb, 4, cudaMemcpyDeviceToHost, s);
         cudaMemcpyAsync(&h[1], blk_off + nscan - 1, 4, cudaMemcpyDeviceToHost, s);
         cudaMemcpyAsync(&h[2], blk + nscan - 1, 4, cudaMemcpyDeviceToHost, s);
-        cudaMemcpyAsync(&h[3], blk_off + (1 + kFirstSmallBin(mi)) * nb, 4, cudaMemcpyDeviceToHost, s);
+        const int light0 = first_light_bin(mi, ctx->tune.heavy_min_k);
+        cudaMemcpyAsync(&h[3], blk_off + (1 + light0) * nb, 4, cudaMemcpyDeviceToHost, s);
         if (cudaStreamSynchronize(s) != cudaSuccess) return bail(fail(RIA_ECUDA, cudaGetErrorString(cudaGetLastError())));
         A = h[0];
         G = (int64_t)h[1] + h[2] - A;
@@ -592,10 +602,13 @@ ria_status run_pipeline(const ria_config* cfg, const Inputs& in, cudaStream_t s,
         if (G_light > 0 && !mi) {
             // the light bins' cuts after the heavy bins' (both warp kernels are bound by the same
             // per-SM shared memory): a warp per tet while the list is short, decided on the device
-            cl.route_at = tune.warp_route;
-            CutArgs cw = cl;
-            cw.next = (unsigned int*)(cnt + 14);
-            launch_cut_warp(cw, s);
+            // (a record with warp_route 0 sends every tet to the thread kernel)
+            if (tune.warp_route > 0) {
+                cl.route_at = tune.warp_route;
+                CutArgs cw = cl;
+                cw.next = (unsigned int*)(cnt + 14);
+                launch_cut_warp(cw, s);
+            }
             launch_cut_fast(cl, s, false);
         }
         if (graph.capturing && graph.finish(s) != cudaSuccess) return bail(fail(RIA_ECUDA, "cut graph launch failed"));
@@ -1841,7 +1854,8 @@ ria_status ria_get_tuning(ria_tuning* t) {
 
 ria_status ria_set_tuning(const ria_tuning* t) {
     if (!t || t->warp_route < 0 || t->warp_blocks_per_sm < 0 || t->mid_threshold < 0 || t->cut_graph < 0 ||
-        t->cut_graph > 2 || !(t->fast_block == 0 || t->fast_block == 32 || t->fast_block == 64 || t->fast_block == 128))
+        t->cut_graph > 2 || !(t->fast_block == 0 || t->fast_block == 32 || t->fast_block == 64 || t->fast_block == 128) ||
+        !(t->heavy_min_k == 0 || (t->heavy_min_k >= 3 && t->heavy_min_k <= 8)))
         return fail(RIA_EINVAL, "tuning out of range");
     int dev = 0;
     ria_status st = current_device(&dev);
@@ -1880,25 +1894,35 @@ ria_status ria_autotune(const ria_config* cfg, int32_t material_interface, const
     if ((st = measure(start, &t0)) != RIA_OK) return st;
     ria_tuning bt = start;
     double bs = t0;
-    const int64_t routes[] = {152 * 8 * 5, 152 * 8 * 10, 152 * 8 * 20, 152 * 8 * 40};
-    const int32_t blocks[] = {0, 4, 2};
-    const int32_t fast[] = {0, 64};
-    const int32_t graph[] = {1, 0};
-    for (int64_t r : routes)
-        for (int32_t b : blocks)
-            for (int32_t f : fast)
-                for (int32_t g : graph) {
-                    ria_tuning t{r, b, f, start.mid_threshold, g};
-                    double x = 0.0;
-                    if ((st = measure(t, &x)) != RIA_OK) {
-                        ria_set_tuning(&start);
-                        return st;
-                    }
-                    if (x < bs) {
-                        bs = x;
-                        bt = t;
-                    }
-                }
+    // coordinate descent: each field over its candidates, the others at their best so far
+    auto field = [&](auto set, std::initializer_list<int64_t> values) -> ria_status {
+        for (int64_t v : values) {
+            ria_tuning t = bt;
+            set(t, v);
+            double x = 0.0;
+            ria_status r = measure(t, &x);
+            if (r != RIA_OK) return r;
+            if (x < bs) {
+                bs = x;
+                bt = t;
+            }
+        }
+        return RIA_OK;
+    };
+    for (int sweep = 0; sweep < 2 && st == RIA_OK; ++sweep) {
+        if (st == RIA_OK) st = field([](ria_tuning& t, int64_t v) { t.heavy_min_k = (int32_t)v; }, {4, 3, 5});
+        if (st == RIA_OK)
+            st = field([](ria_tuning& t, int64_t v) { t.warp_route = v; },
+                       {152 * 8 * 5, 152 * 8 * 10, 152 * 8 * 20, 152 * 8 * 40, 152 * 8 * 80});
+        if (st == RIA_OK) st = field([](ria_tuning& t, int64_t v) { t.warp_blocks_per_sm = (int32_t)v; }, {0, 4, 2});
+        if (st == RIA_OK) st = field([](ria_tuning& t, int64_t v) { t.fast_block = (int32_t)v; }, {0, 32, 64, 128});
+        if (st == RIA_OK) st = field([](ria_tuning& t, int64_t v) { t.mid_threshold = v; }, {4 * 152 * 5, 16 * 152 * 5});
+        if (st == RIA_OK) st = field([](ria_tuning& t, int64_t v) { t.cut_graph = (int32_t)v; }, {1, 0});
+    }
+    if (st != RIA_OK) {
+        ria_set_tuning(&start);
+        return st;
+    }
     if ((st = ria_set_tuning(&bt)) != RIA_OK) return st;
     if (best) *best = bt;
     if (best_s) *best_s = bs;

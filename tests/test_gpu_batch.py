@@ -87,3 +87,54 @@ def test_batch_rejects_bad_problem(pkg, fns, lib):
     f = fns.make_functions([{"type": "zero"}])
     with pytest.raises(pkg.RiaError):
         pkg.grid_batch([(0, f)])
+
+
+def test_tuning_records_do_not_change_results(pkg, fns, lib):
+    """Every tuning record (the heavy/light split, the warp-cut bin size, resident blocks, the thread
+    kernel's block, the cut stage as a CUDA graph or not, on batches and on single calls) gives the same
+    fields, bit for bit."""
+    probs = _problems(fns, 91, 24, "ia")
+    wl = fns.workload_ia_degenerate(res=40)
+    start = pkg.get_tuning()
+    try:
+        ref_batch = pkg.grid_batch(probs)
+        ref_single = pkg.grid_implicit_arrangement(wl.res, wl.funcs)
+        for rec in ({"warp_route": 64, "warp_blocks_per_sm": 1, "fast_block": 32, "cut_graph": 2, "heavy_min_k": 3},
+                    {"warp_route": 0, "warp_blocks_per_sm": 2, "fast_block": 64, "cut_graph": 0, "heavy_min_k": 8},
+                    {"warp_route": 1 << 20, "warp_blocks_per_sm": 0, "fast_block": 128, "cut_graph": 1,
+                     "heavy_min_k": 0}):
+            pkg.set_tuning(dict(start, **rec))
+            got = pkg.grid_batch(probs)
+            for i in range(len(probs)):
+                for k in FIELDS:
+                    assert np.array_equal(got.problem(i)[k], ref_batch.problem(i)[k]), (rec, i, k)
+            got.close()
+            single = pkg.grid_implicit_arrangement(wl.res, wl.funcs)
+            for k in FIELDS:
+                assert np.array_equal(single[k], ref_single[k]), (rec, k)
+            single.close()
+    finally:
+        pkg.set_tuning(start)
+
+
+def test_autotune_installs_a_record(pkg, fns, lib):
+    """The autotuner times its candidate records on a sample and installs the fastest, which is never
+    slower than the record it started from (that record is among the timed ones)."""
+    start = pkg.get_tuning()
+    try:
+        probs = _problems(fns, 92, 32, "ia")
+        best, best_s, default_s = pkg.autotune(probs, reps=1)
+        assert best == pkg.get_tuning()
+        assert 0 < best_s <= default_s
+        assert best["fast_block"] in (0, 32, 64, 128) and best["cut_graph"] in (0, 1, 2)
+        assert best["heavy_min_k"] in (0, 3, 4, 5)
+    finally:
+        pkg.set_tuning(start)
+
+
+def test_bad_tuning_rejected(pkg, lib):
+    start = pkg.get_tuning()
+    for bad in ({"fast_block": 48}, {"cut_graph": 3}, {"warp_route": -1}, {"heavy_min_k": 2}):
+        with pytest.raises(pkg.RiaError):
+            pkg.set_tuning(dict(start, **bad))
+    assert pkg.get_tuning() == start
