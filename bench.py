@@ -493,6 +493,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer end-to-end leg (profiling runs)")
     ap.add_argument("--no-tune", action="store_true", help="--config batch: keep the current tuning record")
+    ap.add_argument("--tuning", default=None,
+                    help="JSON object of ria_tuning fields set before anything runs, e.g. '{\"heavy_min_k\": 3}'")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -529,6 +531,8 @@ def main():
     pkg = importlib.import_module(PKG)
     pkg.build()
     L = pkg.load()
+    if args.tuning:
+        pkg.set_tuning(dict(pkg.get_tuning(), **json.loads(args.tuning)))
     grid = pkg.grid_implicit_arrangement if wl.mode == "ia" else pkg.grid_material_interface
     host = pkg.implicit_arrangement if wl.mode == "ia" else pkg.material_interface
 
@@ -633,6 +637,7 @@ def main():
         "wall_ms_per_step": wall / args.steps * 1e3,
         "e2e": {"value": e2e, "unit": "tets/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
         "gpu_launches": launches,
+        "tuning": pkg.get_tuning(),
         "roofline": {"bound": "hbm", "kernel": "k_sample", "kernel_stage": dom, "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
                      "algorithmic_bytes": ab[dom], "traffic": SAMPLE_TRAFFIC if wl.name == SAMPLE_TRAFFIC_WORKLOAD else None,

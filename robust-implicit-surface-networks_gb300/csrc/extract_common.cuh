@@ -229,21 +229,36 @@ inline uint64_t pow2_at_least(uint64_t x) {
     return p;
 }
 
-// stream-ordered device allocations released when the pool goes out of scope
+// stream-ordered device allocations released when the pool goes out of scope.  Buffers are carved,
+// 256-byte aligned, out of chunks of at least 32 MB: a stage allocates its dozens of buffers with a
+// few cudaMallocAsync calls (after a synchronization the device waits while the host issues them).
 struct Pool {
     cudaStream_t s;
     std::vector<void*> ptrs;
     cudaError_t err = cudaSuccess;
+    char* cur = nullptr;
+    size_t left = 0;
+    static constexpr size_t kChunk = 32ull << 20;
     template <class T>
     T* get(int64_t n) {
-        void* p = nullptr;
         if (n <= 0) n = 1;
-        cudaError_t e = cudaMallocAsync(&p, sizeof(T) * (size_t)n, s);
+        const size_t bytes = (sizeof(T) * (size_t)n + 255) & ~(size_t)255;
+        if (bytes <= left) {
+            T* p = (T*)cur;
+            cur += bytes;
+            left -= bytes;
+            return p;
+        }
+        const size_t size = bytes < kChunk ? kChunk : bytes;
+        void* p = nullptr;
+        cudaError_t e = cudaMallocAsync(&p, size, s);
         if (e != cudaSuccess) {
             err = e;
             return nullptr;
         }
         ptrs.push_back(p);
+        cur = (char*)p + bytes;
+        left = size - bytes;
         return (T*)p;
     }
     ~Pool() {

@@ -43,8 +43,10 @@ struct ExtractCtx {
     uint32_t* fntet;
     uint32_t* foff;
     uint32_t* ftoff;
-    // per face occurrence, from the keys pass: loop start in fgids, (active tet, record face), function
+    // per face occurrence, from the vertex pass: loop start in fgids, loop offset in the record,
+    // (active tet, record face), function
     uint32_t* floop;
+    uint32_t* frec;
     uint64_t* fsrc;
     int32_t* ffunc;
     uint32_t* fgids;  // global vertex ids of every iso face loop, in occurrence order
@@ -85,7 +87,29 @@ __global__ void __launch_bounds__(kBs) k_ia_vert_keys(ExtractCtx C) {
         TetSrc ts{C.a.d_tets, C.a.g.res};
         ts.get(C.a.act_tet[a], tv);
         mask = C.a.act_mask[a];
-        iso_vertex_flags(r, iso);
+        // one walk over the record's faces: the iso flags of its vertices, and the list of its iso
+        // face occurrences for the face pass (tet and record face, loop start in fgids, loop length,
+        // loop offset in the record, function)
+        uint32_t fpos = C.base[a].b, lpos = C.base[a].c;
+        int off = 0;
+        for (int f = 0; f < r.nf; ++f) {
+            const int L = r.len(f);
+            if (r.plane_is_iso(r.supp(f))) {
+                for (int t = 0; t < L; ++t) {
+                    const int v = r.loopv(off + t);
+                    iso[v >> 6] |= 1ull << (v & 63);
+                }
+                const int lf = r.plane_func_local(r.supp(f));
+                C.flen[fpos] = (uint32_t)L;
+                C.floop[fpos] = lpos;
+                C.frec[fpos] = (uint32_t)off;
+                C.fsrc[fpos] = ((uint64_t)a << 16) | (uint64_t)f;
+                C.ffunc[fpos] = lf < 0 ? -1 : local_func(mask, lf);
+                ++fpos;
+                lpos += (uint32_t)L;
+            }
+            off += L;
+        }
         C.iso0[a] = iso[0];
         n = __popcll(iso[0]) + __popcll(iso[1]) + __popcll(iso[2]) + __popcll(iso[3]);
         pos0 = C.base[a].a;
@@ -285,58 +309,63 @@ __global__ void k_vert_emit(ExtractCtx C, int64_t n_new, const uint32_t* __restr
     for (int c = 0; c < 3; ++c) xyz[3 * (int64_t)gid + c] = out[c];
 }
 
-// D5: keys of the iso faces on the tet boundary; every iso face's global vertex ids staged for D7
-__global__ void __launch_bounds__(kBs) k_ia_face_keys(ExtractCtx C) {
-    const int64_t a = (int64_t)blockIdx.x * kBs + threadIdx.x;
-    if (a >= C.a.A) return;
-    IAView r;
-    r.init(C.rs.get(C.a.act_desc[a]));
-    uint64_t iso[4] = {0, 0, 0, 0};
-    if (r.nv <= 64)
-        iso[0] = C.iso0[a];  // computed by the vertex pass
-    else
-        iso_vertex_flags(r, iso);
-    const uint32_t vb = C.base[a].a;
-    uint32_t fpos = C.base[a].b;
-    uint32_t lpos = C.base[a].c;
-    const uint64_t mask = C.a.act_mask[a];
-    int off = 0;
-    for (int f = 0; f < r.nf; ++f) {
-        const int L = r.len(f);
-        if (r.plane_is_iso(r.supp(f))) {
-            uint32_t* g = C.fgids + lpos;
-            for (int t = 0; t < L; ++t) g[t] = C.occ_gid[vb + iso_rank(iso, r.loopv(off + t))];
-            uint64_t occ = OCC_SELF << 62;
-            if (r.bnd(f)) {
-                // (smallest, second smallest, largest) global vertex id (src/extract_mesh.h:68-92)
-                int64_t mn = -1, mx = -1;
-                int mpos = 0;
-                for (int t = 0; t < L; ++t) {
-                    const int64_t v = g[t];
-                    if (t == 0 || v < mn) {
-                        mn = v;
-                        mpos = t;
-                    }
-                    if (t == 0 || v > mx) mx = v;
+// D5: one thread per iso face occurrence (listed by the vertex pass): the global vertex ids of its
+// loop, staged for D7; a face on
+// the tet boundary is keyed by its (smallest, second smallest, largest) vertex id
+// (src/extract_mesh.h:68-92).  The two occurrences of a shared tet face are often in one warp (the
+// tets of a cube are consecutive): lanes with equal keys are grouped and only the lowest, which holds
+// the smaller position, inserts the key.
+__global__ void __launch_bounds__(kBs) k_ia_face_keys(ExtractCtx C, int64_t n) {
+    const int64_t p = (int64_t)blockIdx.x * kBs + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    const bool has = p < n;
+    bool bnd = false;
+    uint64_t k0 = (uint64_t)lane, k1 = ~0ull;  // no boundary key: matches no other lane
+    int64_t mn = 0, second = 0, mx = 0;
+    if (has) {
+        const uint64_t src = C.fsrc[p];
+        const int64_t a = (int64_t)(src >> 16);
+        const int f = (int)(src & 0xFFFF);
+        IAView r;
+        r.init(C.rs.get(C.a.act_desc[a]));
+        uint64_t iso[4] = {0, 0, 0, 0};
+        if (r.nv <= 64)
+            iso[0] = C.iso0[a];  // computed by the vertex pass
+        else
+            iso_vertex_flags(r, iso);
+        const uint32_t vb = C.base[a].a;
+        const int L = (int)C.flen[p], off = (int)C.frec[p];
+        uint32_t* g = C.fgids + C.floop[p];
+        for (int t = 0; t < L; ++t) g[t] = C.occ_gid[vb + iso_rank(iso, r.loopv(off + t))];
+        bnd = r.bnd(f);
+        if (bnd) {
+            int mpos = 0;
+            for (int t = 0; t < L; ++t) {
+                const int64_t v = g[t];
+                if (t == 0 || v < mn) {
+                    mn = v;
+                    mpos = t;
                 }
-                int64_t second = mx + 1;
-                for (int t = 0; t < L; ++t)
-                    if (t != mpos && (int64_t)g[t] < second) second = g[t];
-                int64_t sl = ht_insert_min(C.hb, ((uint64_t)mn << 32) | (uint64_t)second, (uint64_t)mx + 1, fpos);
-                if (sl < 0) raise_status(C.a.status, ST_HASH_FULL);
-                occ = (OCC_EDGE << 62) | (uint64_t)(sl < 0 ? 0 : sl);
+                if (t == 0 || v > mx) mx = v;
             }
-            const int lf = r.plane_func_local(r.supp(f));
-            C.focc[fpos] = occ;
-            C.flen[fpos] = (uint32_t)L;
-            C.floop[fpos] = lpos;
-            C.fsrc[fpos] = ((uint64_t)a << 16) | (uint64_t)f;
-            C.ffunc[fpos] = lf < 0 ? -1 : local_func(mask, lf);
-            ++fpos;
-            lpos += (uint32_t)L;
+            second = mx + 1;
+            for (int t = 0; t < L; ++t)
+                if (t != mpos && (int64_t)g[t] < second) second = g[t];
+            k0 = ((uint64_t)mn << 32) | (uint64_t)second;
+            k1 = (uint64_t)mx + 1;
         }
-        off += L;
     }
+    const unsigned grp = __match_any_sync(0xFFFFFFFFu, k0) & __match_any_sync(0xFFFFFFFFu, k1);
+    const int leader = __ffs(grp) - 1;
+    int64_t sl = 0;
+    if (has && bnd && leader == lane) {
+        sl = ht_insert_min(C.hb, k0, k1, (uint32_t)p);
+        if (sl < 0) raise_status(C.a.status, ST_HASH_FULL);
+    }
+    const uint32_t slo = __shfl_sync(0xFFFFFFFFu, (uint32_t)sl, leader);
+    const uint32_t shi = __shfl_sync(0xFFFFFFFFu, (uint32_t)((uint64_t)sl >> 32), leader);
+    sl = (int64_t)(((uint64_t)shi << 32) | slo);
+    if (has) C.focc[p] = bnd ? ((OCC_EDGE << 62) | (uint64_t)(sl < 0 ? 0 : sl)) : (OCC_SELF << 62);
 }
 
 // D6: owners of the face occurrences, duplicate counts
@@ -459,6 +488,7 @@ cudaError_t run_extract(const ExtractArgs& a, const IASum4* act_sum, ExtractOut&
     C.floop = pool.get<uint32_t>(NF);
     C.fsrc = pool.get<uint64_t>(NF);
     C.ffunc = pool.get<int32_t>(NF);
+    C.frec = pool.get<uint32_t>(NF);
     C.fgids = pool.get<uint32_t>((int64_t)tot.c);
     C.iso0 = pool.get<uint64_t>(A);
     if (pool.err) return pool.err;
@@ -493,8 +523,8 @@ cudaError_t run_extract(const ExtractArgs& a, const IASum4* act_sum, ExtractOut&
         note_launch();
     }
     // faces
-    if (A > 0) {
-        k_ia_face_keys<<<nblk(A), kBs, 0, s>>>(C);
+    if (NF > 0) {
+        k_ia_face_keys<<<nblk(NF), kBs, 0, s>>>(C, NF);
         note_launch();
     }
     if (NF > 0) {

@@ -16,7 +16,10 @@
 //           (a tie would need M = q^2 + q + 1/4, never an integer)
 //   bits    ((e/2 + 1048) << 52) + y; y = 2^53 carries into the exponent
 //
-// Zero, subnormal, negative, infinite and NaN inputs take the hardware square root.
+// Subnormal inputs are normalised first (x = m * 2^k with the leading bit moved to bit 52).  Zero,
+// negative, infinite and NaN inputs are answered from their bits as IEEE 754 defines them: sqrt(+-0)
+// = +-0, sqrt(+inf) = +inf, a NaN stays a (quiet) NaN, a negative input gives a NaN.  So no FP64
+// instruction runs in this function.
 #pragma once
 #include "exact.cuh"
 
@@ -94,14 +97,30 @@ RIA_HD double sqrt_rn_finish(uint64_t x, int e, uint64_t r0) {
     return v;
 }
 
-// s split into x * 2^e with e even; false for zero, subnormal, negative, infinite and NaN
+RIA_HD int clz64(uint64_t v) {
+#if defined(__CUDA_ARCH__)
+    return __clzll((long long)v);
+#else
+    return v ? __builtin_clzll(v) : 64;
+#endif
+}
+
+// s split into x * 2^e with e even and x in [2^52, 2^54); false for zero, negative, infinite and NaN
 RIA_HD bool sqrt_split(double s, uint64_t& x, int& e) {
     uint64_t b;
     std::memcpy(&b, &s, 8);
-    const uint64_t E = b >> 52;
-    if (E - 1 >= 2046) return false;
-    x = (b & ((1ull << 52) - 1)) | (1ull << 52);
-    e = (int)E - 1075;
+    if (b >> 63) return false;  // negative, -0 included
+    const uint64_t E = b >> 52, m = b & ((1ull << 52) - 1);
+    if (E == 2047) return false;  // infinite or NaN
+    if (E == 0) {
+        if (m == 0) return false;  // +0
+        const int sh = clz64(m) - 11;  // subnormal m * 2^-1074: move the leading bit to bit 52
+        x = m << sh;
+        e = -1074 - sh;
+    } else {
+        x = m | (1ull << 52);
+        e = (int)E - 1075;
+    }
     if (e & 1) {
         x <<= 1;
         e -= 1;
@@ -109,10 +128,23 @@ RIA_HD bool sqrt_split(double s, uint64_t& x, int& e) {
     return true;
 }
 
+// the inputs sqrt_split leaves out: +-0, +inf, NaN (quieted), negatives (a quiet NaN)
+RIA_HD double sqrt_special(double s) {
+    uint64_t b;
+    std::memcpy(&b, &s, 8);
+    const uint64_t mag = b & 0x7FFFFFFFFFFFFFFFull;
+    uint64_t out = b;
+    if (mag > 0x7FF0000000000000ull) out = b | (1ull << 51);  // NaN: keep its payload, quiet it
+    else if (mag != 0 && (b >> 63)) out = 0x7FF8000000000000ull;  // negative: the default NaN
+    double v;
+    std::memcpy(&v, &out, 8);
+    return v;
+}
+
 RIA_HD double sqrt_rn(double s) {
     uint64_t x;
     int e;
-    if (!sqrt_split(s, x, e)) return ::sqrt(s);
+    if (!sqrt_split(s, x, e)) return sqrt_special(s);
     return sqrt_rn_finish(x, e, sqrt_seed(x));
 }
 
