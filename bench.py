@@ -216,7 +216,9 @@ def run_batch(args, world, local):
     # the project's autotuner on a sample of the batch (the first 256 grids) chooses the cut's bins,
     # launch shapes and graph capture for this device before anything is timed
     tuned = None
-    if not args.no_tune:
+    if args.tuning:
+        pkg.set_tuning(dict(pkg.get_tuning(), **json.loads(args.tuning)))
+    elif not args.no_tune:
         t0 = time.perf_counter()
         rec, best_s, dflt_s = pkg.autotune(probs[:256], reps=2)
         tuned = {"record": rec, "sample_problems": min(256, len(probs)), "sample_best_ms": best_s * 1e3,

@@ -313,7 +313,7 @@ typedef struct ria_tuning {
     int32_t cut_graph;          /* capture stage c's launches (both streams) as one CUDA graph: 0 never,
                                    1 batched grids (the default), 2 every call */
     int32_t heavy_min_k;        /* smallest active-function count of the heavy bins, cut while the lookup
-                                   pass runs on the light ones: 3 to 8 (0: 4) */
+                                   pass runs on the light ones: 3 to 8 (0: 4; the default record: 6) */
 } ria_tuning;
 /* The current device's tuning record. */
 RIA_API ria_status ria_get_tuning(ria_tuning* tuning);

@@ -50,8 +50,11 @@ ria_status fail(ria_status s, const std::string& msg) {
 
 // the tuning record's defaults (ria_tuning; ria_autotune replaces them per device): 24,320 tets cut
 // a warp each, the warp kernel at its occupancy limit, the thread kernel's block from the tet count,
-// the mid-size variant past 3,040 deferred tets, the cut stage captured as a graph for batched grids
-constexpr ria_tuning kDefaultTuning = {152 * 20 * 8, 0, 0, 4 * 152 * 5, 1, 0};
+// the mid-size variant past 3,040 deferred tets, the cut stage captured as a graph for batched grids,
+// and the heavy bins from six active functions up: on the large degenerate workload (10.5M tets, 32
+// functions) the four- and five-plane tets then run on the light path after the lookup pass, and
+// the cut stage took 1.28 ms against 1.46 ms with the heavy bins from four up
+constexpr ria_tuning kDefaultTuning = {152 * 20 * 8, 0, 0, 4 * 152 * 5, 1, 6};
 
 // the first light bin of the general-case list (bins hold tets of equal active count, heaviest first)
 int first_light_bin(bool mi, int heavy_min_k) {

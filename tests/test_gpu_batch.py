@@ -127,7 +127,7 @@ def test_autotune_installs_a_record(pkg, fns, lib):
         assert best == pkg.get_tuning()
         assert 0 < best_s <= default_s
         assert best["fast_block"] in (0, 32, 64, 128) and best["cut_graph"] in (0, 1, 2)
-        assert best["heavy_min_k"] in (0, 3, 4, 5)
+        assert best["heavy_min_k"] in (0, 3, 4, 5, 6)
     finally:
         pkg.set_tuning(start)
 
