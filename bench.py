@@ -260,7 +260,7 @@ def run_batch(args, world, local):
     # the plain drop-in, one call per problem (same descriptors, same results)
     t0 = time.perf_counter()
     plain_dev = 0.0
-    for r, f in probs:
+    for r, f in ([] if args.no_plain else probs):
         m = pkg.grid_implicit_arrangement(r, f)
         plain_dev += m.timings["total"]
         m.close()
@@ -280,8 +280,9 @@ def run_batch(args, world, local):
                 "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
         "gpu_launches": launches,
         "tuning": tuned if tuned else {"record": pkg.get_tuning()},
-        "per_problem_plain": {"tets_per_s_wall": wl.n_tets / plain_wall, "wall_s": plain_wall,
-                              "device_s": plain_dev, "batch_speedup_wall": plain_wall / (wall / args.steps)},
+        "per_problem_plain": None if args.no_plain else {
+            "tets_per_s_wall": wl.n_tets / plain_wall, "wall_s": plain_wall, "device_s": plain_dev,
+            "batch_speedup_wall": plain_wall / (wall / args.steps)},
         "roofline": {"bound": "hbm", "kernel_stage": "total", "achieved": None, "peak": peak, "unit": "GB/s",
                      "frac": None, "peak_kind": peak_kind, "traffic": None},
         "clocks": clk.summary(),
@@ -495,6 +496,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer end-to-end leg (profiling runs)")
     ap.add_argument("--no-tune", action="store_true", help="--config batch: keep the current tuning record")
+    ap.add_argument("--no-plain", action="store_true", help="--config batch: skip the per-problem plain calls")
     ap.add_argument("--tuning", default=None,
                     help="JSON object of ria_tuning fields set before anything runs, e.g. '{\"heavy_min_k\": 3}'")
     args = ap.parse_args()
