@@ -408,6 +408,17 @@ def sample_fp64_ops(wl):
     return per_vertex * wl.n_verts
 
 
+# FP64 operations of the vertex coordinates per mesh vertex, by simplex size (the reference's formulas,
+# src/extract_mesh.h:111-159; a division counts as one operation): a tet-vertex copies a point, an
+# edge vertex 12, a face vertex 29, a vertex inside a tet 84
+XYZ_FP64_OPS = {1: 0, 2: 12, 3: 29, 4: 84}
+
+# FP64 pipe busy fraction of the warp cut on this workload, from its ncu capture (heavy bins, light
+# bins): the exact predicates run through FP32 and FP64 filters, and few operations reach the pipe
+CUT_FP64_PIPE_BUSY = {"kernel": "k_cut_warp", "heavy_bins": 0.111, "light_bins": 0.034,
+                      "source": "ncu sm__pipe_fp64_cycles_active, one capture of each launch"}
+
+
 def fp64_rate(L):
     """Measured FP64 add/mul and fused multiply-add rates of this GPU (ria_measure_fp64_rate)."""
     import ctypes
@@ -615,6 +626,7 @@ def main():
     n_fit, n_rec = len(m["func_in_tet"]), len(m["rec_bytes"])
     n_fvert = int(L.ria_mesh_count(m._h, pkg.Mesh._FIELDS["face_verts"][0]))
     n_ftet = int(L.ria_mesh_count(m._h, pkg.Mesh._FIELDS["face_tets"][0])) // 2
+    simplex = np.bincount(m["verts"][:, 2], minlength=5) if wl.mode == "ia" else None
     m.close()
     ab = algorithmic_bytes(wl, st, n_fit, n_rec, n_fvert, n_ftet)
     stage_ms = {k: statistics.mean(v) for k, v in stage.items()}
@@ -629,6 +641,16 @@ def main():
             "peak": rates["add"] / 1e9 if rates.get("add") else None, "unit": "G FP64 add/mul per s",
             "peak_kind": "measured (ria_measure_fp64_rate, this run)"}
     fp64["frac"] = fp64["achieved"] / fp64["peak"] if fp64["achieved"] and fp64["peak"] else None
+    # every stage's FP64 fraction beside its HBM one: the sampler's formulas, none in the IA filter
+    # (sign masks only), the cut's from its ncu capture, the vertex coordinates' formulas
+    xyz_ops = int(sum(XYZ_FP64_OPS[t] * int(simplex[t]) for t in XYZ_FP64_OPS)) if simplex is not None else None
+    peak_ops = fp64["peak"] * 1e9 if fp64["peak"] else None
+    stage_fp64 = {
+        "sample": fp64["frac"],
+        "filter": 0.0 if wl.mode == "ia" else None,
+        "cut": CUT_FP64_PIPE_BUSY if wl.name == SAMPLE_TRAFFIC_WORKLOAD else None,
+        "extract": xyz_ops / (stage_ms["extract"] * 1e-3) / peak_ops if xyz_ops is not None and peak_ops else None,
+    }
     line = {
         "metric": METRIC, "value": value, "unit": "tets/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
@@ -647,6 +669,7 @@ def main():
                      "algorithmic_bytes": ab[dom], "traffic": SAMPLE_TRAFFIC if wl.name == SAMPLE_TRAFFIC_WORKLOAD else None,
                      "fp64": fp64,
                      "stage_frac": {k: ab[k] / (stage_ms[k] * 1e-3) / 1e9 / peak for k in stage_ms},
+                     "stage_fp64_frac": stage_fp64,
                      "stage_algorithmic_bytes": ab,
                      "note": "sampling is bound by the FP64 pipe (fp64.frac); the cut and the extraction are "
                              "latency-bound (see the ncu summaries): their HBM fractions are low"},
