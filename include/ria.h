@@ -312,17 +312,21 @@ typedef struct ria_tuning {
     int64_t mid_threshold;      /* deferred tets above which the mid-size variant runs before the exact one */
     int32_t cut_graph;          /* capture stage c's launches (both streams) as one CUDA graph: 0 never,
                                    1 batched grids (the default), 2 every call */
-    int32_t heavy_min_k;        /* smallest active-function count of the heavy bins, cut while the lookup
-                                   pass runs on the light ones: 3 to 8 (0: 4; the default record: 6) */
+    int32_t heavy_min_k;        /* implicit arrangement: smallest active-function count of the heavy bins,
+                                   cut while the lookup pass runs on the light ones: 3 to 8 (0: 4; the
+                                   default record: 6) */
+    int32_t mi_heavy_min_k;     /* material interface: smallest active-material count of the heavy bins,
+                                   whose materials' cells are clipped in parallel: 3 to 8 (0 and the
+                                   default record: 4) */
 } ria_tuning;
 /* The current device's tuning record. */
 RIA_API ria_status ria_get_tuning(ria_tuning* tuning);
 RIA_API ria_status ria_set_tuning(const ria_tuning* tuning);
 /* Project-written autotuner: runs ria_grid_batch on `problems` (a sample of the caller's batches),
  * `reps` times per candidate record with the secondary lookup reset to its seeded state, in a
- * coordinate descent over the fields (heavy_min_k, warp_route, warp_blocks_per_sm, fast_block,
- * mid_threshold, cut_graph; two sweeps, each field over a few values with the others at their best so
- * far), and installs the record with the smallest median device time on the current device.  The
+ * coordinate descent over the fields (heavy_min_k or mi_heavy_min_k, the one of the mode tuned;
+ * warp_route, warp_blocks_per_sm, fast_block, mid_threshold, cut_graph; two sweeps, each field over a
+ * few values with the others at their best so far), and installs the record with the smallest median device time on the current device.  The
  * result never depends on the record.  best_s / default_s (may be NULL): that time, and the time of
  * the record in place when the call started.  Not to be run while other calls use the device. */
 RIA_API ria_status ria_autotune(const ria_config* cfg, int32_t material_interface, const ria_grid_problem* problems,

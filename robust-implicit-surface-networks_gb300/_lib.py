@@ -51,7 +51,8 @@ REQ_IA, REQ_MI, REQ_CSG = 0, 1, 2
 class Tuning(ctypes.Structure):
     """ria_tuning of include/ria.h."""
     _fields_ = [("warp_route", ctypes.c_int64), ("warp_blocks_per_sm", ctypes.c_int32), ("fast_block", ctypes.c_int32),
-                ("mid_threshold", ctypes.c_int64), ("cut_graph", ctypes.c_int32), ("heavy_min_k", ctypes.c_int32)]
+                ("mid_threshold", ctypes.c_int64), ("cut_graph", ctypes.c_int32), ("heavy_min_k", ctypes.c_int32),
+                ("mi_heavy_min_k", ctypes.c_int32)]
 
 
 class Config(ctypes.Structure):

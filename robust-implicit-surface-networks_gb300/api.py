@@ -277,7 +277,8 @@ def grid_batch(problems, mode="ia", **kw) -> BatchMesh:
     return BatchMesh(h)
 
 
-_TUNING_KEYS = ("warp_route", "warp_blocks_per_sm", "fast_block", "mid_threshold", "cut_graph", "heavy_min_k")
+_TUNING_KEYS = ("warp_route", "warp_blocks_per_sm", "fast_block", "mid_threshold", "cut_graph", "heavy_min_k",
+                "mi_heavy_min_k")
 
 
 def get_tuning() -> dict:

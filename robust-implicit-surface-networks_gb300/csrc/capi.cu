@@ -51,10 +51,13 @@ ria_status fail(ria_status s, const std::string& msg) {
 // the tuning record's defaults (ria_tuning; ria_autotune replaces them per device): 24,320 tets cut
 // a warp each, the warp kernel at its occupancy limit, the thread kernel's block from the tet count,
 // the mid-size variant past 3,040 deferred tets, the cut stage captured as a graph for batched grids,
-// and the heavy bins from six active functions up: on the large degenerate workload (10.5M tets, 32
-// functions) the four- and five-plane tets then run on the light path after the lookup pass, and
-// the cut stage took 1.28 ms against 1.46 ms with the heavy bins from four up
-constexpr ria_tuning kDefaultTuning = {152 * 20 * 8, 0, 0, 4 * 152 * 5, 1, 6};
+// and the implicit arrangement's heavy bins from six active functions up: on the large degenerate
+// workload (10.5M tets, 32 functions) the four- and five-plane tets then run on the light path after
+// the lookup pass, and the cut stage took 1.28 ms against 1.46 ms with the heavy bins from four up.
+// The material interface keeps its heavy bins from four materials up: a tet of four or five
+// materials cut serially by one thread takes several times as long as its cells clipped in parallel
+// (the cut stage of 8 materials at res 64 took 3.4 ms against 0.55 ms).
+constexpr ria_tuning kDefaultTuning = {152 * 20 * 8, 0, 0, 4 * 152 * 5, 1, 6, 4};
 
 // the first light bin of the general-case list (bins hold tets of equal active count, heaviest first)
 int first_light_bin(bool mi, int heavy_min_k) {
@@ -465,7 +468,7 @@ ria_status run_pipeline(const ria_config* cfg, const Inputs& in, cudaStream_t s,
         cudaMemcpyAsync(&h[0], blk_off + nb, 4, cudaMemcpyDeviceToHost, s);
         cudaMemcpyAsync(&h[1], blk_off + nscan - 1, 4, cudaMemcpyDeviceToHost, s);
         cudaMemcpyAsync(&h[2], blk + nscan - 1, 4, cudaMemcpyDeviceToHost, s);
-        const int light0 = first_light_bin(mi, ctx->tune.heavy_min_k);
+        const int light0 = first_light_bin(mi, mi ? ctx->tune.mi_heavy_min_k : ctx->tune.heavy_min_k);
         cudaMemcpyAsync(&h[3], blk_off + (1 + light0) * nb, 4, cudaMemcpyDeviceToHost, s);
         if (cudaStreamSynchronize(s) != cudaSuccess) return bail(fail(RIA_ECUDA, cudaGetErrorString(cudaGetLastError())));
         A = h[0];
@@ -1881,7 +1884,8 @@ ria_status ria_get_tuning(ria_tuning* t) {
 ria_status ria_set_tuning(const ria_tuning* t) {
     if (!t || t->warp_route < 0 || t->warp_blocks_per_sm < 0 || t->mid_threshold < 0 || t->cut_graph < 0 ||
         t->cut_graph > 2 || !(t->fast_block == 0 || t->fast_block == 32 || t->fast_block == 64 || t->fast_block == 128) ||
-        !(t->heavy_min_k == 0 || (t->heavy_min_k >= 3 && t->heavy_min_k <= 8)))
+        !(t->heavy_min_k == 0 || (t->heavy_min_k >= 3 && t->heavy_min_k <= 8)) ||
+        !(t->mi_heavy_min_k == 0 || (t->mi_heavy_min_k >= 3 && t->mi_heavy_min_k <= 8)))
         return fail(RIA_EINVAL, "tuning out of range");
     int dev = 0;
     ria_status st = current_device(&dev);
@@ -1939,7 +1943,11 @@ ria_status ria_autotune(const ria_config* cfg, int32_t material_interface, const
         return RIA_OK;
     };
     for (int sweep = 0; sweep < 2 && st == RIA_OK; ++sweep) {
-        if (st == RIA_OK) st = field([](ria_tuning& t, int64_t v) { t.heavy_min_k = (int32_t)v; }, {4, 5, 6, 3});
+        // the heavy/light split of the mode being tuned (the other mode's field is left as it is)
+        if (st == RIA_OK && !material_interface)
+            st = field([](ria_tuning& t, int64_t v) { t.heavy_min_k = (int32_t)v; }, {4, 5, 6, 3});
+        if (st == RIA_OK && material_interface)
+            st = field([](ria_tuning& t, int64_t v) { t.mi_heavy_min_k = (int32_t)v; }, {4, 5, 3});
         if (st == RIA_OK)
             st = field([](ria_tuning& t, int64_t v) { t.warp_route = v; },
                        {152 * 8 * 5, 152 * 8 * 10, 152 * 8 * 20, 152 * 8 * 40, 152 * 8 * 80});

@@ -16,6 +16,7 @@
 #include "launch.hpp"
 #include "lookup2.cuh"
 #include "robust.cuh"
+#include "cut_mi_warp.cuh"
 
 namespace ria {
 
@@ -564,19 +565,20 @@ __global__ void __launch_bounds__(128) k_cut_wait(CutArgs a) {
     if (!done) a.deferred[atomicAdd(a.n_deferred, 1u)] = w.ai;
 }
 
-// Material interface with many materials: one warp per tet, one lane per material.  A material's
-// cell is the tet clipped by its half-spaces against every other material, independent of the other
-// cells, so the lanes clip in parallel and export their cells to shared memory; the lanes then merge
-// them (MIMerge, cut_mi_merge.cuh) into the bytes the serial cut emits.
+// Material interface with four or more materials: one block per tet, one warp per material.  A
+// material's cell is the tet clipped by its half-spaces against every other material, independent of
+// the other cells, so the warps clip the cells in parallel, each step of a clip across the lanes
+// (MIWarpClip, cut_mi_warp.cuh); warp 0 then merges the cells (MIMerge, cut_mi_merge.cuh) into the
+// bytes the serial cut emits.  A cell beyond the clipper's capacities sends the tet to the next
+// variant.
 constexpr int kSplitMaxK = 32;
-// Each lane's clipping state is small and lives in shared memory: kept per thread in local
-// memory, the state of a few active lanes is spread over a warp-interleaved footprint that L1
-// does not hold.  A cell beyond these capacities sends the tet to the exact kernel.
-using SplitClip = MICut<32, 32, 192, 1, 1, 1, false>;
+constexpr int kSplitWarps = 8;
+using SplitClip = MIWarpClip<32, 32, 192>;
 using SplitCell = MICell<32, 32, 192>;
 struct SplitSmem {
     double planes[4 * kSplitMaxK];
-    SplitClip clip[kSplitMaxK];
+    MIPrep prep;
+    SplitClip clip[kSplitWarps];
     SplitCell cells[kSplitMaxK];
     MIMerge<SplitCell> mg;
     int8_t cst[kSplitMaxK];  // 0 cell, 1 no cell, 2 defer
@@ -584,55 +586,61 @@ struct SplitSmem {
     int kk;
 };
 
-__global__ void __launch_bounds__(kSplitMaxK) k_cut_mi_split(CutArgs a) {
+__global__ void __launch_bounds__(32 * kSplitWarps) k_cut_mi_split(CutArgs a) {
     extern __shared__ __align__(16) unsigned char split_smem[];
     SplitSmem& S = *reinterpret_cast<SplitSmem*>(split_smem);
-    const int lane = threadIdx.x;
-    const Lanes L = Lanes::of_thread(lane);
-    SplitClip& c = S.clip[lane];
+    const int warp = threadIdx.x >> 5;
+    const Lanes L = Lanes::of_thread(threadIdx.x & 31);
+    SplitClip& c = S.clip[warp];
     for (int64_t i = blockIdx.x; i < a.n; i += gridDim.x) {
         const uint32_t ai = a.list[i];
-        if (lane == 0) S.kk = gather_planes(a, ai, S.planes, kSplitMaxK);
+        if (threadIdx.x == 0) S.kk = gather_planes(a, ai, S.planes, kSplitMaxK);
         __syncthreads();
         const int k = S.kk;
         if (k > kSplitMaxK) {
-            if (lane == 0) a.deferred[atomicAdd(a.n_deferred, 1u)] = ai;
+            if (threadIdx.x == 0) a.deferred[atomicAdd(a.n_deferred, 1u)] = ai;
             __syncthreads();
             continue;
         }
-        int st = c.prepare(S.planes, k);
-        S.cst[lane] = 1;
-        if (st == CUT_OK && lane < k && c.has_cell(4 + lane)) {
-            bool empty = false;
-            st = c.clip(4 + lane, empty);
-            if (st == CUT_OK && !empty) st = c.export_cell(S.cells[lane]);
-            S.cst[lane] = st != CUT_OK ? 2 : (empty ? 1 : 0);
-        } else if (st != CUT_OK) {
-            S.cst[lane] = 2;
-        }
-        S.has[lane] = S.cst[lane] == 0 ? 1 : 0;
+        if (warp == 0) mi_prepare_lanes(L, S.planes, k, S.prep);
         __syncthreads();
-        bool ok = true;
-        for (int j = 0; j < k; ++j) ok = ok && S.cst[j] != 2;
-        // the merge across the lanes (cut_mi_merge.cuh)
-        const int merged = ok ? S.mg.run(L, S.cells, S.has, k) : CUT_DEFER;
-        bool done = false;
-        if (merged == CUT_OK) {
-            const int size = S.mg.record_size(k);
-            unsigned long long off = 0;
-            if (lane == 0) off = heap_alloc(a, size);
-            off = __shfl_sync(0xFFFFFFFFu, off, 0);
-            if (off + size <= a.heap_cap) {
-                MISummary sum;
-                S.mg.emit(L, S.cells, k, c.rep, a.heap + off, sum);
-                if (lane == 0) {
-                    a.act_desc[ai] = off | a.desc_bit;
-                    a.act_sum[ai] = pack_sum<MISummary>(sum);
-                }
-                done = true;
+        for (int m = warp; m < k; m += kSplitWarps) {
+            int8_t cs = 1;
+            if (S.prep.has_cell(4 + m)) {
+                bool empty = false;
+                int st = c.clip(L, S.planes, k, S.prep, 4 + m, empty);
+                if (st == CUT_OK && !empty) st = c.export_cell(L, S.cells[m]);
+                cs = st != CUT_OK ? 2 : (empty ? 1 : 0);
+            }
+            if (L.lane == 0) {
+                S.cst[m] = cs;
+                S.has[m] = cs == 0 ? 1 : 0;
             }
         }
-        if (!done && lane == 0) a.deferred[atomicAdd(a.n_deferred, 1u)] = ai;
+        __syncthreads();
+        if (warp == 0) {
+            bool ok = true;
+            for (int j = 0; j < k; ++j) ok = ok && S.cst[j] != 2;
+            // the merge across the lanes (cut_mi_merge.cuh)
+            const int merged = ok ? S.mg.run(L, S.cells, S.has, k) : CUT_DEFER;
+            bool done = false;
+            if (merged == CUT_OK) {
+                const int size = S.mg.record_size(k);
+                unsigned long long off = 0;
+                if (L.lane == 0) off = heap_alloc(a, size);
+                off = __shfl_sync(0xFFFFFFFFu, off, 0);
+                if (off + size <= a.heap_cap) {
+                    MISummary sum;
+                    S.mg.emit(L, S.cells, k, S.prep.rep, a.heap + off, sum);
+                    if (L.lane == 0) {
+                        a.act_desc[ai] = off | a.desc_bit;
+                        a.act_sum[ai] = pack_sum<MISummary>(sum);
+                    }
+                    done = true;
+                }
+            }
+            if (!done && L.lane == 0) a.deferred[atomicAdd(a.n_deferred, 1u)] = ai;
+        }
         __syncthreads();
     }
 }
@@ -820,8 +828,8 @@ void launch_cut_mi_split(const CutArgs& a, cudaStream_t s) {
         cudaFuncSetAttribute(k_cut_mi_split, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SplitSmem)) ==
         cudaSuccess;
     (void)attr;
-    const int64_t blocks = a.n < 152 * 32 ? a.n : 152 * 32;
-    k_cut_mi_split<<<(unsigned)blocks, kSplitMaxK, sizeof(SplitSmem), s>>>(a);
+    const int64_t blocks = a.n < 152 * 4 ? a.n : 152 * 4;
+    k_cut_mi_split<<<(unsigned)blocks, 32 * kSplitWarps, sizeof(SplitSmem), s>>>(a);
     note_launch();
 }
 

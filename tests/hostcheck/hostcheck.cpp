@@ -4,6 +4,7 @@
 #include <vector>
 
 #include "../../robust-implicit-surface-networks_gb300/csrc/cut_mi.cuh"
+#include "../../robust-implicit-surface-networks_gb300/csrc/cut_mi_warp.cuh"
 #include "../../robust-implicit-surface-networks_gb300/csrc/variants.cuh"
 #include "../../robust-implicit-surface-networks_gb300/csrc/lookup2.cuh"
 #include "../../robust-implicit-surface-networks_gb300/csrc/cut_ia_warp.cuh"
@@ -68,29 +69,36 @@ extern "C" int hc_ia_cut(int k, const double* planes, int big, uint8_t* buf, int
     return r;
 }
 
-// big == 3: the split path of the device (one clipper per material, then the lane-parallel merge
-// with one lane)
+// big == 3: the split path of the device (the per-tet preparation and one warp clipper per material,
+// then the lane-parallel merge, each with one lane)
 static int mi_split(int k, const double* mats, uint8_t* buf, int cap, uint16_t* summary) {
-    using SplitClip = MICut<32, 32, 192, 1, 1, 1, false>;  // the device's compact clipper
+    using SplitClip = MIWarpClip<32, 32, 192>;  // the device's warp clipper
     using SplitCell = MICell<32, 32, 192>;
     if (k > 32) return -11;
     std::vector<SplitCell> cells(k);
     uint8_t has[32] = {};
-    auto* c = new SplitClip();
+    Lanes L1;
+    auto* prep = new MIPrep();
+    mi_prepare_lanes(L1, mats, k, *prep);
+    auto* c = new MICut<32, 32, 192, 1, 1, 1, false>();  // the serial preparation, to compare with
     int st = c->prepare(mats, k);
+    for (int i = 0; i < k && st == CUT_OK; ++i)
+        if (prep->rep[i] != c->rep[i]) st = CUT_FAIL;
+    auto* cm = new SplitClip();
     for (int m = 0; m < k && st == CUT_OK; ++m) {
-        auto* cm = new SplitClip();
-        st = cm->prepare(mats, k);
-        if (st == CUT_OK && cm->has_cell(4 + m)) {
-            bool empty = false;
-            st = cm->clip(4 + m, empty);
-            if (st == CUT_OK && !empty) {
-                st = cm->export_cell(cells[m]);
-                has[m] = 1;
-            }
+        if (prep->has_cell(4 + m) != c->has_cell(4 + m)) {
+            st = CUT_FAIL;  // the two preparations disagree
+            break;
         }
-        delete cm;
+        if (!prep->has_cell(4 + m)) continue;
+        bool empty = false;
+        st = cm->clip(L1, mats, k, *prep, 4 + m, empty);
+        if (st == CUT_OK && !empty) {
+            st = cm->export_cell(L1, cells[m]);
+            has[m] = 1;
+        }
     }
+    delete cm;
     int r = -10 - st;
     if (st == CUT_OK) {
         auto* mg = new MIMerge<SplitCell>();
@@ -104,13 +112,14 @@ static int mi_split(int k, const double* mats, uint8_t* buf, int cap, uint16_t* 
                 r = -3;
             } else {
                 MISummary s;
-                mg->emit(L, cells.data(), k, c->rep, buf, s);
+                mg->emit(L, cells.data(), k, prep->rep, buf, s);
                 std::memcpy(summary, &s, sizeof(s));
             }
         }
         delete mg;
     }
     delete c;
+    delete prep;
     return r;
 }
 

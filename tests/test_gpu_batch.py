@@ -117,6 +117,32 @@ def test_tuning_records_do_not_change_results(pkg, fns, lib):
         pkg.set_tuning(start)
 
 
+def test_mi_tuning_records_do_not_change_results(pkg, fns, lib):
+    """The material interface's heavy/light split (its heavy bins from three, four, five or eight
+    materials up) and the launch shapes give the same fields, bit for bit, on batches and single calls."""
+    probs = _problems(fns, 93, 16, "mi")
+    wl = fns.workload_mi(res=24)
+    start = pkg.get_tuning()
+    assert start["mi_heavy_min_k"] in (0, 3, 4, 5)
+    try:
+        ref_batch = pkg.grid_batch(probs, mode="mi")
+        ref_single = pkg.grid_material_interface(wl.res, wl.funcs)
+        for rec in ({"mi_heavy_min_k": 3, "fast_block": 32, "cut_graph": 2}, {"mi_heavy_min_k": 5, "cut_graph": 0},
+                    {"mi_heavy_min_k": 8, "fast_block": 128}, {"mi_heavy_min_k": 0}):
+            pkg.set_tuning(dict(start, **rec))
+            got = pkg.grid_batch(probs, mode="mi")
+            for i in range(len(probs)):
+                for k in FIELDS:
+                    assert np.array_equal(got.problem(i)[k], ref_batch.problem(i)[k]), (rec, i, k)
+            got.close()
+            single = pkg.grid_material_interface(wl.res, wl.funcs)
+            for k in FIELDS:
+                assert np.array_equal(single[k], ref_single[k]), (rec, k)
+            single.close()
+    finally:
+        pkg.set_tuning(start)
+
+
 def test_autotune_installs_a_record(pkg, fns, lib):
     """The autotuner times its candidate records on a sample and installs the fastest, which is never
     slower than the record it started from (that record is among the timed ones)."""
@@ -134,7 +160,7 @@ def test_autotune_installs_a_record(pkg, fns, lib):
 
 def test_bad_tuning_rejected(pkg, lib):
     start = pkg.get_tuning()
-    for bad in ({"fast_block": 48}, {"cut_graph": 3}, {"warp_route": -1}, {"heavy_min_k": 2}):
+    for bad in ({"fast_block": 48}, {"cut_graph": 3}, {"warp_route": -1}, {"heavy_min_k": 2}, {"mi_heavy_min_k": 9}):
         with pytest.raises(pkg.RiaError):
             pkg.set_tuning(dict(start, **bad))
     assert pkg.get_tuning() == start
