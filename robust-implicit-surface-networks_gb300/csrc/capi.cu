@@ -412,11 +412,12 @@ ria_status run_pipeline(const ria_config* cfg, const Inputs& in, cudaStream_t s,
 
     // counters: 0 status, 1 n_zero, 2..4 k histogram, 5 heap used, 6 big heap used, 7 deferred by the small
     // variant, 8 unused, 9 deferred by the mid variant, 10..14 the cut routing's counters, 16..18
-    // robust-test tets of types 1, 2 and 3
-    unsigned long long* cnt = tmp.get<unsigned long long>(20, &err);
+    // robust-test tets of types 1, 2 and 3, 20..23 the extraction's occurrence totals
+    constexpr int kCounters = 24;
+    unsigned long long* cnt = tmp.get<unsigned long long>(kCounters, &err);
     uint32_t* status = (uint32_t*)cnt;
     if (err != cudaSuccess) return bail(fail(RIA_ENOMEM, "device allocation failed"));
-    cudaMemsetAsync(cnt, 0, sizeof(unsigned long long) * 20, s);
+    cudaMemsetAsync(cnt, 0, sizeof(unsigned long long) * kCounters, s);
     if (in.d_tets && !in.trusted_tets) {
         // every kernel below indexes through the tets: check them before any of them runs
         launch_check_tets(in.d_tets, in.T, in.V, status, s);
@@ -490,6 +491,27 @@ ria_status run_pipeline(const ria_config* cfg, const Inputs& in, cudaStream_t s,
     ranges.next("ria c cut");
 
     // ---- stage c
+    // The implicit arrangement's extraction scans the cut's per-tet counts; the scan is enqueued before
+    // the cut stage's synchronization, so its totals, the status word and the deferred count come back
+    // in one copy.  Deferred tets change their counts: the bases are then taken again.
+    const bool ia_extract = !mi && !cfg->robust_test;
+    ExtractBases xb;
+    bool bases_ready = false;
+    void* xb_buf = nullptr;
+    if (ia_extract) {
+        xb_buf = tmp.get<uint8_t>((int64_t)extract_bases_bytes(A), &err);
+        if (err != cudaSuccess) return bail(fail(RIA_ENOMEM, "device allocation failed"));
+    }
+    unsigned long long hc[kCounters] = {0};
+    auto read_counters = [&](bool cut_end) -> bool {
+        if (cut_end) cudaEventRecord(ev[3], s);  // the scan belongs to the extraction's time
+        if (ia_extract) launch_extract_bases(A, act_sum, xb_buf, cnt + 20, &xb, s);
+        cudaMemcpyAsync(hc, cnt, sizeof(hc), cudaMemcpyDeviceToHost, s);
+        if (cudaStreamSynchronize(s) != cudaSuccess) return false;
+        for (int i = 0; i < 4; ++i) xb.total[i] = hc[20 + i];
+        bases_ready = ia_extract;
+        return true;
+    };
     CutArgs ca{};
     ca.mi = mi;
     ca.act_tet = M->act_tet;
@@ -641,10 +663,10 @@ ria_status run_pipeline(const ria_config* cfg, const Inputs& in, cudaStream_t s,
             launch_cut_fast(cl, s, false);
         }
         if (graph.capturing && graph.finish(s) != cudaSuccess) return bail(fail(RIA_ECUDA, "cut graph launch failed"));
-        unsigned long long h = 0;
-        cudaMemcpyAsync(&h, cnt + 7, 8, cudaMemcpyDeviceToHost, s);
-        if (cudaStreamSynchronize(s) != cudaSuccess) return bail(fail(RIA_ECUDA, cudaGetErrorString(cudaGetLastError())));
+        if (!read_counters(true)) return bail(fail(RIA_ECUDA, cudaGetErrorString(cudaGetLastError())));
+        unsigned long long h = hc[7];
         const int64_t n_def1 = (int64_t)(h & 0xFFFFFFFFull);
+        if (n_def1 > 0) bases_ready = false;
         // a few deferred tets: straight to the exact kernel (state in shared memory, one tet per
         // block, the shortest per-tet time); many: the mid-size variant first (one tet per thread,
         // every SM full), the exact kernel for what remains
@@ -675,7 +697,7 @@ ria_status run_pipeline(const ria_config* cfg, const Inputs& in, cudaStream_t s,
             launch_cut_big(cb, s);
         }
     }
-    cudaEventRecord(ev[3], s);
+    if (!bases_ready) cudaEventRecord(ev[3], s);  // else recorded before the bases' scan
     ranges.next("ria d extract");
 
     // ---- stage d
@@ -699,18 +721,17 @@ ria_status run_pipeline(const ria_config* cfg, const Inputs& in, cudaStream_t s,
         xa.V = in.V;
         xa.status = status;
         // the extraction reads the status only through its own checks; stop early on cut errors
-        uint32_t hst = 0;
-        cudaMemcpyAsync(&hst, status, 4, cudaMemcpyDeviceToHost, s);
-        cudaStreamSynchronize(s);
+        if (!bases_ready && !read_counters(false)) return bail(fail(RIA_ECUDA, cudaGetErrorString(cudaGetLastError())));
+        const uint32_t hst = (uint32_t)hc[0];
         if (hst) return bail(map_status(hst));
-        cudaError_t e = run_extract(xa, act_sum, M->ex, s);
+        cudaError_t e = run_extract(xa, act_sum, ia_extract ? &xb : nullptr, M->ex, s);
         if (e == cudaErrorNotSupported) return bail(fail(RIA_EINVAL, "material-interface extraction is not available"));
         if (e != cudaSuccess) return bail(fail(RIA_ECUDA, std::string("extract: ") + cudaGetErrorString(e)));
     }
     cudaEventRecord(ev[4], s);
     ranges.end();
 
-    unsigned long long h[20];
+    unsigned long long h[kCounters];
     cudaMemcpyAsync(h, cnt, sizeof(h), cudaMemcpyDeviceToHost, s);
     cudaError_t se = cudaStreamSynchronize(s);
     if (se != cudaSuccess) return bail(fail(RIA_ECUDA, cudaGetErrorString(se)));

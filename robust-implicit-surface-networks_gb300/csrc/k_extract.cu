@@ -35,14 +35,10 @@ struct ExtractCtx {
     uint32_t* occ_gid;     // per vertex occurrence: global vertex id
     uint64_t* focc;        // per face occurrence: OCC_SELF or slot in hb
     uint32_t* fowner;
-    uint32_t* fflag;
-    uint32_t* fgid;
     uint32_t* flen;
     uint32_t* fdup;
-    uint32_t* fnewlen;
-    uint32_t* fntet;
-    uint32_t* foff;
-    uint32_t* ftoff;
+    U4* fsz;    // per face occurrence: (new, loop length if new, tets if new, 0)
+    U4* fscan;  // its exclusive scan: (face id, offset in face_verts, offset in face_tets, 0)
     // per face occurrence, from the vertex pass: loop start in fgids, loop offset in the record,
     // (active tet, record face), function
     uint32_t* floop;
@@ -226,22 +222,60 @@ __global__ void k_vert_gid(ExtractCtx C, int64_t n, uint32_t* __restrict__ gid_s
     if (own == (uint32_t)p) gid_src[gid] = (uint32_t)p;
 }
 
-// D4b: vertex records and coordinates, one thread per new vertex (no idle lanes in the long path)
+// D4b: vertex records and coordinates, one thread per new vertex (no idle lanes in the long path).
+// The key of a vertex on the tet boundary is read back from the hash slot its owner inserted (corner:
+// the vertex id itself), so only a vertex inside its tet goes back to the tet's record.
 __global__ void k_vert_emit(ExtractCtx C, int64_t n_new, const uint32_t* __restrict__ gid_src,
                             int64_t* __restrict__ verts, double* __restrict__ xyz) {
     const int64_t g = (int64_t)blockIdx.x * kBs + threadIdx.x;
     if (g >= n_new) return;
     const uint32_t gid = (uint32_t)g;
-    const uint64_t src = C.vsrc[gid_src[g]];
+    const uint32_t p = gid_src[g];
+    const uint64_t occ = C.vocc[p], src = C.vsrc[p];
     const int64_t a = (int64_t)(src >> 8);
     const int j = (int)(src & 0xFF);
-    IAView r;
-    r.init(C.rs.get(C.a.act_desc[a]));
-    int64_t tv[4];
-    TetSrc ts{C.a.d_tets, C.a.g.res};
     const uint32_t tet = C.a.act_tet[a];
-    ts.get(tet, tv);
-    VertKey k = ia_vertex_key(r, j, tv, C.a.act_mask[a]);
+    const uint64_t ty = occ >> 62, pay = occ & ((1ull << 62) - 1);
+    VertKey k;
+    for (int c = 0; c < 4; ++c) k.sv[c] = -1;
+    k.fn[0] = k.fn[1] = k.fn[2] = -1;
+    if (ty == OCC_CORNER) {
+        k.type = 1;
+        k.sv[0] = (int64_t)pay;
+    } else if (ty == OCC_EDGE) {
+        k.type = 2;
+        if (C.edge64) {
+            const uint64_t key = C.he64.keys[pay];
+            k.sv[0] = (int64_t)(key >> 36);
+            k.sv[1] = (int64_t)((key >> 8) & ((1ull << 28) - 1));
+            k.fn[0] = (int)(key & 0xFF);
+        } else {
+            const ulonglong2 key = C.he.keys[pay];
+            k.sv[0] = (int64_t)(key.x >> 32);
+            k.sv[1] = (int64_t)(key.x & 0xFFFFFFFFull);
+            k.fn[0] = (int)key.y - 1;
+        }
+    } else if (ty == OCC_FACE) {
+        k.type = 3;
+        const ulonglong2 key = C.hf.keys[pay];
+        k.sv[0] = (int64_t)(key.x >> 32);
+        k.sv[1] = (int64_t)(key.x & 0xFFFFFFFFull);
+        k.sv[2] = (int64_t)(key.y >> 32);
+        k.fn[0] = (int)((key.y >> 16) & 0xFFFF);
+        k.fn[1] = (int)(key.y & 0xFFFF);
+    } else {
+        IAView r;
+        r.init(C.rs.get(C.a.act_desc[a]));
+        int64_t tv[4];
+        TetSrc ts{C.a.d_tets, C.a.g.res};
+        ts.get(tet, tv);
+        k = ia_vertex_key(r, j, tv, C.a.act_mask[a]);
+    }
+    // a key read back from a slot is in range unless its insertion failed (status already raised)
+    if (k.sv[0] >= C.a.V || k.sv[1] >= C.a.V || k.sv[2] >= C.a.V || k.fn[0] >= C.a.F || k.fn[1] >= C.a.F) {
+        raise_status(C.a.status, ST_INTERNAL);
+        return;
+    }
     int64_t* rec = verts + 11 * (int64_t)gid;
     rec[0] = tet;
     rec[1] = j;
@@ -375,45 +409,63 @@ __global__ void k_face_owner(ExtractCtx C, int64_t n) {
     const uint64_t occ = C.focc[p];
     uint32_t own = (occ >> 62) == OCC_SELF ? (uint32_t)p : C.hb.owner[occ & ((1ull << 62) - 1)];
     C.fowner[p] = own;
-    C.fflag[p] = own == (uint32_t)p;
     if (own != (uint32_t)p) atomicAdd(&C.fdup[own], 1u);
 }
 
+// the counts the three face numberings scan, as one U4 per occurrence (one scan for all three)
 __global__ void k_face_sizes(ExtractCtx C, int64_t n) {
     const int64_t p = (int64_t)blockIdx.x * kBs + threadIdx.x;
     if (p >= n) return;
-    const bool isnew = C.fflag[p];
-    C.fnewlen[p] = isnew ? C.flen[p] : 0;
-    C.fntet[p] = isnew ? 1 + C.fdup[p] : 0;
-    if (isnew && C.fdup[p] > 1) raise_status(C.a.status, ST_NONMANIFOLD);
+    const bool isnew = C.fowner[p] == (uint32_t)p;
+    const uint32_t dup = isnew ? C.fdup[p] : 0;
+    C.fsz[p] = U4{isnew ? 1u : 0u, isnew ? C.flen[p] : 0u, isnew ? 1 + dup : 0u, 0u};
+    if (dup > 1) raise_status(C.a.status, ST_NONMANIFOLD);
+}
+
+// totals of the vertex numbering and of the three face numberings: (vertices, faces, face vertices,
+// face tets)
+__global__ void k_ia_totals(ExtractCtx C, int64_t NV, int64_t NF, int64_t* __restrict__ d) {
+    if (threadIdx.x != 0) return;
+    d[0] = NV ? (int64_t)C.vflag[NV - 1] + (int64_t)C.vgid_new[NV - 1] : 0;
+    const U4 z{0, 0, 0, 0};
+    const U4 f = NF ? U4Sum()(C.fsz[NF - 1], C.fscan[NF - 1]) : z;
+    d[1] = f.a;
+    d[2] = f.b;
+    d[3] = f.c;
 }
 
 // D7: face vertex lists, function ids and tet-face lists, one thread per face occurrence
 __global__ void __launch_bounds__(kBs) k_ia_face_emit(ExtractCtx C, int64_t n, int64_t* __restrict__ face_offsets,
                                                       int64_t* __restrict__ face_verts,
                                                       int64_t* __restrict__ face_tet_offsets,
-                                                      int64_t* __restrict__ face_tets, int64_t* __restrict__ face_func) {
+                                                      int64_t* __restrict__ face_tets, int64_t* __restrict__ face_func,
+                                                      int64_t n_faces, int64_t n_fv, int64_t n_ft) {
     const int64_t p = (int64_t)blockIdx.x * kBs + threadIdx.x;
     if (p >= n) return;
+    if (p == 0) {  // the closing entries of the two offset arrays
+        face_offsets[n_faces] = n_fv;
+        face_tet_offsets[n_faces] = n_ft;
+    }
     const uint32_t own = C.fowner[p];
     const uint64_t src = C.fsrc[p];
     const int64_t tet = C.a.act_tet[src >> 16];
     const int64_t f = (int64_t)(src & 0xFFFF);
     if (own == (uint32_t)p) {
-        const uint32_t gid = C.fgid[p];
-        const uint32_t vo = C.foff[p];
+        const U4 sc = C.fscan[p];
+        const uint32_t gid = sc.a;
+        const uint32_t vo = sc.b;
         const uint32_t L = C.flen[p];
         const uint32_t* g = C.fgids + C.floop[p];
         face_offsets[gid] = vo;
         for (uint32_t t = 0; t < L; ++t) face_verts[vo + t] = g[t];
-        const uint32_t to = C.ftoff[p];
+        const uint32_t to = sc.c;
         face_tet_offsets[gid] = to;
         face_tets[2 * (int64_t)to] = tet;
         face_tets[2 * (int64_t)to + 1] = f;
         face_func[2 * (int64_t)gid] = C.ffunc[p];
         face_func[2 * (int64_t)gid + 1] = -1;
     } else {
-        const uint32_t to = C.ftoff[own] + 1;
+        const uint32_t to = C.fscan[own].c + 1;
         face_tets[2 * (int64_t)to] = tet;
         face_tets[2 * (int64_t)to + 1] = f;
     }
@@ -423,7 +475,54 @@ __global__ void __launch_bounds__(kBs) k_ia_face_emit(ExtractCtx C, int64_t n, i
 
 cudaError_t run_extract_mi(const ExtractArgs& a, const IASum4* act_sum, ExtractOut& out, cudaStream_t s);
 
-cudaError_t run_extract(const ExtractArgs& a, const IASum4* act_sum, ExtractOut& out, cudaStream_t s) {
+namespace {
+
+__global__ void k_bases_total(int64_t A, const U4* __restrict__ bin, const U4* __restrict__ base,
+                              unsigned long long* __restrict__ totals) {
+    const U4 t = U4Sum()(bin[A - 1], base[A - 1]);
+    totals[0] = t.a;
+    totals[1] = t.b;
+    totals[2] = t.c;
+    totals[3] = t.d;
+}
+
+size_t bases_scan_bytes(int64_t A) {
+    size_t bytes = 0;
+    cub::DeviceScan::ExclusiveScan(nullptr, bytes, (const U4*)nullptr, (U4*)nullptr, U4Sum(), U4{0, 0, 0, 0}, A,
+                                   (cudaStream_t)0);
+    return bytes;
+}
+
+}  // namespace
+
+size_t extract_bases_bytes(int64_t A) {
+    if (A <= 0) return 256;
+    const size_t arr = (sizeof(U4) * (size_t)A + 255) & ~(size_t)255;
+    return 2 * arr + bases_scan_bytes(A);
+}
+
+void launch_extract_bases(int64_t A, const IASum4* act_sum, void* buf, unsigned long long* totals, ExtractBases* out,
+                          cudaStream_t s) {
+    out->base = nullptr;
+    if (A <= 0) {
+        cudaMemsetAsync(totals, 0, 4 * sizeof(unsigned long long), s);
+        return;
+    }
+    const size_t arr = (sizeof(U4) * (size_t)A + 255) & ~(size_t)255;
+    U4* bin = (U4*)buf;
+    U4* base = (U4*)((char*)buf + arr);
+    void* tmp = (char*)buf + 2 * arr;
+    size_t bytes = bases_scan_bytes(A);
+    k_base_in<<<nblk(A), kBs, 0, s>>>(A, act_sum, bin);
+    note_launch();
+    cub::DeviceScan::ExclusiveScan(tmp, bytes, bin, base, U4Sum(), U4{0, 0, 0, 0}, A, s);
+    k_bases_total<<<1, 1, 0, s>>>(A, bin, base, totals);
+    note_launch();
+    out->base = base;
+}
+
+cudaError_t run_extract(const ExtractArgs& a, const IASum4* act_sum, const ExtractBases* pre, ExtractOut& out,
+                        cudaStream_t s) {
     if (a.mi) return run_extract_mi(a, act_sum, out, s);
     Pool pool{s};
     ExtractCtx C;
@@ -431,27 +530,21 @@ cudaError_t run_extract(const ExtractArgs& a, const IASum4* act_sum, ExtractOut&
     C.rs = RecSrc{a.heap, a.heap_big, a.table, a.table_off};
     const int64_t A = a.A;
     out = ExtractOut();
-    // bases
-    U4* bin = pool.get<U4>(A);
-    U4* base = pool.get<U4>(A);
-    if (pool.err) return pool.err;
+    // bases: prepared by the caller (their totals read with the cut stage's synchronization), or here
     U4 tot{0, 0, 0, 0};
-    if (A > 0) {
-        {
-            k_base_in<<<nblk(A), kBs, 0, s>>>(A, act_sum, bin);
-            note_launch();
-        }
-        size_t bytes = 0;
-        cub::DeviceScan::ExclusiveScan(nullptr, bytes, bin, base, U4Sum(), U4{0, 0, 0, 0}, A, s);
-        void* tmp = pool.get<uint8_t>((int64_t)bytes);
+    const U4* base = nullptr;
+    if (pre && (pre->base || A == 0)) {
+        base = (const U4*)pre->base;
+        tot = U4{(uint32_t)pre->total[0], (uint32_t)pre->total[1], (uint32_t)pre->total[2], (uint32_t)pre->total[3]};
+    } else if (A > 0) {
+        U4* bin = pool.get<U4>(A);
+        U4* b = pool.get<U4>(A);
         if (pool.err) return pool.err;
-        cub::DeviceScan::ExclusiveScan(tmp, bytes, bin, base, U4Sum(), U4{0, 0, 0, 0}, A, s);
-        U4 h[2];
-        cudaMemcpyAsync(&h[0], bin + A - 1, sizeof(U4), cudaMemcpyDeviceToHost, s);
-        cudaMemcpyAsync(&h[1], base + A - 1, sizeof(U4), cudaMemcpyDeviceToHost, s);
-        cudaError_t e = cudaStreamSynchronize(s);
+        k_base_in<<<nblk(A), kBs, 0, s>>>(A, act_sum, bin);
+        note_launch();
+        const cudaError_t e = exscan_u4(bin, b, A, &tot, pool, s);
         if (e != cudaSuccess) return e;
-        tot = U4Sum()(h[0], h[1]);
+        base = b;
     }
     C.base = base;
     const int64_t NV = tot.a, NF = tot.b, NB = tot.d;
@@ -477,20 +570,23 @@ cudaError_t run_extract(const ExtractArgs& a, const IASum4* act_sum, ExtractOut&
     C.occ_gid = pool.get<uint32_t>(NV);
     C.focc = pool.get<uint64_t>(NF);
     C.fowner = pool.get<uint32_t>(NF);
-    C.fflag = pool.get<uint32_t>(NF);
-    C.fgid = pool.get<uint32_t>(NF);
     C.flen = pool.get<uint32_t>(NF);
     C.fdup = pool.get<uint32_t>(NF);
-    C.fnewlen = pool.get<uint32_t>(NF);
-    C.fntet = pool.get<uint32_t>(NF);
-    C.foff = pool.get<uint32_t>(NF);
-    C.ftoff = pool.get<uint32_t>(NF);
+    C.fsz = pool.get<U4>(NF);
+    C.fscan = pool.get<U4>(NF);
     C.floop = pool.get<uint32_t>(NF);
     C.fsrc = pool.get<uint64_t>(NF);
     C.ffunc = pool.get<int32_t>(NF);
     C.frec = pool.get<uint32_t>(NF);
     C.fgids = pool.get<uint32_t>((int64_t)tot.c);
     C.iso0 = pool.get<uint64_t>(A);
+    uint32_t* gid_src = pool.get<uint32_t>(NV);  // the occurrence of each new vertex, by id
+    int64_t* d_tots = pool.get<int64_t>(4);
+    size_t vscan_bytes = 0, fscan_bytes = 0;
+    if (NV > 0) cub::DeviceScan::ExclusiveSum(nullptr, vscan_bytes, C.vflag, C.vgid_new, NV, s);
+    if (NF > 0)
+        cub::DeviceScan::ExclusiveScan(nullptr, fscan_bytes, C.fsz, C.fscan, U4Sum(), U4{0, 0, 0, 0}, NF, s);
+    void* scan_tmp = pool.get<uint8_t>((int64_t)std::max(vscan_bytes, fscan_bytes));
     if (pool.err) return pool.err;
     cudaMemsetAsync(C.corner_owner, 0xFF, sizeof(uint32_t) * (size_t)(a.V > 0 ? a.V : 1), s);
     for (HashTab* h : {&C.he, &C.hf, &C.hb}) {
@@ -511,14 +607,8 @@ cudaError_t run_extract(const ExtractArgs& a, const IASum4* act_sum, ExtractOut&
     if (NV > 0) {
         k_vert_owner<<<nblk(NV), kBs, 0, s>>>(C, NV);
         note_launch();
-    }
-    cudaError_t e = exscan_u32(C.vflag, C.vgid_new, NV, s);
-    if (e != cudaSuccess) return e;
-    // the occurrence of each new vertex, by id (sized by the occurrences: the vertex count is read
-    // together with the face counts, in one synchronization)
-    uint32_t* gid_src = pool.get<uint32_t>(NV);
-    if (pool.err) return pool.err;
-    if (NV > 0) {
+        cub::DeviceScan::ExclusiveSum(scan_tmp, vscan_bytes, C.vflag, C.vgid_new, NV, s);
+        // the vertex count is read together with the face counts, in one synchronization
         k_vert_gid<<<nblk(NV), kBs, 0, s>>>(C, NV, gid_src);
         note_launch();
     }
@@ -526,25 +616,18 @@ cudaError_t run_extract(const ExtractArgs& a, const IASum4* act_sum, ExtractOut&
     if (NF > 0) {
         k_ia_face_keys<<<nblk(NF), kBs, 0, s>>>(C, NF);
         note_launch();
-    }
-    if (NF > 0) {
         k_face_owner<<<nblk(NF), kBs, 0, s>>>(C, NF);
         note_launch();
-    }
-    if (NF > 0) {
         k_face_sizes<<<nblk(NF), kBs, 0, s>>>(C, NF);
         note_launch();
+        cub::DeviceScan::ExclusiveScan(scan_tmp, fscan_bytes, C.fsz, C.fscan, U4Sum(), U4{0, 0, 0, 0}, NF, s);
     }
-    if ((e = exscan_u32(C.fflag, C.fgid, NF, s)) != cudaSuccess) return e;
-    if ((e = exscan_u32(C.fnewlen, C.foff, NF, s)) != cudaSuccess) return e;
-    if ((e = exscan_u32(C.fntet, C.ftoff, NF, s)) != cudaSuccess) return e;
-    ScanTotals st;
-    st.add(C.vflag, C.vgid_new, NV);
-    st.add(C.fflag, C.fgid, NF);
-    st.add(C.fnewlen, C.foff, NF);
-    st.add(C.fntet, C.ftoff, NF);
+    k_ia_totals<<<1, 32, 0, s>>>(C, NV, NF, d_tots);
+    note_launch();
     int64_t tots[4] = {0, 0, 0, 0};
-    if ((e = read_totals(st, tots, pool, s)) != cudaSuccess) return e;
+    cudaError_t e = cudaMemcpyAsync(tots, d_tots, sizeof(tots), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return e;
     const int64_t n_verts = tots[0], n_faces = tots[1], n_fv = tots[2], n_ft = tots[3];
     out.n_verts = n_verts;
     if ((e = cudaMallocAsync((void**)&out.xyz, sizeof(double) * 3 * (size_t)(n_verts > 0 ? n_verts : 1), s)) !=
@@ -572,16 +655,11 @@ cudaError_t run_extract(const ExtractArgs& a, const IASum4* act_sum, ExtractOut&
         return e;
     if (NF > 0) {
         k_ia_face_emit<<<nblk(NF), kBs, 0, s>>>(C, NF, out.face_offsets, out.face_verts, out.face_tet_offsets,
-                                                out.face_tets, out.face_func);
+                                                out.face_tets, out.face_func, n_faces, n_fv, n_ft);
         note_launch();
-    }
-    {
-        k_set_last<<<1, 1, 0, s>>>(out.face_offsets, n_faces, C.fnewlen, C.foff, NF);
-        note_launch();
-    }
-    {
-        k_set_last<<<1, 1, 0, s>>>(out.face_tet_offsets, n_faces, C.fntet, C.ftoff, NF);
-        note_launch();
+    } else {
+        cudaMemsetAsync(out.face_offsets, 0, sizeof(int64_t), s);
+        cudaMemsetAsync(out.face_tet_offsets, 0, sizeof(int64_t), s);
     }
     return cudaGetLastError();
 }
