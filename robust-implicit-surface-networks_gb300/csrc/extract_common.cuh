@@ -112,6 +112,66 @@ __device__ __forceinline__ VertKey ia_vertex_key(const IAView& r, int j, const i
     return k;
 }
 
+// ia_vertex_key's result computed on registers only (no locally indexed arrays): the labels are
+// sorted, so the tet-face labels (below 4) come first and the function labels after them in order.
+__device__ __forceinline__ int64_t pick4(int64_t t0, int64_t t1, int64_t t2, int64_t t3, int c) {
+    return c == 0 ? t0 : (c == 1 ? t1 : (c == 2 ? t2 : t3));
+}
+
+__device__ __forceinline__ VertKey ia_vertex_key_r(const uint8_t* lab, int64_t t0, int64_t t1, int64_t t2,
+                                                   int64_t t3, uint64_t mask) {
+    VertKey k;
+    const int l0 = lab[0], l1 = lab[1], l2 = lab[2];
+    const int nb = (l0 < 4 ? 1 : 0) + (l1 < 4 ? 1 : 0) + (l2 < 4 ? 1 : 0);
+    k.fn[0] = nb <= 2 ? local_func(mask, (nb == 0 ? l0 : (nb == 1 ? l1 : l2)) - 4) : -1;
+    k.fn[1] = nb <= 1 ? local_func(mask, (nb == 0 ? l1 : l2) - 4) : -1;
+    k.fn[2] = nb == 0 ? local_func(mask, l2 - 4) : -1;
+    const uint32_t fm = (l0 < 4 ? 1u << l0 : 0u) | (l1 < 4 ? 1u << l1 : 0u) | (l2 < 4 ? 1u << l2 : 0u);
+    const uint32_t cm = 0xFu & ~fm;  // the corners off every face label, ascending
+    const int ca = __ffs(cm) - 1;
+    const uint32_t cm2 = cm & (cm - 1);
+    const int cb = __ffs(cm2) - 1;
+    const int cc = __ffs(cm2 & (cm2 - 1)) - 1;
+    k.sv[0] = k.sv[1] = k.sv[2] = k.sv[3] = -1;
+    if (nb == 3) {
+        k.type = 1;
+        k.sv[0] = pick4(t0, t1, t2, t3, ca);
+    } else if (nb == 2) {
+        const int64_t x = pick4(t0, t1, t2, t3, ca), y = pick4(t0, t1, t2, t3, cb);
+        k.type = 2;
+        k.sv[0] = x < y ? x : y;
+        k.sv[1] = x < y ? y : x;
+    } else if (nb == 1) {
+        int64_t x = pick4(t0, t1, t2, t3, ca), y = pick4(t0, t1, t2, t3, cb), z = pick4(t0, t1, t2, t3, cc);
+        if (y < x) {
+            const int64_t u = x;
+            x = y;
+            y = u;
+        }
+        if (z < y) {
+            const int64_t u = y;
+            y = z;
+            z = u;
+        }
+        if (y < x) {
+            const int64_t u = x;
+            x = y;
+            y = u;
+        }
+        k.type = 3;
+        k.sv[0] = x;
+        k.sv[1] = y;
+        k.sv[2] = z;
+    } else {
+        k.type = 4;
+        k.sv[0] = t0;
+        k.sv[1] = t1;
+        k.sv[2] = t2;
+        k.sv[3] = t3;
+    }
+    return k;
+}
+
 struct MIKey {
     int type;  // 1 corner, 2 edge, 3 face, 4 interior, 0 not on an interface
     int64_t sv[4];
@@ -265,6 +325,40 @@ struct Pool {
         for (void* p : ptrs) cudaFreeAsync(p, s);
     }
 };
+
+// Several buffers filled with a 32-bit pattern in one launch (the dedup tables' empty keys and
+// owners, the duplicate counters): one wide grid-stride pass instead of a memset per buffer.
+// Buffers start 16-byte aligned (Pool hands out 256-byte aligned blocks) and hold whole words.
+struct FillList {
+    uint32_t* p[8];
+    uint64_t words[8];
+    uint32_t val[8];
+    int n = 0;
+    void add(void* ptr, uint64_t bytes, uint32_t v) {
+        p[n] = (uint32_t*)ptr;
+        words[n] = bytes / 4;
+        val[n] = v;
+        ++n;
+    }
+};
+
+static __global__ void __launch_bounds__(256) k_fill(FillList L) {
+    const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x, nth = (uint64_t)gridDim.x * blockDim.x;
+    for (int i = 0; i < L.n; ++i) {
+        uint32_t* p = L.p[i];
+        const uint64_t w = L.words[i], n4 = w / 4;
+        const uint32_t v = L.val[i];
+        uint4* q = reinterpret_cast<uint4*>(p);
+        for (uint64_t u = tid; u < n4; u += nth) q[u] = make_uint4(v, v, v, v);
+        for (uint64_t u = 4 * n4 + tid; u < w; u += nth) p[u] = v;
+    }
+}
+
+inline void launch_fill(const FillList& L, cudaStream_t s) {
+    if (L.n == 0) return;
+    k_fill<<<152 * 8, 256, 0, s>>>(L);
+    note_launch();
+}
 
 inline cudaError_t exscan_u32(const uint32_t* in, uint32_t* out, int64_t n, cudaStream_t s) {
     if (n == 0) return cudaSuccess;

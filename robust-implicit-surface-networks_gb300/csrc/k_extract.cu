@@ -49,15 +49,54 @@ struct ExtractCtx {
     uint64_t* iso0;   // per active tet: iso flags of its first 64 record vertices, from the vertex pass
 };
 
-// D2: keys of the iso vertices.  A warp takes 32 consecutive active tets, whose iso-vertex
-// occurrences are consecutive positions; every round, each lane takes one occurrence (its tet found
-// by a search over the lanes' counts, its local vertex as the r-th iso flag).  Lanes of a round with
-// equal keys are grouped (__match_any_sync), and only the group's lowest lane, which holds the
-// group's smallest position, inserts the key and lowers the owner; the others take its slot.  So
-// every lane works on every round, and each key reaches the global tables about once per warp.
-__device__ __forceinline__ int nth_set_bit(uint64_t x, int n) {
-    for (int k = 0; k < n; ++k) x &= x - 1;
-    return __ffsll((long long)x) - 1;
+// D2a: one thread per active tet.  One walk over the record's faces gives the iso flags of its
+// vertices and the list of its iso face occurrences for the face pass; the tet's iso vertex
+// occurrences are listed at their serial positions (consecutive per tet, in local vertex order).
+__global__ void __launch_bounds__(kBs) k_ia_vert_list(ExtractCtx C) {
+    const int64_t a = (int64_t)blockIdx.x * kBs + threadIdx.x;
+    if (a >= C.a.A) return;
+    const uint8_t* rec = C.rs.get(C.a.act_desc[a]);
+    IAView r;
+    r.init(rec);
+    const uint64_t mask = C.a.act_mask[a];
+    const U4 b = C.base[a];
+    uint64_t i0 = 0, i1 = 0, i2 = 0, i3 = 0;  // iso flags of local vertices 0..255
+    uint32_t fpos = b.b, lpos = b.c;
+    int off = 0;
+    for (int f = 0; f < r.nf; ++f) {
+        const int L = r.len(f);
+        if (r.plane_is_iso(r.supp(f))) {
+            for (int t = 0; t < L; ++t) {
+                const int v = r.loopv(off + t);
+                const uint64_t bit = 1ull << (v & 63);
+                const int w = v >> 6;
+                i0 |= w == 0 ? bit : 0;
+                i1 |= w == 1 ? bit : 0;
+                i2 |= w == 2 ? bit : 0;
+                i3 |= w == 3 ? bit : 0;
+            }
+            const int lf = r.plane_func_local(r.supp(f));
+            C.flen[fpos] = (uint32_t)L;
+            C.floop[fpos] = lpos;
+            C.frec[fpos] = (uint32_t)off;
+            C.fsrc[fpos] = ((uint64_t)a << 16) | (uint64_t)f;
+            C.ffunc[fpos] = lf < 0 ? -1 : local_func(mask, lf);
+            ++fpos;
+            lpos += (uint32_t)L;
+        }
+        off += L;
+    }
+    C.iso0[a] = i0;
+    uint32_t p = b.a;
+#pragma unroll
+    for (int w = 0; w < 4; ++w) {
+        uint64_t x = w == 0 ? i0 : (w == 1 ? i1 : (w == 2 ? i2 : i3));
+        while (x) {
+            const int bit = __ffsll((long long)x) - 1;
+            x &= x - 1;
+            C.vsrc[p++] = ((uint64_t)a << 8) | (uint64_t)(64 * w + bit);
+        }
+    }
 }
 
 __device__ __forceinline__ uint64_t shfl64(uint64_t v, int src) {
@@ -66,134 +105,67 @@ __device__ __forceinline__ uint64_t shfl64(uint64_t v, int src) {
     return ((uint64_t)hi << 32) | lo;
 }
 
-__global__ void __launch_bounds__(kBs) k_ia_vert_keys(ExtractCtx C) {
-    const int64_t a = (int64_t)blockIdx.x * kBs + threadIdx.x;
+// D2b: keys of the iso vertex occurrences, one thread per occurrence (a warp's occurrences belong to
+// one tet or to neighbouring ones, which share edges and faces).  Lanes with equal keys are grouped
+// (__match_any_sync) and only the group's lowest lane, which holds the group's smallest position,
+// inserts the key and lowers the owner; the others take its slot.  So each key reaches the global
+// tables about once per warp.
+__global__ void __launch_bounds__(kBs) k_ia_vert_keys(ExtractCtx C, int64_t NV) {
+    const int64_t p = (int64_t)blockIdx.x * kBs + threadIdx.x;
     const int lane = threadIdx.x & 31;
-    const bool valid = a < C.a.A;
-    const uint8_t* rec = nullptr;
-    int64_t tv[4] = {0, 0, 0, 0};
-    uint64_t mask = 0;
-    uint64_t iso[4] = {0, 0, 0, 0};
-    int n = 0;
-    uint32_t pos0 = 0;
-    if (valid) {
-        rec = C.rs.get(C.a.act_desc[a]);
+    const bool has = p < NV;
+    int type = 0;
+    VertKey k;
+    uint64_t k0 = (uint64_t)lane, k1 = ~0ull;  // lanes without a keyed occurrence match no one
+    if (has) {
+        const uint64_t src = C.vsrc[p];
+        const int64_t a = (int64_t)(src >> 8);
+        const int j = (int)(src & 0xFF);
         IAView r;
-        r.init(rec);
+        r.init(C.rs.get(C.a.act_desc[a]));
+        int64_t tv[4];
         TetSrc ts{C.a.d_tets, C.a.g.res};
         ts.get(C.a.act_tet[a], tv);
-        mask = C.a.act_mask[a];
-        // one walk over the record's faces: the iso flags of its vertices, and the list of its iso
-        // face occurrences for the face pass (tet and record face, loop start in fgids, loop length,
-        // loop offset in the record, function)
-        uint32_t fpos = C.base[a].b, lpos = C.base[a].c;
-        int off = 0;
-        for (int f = 0; f < r.nf; ++f) {
-            const int L = r.len(f);
-            if (r.plane_is_iso(r.supp(f))) {
-                for (int t = 0; t < L; ++t) {
-                    const int v = r.loopv(off + t);
-                    iso[v >> 6] |= 1ull << (v & 63);
-                }
-                const int lf = r.plane_func_local(r.supp(f));
-                C.flen[fpos] = (uint32_t)L;
-                C.floop[fpos] = lpos;
-                C.frec[fpos] = (uint32_t)off;
-                C.fsrc[fpos] = ((uint64_t)a << 16) | (uint64_t)f;
-                C.ffunc[fpos] = lf < 0 ? -1 : local_func(mask, lf);
-                ++fpos;
-                lpos += (uint32_t)L;
-            }
-            off += L;
+        k = ia_vertex_key_r(r.vlab + 3 * j, tv[0], tv[1], tv[2], tv[3], C.a.act_mask[a]);
+        type = k.type;
+        if (type == 1) {
+            k0 = (uint64_t)k.sv[0];
+            k1 = 1;
+        } else if (type == 2) {
+            k0 = ((uint64_t)k.sv[0] << 32) | (uint64_t)k.sv[1];
+            k1 = ((uint64_t)k.fn[0] << 8) | 2;
+        } else if (type == 3) {
+            k0 = ((uint64_t)k.sv[0] << 32) | (uint64_t)k.sv[1];
+            k1 = ((uint64_t)k.sv[2] << 32) | ((uint64_t)k.fn[0] << 16) | ((uint64_t)k.fn[1] << 4) | 3;
         }
-        C.iso0[a] = iso[0];
-        n = __popcll(iso[0]) + __popcll(iso[1]) + __popcll(iso[2]) + __popcll(iso[3]);
-        pos0 = C.base[a].a;
     }
-    int incl = n;
-    for (int o = 1; o < 32; o <<= 1) {
-        const int v = __shfl_up_sync(0xFFFFFFFFu, incl, o);
-        if (lane >= o) incl += v;
+    const unsigned grp = __match_any_sync(0xFFFFFFFFu, k0) & __match_any_sync(0xFFFFFFFFu, k1);
+    const int leader = __ffs(grp) - 1;
+    const uint32_t pos = (uint32_t)p;
+    int64_t slot = 0;
+    if (has && leader == lane) {
+        if (type == 1) {
+            atomicMin(&C.corner_owner[k.sv[0]], pos);
+        } else if (type == 2) {
+            slot = C.edge64 ? ht64_insert_min(C.he64, ((uint64_t)k.sv[0] << 36) | ((uint64_t)k.sv[1] << 8) |
+                                                          (uint64_t)k.fn[0], pos)
+                            : ht_insert_min(C.he, ((uint64_t)k.sv[0] << 32) | (uint64_t)k.sv[1],
+                                            (uint64_t)k.fn[0] + 1, pos);
+            if (slot < 0) raise_status(C.a.status, ST_HASH_FULL);
+        } else if (type == 3) {
+            slot = ht_insert_min(C.hf, ((uint64_t)k.sv[0] << 32) | (uint64_t)k.sv[1],
+                                 ((uint64_t)k.sv[2] << 32) | ((uint64_t)k.fn[0] << 16) | (uint64_t)k.fn[1], pos);
+            if (slot < 0) raise_status(C.a.status, ST_HASH_FULL);
+        }
     }
-    const int total = __shfl_sync(0xFFFFFFFFu, incl, 31);
-    const uint32_t wpos = __shfl_sync(0xFFFFFFFFu, pos0, 0);  // lane 0's tet opens the warp's positions
-    const int64_t a0 = a - lane;
-    for (int base = 0; base < total; base += 32) {
-        const int i = base + lane;
-        const bool has = i < total;
-        // owner lane: the number of lanes whose inclusive count is at most i
-        int owner = 0;
-        for (int step = 16; step > 0; step >>= 1) {
-            const int v = __shfl_sync(0xFFFFFFFFu, incl, owner + step - 1);
-            if (has && v <= i) owner += step;
-        }
-        const int excl = __shfl_sync(0xFFFFFFFFu, incl - n, owner);
-        const uint64_t rp = shfl64((uint64_t)rec, owner);
-        int64_t otv[4];
-        for (int c = 0; c < 4; ++c) otv[c] = (int64_t)shfl64((uint64_t)tv[c], owner);
-        const uint64_t omask = shfl64(mask, owner);
-        uint64_t oiso[4];
-        for (int w = 0; w < 4; ++w) oiso[w] = shfl64(iso[w], owner);
-        int type = 0, j = 0;
-        VertKey k;
-        uint64_t k0 = (uint64_t)lane, k1 = ~0ull;  // lanes without a keyed occurrence match no one
-        if (has) {
-            int rr = i - excl;
-            for (int w = 0; w < 4; ++w) {
-                const int c = __popcll(oiso[w]);
-                if (rr < c) {
-                    j = 64 * w + nth_set_bit(oiso[w], rr);
-                    break;
-                }
-                rr -= c;
-            }
-            IAView r;
-            r.init((const uint8_t*)rp);
-            k = ia_vertex_key(r, j, otv, omask);
-            type = k.type;
-            if (type == 1) {
-                k0 = (uint64_t)k.sv[0];
-                k1 = 1;
-            } else if (type == 2) {
-                k0 = ((uint64_t)k.sv[0] << 32) | (uint64_t)k.sv[1];
-                k1 = ((uint64_t)k.fn[0] << 8) | 2;
-            } else if (type == 3) {
-                k0 = ((uint64_t)k.sv[0] << 32) | (uint64_t)k.sv[1];
-                k1 = ((uint64_t)k.sv[2] << 32) | ((uint64_t)k.fn[0] << 16) | ((uint64_t)k.fn[1] << 4) | 3;
-            } else {
-                k0 = (uint64_t)lane;  // inside the tet: always new
-                k1 = ~0ull;
-            }
-        }
-        const unsigned grp = __match_any_sync(0xFFFFFFFFu, k0) & __match_any_sync(0xFFFFFFFFu, k1);
-        const int leader = __ffs(grp) - 1;
-        const uint32_t pos = wpos + (uint32_t)i;
-        int64_t slot = 0;
-        if (has && leader == lane) {
-            if (type == 1) {
-                atomicMin(&C.corner_owner[k.sv[0]], pos);
-            } else if (type == 2) {
-                slot = C.edge64 ? ht64_insert_min(C.he64, ((uint64_t)k.sv[0] << 36) | ((uint64_t)k.sv[1] << 8) |
-                                                              (uint64_t)k.fn[0], pos)
-                                : ht_insert_min(C.he, ((uint64_t)k.sv[0] << 32) | (uint64_t)k.sv[1],
-                                                (uint64_t)k.fn[0] + 1, pos);
-                if (slot < 0) raise_status(C.a.status, ST_HASH_FULL);
-            } else if (type == 3) {
-                slot = ht_insert_min(C.hf, ((uint64_t)k.sv[0] << 32) | (uint64_t)k.sv[1],
-                                     ((uint64_t)k.sv[2] << 32) | ((uint64_t)k.fn[0] << 16) | (uint64_t)k.fn[1], pos);
-                if (slot < 0) raise_status(C.a.status, ST_HASH_FULL);
-            }
-        }
-        slot = (int64_t)shfl64((uint64_t)slot, leader);
-        if (has) {
-            uint64_t occ;
-            if (type == 1) occ = (OCC_CORNER << 62) | (uint64_t)k.sv[0];
-            else if (type == 2) occ = (OCC_EDGE << 62) | (uint64_t)(slot < 0 ? 0 : slot);
-            else if (type == 3) occ = (OCC_FACE << 62) | (uint64_t)(slot < 0 ? 0 : slot);
-            else occ = OCC_SELF << 62;
-            C.vocc[pos] = occ;
-            C.vsrc[pos] = ((uint64_t)(a0 + owner) << 8) | (uint64_t)j;
-        }
+    slot = (int64_t)shfl64((uint64_t)slot, leader);
+    if (has) {
+        uint64_t occ;
+        if (type == 1) occ = (OCC_CORNER << 62) | (uint64_t)k.sv[0];
+        else if (type == 2) occ = (OCC_EDGE << 62) | (uint64_t)(slot < 0 ? 0 : slot);
+        else if (type == 3) occ = (OCC_FACE << 62) | (uint64_t)(slot < 0 ? 0 : slot);
+        else occ = OCC_SELF << 62;
+        C.vocc[p] = occ;
     }
 }
 
@@ -225,12 +197,7 @@ __global__ void k_vert_gid(ExtractCtx C, int64_t n, uint32_t* __restrict__ gid_s
 // D4b: vertex records and coordinates, one thread per new vertex (no idle lanes in the long path).
 // The key of a vertex on the tet boundary is read back from the hash slot its owner inserted (corner:
 // the vertex id itself), so only a vertex inside its tet goes back to the tet's record.
-__global__ void k_vert_emit(ExtractCtx C, int64_t n_new, const uint32_t* __restrict__ gid_src,
-                            int64_t* __restrict__ verts, double* __restrict__ xyz) {
-    const int64_t g = (int64_t)blockIdx.x * kBs + threadIdx.x;
-    if (g >= n_new) return;
-    const uint32_t gid = (uint32_t)g;
-    const uint32_t p = gid_src[g];
+__device__ __forceinline__ void vert_emit_one(const ExtractCtx& C, uint32_t p, int64_t* rec, double* xyz) {
     const uint64_t occ = C.vocc[p], src = C.vsrc[p];
     const int64_t a = (int64_t)(src >> 8);
     const int j = (int)(src & 0xFF);
@@ -269,14 +236,15 @@ __global__ void k_vert_emit(ExtractCtx C, int64_t n_new, const uint32_t* __restr
         int64_t tv[4];
         TetSrc ts{C.a.d_tets, C.a.g.res};
         ts.get(tet, tv);
-        k = ia_vertex_key(r, j, tv, C.a.act_mask[a]);
+        k = ia_vertex_key_r(r.vlab + 3 * j, tv[0], tv[1], tv[2], tv[3], C.a.act_mask[a]);
     }
     // a key read back from a slot is in range unless its insertion failed (status already raised)
     if (k.sv[0] >= C.a.V || k.sv[1] >= C.a.V || k.sv[2] >= C.a.V || k.fn[0] >= C.a.F || k.fn[1] >= C.a.F) {
         raise_status(C.a.status, ST_INTERNAL);
+        for (int c = 0; c < 11; ++c) rec[c] = -1;
+        for (int c = 0; c < 3; ++c) xyz[c] = 0.0;
         return;
     }
-    int64_t* rec = verts + 11 * (int64_t)gid;
     rec[0] = tet;
     rec[1] = j;
     rec[2] = k.type;
@@ -340,7 +308,21 @@ __global__ void k_vert_emit(ExtractCtx C, int64_t n_new, const uint32_t* __restr
         default:
             ps.get(k.sv[0], out);
     }
-    for (int c = 0; c < 3; ++c) xyz[3 * (int64_t)gid + c] = out[c];
+    for (int c = 0; c < 3; ++c) xyz[c] = out[c];
+}
+
+// The block's records and coordinates are staged in shared memory and stored as contiguous runs.
+__global__ void __launch_bounds__(kBs) k_vert_emit(ExtractCtx C, int64_t n_new, const uint32_t* __restrict__ gid_src,
+                                                   int64_t* __restrict__ verts, double* __restrict__ xyz) {
+    __shared__ int64_t srec[kBs * 11];
+    __shared__ double sxyz[kBs * 3];
+    const int64_t g0 = (int64_t)blockIdx.x * kBs;
+    const int64_t g = g0 + threadIdx.x;
+    if (g < n_new) vert_emit_one(C, gid_src[g], srec + 11 * threadIdx.x, sxyz + 3 * threadIdx.x);
+    __syncthreads();
+    const int nb = (int)(n_new - g0 < kBs ? n_new - g0 : kBs);
+    for (int i = threadIdx.x; i < 11 * nb; i += kBs) verts[11 * g0 + i] = srec[i];
+    for (int i = threadIdx.x; i < 3 * nb; i += kBs) xyz[3 * g0 + i] = sxyz[i];
 }
 
 // D5: one thread per iso face occurrence (listed by the vertex pass): the global vertex ids of its
@@ -588,23 +570,27 @@ cudaError_t run_extract(const ExtractArgs& a, const IASum4* act_sum, const Extra
         cub::DeviceScan::ExclusiveScan(nullptr, fscan_bytes, C.fsz, C.fscan, U4Sum(), U4{0, 0, 0, 0}, NF, s);
     void* scan_tmp = pool.get<uint8_t>((int64_t)std::max(vscan_bytes, fscan_bytes));
     if (pool.err) return pool.err;
-    cudaMemsetAsync(C.corner_owner, 0xFF, sizeof(uint32_t) * (size_t)(a.V > 0 ? a.V : 1), s);
+    FillList fill;
+    fill.add(C.corner_owner, sizeof(uint32_t) * (size_t)(a.V > 0 ? a.V : 1), ~0u);
     for (HashTab* h : {&C.he, &C.hf, &C.hb}) {
         if (!h->keys) continue;
-        cudaMemsetAsync(h->keys, 0xFF, sizeof(ulonglong2) * (h->cap_mask + 1), s);
-        cudaMemsetAsync(h->owner, 0xFF, sizeof(uint32_t) * (h->cap_mask + 1), s);
+        fill.add(h->keys, sizeof(ulonglong2) * (h->cap_mask + 1), ~0u);
+        fill.add(h->owner, sizeof(uint32_t) * (h->cap_mask + 1), ~0u);
     }
     if (C.edge64) {
-        cudaMemsetAsync(C.he64.keys, 0xFF, sizeof(unsigned long long) * (C.he64.cap_mask + 1), s);
-        cudaMemsetAsync(C.he64.owner, 0xFF, sizeof(uint32_t) * (C.he64.cap_mask + 1), s);
+        fill.add(C.he64.keys, sizeof(unsigned long long) * (C.he64.cap_mask + 1), ~0u);
+        fill.add(C.he64.owner, sizeof(uint32_t) * (C.he64.cap_mask + 1), ~0u);
     }
-    cudaMemsetAsync(C.fdup, 0, sizeof(uint32_t) * (size_t)(NF > 0 ? NF : 1), s);
+    fill.add(C.fdup, sizeof(uint32_t) * (size_t)(NF > 0 ? NF : 1), 0u);
+    launch_fill(fill, s);
     // vertices
     if (A > 0) {
-        k_ia_vert_keys<<<nblk(A), kBs, 0, s>>>(C);
+        k_ia_vert_list<<<nblk(A), kBs, 0, s>>>(C);
         note_launch();
     }
     if (NV > 0) {
+        k_ia_vert_keys<<<nblk(NV), kBs, 0, s>>>(C, NV);
+        note_launch();
         k_vert_owner<<<nblk(NV), kBs, 0, s>>>(C, NV);
         note_launch();
         cub::DeviceScan::ExclusiveSum(scan_tmp, vscan_bytes, C.vflag, C.vgid_new, NV, s);
