@@ -110,12 +110,9 @@ struct StageRanges {
 
 // A second stream per host thread and device, for work that overlaps the caller's stream inside one
 // call; created on first use and kept for the life of the thread's process, like the tables.
-struct AuxStream {
-    cudaStream_t s = nullptr;
-    cudaEvent_t fork = nullptr, join = nullptr;
-};
+}  // namespace
 
-cudaError_t aux_stream(AuxStream** out) {
+cudaError_t ria::aux_stream(AuxStream** out) {
     thread_local std::vector<AuxStream> aux;
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
@@ -130,6 +127,21 @@ cudaError_t aux_stream(AuxStream** out) {
     *out = &a;
     return cudaSuccess;
 }
+
+cudaError_t ria::pinned_words(uint64_t** out) {
+    thread_local uint64_t* buf = nullptr;  // kept for the thread's lifetime
+    if (!buf) {
+        cudaError_t e = cudaHostAlloc((void**)&buf, 64 * sizeof(uint64_t), cudaHostAllocPortable);
+        if (e != cudaSuccess) {
+            buf = nullptr;
+            return e;
+        }
+    }
+    *out = buf;
+    return cudaSuccess;
+}
+
+namespace {
 
 // A stream capture of the cut stage's launches: ended, instantiated and launched by finish(); the
 // graph is released after the stream has run it (the destructor waits for the stream).
@@ -701,8 +713,8 @@ ria_status run_pipeline(const ria_config* cfg, const Inputs& in, cudaStream_t s,
     ranges.next("ria d extract");
 
     // ---- stage d
+    ExtractArgs xa{};
     if (!cfg->robust_test) {
-        ExtractArgs xa{};
         xa.mi = mi;
         xa.A = A;
         xa.act_tet = M->act_tet;
@@ -735,6 +747,20 @@ ria_status run_pipeline(const ria_config* cfg, const Inputs& in, cudaStream_t s,
     cudaMemcpyAsync(h, cnt, sizeof(h), cudaMemcpyDeviceToHost, s);
     cudaError_t se = cudaStreamSynchronize(s);
     if (se != cudaSuccess) return bail(fail(RIA_ECUDA, cudaGetErrorString(se)));
+    if (ia_extract && ((uint32_t)h[0] & ST_HASH_FULL) && xa.tight_tables) {
+        // the extraction's tight dedup tables overflowed (rare): again, with worst-case tables
+        for (void* p : {(void*)M->ex.xyz, (void*)M->ex.verts, (void*)M->ex.face_offsets, (void*)M->ex.face_verts,
+                        (void*)M->ex.face_tet_offsets, (void*)M->ex.face_tets, (void*)M->ex.face_func})
+            if (p) cudaFreeAsync(p, s);
+        M->ex = ExtractOut();
+        cudaMemsetAsync(status, 0, sizeof(uint32_t), s);  // the extraction raised nothing else: it would be an error
+        xa.tight_tables = false;
+        cudaError_t e = run_extract(xa, act_sum, bases_ready ? &xb : nullptr, M->ex, s);
+        if (e != cudaSuccess) return bail(fail(RIA_ECUDA, std::string("extract: ") + cudaGetErrorString(e)));
+        cudaEventRecord(ev[4], s);
+        cudaMemcpyAsync(h, cnt, sizeof(h), cudaMemcpyDeviceToHost, s);
+        if ((se = cudaStreamSynchronize(s)) != cudaSuccess) return bail(fail(RIA_ECUDA, cudaGetErrorString(se)));
+    }
     ria_status ms = map_status((uint32_t)h[0]);
     if (ms != RIA_OK) return bail(ms);
     M->stats[RIA_STAT_NUM_PTS] = in.V;

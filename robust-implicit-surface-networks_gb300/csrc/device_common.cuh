@@ -184,6 +184,7 @@ struct HashTab {
     ulonglong2* keys;  // all bits set = empty
     uint32_t* owner;   // smallest occurrence position seen for the key
     uint64_t cap_mask;
+    uint64_t probe_limit = 0;  // probes before an insert gives up (0: the whole table)
 };
 
 __device__ __forceinline__ uint64_t mix64(uint64_t x) {
@@ -218,11 +219,13 @@ struct HashTab64 {
     unsigned long long* keys;
     uint32_t* owner;
     uint64_t cap_mask;
+    uint64_t probe_limit = 0;  // probes before an insert gives up (0: the whole table)
 };
 
 __device__ __forceinline__ int64_t ht64_insert_min(const HashTab64& h, uint64_t key, uint32_t pos) {
     uint64_t slot = mix64(key) & h.cap_mask;
-    for (uint64_t probe = 0; probe <= h.cap_mask; ++probe) {
+    const uint64_t lim = h.probe_limit ? h.probe_limit : h.cap_mask + 1;
+    for (uint64_t probe = 0; probe < lim; ++probe) {
         const unsigned long long old = atomicCAS(&h.keys[slot], ~0ull, (unsigned long long)key);
         if (old == ~0ull || old == key) {
             atomicMin(&h.owner[slot], pos);
@@ -236,7 +239,8 @@ __device__ __forceinline__ int64_t ht64_insert_min(const HashTab64& h, uint64_t 
 // Insert (k0, k1) and lower its owner to `pos`; returns the slot or -1 when the table is full.
 __device__ __forceinline__ int64_t ht_insert_min(const HashTab& h, uint64_t k0, uint64_t k1, uint32_t pos) {
     uint64_t slot = mix64(k0 * 0x9E3779B97F4A7C15ull ^ mix64(k1)) & h.cap_mask;
-    for (uint64_t probe = 0; probe <= h.cap_mask; ++probe) {
+    const uint64_t lim = h.probe_limit ? h.probe_limit : h.cap_mask + 1;
+    for (uint64_t probe = 0; probe < lim; ++probe) {
         uint64_t olo, ohi;
         if (cas128(&h.keys[slot], k0, k1, olo, ohi) || (olo == k0 && ohi == k1)) {
             atomicMin(&h.owner[slot], pos);

@@ -298,11 +298,17 @@ struct Pool {
     cudaError_t err = cudaSuccess;
     char* cur = nullptr;
     size_t left = 0;
+    bool measuring = false;  // get() only adds up the bytes (reserve() then takes them in one allocation)
+    size_t measured = 0;
     static constexpr size_t kChunk = 32ull << 20;
     template <class T>
     T* get(int64_t n) {
         if (n <= 0) n = 1;
         const size_t bytes = (sizeof(T) * (size_t)n + 255) & ~(size_t)255;
+        if (measuring) {
+            measured += bytes;
+            return nullptr;
+        }
         if (bytes <= left) {
             T* p = (T*)cur;
             cur += bytes;
@@ -320,6 +326,19 @@ struct Pool {
         cur = (char*)p + bytes;
         left = size - bytes;
         return (T*)p;
+    }
+    // one chunk for `bytes` more (a call's buffers carved from it with no further allocation)
+    void reserve(size_t bytes) {
+        if (bytes <= left) return;
+        void* p = nullptr;
+        cudaError_t e = cudaMallocAsync(&p, bytes, s);
+        if (e != cudaSuccess) {
+            err = e;
+            return;
+        }
+        ptrs.push_back(p);
+        cur = (char*)p;
+        left = bytes;
     }
     ~Pool() {
         for (void* p : ptrs) cudaFreeAsync(p, s);

@@ -47,21 +47,142 @@ struct ExtractCtx {
     int32_t* ffunc;
     uint32_t* fgids;  // global vertex ids of every iso face loop, in occurrence order
     uint64_t* iso0;   // per active tet: iso flags of its first 64 record vertices, from the vertex pass
+    // per table record (the one-plane entries and the secondary lookup's records, shared by many tets):
+    // what the vertex pass reads from its walk, summarised once per call for the entries its tets use
+    uint32_t* tsum_state;  // 0 unused, 1 used (walked by each tet: too many vertices or faces), 2 summarised
+    uint64_t* tsum;        // kTsumWords words per entry: iso flags, iso face count, then one word per face
+    uint32_t tsum_n;
+    U4 tot;  // totals of the bases (vertex occurrences, face occurrences, loop vertices, boundary faces)
 };
+
+constexpr int kTsumFaces = 6;
+constexpr int kTsumWords = 2 + kTsumFaces;
+
+// the table entries this call's tets use
+__global__ void k_tsum_mark(ExtractCtx C) {
+    const int64_t a = (int64_t)blockIdx.x * kBs + threadIdx.x;
+    if (a >= C.a.A) return;
+    const uint64_t d = C.a.act_desc[a];
+    const uint32_t e = (uint32_t)(d & 0xFFFFFFFFull);
+    // most tets share a few entries: a store only while the entry is unmarked
+    if ((d & kTableBit) && e < C.tsum_n && C.tsum_state[e] == 0u) C.tsum_state[e] = 1u;
+}
+
+// one walk per used entry: its iso flags and iso faces (record face, loop length, loop offset, local
+// function), when they fit the summary
+__global__ void k_tsum_build(ExtractCtx C) {
+    const uint32_t e = blockIdx.x * kBs + threadIdx.x;
+    if (e >= C.tsum_n || C.tsum_state[e] != 1u) return;
+    IAView r;
+    r.init(C.rs.get(kTableBit | (uint64_t)e));
+    uint64_t i0 = 0, rest = 0;
+    uint64_t fw[kTsumFaces];
+    int nfc = 0, off = 0;
+    for (int f = 0; f < r.nf; ++f) {
+        const int L = r.len(f);
+        if (r.plane_is_iso(r.supp(f))) {
+            for (int t = 0; t < L; ++t) {
+                const int v = r.loopv(off + t);
+                if (v < 64) i0 |= 1ull << v;
+                else rest = 1;
+            }
+            if (nfc < kTsumFaces)
+                fw[nfc] = (uint64_t)f | ((uint64_t)L << 16) | ((uint64_t)off << 32) |
+                          ((uint64_t)(uint8_t)(int8_t)r.plane_func_local(r.supp(f)) << 48);
+            ++nfc;
+        }
+        off += L;
+    }
+    if (nfc > kTsumFaces || rest || off >= 0x10000) return;  // stays 1: walked by each tet
+    uint64_t* sd = C.tsum + (size_t)kTsumWords * e;
+    sd[0] = i0;
+    sd[1] = (uint64_t)nfc;
+    for (int k = 0; k < nfc; ++k) sd[2 + k] = fw[k];
+    C.tsum_state[e] = 2u;
+}
+
+// one iso face occurrence of the vertex pass: (record face, loop length, loop offset, local function)
+__device__ __forceinline__ void list_iso_face(const ExtractCtx& C, int64_t a, uint64_t mask, uint32_t& fpos,
+                                              uint32_t& lpos, int f, int L, int off, int lf) {
+    if (fpos >= C.tot.b || lpos + (uint32_t)L > C.tot.c) {  // counts and record disagree: never written
+        raise_status(C.a.status, ST_INTERNAL);
+        return;
+    }
+    C.flen[fpos] = (uint32_t)L;
+    C.floop[fpos] = lpos;
+    C.frec[fpos] = (uint32_t)off;
+    C.fsrc[fpos] = ((uint64_t)a << 16) | (uint64_t)f;
+    C.ffunc[fpos] = lf < 0 ? -1 : local_func(mask, lf);
+    ++fpos;
+    lpos += (uint32_t)L;
+}
+
+__device__ __forceinline__ void list_iso_vertices(const ExtractCtx& C, int64_t a, uint32_t p, uint64_t i0, uint64_t i1,
+                                                  uint64_t i2, uint64_t i3) {
+#pragma unroll
+    for (int w = 0; w < 4; ++w) {
+        uint64_t x = w == 0 ? i0 : (w == 1 ? i1 : (w == 2 ? i2 : i3));
+        while (x) {
+            const int bit = __ffsll((long long)x) - 1;
+            x &= x - 1;
+            if (p >= C.tot.a) {  // counts and record disagree: never written
+                raise_status(C.a.status, ST_INTERNAL);
+                return;
+            }
+            C.vsrc[p++] = ((uint64_t)a << 8) | (uint64_t)(64 * w + bit);
+        }
+    }
+}
 
 // D2a: one thread per active tet.  One walk over the record's faces gives the iso flags of its
 // vertices and the list of its iso face occurrences for the face pass; the tet's iso vertex
-// occurrences are listed at their serial positions (consecutive per tet, in local vertex order).
+// occurrences are listed at their serial positions (consecutive per tet, in local vertex order).  A
+// table record (most tets: one plane, or two planes through the secondary lookup) was walked once
+// for the call (k_tsum_build); its tets read that summary.
 __global__ void __launch_bounds__(kBs) k_ia_vert_list(ExtractCtx C) {
     const int64_t a = (int64_t)blockIdx.x * kBs + threadIdx.x;
     if (a >= C.a.A) return;
-    const uint8_t* rec = C.rs.get(C.a.act_desc[a]);
-    IAView r;
-    r.init(rec);
+    const uint64_t d = C.a.act_desc[a];
     const uint64_t mask = C.a.act_mask[a];
     const U4 b = C.base[a];
-    uint64_t i0 = 0, i1 = 0, i2 = 0, i3 = 0;  // iso flags of local vertices 0..255
     uint32_t fpos = b.b, lpos = b.c;
+    const uint32_t e = (uint32_t)(d & 0xFFFFFFFFull);
+    const bool tab = (d & kTableBit) && e < C.tsum_n;
+    bool summ = tab && C.tsum_state[e] == 2u;
+    const U4 bn = a + 1 < C.a.A ? C.base[a + 1] : C.tot;  // the next tet's bases: this tet's counts
+    const uint64_t* sd = C.tsum + (size_t)kTsumWords * e;
+    uint64_t s0 = 0, s1 = 0;
+    if (summ) {
+        s0 = sd[0];
+        s1 = sd[1];
+        // the summary must agree with the counts this tet's bases were scanned from
+        if (s1 > (uint64_t)kTsumFaces || s1 != (uint64_t)(bn.b - b.b) || (uint32_t)__popcll(s0) != bn.a - b.a)
+            summ = false;
+    }
+    uint64_t fws[kTsumFaces];
+    if (summ) {
+        uint32_t loops = 0;
+        for (int k = 0; k < kTsumFaces; ++k) {
+            fws[k] = k < (int)s1 ? sd[2 + k] : 0;
+            loops += (uint32_t)((fws[k] >> 16) & 0xFFFF);
+        }
+        if (loops != bn.c - b.c) summ = false;
+    }
+    if (summ) {
+        const uint64_t i0 = s0;
+        for (int k = 0; k < kTsumFaces; ++k) {
+            if (k >= (int)s1) break;
+            const uint64_t fw = fws[k];
+            list_iso_face(C, a, mask, fpos, lpos, (int)(fw & 0xFFFF), (int)((fw >> 16) & 0xFFFF),
+                          (int)((fw >> 32) & 0xFFFF), (int)(int8_t)(fw >> 48));
+        }
+        C.iso0[a] = i0;
+        list_iso_vertices(C, a, b.a, i0, 0, 0, 0);
+        return;
+    }
+    IAView r;
+    r.init(C.rs.get(d));
+    uint64_t i0 = 0, i1 = 0, i2 = 0, i3 = 0;  // iso flags of local vertices 0..255
     int off = 0;
     for (int f = 0; f < r.nf; ++f) {
         const int L = r.len(f);
@@ -75,28 +196,12 @@ __global__ void __launch_bounds__(kBs) k_ia_vert_list(ExtractCtx C) {
                 i2 |= w == 2 ? bit : 0;
                 i3 |= w == 3 ? bit : 0;
             }
-            const int lf = r.plane_func_local(r.supp(f));
-            C.flen[fpos] = (uint32_t)L;
-            C.floop[fpos] = lpos;
-            C.frec[fpos] = (uint32_t)off;
-            C.fsrc[fpos] = ((uint64_t)a << 16) | (uint64_t)f;
-            C.ffunc[fpos] = lf < 0 ? -1 : local_func(mask, lf);
-            ++fpos;
-            lpos += (uint32_t)L;
+            list_iso_face(C, a, mask, fpos, lpos, f, L, off, r.plane_func_local(r.supp(f)));
         }
         off += L;
     }
     C.iso0[a] = i0;
-    uint32_t p = b.a;
-#pragma unroll
-    for (int w = 0; w < 4; ++w) {
-        uint64_t x = w == 0 ? i0 : (w == 1 ? i1 : (w == 2 ? i2 : i3));
-        while (x) {
-            const int bit = __ffsll((long long)x) - 1;
-            x &= x - 1;
-            C.vsrc[p++] = ((uint64_t)a << 8) | (uint64_t)(64 * w + bit);
-        }
-    }
+    list_iso_vertices(C, a, b.a, i0, i1, i2, i3);
 }
 
 __device__ __forceinline__ uint64_t shfl64(uint64_t v, int src) {
@@ -113,13 +218,17 @@ __device__ __forceinline__ uint64_t shfl64(uint64_t v, int src) {
 __global__ void __launch_bounds__(kBs) k_ia_vert_keys(ExtractCtx C, int64_t NV) {
     const int64_t p = (int64_t)blockIdx.x * kBs + threadIdx.x;
     const int lane = threadIdx.x & 31;
-    const bool has = p < NV;
+    bool has = p < NV;
+    const uint64_t src = has ? C.vsrc[p] : 0;
+    const int64_t a = (int64_t)(src >> 8);
+    if (has && a >= C.a.A) {  // an occurrence the list pass could not write (status raised there)
+        raise_status(C.a.status, ST_INTERNAL);
+        has = false;
+    }
     int type = 0;
     VertKey k;
     uint64_t k0 = (uint64_t)lane, k1 = ~0ull;  // lanes without a keyed occurrence match no one
     if (has) {
-        const uint64_t src = C.vsrc[p];
-        const int64_t a = (int64_t)(src >> 8);
         const int j = (int)(src & 0xFF);
         IAView r;
         r.init(C.rs.get(C.a.act_desc[a]));
@@ -180,6 +289,7 @@ __global__ void k_vert_owner(ExtractCtx C, int64_t n) {
     else if (ty == OCC_CORNER) own = C.corner_owner[pay];
     else if (ty == OCC_EDGE) own = C.edge64 ? C.he64.owner[pay] : C.he.owner[pay];
     else own = C.hf.owner[pay];
+    if (own > (uint32_t)p) own = (uint32_t)p;  // only after a failed insert (ST_HASH_FULL already raised)
     C.vowner[p] = own;
     C.vflag[p] = own == (uint32_t)p ? 1u : 0u;
 }
@@ -201,6 +311,12 @@ __device__ __forceinline__ void vert_emit_one(const ExtractCtx& C, uint32_t p, i
     const uint64_t occ = C.vocc[p], src = C.vsrc[p];
     const int64_t a = (int64_t)(src >> 8);
     const int j = (int)(src & 0xFF);
+    if (a >= C.a.A) {
+        raise_status(C.a.status, ST_INTERNAL);
+        for (int c = 0; c < 11; ++c) rec[c] = -1;
+        for (int c = 0; c < 3; ++c) xyz[c] = 0.0;
+        return;
+    }
     const uint32_t tet = C.a.act_tet[a];
     const uint64_t ty = occ >> 62, pay = occ & ((1ull << 62) - 1);
     VertKey k;
@@ -340,7 +456,7 @@ __global__ void __launch_bounds__(kBs) k_ia_face_keys(ExtractCtx C, int64_t n) {
     int64_t mn = 0, second = 0, mx = 0;
     if (has) {
         const uint64_t src = C.fsrc[p];
-        const int64_t a = (int64_t)(src >> 16);
+        const int64_t a = (int64_t)(src >> 16) < C.a.A ? (int64_t)(src >> 16) : 0;  // (a list-pass failure is already raised)
         const int f = (int)(src & 0xFFFF);
         IAView r;
         r.init(C.rs.get(C.a.act_desc[a]));
@@ -350,7 +466,8 @@ __global__ void __launch_bounds__(kBs) k_ia_face_keys(ExtractCtx C, int64_t n) {
         else
             iso_vertex_flags(r, iso);
         const uint32_t vb = C.base[a].a;
-        const int L = (int)C.flen[p], off = (int)C.frec[p];
+        const int L = (uint64_t)C.floop[p] + C.flen[p] <= (uint64_t)C.tot.c ? (int)C.flen[p] : 0;  // (else already raised)
+        const int off = (int)C.frec[p];
         uint32_t* g = C.fgids + C.floop[p];
         for (int t = 0; t < L; ++t) g[t] = C.occ_gid[vb + iso_rank(iso, r.loopv(off + t))];
         bnd = r.bnd(f);
@@ -390,6 +507,7 @@ __global__ void k_face_owner(ExtractCtx C, int64_t n) {
     if (p >= n) return;
     const uint64_t occ = C.focc[p];
     uint32_t own = (occ >> 62) == OCC_SELF ? (uint32_t)p : C.hb.owner[occ & ((1ull << 62) - 1)];
+    if (own > (uint32_t)p) own = (uint32_t)p;  // only after a failed insert (ST_HASH_FULL already raised)
     C.fowner[p] = own;
     if (own != (uint32_t)p) atomicAdd(&C.fdup[own], 1u);
 }
@@ -430,7 +548,7 @@ __global__ void __launch_bounds__(kBs) k_ia_face_emit(ExtractCtx C, int64_t n, i
     }
     const uint32_t own = C.fowner[p];
     const uint64_t src = C.fsrc[p];
-    const int64_t tet = C.a.act_tet[src >> 16];
+    const int64_t tet = C.a.act_tet[(int64_t)(src >> 16) < C.a.A ? (int64_t)(src >> 16) : 0];
     const int64_t f = (int64_t)(src & 0xFFFF);
     if (own == (uint32_t)p) {
         const U4 sc = C.fscan[p];
@@ -529,46 +647,67 @@ cudaError_t run_extract(const ExtractArgs& a, const IASum4* act_sum, const Extra
         base = b;
     }
     C.base = base;
+    C.tot = tot;
     const int64_t NV = tot.a, NF = tot.b, NB = tot.d;
-    // tables
-    C.corner_owner = pool.get<uint32_t>(a.V);
-    const uint64_t cap_e = pow2_at_least((uint64_t)NV), cap_f = pow2_at_least((uint64_t)NV / 2 + 1);
-    const uint64_t cap_b = pow2_at_least(2 * (uint64_t)NB + 1);
+    // tables: tight, sized for the usual share of distinct keys (bounded probing; an overflow raises
+    // ST_HASH_FULL and the caller runs the extraction again with worst-case sizes), or worst case: a
+    // slot per occurrence that could hold a distinct key
+    const bool tight = a.tight_tables;
+    const uint64_t cap_e = pow2_at_least(tight ? (uint64_t)NV / 2 + 1 : (uint64_t)NV);
+    const uint64_t cap_f = pow2_at_least(tight ? (uint64_t)NV / 16 + 1 : (uint64_t)NV / 2 + 1);
+    const uint64_t cap_b = pow2_at_least(tight ? (uint64_t)NB + 1 : 2 * (uint64_t)NB + 1);
+    const uint64_t probes = tight ? 4096 : 0;
     C.edge64 = a.V < (1ll << 28) && a.F <= 256;
-    if (C.edge64) {
-        C.he = HashTab{nullptr, nullptr, 0};
-        C.he64 = HashTab64{pool.get<unsigned long long>((int64_t)cap_e), pool.get<uint32_t>((int64_t)cap_e), cap_e - 1};
-    } else {
-        C.he = HashTab{pool.get<ulonglong2>((int64_t)cap_e), pool.get<uint32_t>((int64_t)cap_e), cap_e - 1};
-        C.he64 = HashTab64{nullptr, nullptr, 0};
-    }
-    C.hf = HashTab{pool.get<ulonglong2>((int64_t)cap_f), pool.get<uint32_t>((int64_t)cap_f), cap_f - 1};
-    C.hb = HashTab{pool.get<ulonglong2>((int64_t)cap_b), pool.get<uint32_t>((int64_t)cap_b), cap_b - 1};
-    C.vocc = pool.get<uint64_t>(NV);
-    C.vsrc = pool.get<uint64_t>(NV);
-    C.vowner = pool.get<uint32_t>(NV);
-    C.vflag = pool.get<uint32_t>(NV);
-    C.vgid_new = pool.get<uint32_t>(NV);
-    C.occ_gid = pool.get<uint32_t>(NV);
-    C.focc = pool.get<uint64_t>(NF);
-    C.fowner = pool.get<uint32_t>(NF);
-    C.flen = pool.get<uint32_t>(NF);
-    C.fdup = pool.get<uint32_t>(NF);
-    C.fsz = pool.get<U4>(NF);
-    C.fscan = pool.get<U4>(NF);
-    C.floop = pool.get<uint32_t>(NF);
-    C.fsrc = pool.get<uint64_t>(NF);
-    C.ffunc = pool.get<int32_t>(NF);
-    C.frec = pool.get<uint32_t>(NF);
-    C.fgids = pool.get<uint32_t>((int64_t)tot.c);
-    C.iso0 = pool.get<uint64_t>(A);
-    uint32_t* gid_src = pool.get<uint32_t>(NV);  // the occurrence of each new vertex, by id
-    int64_t* d_tots = pool.get<int64_t>(4);
+    C.tsum_n = (uint32_t)(kTablePatterns + kCacheEntries);
+    uint32_t* gid_src = nullptr;  // the occurrence of each new vertex, by id
+    int64_t* d_tots = nullptr;
+    void* scan_tmp = nullptr;
     size_t vscan_bytes = 0, fscan_bytes = 0;
     if (NV > 0) cub::DeviceScan::ExclusiveSum(nullptr, vscan_bytes, C.vflag, C.vgid_new, NV, s);
     if (NF > 0)
         cub::DeviceScan::ExclusiveScan(nullptr, fscan_bytes, C.fsz, C.fscan, U4Sum(), U4{0, 0, 0, 0}, NF, s);
-    void* scan_tmp = pool.get<uint8_t>((int64_t)std::max(vscan_bytes, fscan_bytes));
+    // every buffer of the call carved from one allocation: the sizes are added up first
+    auto carve = [&](Pool& P) {
+        C.corner_owner = P.get<uint32_t>(a.V);
+        if (C.edge64) {
+            C.he = HashTab{nullptr, nullptr, 0};
+            C.he64 = HashTab64{P.get<unsigned long long>((int64_t)cap_e), P.get<uint32_t>((int64_t)cap_e), cap_e - 1,
+                               probes};
+        } else {
+            C.he = HashTab{P.get<ulonglong2>((int64_t)cap_e), P.get<uint32_t>((int64_t)cap_e), cap_e - 1, probes};
+            C.he64 = HashTab64{nullptr, nullptr, 0};
+        }
+        C.hf = HashTab{P.get<ulonglong2>((int64_t)cap_f), P.get<uint32_t>((int64_t)cap_f), cap_f - 1, probes};
+        C.hb = HashTab{P.get<ulonglong2>((int64_t)cap_b), P.get<uint32_t>((int64_t)cap_b), cap_b - 1, probes};
+        C.vocc = P.get<uint64_t>(NV);
+        C.vsrc = P.get<uint64_t>(NV);
+        C.vowner = P.get<uint32_t>(NV);
+        C.vflag = P.get<uint32_t>(NV);
+        C.vgid_new = P.get<uint32_t>(NV);
+        C.occ_gid = P.get<uint32_t>(NV);
+        C.focc = P.get<uint64_t>(NF);
+        C.fowner = P.get<uint32_t>(NF);
+        C.flen = P.get<uint32_t>(NF);
+        C.fdup = P.get<uint32_t>(NF);
+        C.fsz = P.get<U4>(NF);
+        C.fscan = P.get<U4>(NF);
+        C.floop = P.get<uint32_t>(NF);
+        C.fsrc = P.get<uint64_t>(NF);
+        C.ffunc = P.get<int32_t>(NF);
+        C.frec = P.get<uint32_t>(NF);
+        C.fgids = P.get<uint32_t>((int64_t)tot.c);
+        C.iso0 = P.get<uint64_t>(A);
+        C.tsum_state = P.get<uint32_t>(C.tsum_n);
+        C.tsum = P.get<uint64_t>((int64_t)kTsumWords * C.tsum_n);
+        gid_src = P.get<uint32_t>(NV);
+        d_tots = P.get<int64_t>(8);
+        scan_tmp = P.get<uint8_t>((int64_t)std::max(vscan_bytes, fscan_bytes));
+    };
+    pool.measuring = true;
+    carve(pool);
+    pool.measuring = false;
+    pool.reserve(pool.measured);
+    carve(pool);
     if (pool.err) return pool.err;
     FillList fill;
     fill.add(C.corner_owner, sizeof(uint32_t) * (size_t)(a.V > 0 ? a.V : 1), ~0u);
@@ -582,22 +721,55 @@ cudaError_t run_extract(const ExtractArgs& a, const IASum4* act_sum, const Extra
         fill.add(C.he64.owner, sizeof(uint32_t) * (C.he64.cap_mask + 1), ~0u);
     }
     fill.add(C.fdup, sizeof(uint32_t) * (size_t)(NF > 0 ? NF : 1), 0u);
-    launch_fill(fill, s);
-    // vertices
+    uint64_t* pin = nullptr;
+    AuxStream* aux = nullptr;
+    cudaError_t e = pinned_words(&pin);
+    if (e == cudaSuccess) e = aux_stream(&aux);
+    if (e != cudaSuccess) return e;
+    // whatever path leaves this function, the call's stream waits for the second stream's work before
+    // the temporaries are released on it (this guard is destroyed before the pool)
+    struct JoinAux {
+        cudaStream_t s;
+        AuxStream* aux;
+        bool armed = false;
+        ~JoinAux() {
+            if (armed) cudaStreamWaitEvent(s, aux->join, 0);
+        }
+    } join_aux{s, aux};
+    // the tables are filled on the second stream (bound by HBM bandwidth) while the occurrence list is
+    // built (bound by memory latency); the key pass waits for both
+    cudaEventRecord(aux->fork, s);
+    cudaStreamWaitEvent(aux->s, aux->fork, 0);
+    launch_fill(fill, aux->s);
+    cudaEventRecord(aux->join, aux->s);
+    join_aux.armed = true;
+    // vertices: the table entries in use summarised, then the occurrence list
+    cudaMemsetAsync(C.tsum_state, 0, sizeof(uint32_t) * C.tsum_n, s);
     if (A > 0) {
+        k_tsum_mark<<<nblk(A), kBs, 0, s>>>(C);
+        note_launch();
+        k_tsum_build<<<nblk(C.tsum_n), kBs, 0, s>>>(C);
+        note_launch();
         k_ia_vert_list<<<nblk(A), kBs, 0, s>>>(C);
         note_launch();
     }
+    cudaStreamWaitEvent(s, aux->join, 0);
     if (NV > 0) {
         k_ia_vert_keys<<<nblk(NV), kBs, 0, s>>>(C, NV);
         note_launch();
         k_vert_owner<<<nblk(NV), kBs, 0, s>>>(C, NV);
         note_launch();
         cub::DeviceScan::ExclusiveSum(scan_tmp, vscan_bytes, C.vflag, C.vgid_new, NV, s);
-        // the vertex count is read together with the face counts, in one synchronization
         k_vert_gid<<<nblk(NV), kBs, 0, s>>>(C, NV, gid_src);
         note_launch();
     }
+    // The vertex count goes to pinned host memory while the face pass runs; as soon as it arrives the
+    // vertex outputs are allocated and the vertex records (bound by the FP64 pipe: divisions) are
+    // emitted on the second stream, beside the face pass (bound by memory latency).
+    k_ia_totals<<<1, 32, 0, s>>>(C, NV, 0, d_tots);
+    note_launch();
+    cudaMemcpyAsync(pin, d_tots, sizeof(int64_t), cudaMemcpyDeviceToHost, s);
+    cudaEventRecord(aux->fork, s);
     // faces
     if (NF > 0) {
         k_ia_face_keys<<<nblk(NF), kBs, 0, s>>>(C, NF);
@@ -608,24 +780,27 @@ cudaError_t run_extract(const ExtractArgs& a, const IASum4* act_sum, const Extra
         note_launch();
         cub::DeviceScan::ExclusiveScan(scan_tmp, fscan_bytes, C.fsz, C.fscan, U4Sum(), U4{0, 0, 0, 0}, NF, s);
     }
-    k_ia_totals<<<1, 32, 0, s>>>(C, NV, NF, d_tots);
+    k_ia_totals<<<1, 32, 0, s>>>(C, 0, NF, d_tots + 4);
     note_launch();
-    int64_t tots[4] = {0, 0, 0, 0};
-    cudaError_t e = cudaMemcpyAsync(tots, d_tots, sizeof(tots), cudaMemcpyDeviceToHost, s);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-    if (e != cudaSuccess) return e;
-    const int64_t n_verts = tots[0], n_faces = tots[1], n_fv = tots[2], n_ft = tots[3];
+    cudaMemcpyAsync(pin + 1, d_tots + 5, 3 * sizeof(int64_t), cudaMemcpyDeviceToHost, s);
+    if ((e = cudaEventSynchronize(aux->fork)) != cudaSuccess) return e;
+    const int64_t n_verts = (int64_t)pin[0];
     out.n_verts = n_verts;
-    if ((e = cudaMallocAsync((void**)&out.xyz, sizeof(double) * 3 * (size_t)(n_verts > 0 ? n_verts : 1), s)) !=
+    cudaStreamWaitEvent(aux->s, aux->fork, 0);
+    if ((e = cudaMallocAsync((void**)&out.xyz, sizeof(double) * 3 * (size_t)(n_verts > 0 ? n_verts : 1), aux->s)) !=
         cudaSuccess)
         return e;
-    if ((e = cudaMallocAsync((void**)&out.verts, sizeof(int64_t) * 11 * (size_t)(n_verts > 0 ? n_verts : 1), s)) !=
-        cudaSuccess)
+    if ((e = cudaMallocAsync((void**)&out.verts, sizeof(int64_t) * 11 * (size_t)(n_verts > 0 ? n_verts : 1),
+                             aux->s)) != cudaSuccess)
         return e;
     if (n_verts > 0) {
-        k_vert_emit<<<nblk(n_verts), kBs, 0, s>>>(C, n_verts, gid_src, out.verts, out.xyz);
+        k_vert_emit<<<nblk(n_verts), kBs, 0, aux->s>>>(C, n_verts, gid_src, out.verts, out.xyz);
         note_launch();
     }
+    cudaEventRecord(aux->join, aux->s);
+    cudaEventRecord(aux->fork, s);  // after the face totals' copy
+    if ((e = cudaEventSynchronize(aux->fork)) != cudaSuccess) return e;
+    const int64_t n_faces = (int64_t)pin[1], n_fv = (int64_t)pin[2], n_ft = (int64_t)pin[3];
     out.n_faces = n_faces;
     out.n_face_verts = n_fv;
     out.n_face_tets = n_ft;
@@ -647,7 +822,7 @@ cudaError_t run_extract(const ExtractArgs& a, const IASum4* act_sum, const Extra
         cudaMemsetAsync(out.face_offsets, 0, sizeof(int64_t), s);
         cudaMemsetAsync(out.face_tet_offsets, 0, sizeof(int64_t), s);
     }
-    return cudaGetLastError();
+    return cudaGetLastError();  // the guard joins the second stream: the call's stream then owns every output
 }
 
 // ---- CSG pruning (src/csg.cpp:55-116): a face separates the shape's inside from its outside when the

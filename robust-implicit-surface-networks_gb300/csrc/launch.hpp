@@ -215,6 +215,17 @@ void launch_build_table(bool mi, uint8_t* table, uint32_t* table_off, IASum4* ta
 void launch_robust(const CutArgs& a, void* scratch, int64_t scratch_slots, unsigned long long* n_fail,
                    cudaStream_t s);
 
+// A second stream of the current device for the calling thread, with events to fork work onto it
+// and join it back (capi.cu); each thread runs one call at a time, so a call may use it freely.
+struct AuxStream {
+    cudaStream_t s = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
+};
+cudaError_t aux_stream(AuxStream** out);
+// 64 words of pinned host memory for the calling thread: counters copied there arrive while the
+// stream keeps working (the copy into pageable memory would wait for the whole stream).
+cudaError_t pinned_words(uint64_t** out);
+
 // ---- stage d (k_extract.cu)
 struct ExtractArgs {
     bool mi;
@@ -234,6 +245,10 @@ struct ExtractArgs {
     GridDesc g;
     int64_t V;
     uint32_t* status;
+    // implicit arrangement: dedup tables sized for the usual load, with bounded probing; an insert
+    // that runs out raises ST_HASH_FULL and the caller runs the extraction again with tables sized
+    // for the worst case (tight_tables = false)
+    bool tight_tables = true;
 };
 struct ExtractOut {
     int64_t n_verts = 0, n_faces = 0, n_face_verts = 0, n_face_tets = 0;

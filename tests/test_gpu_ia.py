@@ -124,6 +124,26 @@ def test_degenerate_workload(pkg, fns, oracle, lib, res):
     assert_mesh_equal(mesh, oracle.run("ia", pts, tets, fv, threads=os.cpu_count() or 1))
 
 
+@pytest.mark.parametrize("seed,nplanes,res", [(7, 20, 6), (11, 18, 6)])
+def test_dense_planes_overflow_tight_tables(pkg, fns, oracle, lib, seed, nplanes, res):
+    """Many planes on a small grid: vertices where two planes cross a tet face (keyed by the face
+    table) outnumber the extraction's tight table (a slot per 16 vertex occurrences, at least 1,024),
+    so its inserts overflow and the call runs the extraction again with worst-case tables.  The mesh
+    must still equal the oracle's."""
+    rng = np.random.default_rng(seed)
+    funcs = fns.make_functions([fns.random_function_spec(rng, "plane") for _ in range(nplanes)])
+    mesh = pkg.grid_implicit_arrangement(res, funcs)
+    pts, tets = fns.generate_tet_mesh(res)
+    fv = oracle.sample(funcs, pts)
+    ref = oracle.run("ia", pts, tets, fv)
+    occurrences = int(ref["tet_vert_offsets"][-1])  # iso vertex occurrences, as the extraction counts them
+    cap = 1024
+    while cap < occurrences // 16 + 1:
+        cap *= 2
+    assert (ref["verts"].reshape(-1, 11)[:, 2] == 3).sum() > cap
+    assert_mesh_equal(mesh, ref)
+
+
 def test_batch_api_records(pkg, oracle, lib):
     rng = np.random.default_rng(3)
     rows = []
