@@ -503,25 +503,26 @@ ria_status run_pipeline(const ria_config* cfg, const Inputs& in, cudaStream_t s,
     ranges.next("ria c cut");
 
     // ---- stage c
-    // The implicit arrangement's extraction scans the cut's per-tet counts; the scan is enqueued before
-    // the cut stage's synchronization, so its totals, the status word and the deferred count come back
-    // in one copy.  Deferred tets change their counts: the bases are then taken again.
+    // The extraction scans the cut's per-tet counts; the scan is enqueued before the cut stage's
+    // synchronization, so its totals, the status word and the deferred count come back in one copy.
+    // Deferred tets change their counts: the bases are then taken again.
     const bool ia_extract = !mi && !cfg->robust_test;
+    const bool prep_bases = !cfg->robust_test;  // both extractions start from the same scan
     ExtractBases xb;
     bool bases_ready = false;
     void* xb_buf = nullptr;
-    if (ia_extract) {
+    if (prep_bases) {
         xb_buf = tmp.get<uint8_t>((int64_t)extract_bases_bytes(A), &err);
         if (err != cudaSuccess) return bail(fail(RIA_ENOMEM, "device allocation failed"));
     }
     unsigned long long hc[kCounters] = {0};
     auto read_counters = [&](bool cut_end) -> bool {
         if (cut_end) cudaEventRecord(ev[3], s);  // the scan belongs to the extraction's time
-        if (ia_extract) launch_extract_bases(A, act_sum, xb_buf, cnt + 20, &xb, s);
+        if (prep_bases) launch_extract_bases(A, act_sum, xb_buf, cnt + 20, &xb, s);
         cudaMemcpyAsync(hc, cnt, sizeof(hc), cudaMemcpyDeviceToHost, s);
         if (cudaStreamSynchronize(s) != cudaSuccess) return false;
         for (int i = 0; i < 4; ++i) xb.total[i] = hc[20 + i];
-        bases_ready = ia_extract;
+        bases_ready = prep_bases;
         return true;
     };
     CutArgs ca{};
@@ -736,7 +737,7 @@ ria_status run_pipeline(const ria_config* cfg, const Inputs& in, cudaStream_t s,
         if (!bases_ready && !read_counters(false)) return bail(fail(RIA_ECUDA, cudaGetErrorString(cudaGetLastError())));
         const uint32_t hst = (uint32_t)hc[0];
         if (hst) return bail(map_status(hst));
-        cudaError_t e = run_extract(xa, act_sum, ia_extract ? &xb : nullptr, M->ex, s);
+        cudaError_t e = run_extract(xa, act_sum, prep_bases ? &xb : nullptr, M->ex, s);
         if (e == cudaErrorNotSupported) return bail(fail(RIA_EINVAL, "material-interface extraction is not available"));
         if (e != cudaSuccess) return bail(fail(RIA_ECUDA, std::string("extract: ") + cudaGetErrorString(e)));
     }

@@ -349,11 +349,17 @@ struct Pool {
 // owners, the duplicate counters): one wide grid-stride pass instead of a memset per buffer.
 // Buffers start 16-byte aligned (Pool hands out 256-byte aligned blocks) and hold whole words.
 struct FillList {
-    uint32_t* p[8];
-    uint64_t words[8];
-    uint32_t val[8];
+    static constexpr int kMax = 16;
+    uint32_t* p[kMax];
+    uint64_t words[kMax];
+    uint32_t val[kMax];
     int n = 0;
+    bool overflow = false;  // more buffers than kMax: launch_fill fills none and reports it
     void add(void* ptr, uint64_t bytes, uint32_t v) {
+        if (n >= kMax) {
+            overflow = true;
+            return;
+        }
         p[n] = (uint32_t*)ptr;
         words[n] = bytes / 4;
         val[n] = v;
@@ -373,10 +379,12 @@ static __global__ void __launch_bounds__(256) k_fill(FillList L) {
     }
 }
 
-inline void launch_fill(const FillList& L, cudaStream_t s) {
-    if (L.n == 0) return;
+inline cudaError_t launch_fill(const FillList& L, cudaStream_t s) {
+    if (L.overflow) return cudaErrorInvalidValue;
+    if (L.n == 0) return cudaSuccess;
     k_fill<<<152 * 8, 256, 0, s>>>(L);
     note_launch();
+    return cudaSuccess;
 }
 
 inline cudaError_t exscan_u32(const uint32_t* in, uint32_t* out, int64_t n, cudaStream_t s) {

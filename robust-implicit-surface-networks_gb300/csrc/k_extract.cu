@@ -573,7 +573,8 @@ __global__ void __launch_bounds__(kBs) k_ia_face_emit(ExtractCtx C, int64_t n, i
 
 }  // namespace
 
-cudaError_t run_extract_mi(const ExtractArgs& a, const IASum4* act_sum, ExtractOut& out, cudaStream_t s);
+cudaError_t run_extract_mi(const ExtractArgs& a, const IASum4* act_sum, const ExtractBases* pre, ExtractOut& out,
+                           cudaStream_t s);
 
 namespace {
 
@@ -623,7 +624,7 @@ void launch_extract_bases(int64_t A, const IASum4* act_sum, void* buf, unsigned 
 
 cudaError_t run_extract(const ExtractArgs& a, const IASum4* act_sum, const ExtractBases* pre, ExtractOut& out,
                         cudaStream_t s) {
-    if (a.mi) return run_extract_mi(a, act_sum, out, s);
+    if (a.mi) return run_extract_mi(a, act_sum, pre, out, s);
     Pool pool{s};
     ExtractCtx C;
     C.a = a;
@@ -740,7 +741,7 @@ cudaError_t run_extract(const ExtractArgs& a, const IASum4* act_sum, const Extra
     // built (bound by memory latency); the key pass waits for both
     cudaEventRecord(aux->fork, s);
     cudaStreamWaitEvent(aux->s, aux->fork, 0);
-    launch_fill(fill, aux->s);
+    if ((e = launch_fill(fill, aux->s)) != cudaSuccess) return e;
     cudaEventRecord(aux->join, aux->s);
     join_aux.armed = true;
     // vertices: the table entries in use summarised, then the occurrence list

@@ -256,6 +256,29 @@ __global__ void k_mi_final_counts(int64_t A, const IASum4* __restrict__ sum, con
     out[a] = U4{(uint32_t)s.a + e.a, (uint32_t)s.b + e.b, (uint32_t)s.c + e.c, 0};
 }
 
+// totals of the final positions (vertex occurrences, faces, loop vertices) and whether any boundary
+// face became an interface; with `nv`, the number of new vertices as well
+__global__ void k_mi_totals(int64_t A, const U4* __restrict__ fin, const U4* __restrict__ vbase,
+                            const uint32_t* __restrict__ any_emit, int64_t nv, const uint32_t* __restrict__ vflag,
+                            const uint32_t* __restrict__ vgid_new, int64_t* __restrict__ d) {
+    if (nv >= 0) {
+        d[4] = nv ? (int64_t)vflag[nv - 1] + (int64_t)vgid_new[nv - 1] : 0;
+        return;
+    }
+    const U4 t = A ? U4Sum()(fin[A - 1], vbase[A - 1]) : U4{0, 0, 0, 0};
+    d[0] = t.a;
+    d[1] = t.b;
+    d[2] = t.c;
+    d[3] = *any_emit;
+}
+
+// closing entries of the two offset arrays
+__global__ void k_mi_close(int64_t* __restrict__ face_offsets, int64_t* __restrict__ face_tet_offsets, int64_t NF,
+                           int64_t NL) {
+    face_offsets[NF] = NL;
+    face_tet_offsets[NF] = NF;
+}
+
 // M6 (only with emitted faces): occurrences at their final positions; owners recomputed
 __global__ void __launch_bounds__(kBs) k_mi_final_occ(MICtx C) {
     const int64_t a = (int64_t)blockIdx.x * kBs + threadIdx.x;
@@ -311,11 +334,17 @@ __global__ void k_mi_owner(MICtx C, int64_t n) {
 }
 
 // M7: vertex records and coordinates (compute_MI_vert_xyz: differences of consecutive materials)
+// the global vertex id of every occurrence (the face pass reads them)
+__global__ void k_mi_gid(MICtx C, int64_t n) {
+    const int64_t p = (int64_t)blockIdx.x * kBs + threadIdx.x;
+    if (p >= n) return;
+    C.occ_gid[p] = C.vgid_new[C.vowner[p]];
+}
+
 __global__ void k_mi_vert_emit(MICtx C, int64_t n, int64_t* __restrict__ verts, double* __restrict__ xyz) {
     const int64_t p = (int64_t)blockIdx.x * kBs + threadIdx.x;
     if (p >= n) return;
     const uint32_t own = C.vowner[p];
-    C.occ_gid[p] = C.vgid_new[own];
     if (own != (uint32_t)p) return;
     const uint32_t gid = C.vgid_new[p];
     const uint64_t src = C.vsrc[p];
@@ -463,48 +492,80 @@ __global__ void __launch_bounds__(kBs) k_mi_face_emit(MICtx C, bool with_extra, 
 
 }  // namespace
 
-cudaError_t run_extract_mi(const ExtractArgs& a, const IASum4* act_sum, ExtractOut& out, cudaStream_t s) {
+cudaError_t run_extract_mi(const ExtractArgs& a, const IASum4* act_sum, const ExtractBases* pre, ExtractOut& out,
+                           cudaStream_t s) {
     Pool pool{s};
     MICtx C;
     C.a = a;
     C.rs = RecSrc{a.heap, a.heap_big, a.table, a.table_off};
     const int64_t A = a.A;
     out = ExtractOut();
-    U4* bin = pool.get<U4>(A);
-    U4* base0 = pool.get<U4>(A);
-    if (pool.err) return pool.err;
-    if (A > 0) {
-        k_base_in<<<nblk(A), kBs, 0, s>>>(A, act_sum, bin);
-        note_launch();
+    // phase-0 bases: prepared by the caller (their totals read with the cut stage's synchronization),
+    // or here
+    U4 tot{0, 0, 0, 0};
+    if (pre && (pre->base || A == 0)) {
+        C.base0 = (const U4*)pre->base;
+        tot = U4{(uint32_t)pre->total[0], (uint32_t)pre->total[1], (uint32_t)pre->total[2], (uint32_t)pre->total[3]};
+    } else {
+        U4* bin = pool.get<U4>(A);
+        U4* base0 = pool.get<U4>(A);
+        if (pool.err) return pool.err;
+        if (A > 0) {
+            k_base_in<<<nblk(A), kBs, 0, s>>>(A, act_sum, bin);
+            note_launch();
+        }
+        cudaError_t e = exscan_u4(bin, base0, A, &tot, pool, s);
+        if (e != cudaSuccess) return e;
+        C.base0 = base0;
     }
-    U4 tot;
-    cudaError_t e = exscan_u4(bin, base0, A, &tot, pool, s);
-    if (e != cudaSuccess) return e;
-    C.base0 = base0;
     const int64_t NV0 = tot.a, NB = tot.d;
     const uint64_t cap_e = pow2_at_least((uint64_t)NV0), cap_f = pow2_at_least((uint64_t)NV0 / 2 + 1);
     const uint64_t cap_b = pow2_at_least(2 * (uint64_t)NB + 1);
-    C.corner_owner = pool.get<uint32_t>(a.V);
-    C.he = HashTab{pool.get<ulonglong2>((int64_t)cap_e), pool.get<uint32_t>((int64_t)cap_e), cap_e - 1};
-    C.hf = HashTab{pool.get<ulonglong2>((int64_t)cap_f), pool.get<uint32_t>((int64_t)cap_f), cap_f - 1};
-    C.hb = HashTab{pool.get<ulonglong2>((int64_t)cap_b), pool.get<uint32_t>((int64_t)cap_b), cap_b - 1};
-    C.hb_count = pool.get<uint32_t>((int64_t)cap_b);
-    C.vocc0 = pool.get<uint64_t>(NV0);
-    C.vsrc0 = pool.get<uint64_t>(NV0);
-    C.ident = pool.get<uint32_t>(NV0);
-    C.bslot = pool.get<uint64_t>(NB);
-    C.bmask = pool.get<uint64_t>(NB);
-    C.bemit = pool.get<uint32_t>(NB);
-    C.any_emit = pool.get<uint32_t>(1);
-    C.extra = nullptr;
+    uint64_t* pin = nullptr;
+    AuxStream* aux = nullptr;
+    cudaError_t e = pinned_words(&pin);
+    if (e == cudaSuccess) e = aux_stream(&aux);
+    if (e != cudaSuccess) return e;
+    // every buffer of the first phases carved from one allocation (the sizes are added up first)
+    U4 *fin = nullptr, *vbase = nullptr;
+    int64_t* d_tot = nullptr;
+    void* scan_tmp = nullptr;
+    size_t fscan_bytes = 0;
+    if (A > 0) cub::DeviceScan::ExclusiveScan(nullptr, fscan_bytes, fin, vbase, U4Sum(), U4{0, 0, 0, 0}, A, s);
+    auto carve = [&](Pool& P) {
+        C.corner_owner = P.get<uint32_t>(a.V);
+        C.he = HashTab{P.get<ulonglong2>((int64_t)cap_e), P.get<uint32_t>((int64_t)cap_e), cap_e - 1};
+        C.hf = HashTab{P.get<ulonglong2>((int64_t)cap_f), P.get<uint32_t>((int64_t)cap_f), cap_f - 1};
+        C.hb = HashTab{P.get<ulonglong2>((int64_t)cap_b), P.get<uint32_t>((int64_t)cap_b), cap_b - 1};
+        C.hb_count = P.get<uint32_t>((int64_t)cap_b);
+        C.vocc0 = P.get<uint64_t>(NV0);
+        C.vsrc0 = P.get<uint64_t>(NV0);
+        C.ident = P.get<uint32_t>(NV0);
+        C.bslot = P.get<uint64_t>(NB);
+        C.bmask = P.get<uint64_t>(NB);
+        C.bemit = P.get<uint32_t>(NB);
+        C.any_emit = P.get<uint32_t>(1);
+        C.extra = P.get<U4>(A);
+        fin = P.get<U4>(A);
+        vbase = P.get<U4>(A);
+        d_tot = P.get<int64_t>(8);
+        scan_tmp = P.get<uint8_t>((int64_t)fscan_bytes);
+    };
+    pool.measuring = true;
+    carve(pool);
+    pool.measuring = false;
+    pool.reserve(pool.measured);
+    carve(pool);
     if (pool.err) return pool.err;
-    cudaMemsetAsync(C.corner_owner, 0xFF, sizeof(uint32_t) * (size_t)(a.V > 0 ? a.V : 1), s);
+    FillList fill;
+    fill.add(C.corner_owner, sizeof(uint32_t) * (size_t)(a.V > 0 ? a.V : 1), ~0u);
     for (HashTab* h : {&C.he, &C.hf, &C.hb}) {
-        cudaMemsetAsync(h->keys, 0xFF, sizeof(ulonglong2) * (h->cap_mask + 1), s);
-        cudaMemsetAsync(h->owner, 0xFF, sizeof(uint32_t) * (h->cap_mask + 1), s);
+        fill.add(h->keys, sizeof(ulonglong2) * (h->cap_mask + 1), ~0u);
+        fill.add(h->owner, sizeof(uint32_t) * (h->cap_mask + 1), ~0u);
     }
-    cudaMemsetAsync(C.hb_count, 0, sizeof(uint32_t) * cap_b, s);
-    cudaMemsetAsync(C.any_emit, 0, sizeof(uint32_t), s);
+    fill.add(C.hb_count, sizeof(uint32_t) * cap_b, 0u);
+    fill.add(C.any_emit, sizeof(uint32_t), 0u);
+    if ((e = launch_fill(fill, s)) != cudaSuccess) return e;
     if (A > 0) {
         k_mi_vert_keys<<<nblk(A), kBs, 0, s>>>(C);
         note_launch();
@@ -521,62 +582,72 @@ cudaError_t run_extract_mi(const ExtractArgs& a, const IASum4* act_sum, ExtractO
         k_mi_bnd_emit<<<nblk(NB), kBs, 0, s>>>(C, NB);
         note_launch();
     }
-    uint32_t h_emit = 0;
-    cudaMemcpyAsync(&h_emit, C.any_emit, 4, cudaMemcpyDeviceToHost, s);
-    if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return e;
-
-    // final positions
-    U4* fin = pool.get<U4>(A);
-    U4* vbase = pool.get<U4>(A);
-    if (pool.err) return pool.err;
-    if (h_emit) {
-        C.extra = pool.get<U4>(A);
-        if (pool.err) return pool.err;
+    // final positions: the emitted boundary faces' counts (zero when none became an interface) added
+    // to the phase-0 counts; their totals and the emission flag come back in one synchronization
+    if (A > 0) {
         k_mi_extra<<<nblk(A), kBs, 0, s>>>(C);
         note_launch();
-    }
-    if (A > 0) {
         k_mi_final_counts<<<nblk(A), kBs, 0, s>>>(A, act_sum, C.extra, fin);
         note_launch();
+        cub::DeviceScan::ExclusiveScan(scan_tmp, fscan_bytes, fin, vbase, U4Sum(), U4{0, 0, 0, 0}, A, s);
     }
-    U4 ftot;
-    if ((e = exscan_u4(fin, vbase, A, &ftot, pool, s)) != cudaSuccess) return e;
+    k_mi_totals<<<1, 1, 0, s>>>(A, fin, vbase, C.any_emit, -1, nullptr, nullptr, d_tot);
+    note_launch();
+    cudaMemcpyAsync(pin, d_tot, 4 * sizeof(int64_t), cudaMemcpyDeviceToHost, s);
+    if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return e;
+    const int64_t NV = (int64_t)pin[0], NF = (int64_t)pin[1], NL = (int64_t)pin[2];
+    const bool h_emit = pin[3] != 0;
     C.vbase = vbase;
-    const int64_t NV = ftot.a, NF = ftot.b, NL = ftot.c;
+    size_t vscan_bytes = 0;
+    if (NV > 0) cub::DeviceScan::ExclusiveSum(nullptr, vscan_bytes, (const uint32_t*)nullptr, (uint32_t*)nullptr, NV, s);
+    void* vscan_tmp = nullptr;
+    auto carve2 = [&](Pool& P) {
+        if (h_emit) {
+            C.vocc = P.get<uint64_t>(NV);
+            C.vsrc = P.get<uint64_t>(NV);
+        }
+        C.vowner = P.get<uint32_t>(NV);
+        C.vflag = P.get<uint32_t>(NV);
+        C.vgid_new = P.get<uint32_t>(NV);
+        C.occ_gid = P.get<uint32_t>(NV);
+        vscan_tmp = P.get<uint8_t>((int64_t)vscan_bytes);
+    };
+    pool.measuring = true;
+    pool.measured = 0;
+    carve2(pool);
+    pool.measuring = false;
+    pool.reserve(pool.measured);
+    carve2(pool);
+    if (pool.err) return pool.err;
     if (h_emit) {
-        C.vocc = pool.get<uint64_t>(NV);
-        C.vsrc = pool.get<uint64_t>(NV);
-        if (pool.err) return pool.err;
-        cudaMemsetAsync(C.corner_owner, 0xFF, sizeof(uint32_t) * (size_t)(a.V > 0 ? a.V : 1), s);
-        cudaMemsetAsync(C.he.owner, 0xFF, sizeof(uint32_t) * (C.he.cap_mask + 1), s);
-        cudaMemsetAsync(C.hf.owner, 0xFF, sizeof(uint32_t) * (C.hf.cap_mask + 1), s);
+        FillList refill;
+        refill.add(C.corner_owner, sizeof(uint32_t) * (size_t)(a.V > 0 ? a.V : 1), ~0u);
+        refill.add(C.he.owner, sizeof(uint32_t) * (C.he.cap_mask + 1), ~0u);
+        refill.add(C.hf.owner, sizeof(uint32_t) * (C.hf.cap_mask + 1), ~0u);
+        if ((e = launch_fill(refill, s)) != cudaSuccess) return e;
         k_mi_final_occ<<<nblk(A), kBs, 0, s>>>(C);
         note_launch();
     } else {
         C.vocc = C.vocc0;
         C.vsrc = C.vsrc0;
     }
-    C.vowner = pool.get<uint32_t>(NV);
-    C.vflag = pool.get<uint32_t>(NV);
-    C.vgid_new = pool.get<uint32_t>(NV);
-    C.occ_gid = pool.get<uint32_t>(NV);
-    if (pool.err) return pool.err;
     if (NV > 0) {
         k_mi_owner<<<nblk(NV), kBs, 0, s>>>(C, NV);
         note_launch();
+        cub::DeviceScan::ExclusiveSum(vscan_tmp, vscan_bytes, C.vflag, C.vgid_new, NV, s);
+        k_mi_gid<<<nblk(NV), kBs, 0, s>>>(C, NV);
+        note_launch();
     }
-    if ((e = exscan_u32(C.vflag, C.vgid_new, NV, s)) != cudaSuccess) return e;
-    int64_t n_verts = 0;
-    if ((e = scan_total(C.vflag, C.vgid_new, NV, &n_verts, s)) != cudaSuccess) return e;
-    out.n_verts = n_verts;
+    // the vertex count goes to pinned memory while the faces are emitted; the vertex outputs are
+    // allocated when it arrives
+    k_mi_totals<<<1, 1, 0, s>>>(A, nullptr, nullptr, nullptr, NV, C.vflag, C.vgid_new, d_tot);
+    note_launch();
+    cudaMemcpyAsync(pin + 4, d_tot + 4, sizeof(int64_t), cudaMemcpyDeviceToHost, s);
+    cudaEventRecord(aux->fork, s);
     out.n_faces = NF;
     out.n_face_verts = NL;
     out.n_face_tets = NF;
-    if ((e = cudaMallocAsync((void**)&out.xyz, sizeof(double) * 3 * (size_t)(n_verts > 0 ? n_verts : 1), s)) !=
-            cudaSuccess ||
-        (e = cudaMallocAsync((void**)&out.verts, sizeof(int64_t) * 11 * (size_t)(n_verts > 0 ? n_verts : 1), s)) !=
-            cudaSuccess ||
-        (e = cudaMallocAsync((void**)&out.face_offsets, sizeof(int64_t) * (size_t)(NF + 1), s)) != cudaSuccess ||
+    if ((e = cudaMallocAsync((void**)&out.face_offsets, sizeof(int64_t) * (size_t)(NF + 1), s)) != cudaSuccess ||
         (e = cudaMallocAsync((void**)&out.face_verts, sizeof(int64_t) * (size_t)(NL > 0 ? NL : 1), s)) != cudaSuccess ||
         (e = cudaMallocAsync((void**)&out.face_tet_offsets, sizeof(int64_t) * (size_t)(NF + 1), s)) != cudaSuccess ||
         (e = cudaMallocAsync((void**)&out.face_tets, sizeof(int64_t) * 2 * (size_t)(NF > 0 ? NF : 1), s)) !=
@@ -584,21 +655,25 @@ cudaError_t run_extract_mi(const ExtractArgs& a, const IASum4* act_sum, ExtractO
         (e = cudaMallocAsync((void**)&out.face_func, sizeof(int64_t) * 2 * (size_t)(NF > 0 ? NF : 1), s)) !=
             cudaSuccess)
         return e;
+    if (A > 0) {
+        k_mi_face_emit<<<nblk(A), kBs, 0, s>>>(C, h_emit, out.face_offsets, out.face_verts, out.face_tet_offsets,
+                                             out.face_tets, out.face_func);
+        note_launch();
+    }
+    k_mi_close<<<1, 1, 0, s>>>(out.face_offsets, out.face_tet_offsets, NF, NL);
+    note_launch();
+    if ((e = cudaEventSynchronize(aux->fork)) != cudaSuccess) return e;
+    const int64_t n_verts = (int64_t)pin[4];
+    out.n_verts = n_verts;
+    if ((e = cudaMallocAsync((void**)&out.xyz, sizeof(double) * 3 * (size_t)(n_verts > 0 ? n_verts : 1), s)) !=
+            cudaSuccess ||
+        (e = cudaMallocAsync((void**)&out.verts, sizeof(int64_t) * 11 * (size_t)(n_verts > 0 ? n_verts : 1), s)) !=
+            cudaSuccess)
+        return e;
     if (NV > 0) {
         k_mi_vert_emit<<<nblk(NV), kBs, 0, s>>>(C, NV, out.verts, out.xyz);
         note_launch();
     }
-    if (A > 0) {
-        k_mi_face_emit<<<nblk(A), kBs, 0, s>>>(C, h_emit != 0, out.face_offsets, out.face_verts, out.face_tet_offsets,
-                                             out.face_tets, out.face_func);
-        note_launch();
-    }
-    // closing offsets
-    int64_t last[2] = {NL, NF};
-    cudaMemcpyAsync(out.face_offsets + NF, &last[0], 8, cudaMemcpyHostToDevice, s);
-    cudaMemcpyAsync(out.face_tet_offsets + NF, &last[1], 8, cudaMemcpyHostToDevice, s);
-    e = cudaStreamSynchronize(s);
-    if (e != cudaSuccess) return e;
     return cudaGetLastError();
 }
 

@@ -260,11 +260,11 @@ struct ExtractOut {
     int64_t* face_tets = nullptr;
     int64_t* face_func = nullptr;
 };
-// Occurrence bases of the implicit-arrangement extraction (the exclusive scan of the per-tet counts
-// of the cut), prepared before run_extract so that their totals come back with the cut stage's
-// synchronization.  launch_extract_bases enqueues the scan into `buf` (extract_bases_bytes(A) device
-// bytes) and writes the four totals (vertex occurrences, face occurrences, loop vertices, boundary
-// faces) to the device counters `totals`; the caller copies them into ExtractBases::total.
+// Occurrence bases of the extraction (the exclusive scan of the per-tet counts of the cut; material
+// interface: of its phase-0 counts), prepared before run_extract so that their totals come back with
+// the cut stage's synchronization.  launch_extract_bases enqueues the scan into `buf`
+// (extract_bases_bytes(A) device bytes) and writes the four totals (the counts' four fields) to the
+// device counters `totals`; the caller copies them into ExtractBases::total.
 struct ExtractBases {
     const void* base = nullptr;
     uint64_t total[4] = {0, 0, 0, 0};
@@ -272,8 +272,8 @@ struct ExtractBases {
 size_t extract_bases_bytes(int64_t A);
 void launch_extract_bases(int64_t A, const IASum4* act_sum, void* buf, unsigned long long* totals, ExtractBases* out,
                           cudaStream_t s);
-// Runs the whole extraction; allocates the outputs with cudaMallocAsync on `s`.  `pre` (implicit
-// arrangement, may be null): bases prepared by launch_extract_bases on the same records.
+// Runs the whole extraction; allocates the outputs with cudaMallocAsync on `s`.  `pre` (may be null):
+// bases prepared by launch_extract_bases on the same records.
 cudaError_t run_extract(const ExtractArgs& a, const IASum4* act_sum, const ExtractBases* pre, ExtractOut& out,
                         cudaStream_t s);
 
