@@ -512,15 +512,24 @@ ria_status run_pipeline(const ria_config* cfg, const Inputs& in, cudaStream_t s,
     bool bases_ready = false;
     void* xb_buf = nullptr;
     if (prep_bases) {
-        xb_buf = tmp.get<uint8_t>((int64_t)extract_bases_bytes(A), &err);
+        xb_buf = tmp.get<uint8_t>((int64_t)extract_bases_bytes(A, ia_extract), &err);
         if (err != cudaSuccess) return bail(fail(RIA_ENOMEM, "device allocation failed"));
     }
     unsigned long long hc[kCounters] = {0};
+    // The counters go to pinned memory and the host waits on an event, so the table-record summaries
+    // (implicit arrangement), enqueued after the copy, run while the host wakes and issues the
+    // extraction.
     auto read_counters = [&](bool cut_end) -> bool {
+        uint64_t* pin = nullptr;
+        AuxStream* ax = nullptr;
+        if (pinned_words(&pin) != cudaSuccess || aux_stream(&ax) != cudaSuccess) return false;
         if (cut_end) cudaEventRecord(ev[3], s);  // the scan belongs to the extraction's time
         if (prep_bases) launch_extract_bases(A, act_sum, xb_buf, cnt + 20, &xb, s);
-        cudaMemcpyAsync(hc, cnt, sizeof(hc), cudaMemcpyDeviceToHost, s);
-        if (cudaStreamSynchronize(s) != cudaSuccess) return false;
+        cudaMemcpyAsync(pin, cnt, sizeof(hc), cudaMemcpyDeviceToHost, s);
+        cudaEventRecord(ax->fork, s);
+        if (prep_bases && ia_extract) launch_table_summaries(A, M->act_desc, M->table, M->table_off, xb_buf, &xb, s);
+        if (cudaEventSynchronize(ax->fork) != cudaSuccess) return false;
+        std::memcpy(hc, pin, sizeof(hc));
         for (int i = 0; i < 4; ++i) xb.total[i] = hc[20 + i];
         bases_ready = prep_bases;
         return true;

@@ -596,15 +596,24 @@ size_t bases_scan_bytes(int64_t A) {
 
 }  // namespace
 
-size_t extract_bases_bytes(int64_t A) {
-    if (A <= 0) return 256;
+namespace {
+constexpr uint32_t kTsumEntries = (uint32_t)(kTablePatterns + kCacheEntries);
+constexpr size_t kTsumStateBytes = (sizeof(uint32_t) * kTsumEntries + 255) & ~(size_t)255;
+constexpr size_t kTsumBytes = sizeof(uint64_t) * kTsumWords * (size_t)kTsumEntries;
+}  // namespace
+
+size_t extract_bases_bytes(int64_t A, bool summaries) {
+    const size_t extra = summaries ? kTsumStateBytes + kTsumBytes : 0;
+    if (A <= 0) return 256 + extra;
     const size_t arr = (sizeof(U4) * (size_t)A + 255) & ~(size_t)255;
-    return 2 * arr + bases_scan_bytes(A);
+    return 2 * arr + ((bases_scan_bytes(A) + 255) & ~(size_t)255) + extra;
 }
 
 void launch_extract_bases(int64_t A, const IASum4* act_sum, void* buf, unsigned long long* totals, ExtractBases* out,
                           cudaStream_t s) {
     out->base = nullptr;
+    out->tsum_state = nullptr;
+    out->tsum = nullptr;
     if (A <= 0) {
         cudaMemsetAsync(totals, 0, 4 * sizeof(unsigned long long), s);
         return;
@@ -620,6 +629,29 @@ void launch_extract_bases(int64_t A, const IASum4* act_sum, void* buf, unsigned 
     k_bases_total<<<1, 1, 0, s>>>(A, bin, base, totals);
     note_launch();
     out->base = base;
+}
+
+void launch_table_summaries(int64_t A, const uint64_t* act_desc, const uint8_t* table, const uint32_t* table_off,
+                            void* buf, ExtractBases* out, cudaStream_t s) {
+    out->tsum_state = nullptr;
+    out->tsum = nullptr;
+    if (A <= 0 || !act_desc || !table || !table_off) return;
+    const size_t arr = (sizeof(U4) * (size_t)A + 255) & ~(size_t)255;
+    char* t = (char*)buf + 2 * arr + ((bases_scan_bytes(A) + 255) & ~(size_t)255);
+    ExtractCtx C{};
+    C.a.A = A;
+    C.a.act_desc = act_desc;
+    C.rs = RecSrc{nullptr, nullptr, table, table_off};
+    C.tsum_n = kTsumEntries;
+    C.tsum_state = (uint32_t*)t;
+    C.tsum = (uint64_t*)(t + kTsumStateBytes);
+    cudaMemsetAsync(C.tsum_state, 0, sizeof(uint32_t) * kTsumEntries, s);
+    k_tsum_mark<<<nblk(A), kBs, 0, s>>>(C);
+    note_launch();
+    k_tsum_build<<<nblk(kTsumEntries), kBs, 0, s>>>(C);
+    note_launch();
+    out->tsum_state = C.tsum_state;
+    out->tsum = C.tsum;
 }
 
 cudaError_t run_extract(const ExtractArgs& a, const IASum4* act_sum, const ExtractBases* pre, ExtractOut& out,
@@ -660,6 +692,7 @@ cudaError_t run_extract(const ExtractArgs& a, const IASum4* act_sum, const Extra
     const uint64_t probes = tight ? 4096 : 0;
     C.edge64 = a.V < (1ll << 28) && a.F <= 256;
     C.tsum_n = (uint32_t)(kTablePatterns + kCacheEntries);
+    const bool tsum_ready = pre && pre->tsum_state;  // summarised before the cut stage's synchronization
     uint32_t* gid_src = nullptr;  // the occurrence of each new vertex, by id
     int64_t* d_tots = nullptr;
     void* scan_tmp = nullptr;
@@ -698,8 +731,13 @@ cudaError_t run_extract(const ExtractArgs& a, const IASum4* act_sum, const Extra
         C.frec = P.get<uint32_t>(NF);
         C.fgids = P.get<uint32_t>((int64_t)tot.c);
         C.iso0 = P.get<uint64_t>(A);
-        C.tsum_state = P.get<uint32_t>(C.tsum_n);
-        C.tsum = P.get<uint64_t>((int64_t)kTsumWords * C.tsum_n);
+        if (tsum_ready) {
+            C.tsum_state = pre->tsum_state;
+            C.tsum = pre->tsum;
+        } else {
+            C.tsum_state = P.get<uint32_t>(C.tsum_n);
+            C.tsum = P.get<uint64_t>((int64_t)kTsumWords * C.tsum_n);
+        }
         gid_src = P.get<uint32_t>(NV);
         d_tots = P.get<int64_t>(8);
         scan_tmp = P.get<uint8_t>((int64_t)std::max(vscan_bytes, fscan_bytes));
@@ -744,13 +782,16 @@ cudaError_t run_extract(const ExtractArgs& a, const IASum4* act_sum, const Extra
     if ((e = launch_fill(fill, aux->s)) != cudaSuccess) return e;
     cudaEventRecord(aux->join, aux->s);
     join_aux.armed = true;
-    // vertices: the table entries in use summarised, then the occurrence list
-    cudaMemsetAsync(C.tsum_state, 0, sizeof(uint32_t) * C.tsum_n, s);
+    // vertices: the table entries in use summarised (unless that was done with the bases), then the
+    // occurrence list
+    if (!tsum_ready) cudaMemsetAsync(C.tsum_state, 0, sizeof(uint32_t) * C.tsum_n, s);
     if (A > 0) {
-        k_tsum_mark<<<nblk(A), kBs, 0, s>>>(C);
-        note_launch();
-        k_tsum_build<<<nblk(C.tsum_n), kBs, 0, s>>>(C);
-        note_launch();
+        if (!tsum_ready) {
+            k_tsum_mark<<<nblk(A), kBs, 0, s>>>(C);
+            note_launch();
+            k_tsum_build<<<nblk(C.tsum_n), kBs, 0, s>>>(C);
+            note_launch();
+        }
         k_ia_vert_list<<<nblk(A), kBs, 0, s>>>(C);
         note_launch();
     }

@@ -265,13 +265,20 @@ struct ExtractOut {
 // the cut stage's synchronization.  launch_extract_bases enqueues the scan into `buf`
 // (extract_bases_bytes(A) device bytes) and writes the four totals (the counts' four fields) to the
 // device counters `totals`; the caller copies them into ExtractBases::total.
+// launch_table_summaries (implicit arrangement) summarises the table records the tets use (see the
+// extraction's vertex pass), so that this work too is enqueued before the extraction is issued.
 struct ExtractBases {
     const void* base = nullptr;
     uint64_t total[4] = {0, 0, 0, 0};
+    uint32_t* tsum_state = nullptr;  // the table-record summaries, when prepared
+    uint64_t* tsum = nullptr;
 };
-size_t extract_bases_bytes(int64_t A);
+size_t extract_bases_bytes(int64_t A, bool summaries);
 void launch_extract_bases(int64_t A, const IASum4* act_sum, void* buf, unsigned long long* totals, ExtractBases* out,
                           cudaStream_t s);
+// the summaries, into the same buffer (sized with summaries = true), after launch_extract_bases
+void launch_table_summaries(int64_t A, const uint64_t* act_desc, const uint8_t* table, const uint32_t* table_off,
+                            void* buf, ExtractBases* out, cudaStream_t s);
 // Runs the whole extraction; allocates the outputs with cudaMallocAsync on `s`.  `pre` (may be null):
 // bases prepared by launch_extract_bases on the same records.
 cudaError_t run_extract(const ExtractArgs& a, const IASum4* act_sum, const ExtractBases* pre, ExtractOut& out,
