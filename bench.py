@@ -384,9 +384,10 @@ def run_serve(args, world, local):
 
 def algorithmic_bytes(wl, st, n_fit, n_rec, n_face_verts, n_face_tets):
     """Bytes each stage must move at least: n_fit = sum of active functions over the active tets,
-    n_rec = record bytes; the extraction reads the active lists and every record once and writes the
-    points, the vertex records (11 int64) and the face lists (vertex ids, offsets, (tet, face) pairs,
-    function pairs)."""
+    n_rec = record bytes; the extraction reads the active lists and every record once, writes one
+    dedup-table slot per distinct vertex key (16 bytes: key and owner), and writes the points, the
+    vertex records (11 int64) and the face lists (vertex ids, offsets, (tet, face) pairs, function
+    pairs)."""
     V, T, F = wl.n_verts, wl.n_tets, len(wl.funcs)
     A = st["num_intersecting_tet"]
     nv, nf = st["num_verts"], st["num_faces"]
@@ -394,7 +395,8 @@ def algorithmic_bytes(wl, st, n_fit, n_rec, n_face_verts, n_face_tets):
         "sample": 8 * V * F + 16 * V,           # values written + per-vertex masks written
         "filter": 16 * V + 28 * A,              # masks read once + active-tet lists written
         "cut": 32 * n_fit + n_rec,              # corner values read + records written
-        "extract": 20 * A + n_rec + 24 * nv + 88 * nv + 8 * n_face_verts + 16 * nf + 16 * n_face_tets + 16 * nf,
+        "extract": 20 * A + n_rec + 16 * nv + 24 * nv + 88 * nv + 8 * n_face_verts + 16 * nf + 16 * n_face_tets
+                   + 16 * nf,
     }
 
 
