@@ -10,6 +10,7 @@
 // (a direct-mapped array for tet vertices, a 128-bit open-addressing hash otherwise); an occurrence
 // is new iff it owns its key, and the new occurrences are numbered by one more scan.  The result is
 // the reference's numbering exactly.
+#include "div_rn.cuh"
 #include "extract_common.cuh"
 #include "launch.hpp"
 
@@ -367,7 +368,8 @@ __device__ __forceinline__ void vert_emit_one(const ExtractCtx& C, uint32_t p, i
     for (int c = 0; c < 4; ++c) rec[3 + c] = k.sv[c];
     for (int c = 0; c < 3; ++c) rec[7 + c] = k.fn[c];
     rec[10] = -1;
-    // coordinates, with the reference's formulas and operation order
+    // coordinates, with the reference's formulas and operation order (divisions correctly rounded on the
+    // integer pipe, div_rn.cuh: the same bits as the FP64 division)
     PtSrc ps{C.a.d_pts, C.a.coords, (int)C.a.g.res + 1};
     const double* fv = C.a.fv;
     const int F = C.a.F;
@@ -378,7 +380,7 @@ __device__ __forceinline__ void vert_emit_one(const ExtractCtx& C, uint32_t p, i
             ps.get(k.sv[0], p1);
             ps.get(k.sv[1], p2);
             double f1 = fv[k.sv[0] * F + k.fn[0]], f2 = fv[k.sv[1] * F + k.fn[0]];
-            double b0 = f2 / (f2 - f1);
+            double b0 = div_rn(f2, f2 - f1);
             double b1 = 1 - b0;
             for (int c = 0; c < 3; ++c) out[c] = b0 * p1[c] + b1 * p2[c];
             break;
@@ -395,7 +397,7 @@ __device__ __forceinline__ void vert_emit_one(const ExtractCtx& C, uint32_t p, i
             double n2 = a1[0] * a2[2] - a1[2] * a2[0];
             double n3 = a1[1] * a2[0] - a1[0] * a2[1];
             double d = n1 + n2 + n3;
-            double w0 = n1 / d, w1 = n2 / d, w2 = n3 / d;
+            double w0 = div_rn(n1, d), w1 = div_rn(n2, d), w2 = div_rn(n3, d);
             for (int c = 0; c < 3; ++c) out[c] = w0 * P[0][c] + w1 * P[1][c] + w2 * P[2][c];
             break;
         }
@@ -417,7 +419,7 @@ __device__ __forceinline__ void vert_emit_one(const ExtractCtx& C, uint32_t p, i
             double n4 = p1[2] * (p2[0] * p3[1] - p2[1] * p3[0]) + p1[1] * (p2[2] * p3[0] - p2[0] * p3[2]) +
                         p1[0] * (p2[1] * p3[2] - p2[2] * p3[1]);
             double d = n1 + n2 + n3 + n4;
-            double w0 = n1 / d, w1 = n2 / d, w2 = n3 / d, w3 = n4 / d;
+            double w0 = div_rn(n1, d), w1 = div_rn(n2, d), w2 = div_rn(n3, d), w3 = div_rn(n4, d);
             for (int c = 0; c < 3; ++c) out[c] = w0 * P[0][c] + w1 * P[1][c] + w2 * P[2][c] + w3 * P[3][c];
             break;
         }

@@ -13,6 +13,7 @@
 // a consistent identity); only when some boundary face becomes an interface (degenerate inputs) are
 // the positions recomputed with the phase-1 corners in place.  Scans number the new vertices and the
 // faces in the reference's order.
+#include "div_rn.cuh"
 #include "extract_common.cuh"
 #include "launch.hpp"
 
@@ -374,7 +375,7 @@ __global__ void k_mi_vert_emit(MICtx C, int64_t n, int64_t* __restrict__ verts, 
             ps.get(k.sv[0], p1);
             ps.get(k.sv[1], p2);
             double f1 = diff(k.sv[0], 0, 1), f2 = diff(k.sv[1], 0, 1);
-            double b0 = f2 / (f2 - f1);
+            double b0 = div_rn(f2, f2 - f1);
             double b1 = 1 - b0;
             for (int c = 0; c < 3; ++c) out[c] = b0 * p1[c] + b1 * p2[c];
             break;
@@ -391,7 +392,7 @@ __global__ void k_mi_vert_emit(MICtx C, int64_t n, int64_t* __restrict__ verts, 
             double n2 = a1[0] * a2[2] - a1[2] * a2[0];
             double n3 = a1[1] * a2[0] - a1[0] * a2[1];
             double d = n1 + n2 + n3;
-            double w0 = n1 / d, w1 = n2 / d, w2 = n3 / d;
+            double w0 = div_rn(n1, d), w1 = div_rn(n2, d), w2 = div_rn(n3, d);
             for (int c = 0; c < 3; ++c) out[c] = w0 * P[0][c] + w1 * P[1][c] + w2 * P[2][c];
             break;
         }
@@ -413,7 +414,7 @@ __global__ void k_mi_vert_emit(MICtx C, int64_t n, int64_t* __restrict__ verts, 
             double n4 = p1[2] * (p2[0] * p3[1] - p2[1] * p3[0]) + p1[1] * (p2[2] * p3[0] - p2[0] * p3[2]) +
                         p1[0] * (p2[1] * p3[2] - p2[2] * p3[1]);
             double d = n1 + n2 + n3 + n4;
-            double w0 = n1 / d, w1 = n2 / d, w2 = n3 / d, w3 = n4 / d;
+            double w0 = div_rn(n1, d), w1 = div_rn(n2, d), w2 = div_rn(n3, d), w3 = div_rn(n4, d);
             for (int c = 0; c < 3; ++c) out[c] = w0 * P[0][c] + w1 * P[1][c] + w2 * P[2][c] + w3 * P[3][c];
             break;
         }

@@ -88,6 +88,17 @@ def sqrt_rn(values, perturb=0):
     return out
 
 
+def div_rn(a, b):
+    """The vertex emission's integer-pipe division over two arrays."""
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    out = np.empty_like(a)
+    L = lib()
+    L.hc_div_rn.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64]
+    L.hc_div_rn(a.ctypes.data, b.ctypes.data, out.ctypes.data, a.size)
+    return out
+
+
 def robust(mode, rows, forge=0):
     """The device's robust-test outcome of one tet (0 ok, 1 counts differ, 2 the given order fails, 3 the
     reversed order fails); forge 1..3 plants that outcome in the cut wrapper of the harness."""

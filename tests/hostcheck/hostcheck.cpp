@@ -9,6 +9,7 @@
 #include "../../robust-implicit-surface-networks_gb300/csrc/lookup2.cuh"
 #include "../../robust-implicit-surface-networks_gb300/csrc/cut_ia_warp.cuh"
 #include "../../robust-implicit-surface-networks_gb300/csrc/sqrt_rn.cuh"
+#include "../../robust-implicit-surface-networks_gb300/csrc/div_rn.cuh"
 #include "../../robust-implicit-surface-networks_gb300/csrc/robust.cuh"
 
 using namespace ria;
@@ -254,6 +255,11 @@ extern "C" void hc_sqrt_rn(const double* in, double* out, int64_t n, int perturb
         const uint64_t r0 = sqrt_seed(x);
         out[i] = sqrt_rn_finish(x, e, (uint64_t)((int64_t)r0 + perturb * (int64_t)(r0 >> 20)));
     }
+}
+
+// the vertex emission's division (div_rn.cuh)
+extern "C" void hc_div_rn(const double* a, const double* b, double* out, int64_t n) {
+    for (int64_t i = 0; i < n; ++i) out[i] = div_rn(a[i], b[i]);
 }
 
 // ---- robust test (robust.cuh): the device's per-tet classification with a cut wrapper that can forge

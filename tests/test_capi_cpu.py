@@ -380,6 +380,55 @@ def test_sampler_square_root_is_correctly_rounded(hc):
         assert same.all(), (perturb, v[~same][:4])
 
 
+def test_vertex_division_is_correctly_rounded(hc):
+    """The vertex emission's division (div_rn.cuh: reciprocal by Newton steps in integer arithmetic,
+    finished from the exact remainder) against IEEE 754 division (numpy), bit for bit: random bit
+    patterns over the whole range (zero, subnormal, infinite and NaN operands and out-of-range
+    quotients go to the FP64 instruction), normal operands of every significand and nearby exponents,
+    divisors at both ends of a binade (the reciprocal seed's extremes), exact quotients and quotients
+    one unit off them (a quotient of two doubles is never halfway between two doubles, so these are
+    the cases that test the remainder's fix-up), and the emission's own operands f2 / (f2 - f1)."""
+    rng = np.random.default_rng(29)
+    n = 400_000
+
+    def bits(lo, hi, size):
+        return rng.integers(lo, hi, size=size, dtype=np.uint64).view(np.float64)
+
+    pairs = [(bits(0, 2**64 - 1, n), bits(0, 2**64 - 1, n))]
+    e = rng.integers(1000, 1050, size=n).astype(np.uint64)
+    fa = rng.integers(0, 2**52, size=n, dtype=np.uint64)
+    fb = rng.integers(0, 2**52, size=n, dtype=np.uint64)
+    sa = rng.integers(0, 2, size=n).astype(np.uint64) << np.uint64(63)
+    a = (sa | (e << np.uint64(52)) | fa).view(np.float64)
+    b = ((rng.integers(1000, 1050, size=n).astype(np.uint64) << np.uint64(52)) | fb).view(np.float64)
+    pairs.append((a, b))
+    # divisors at the ends of a binade, and just inside them
+    for fr in (0, 1, 2**29 - 1, 2**29, 2**52 - 1, 2**52 - 2**29, 2**52 - 2):
+        bb = ((rng.integers(1000, 1050, size=n // 8).astype(np.uint64) << np.uint64(52)) | np.uint64(fr)).view(np.float64)
+        pairs.append((a[: n // 8], bb))
+    # exact quotients, and one unit off: q * b with integer-like q
+    q = rng.integers(1, 2**26, size=n).astype(np.float64)
+    bq = rng.uniform(0.5, 2.0, size=n)
+    prod = q * bq
+    pairs += [(prod, bq), (np.nextafter(prod, np.inf), bq), (np.nextafter(prod, 0), bq)]
+    # exact quotients of odd significands
+    odd = (rng.integers(2**52, 2**53, size=n, dtype=np.uint64) | np.uint64(1)).astype(np.float64)
+    pairs += [(odd, np.full(n, 2.0)), (odd * 3.0, np.full(n, 6.0)), (odd, np.full(n, 0.25))]
+    # the emission's operands: values of a function at two corners across a crossing
+    f1 = rng.uniform(-1, 1, n) * 10.0 ** rng.uniform(-12, 2, n)
+    f2 = -np.sign(f1) * rng.uniform(0, 1, n) * 10.0 ** rng.uniform(-12, 2, n)
+    with np.errstate(all="ignore"):
+        pairs.append((f2, f2 - f1))
+    pairs.append((np.array([0.0, -0.0, 1.0, 1.0, np.inf, 1.0, np.nan, 5e-324, 1.0, 1e308, 1e-308, 3.0]),
+                  np.array([1.0, 1.0, 0.0, -0.0, 2.0, np.inf, 1.0, 1.0, 5e-324, 1e-10, 1e10, 3.0])))
+    with np.errstate(all="ignore"):
+        for x, y in pairs:
+            ref = x / y
+            out = hc.div_rn(x, y)
+            same = (out.view(np.uint64) == ref.view(np.uint64)) | (np.isnan(out) & np.isnan(ref))
+            assert same.all(), (x[~same][:3], y[~same][:3], out[~same][:3], ref[~same][:3])
+
+
 def _stress_fixtures(per_noise=1):
     """The near-degenerate robustness sets (tests/golden/stress): the first instances of every noise
     level of both modes."""

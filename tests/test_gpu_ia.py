@@ -124,6 +124,25 @@ def test_degenerate_workload(pkg, fns, oracle, lib, res):
     assert_mesh_equal(mesh, oracle.run("ia", pts, tets, fv, threads=os.cpu_count() or 1))
 
 
+def test_vertex_coordinates_bit_identical(pkg, fns, oracle, lib):
+    """The vertex coordinates divide on the integer pipe (div_rn.cuh) with the reference's formula
+    order: the same bits as the oracle's C arithmetic, for edge, face and interior vertices (implicit
+    arrangement) and for the material interface."""
+    seen = set()
+    for mode, wl in (("ia", fns.workload_ia_degenerate(res=24)), ("mi", fns.workload_mi(res=24)),
+                     ("ia", fns.workload_ia_small(res=16))):
+        run = pkg.grid_implicit_arrangement if mode == "ia" else pkg.grid_material_interface
+        mesh = run(wl.res, wl.funcs)
+        pts, tets = fns.generate_tet_mesh(wl.res)
+        fv = oracle.sample(wl.funcs, pts)
+        ref = oracle.run(mode, pts, tets, fv)
+        assert np.array_equal(mesh["verts"], ref["verts"])
+        assert np.array_equal(mesh["xyz"].view(np.uint64), ref["xyz"].view(np.uint64)), mode
+        seen.update(np.unique(ref["verts"].reshape(-1, 11)[:, 2]).tolist())
+        mesh.close()
+    assert {2, 3} <= seen
+
+
 @pytest.mark.parametrize("seed,nplanes,res", [(7, 20, 6), (11, 18, 6)])
 def test_dense_planes_overflow_tight_tables(pkg, fns, oracle, lib, seed, nplanes, res):
     """Many planes on a small grid: vertices where two planes cross a tet face (keyed by the face
