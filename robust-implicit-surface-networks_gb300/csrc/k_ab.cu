@@ -133,9 +133,13 @@ __device__ __forceinline__ double combine_from_sum(const ria_function& f, double
             v = 0.0;
     }
     // negation flips the sign bit (IEEE 754 negate, exact for every value, NaN included); done on the
-    // integer pipe, since the FP64 pipe bounds this kernel
-    const long long flip = f.flipped ? (long long)0x8000000000000000ull : 0ll;
-    return __longlong_as_double(__double_as_longlong(v) ^ flip);
+    // integer pipe, since the FP64 pipe bounds this kernel.  The XOR is written in PTX: written in C++,
+    // the compiler recognises a conditional floating-point negation and issues it as an FP64
+    // addition (one per function and vertex, whether or not the function is flipped)
+    unsigned long long b = (unsigned long long)__double_as_longlong(v);
+    const unsigned long long flip = f.flipped ? 0x8000000000000000ull : 0ull;
+    asm("xor.b64 %0, %0, %1;" : "+l"(b) : "l"(flip));
+    return __longlong_as_double((long long)b);
 }
 
 __device__ __forceinline__ double combine_parts(const ria_function& f, const double w0[3], const double w1[3]) {
