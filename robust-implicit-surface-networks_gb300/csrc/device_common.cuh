@@ -18,14 +18,31 @@ enum : uint32_t {
 
 __device__ __forceinline__ void raise_status(uint32_t* st, uint32_t bits) { atomicOr(st, bits); }
 
-// tet t of the tet5 grid with `res` cubes per axis (src/io.cpp:125-147)
+// tet t of the tet5 grid with `res` cubes per axis (src/io.cpp:125-147).  Calls keep t below 2^31
+// (the pipeline's limit on tets), so the cube and its coordinates come from 32-bit divisions (a
+// 64-bit division is a long software sequence on the GPU); larger indices take the 64-bit path.
 __device__ __forceinline__ void grid_tet(int64_t t, int64_t res, int64_t v[4]) {
     const int64_t N = res + 1;
-    int64_t c = t / 5;
-    int sub = (int)(t - 5 * c);
-    int64_t i = c / (res * res);
-    int64_t j = (c / res) % res;
-    int64_t k = c % res;
+    int64_t i, j, k;
+    int sub;
+    if (((uint64_t)t >> 31) == 0 && ((uint64_t)res >> 15) == 0) {
+        const uint32_t tt = (uint32_t)t, R = (uint32_t)res;
+        const uint32_t c = tt / 5u;
+        sub = (int)(tt - 5u * c);
+        const uint32_t rr = R * R;
+        const uint32_t ii = c / rr;
+        const uint32_t rem = c - ii * rr;
+        const uint32_t jj = rem / R;
+        i = ii;
+        j = jj;
+        k = rem - jj * R;
+    } else {
+        const int64_t c = t / 5;
+        sub = (int)(t - 5 * c);
+        i = c / (res * res);
+        j = (c / res) % res;
+        k = c % res;
+    }
     int64_t v0 = i * N * N + j * N + k, v1 = (i + 1) * N * N + j * N + k;
     int64_t v2 = (i + 1) * N * N + (j + 1) * N + k, v3 = i * N * N + (j + 1) * N + k;
     int64_t v4 = v0 + 1, v5 = v1 + 1, v6 = v2 + 1, v7 = v3 + 1;
