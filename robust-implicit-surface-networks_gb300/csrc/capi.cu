@@ -67,6 +67,16 @@ int first_light_bin(bool mi, int heavy_min_k) {
     return b < 1 ? 1 : (b > kGenBins ? kGenBins : b);
 }
 
+// four 32-bit counts gathered into one place (one copy to the host instead of four)
+__global__ void k_gather4(const uint32_t* a, const uint32_t* b, const uint32_t* c, const uint32_t* d, uint32_t* out) {
+    if (threadIdx.x == 0) {
+        out[0] = *a;
+        out[1] = *b;
+        out[2] = *c;
+        out[3] = *d;
+    }
+}
+
 struct DeviceCtx {
     bool ready[2] = {false, false};
     uint8_t* table[2] = {nullptr, nullptr};      // 81 patterns, then the secondary-lookup templates
@@ -424,8 +434,9 @@ ria_status run_pipeline(const ria_config* cfg, const Inputs& in, cudaStream_t s,
 
     // counters: 0 status, 1 n_zero, 2..4 k histogram, 5 heap used, 6 big heap used, 7 deferred by the small
     // variant, 8 unused, 9 deferred by the mid variant, 10..14 the cut routing's counters, 16..18
-    // robust-test tets of types 1, 2 and 3, 20..23 the extraction's occurrence totals
-    constexpr int kCounters = 24;
+    // robust-test tets of types 1, 2 and 3, 20..23 the extraction's occurrence totals, 24..25 the
+    // filter's counts gathered for the host
+    constexpr int kCounters = 26;
     unsigned long long* cnt = tmp.get<unsigned long long>(kCounters, &err);
     uint32_t* status = (uint32_t*)cnt;
     if (err != cudaSuccess) return bail(fail(RIA_ENOMEM, "device allocation failed"));
@@ -477,12 +488,15 @@ ria_status run_pipeline(const ria_config* cfg, const Inputs& in, cudaStream_t s,
         uint8_t* scan_tmp = tmp.get<uint8_t>((int64_t)bytes, &err);
         if (err != cudaSuccess) return bail(fail(RIA_ENOMEM, "device allocation failed"));
         cub::DeviceScan::ExclusiveSum(scan_tmp, bytes, blk, blk_off, nscan, s);
-        uint32_t h[4];
-        cudaMemcpyAsync(&h[0], blk_off + nb, 4, cudaMemcpyDeviceToHost, s);
-        cudaMemcpyAsync(&h[1], blk_off + nscan - 1, 4, cudaMemcpyDeviceToHost, s);
-        cudaMemcpyAsync(&h[2], blk + nscan - 1, 4, cudaMemcpyDeviceToHost, s);
+        // the four counts gathered on the device and read with one copy (each copy into pageable memory
+        // waits for the stream on its own)
         const int light0 = first_light_bin(mi, mi ? ctx->tune.mi_heavy_min_k : ctx->tune.heavy_min_k);
-        cudaMemcpyAsync(&h[3], blk_off + (1 + light0) * nb, 4, cudaMemcpyDeviceToHost, s);
+        uint32_t* d_h = (uint32_t*)(cnt + 24);  // counters 24..25
+        k_gather4<<<1, 32, 0, s>>>(blk_off + nb, blk_off + nscan - 1, blk + nscan - 1, blk_off + (1 + light0) * nb,
+                                   d_h);
+        note_launch();
+        uint32_t h[4];
+        cudaMemcpyAsync(h, d_h, sizeof(h), cudaMemcpyDeviceToHost, s);
         if (cudaStreamSynchronize(s) != cudaSuccess) return bail(fail(RIA_ECUDA, cudaGetErrorString(cudaGetLastError())));
         A = h[0];
         G = (int64_t)h[1] + h[2] - A;
