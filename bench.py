@@ -46,7 +46,7 @@ METRIC = "tets/s (arrangement+extract) on 1 GB300"
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one k_sample launch on the large
 # degenerate workload, from one ncu capture of that launch
 SAMPLE_TRAFFIC_WORKLOAD = "ia-degenerate-32func-res128"
-SAMPLE_TRAFFIC = 4809728 + 521974528
+SAMPLE_TRAFFIC = 4495360 + 521597184
 
 
 def _peaks():
