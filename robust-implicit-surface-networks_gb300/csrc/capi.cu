@@ -433,7 +433,7 @@ ria_status run_pipeline(const ria_config* cfg, const Inputs& in, cudaStream_t s,
     cudaEventRecord(ev[0], s);
 
     // counters: 0 status, 1 n_zero, 2..4 k histogram, 5 heap used, 6 big heap used, 7 deferred by the small
-    // variant, 8 unused, 9 deferred by the mid variant, 10..14 the cut routing's counters, 16..18
+    // variant, 8 unused, 9 deferred by the mid variant, 10..15 and 19 the cut routing's counters, 16..18
     // robust-test tets of types 1, 2 and 3, 20..23 the extraction's occurrence totals, 24..25 the
     // filter's counts gathered for the host
     constexpr int kCounters = 26;
@@ -610,6 +610,8 @@ ria_status run_pipeline(const ria_config* cfg, const Inputs& in, cudaStream_t s,
         uint32_t* rest = prep ? tmp.get<uint32_t>(G_light, &err) : nullptr;
         WaitRec* waitl = prep ? tmp.get<WaitRec>(G_light, &err) : nullptr;
         uint32_t* owners = prep && !mi ? tmp.get<uint32_t>(G_light, &err) : nullptr;
+        // the light warp cut's overflow (tets beyond its smaller state), for the full warp variant
+        uint32_t* over = G_light > 0 && !mi ? tmp.get<uint32_t>(G_light, &err) : nullptr;
         if (err != cudaSuccess) return bail(fail(RIA_ENOMEM, "device allocation failed"));
         AuxStream* aux = nullptr;
         if (G_mid > 0 && G_light > 0 && aux_stream(&aux) != cudaSuccess)
@@ -692,9 +694,19 @@ ria_status run_pipeline(const ria_config* cfg, const Inputs& in, cudaStream_t s,
             // (a record with warp_route 0 sends every tet to the thread kernel)
             if (tune.warp_route > 0) {
                 cl.route_at = tune.warp_route;
+                // the smaller warp state first (about twice the resident warps); the tets it cannot
+                // hold then go to the full warp variant
                 CutArgs cw = cl;
                 cw.next = (unsigned int*)(cnt + 14);
-                launch_cut_warp(cw, s);
+                cw.deferred = over;
+                cw.n_deferred = (unsigned int*)(cnt + 15);
+                launch_cut_warp(cw, s, true);
+                CutArgs cv = ca;
+                cv.list = over;
+                cv.n = G_light;
+                cv.n_dev = (unsigned int*)(cnt + 15);
+                cv.next = (unsigned int*)(cnt + 19);
+                launch_cut_warp(cv, s);
             }
             launch_cut_fast(cl, s, false);
         }

@@ -645,16 +645,17 @@ __global__ void __launch_bounds__(32 * kSplitWarps) k_cut_mi_split(CutArgs a) {
     }
 }
 
-// One warp per tet, its state in shared memory (IAWarpCutDev, cut_ia_warp.cuh): the heavy bins of
-// the implicit arrangement.  A tet beyond the warp variant's capacity goes to the deferred list.
+// One warp per tet, its state in shared memory (IAWarpCutDev or IAWarpCutLight, cut_ia_warp.cuh): the
+// heavy bins of the implicit arrangement, and the light bins' leftovers.  A tet beyond the state's
+// capacity goes to the deferred list.
 constexpr int kCutWarps = 4;  // warps per block
 
-template <int G>
+template <int G, class State>
 __global__ void __launch_bounds__(32 * kCutWarps) k_cut_warp(CutArgs a) {
     constexpr int kGroups = 32 * kCutWarps / G;  // groups (one tet each) per block
     extern __shared__ __align__(16) unsigned char warp_smem[];
     const int gib = threadIdx.x / G;
-    IAWarpCutDev& S = reinterpret_cast<IAWarpCutDev*>(warp_smem)[gib];
+    State& S = reinterpret_cast<State*>(warp_smem)[gib];
     const LanesG<G> L = LanesG<G>::of_thread((int)(threadIdx.x & 31));
     const int lane = L.lane;
     const int64_t n = a.n_dev ? (a.n < (int64_t)*a.n_dev ? a.n : (int64_t)*a.n_dev) : a.n;
@@ -863,33 +864,36 @@ void launch_cut_prep(const CutArgs& a, cudaStream_t s) {
     note_launch();
 }
 
-template <int G>
+template <int G, class State>
 void launch_warp_groups(const CutArgs& a, cudaStream_t s) {
     constexpr int kGroups = 32 * kCutWarps / G;
-    constexpr size_t smem = sizeof(IAWarpCutDev) * kGroups;
+    constexpr size_t smem = sizeof(State) * kGroups;
     // the shared-memory size, then the resident blocks on the device: once per process
     // (thread-safe static initialisation); the groups take tets from the list
     static const int2 occ = [] {  // (SMs, resident blocks per SM)
-        cudaFuncSetAttribute(k_cut_warp<G>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaFuncSetAttribute(k_cut_warp<G, State>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         int dev = 0, sms = 0, per_sm = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cut_warp<G>, 32 * kCutWarps, smem);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cut_warp<G, State>, 32 * kCutWarps, smem);
         return make_int2(sms > 0 ? sms : 152, per_sm > 0 ? per_sm : 1);
     }();
     const int per_sm = a.warp_blocks_per_sm > 0 && a.warp_blocks_per_sm < occ.y ? a.warp_blocks_per_sm : occ.y;
     const int64_t resident = (int64_t)occ.x * per_sm;
     const int64_t want = (a.n + kGroups - 1) / kGroups;
     const int64_t blocks = want < resident ? want : resident;
-    k_cut_warp<G><<<(unsigned)blocks, 32 * kCutWarps, smem, s>>>(a);
+    k_cut_warp<G, State><<<(unsigned)blocks, 32 * kCutWarps, smem, s>>>(a);
     note_launch();
 }
 
 // Whole warps: half-warp groups (two tets per warp) measured slower on the large config, as the
 // two halves' data-dependent phases diverge.
-void launch_cut_warp(const CutArgs& a, cudaStream_t s) {
+void launch_cut_warp(const CutArgs& a, cudaStream_t s, bool light) {
     if (a.n == 0) return;
-    launch_warp_groups<32>(a, s);
+    if (light)
+        launch_warp_groups<32, IAWarpCutLight>(a, s);
+    else
+        launch_warp_groups<32, IAWarpCutDev>(a, s);
 }
 
 void launch_cut_fast(const CutArgs& a, cudaStream_t s, bool mid) {

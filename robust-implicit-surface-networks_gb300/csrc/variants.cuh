@@ -21,4 +21,7 @@ using MICutMid = MICut<96, 96, 640, 128, 128, 1024, false>;
 using MICutBig = MICut<255, 255, 2048, 255, 512, 4096, true>;
 // warp variant: one warp per tet, state in shared memory, exact predicates (32 cells)
 using IAWarpCutDev = IAWarpCut<64, 128, 640>;
+// the same for the light bins' leftovers (three to five distinct planes): half the vertex and face
+// room, so about twice the resident warps per SM; a tet that does not fit goes to IAWarpCutDev
+using IAWarpCutLight = IAWarpCut<32, 64, 320>;
 }  // namespace ria

@@ -31,7 +31,7 @@ def cut(mode, rows, big):
     buf = np.zeros(1 << 16, dtype=np.uint8)
     summ = np.zeros(8, dtype=np.uint16)
     f = lib().hc_ia_cut if mode == "ia" else lib().hc_mi_cut
-    variant = {"mid": 2, "warp": 3}.get(big, 1 if big is True else 0)
+    variant = {"mid": 2, "warp": 3, "warp_light": 4}.get(big, 1 if big is True else 0)
     n = f(rows.shape[0], rows.ctypes.data, variant, buf.ctypes.data, buf.size,
           summ.ctypes.data)
     if n < 0:

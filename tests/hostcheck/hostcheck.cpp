@@ -26,9 +26,36 @@ static int finish(C* c, int st, uint8_t* buf, int cap, uint16_t* summary) {
     return n;
 }
 
+// one tet through a warp variant's state (one lane: its lane-parallel loops run serially)
+template <class W>
+int warp_cut(int k, const double* planes, uint8_t* buf, int cap, uint16_t* summary) {
+    if (k > kWarpMaxK) return -11;
+    auto* c = new W();
+    for (int i = 0; i < 4 * k; ++i) c->pl[i] = planes[i];
+    Lanes L;
+    int st = c->run(L, k);
+    int r = 0;
+    if (st != CUT_OK) {
+        r = -10 - st;
+    } else {
+        c->canonicalize(L);
+        r = c->record_size();
+        if (r > cap) {
+            r = -3;
+        } else {
+            IASummary s;
+            c->emit(L, buf, s);
+            std::memcpy(summary, &s, sizeof(s));
+        }
+    }
+    delete c;
+    return r;
+}
+
 // big: 0 the small filtered variant, 1 the exact variant, 2 the mid-size filtered variant, 3 the
-// warp variant (one lane: its lane-parallel loops run serially)
+// warp variant, 4 the warp variant's light state (one lane: its lane-parallel loops run serially)
 extern "C" int hc_ia_cut(int k, const double* planes, int big, uint8_t* buf, int cap, uint16_t* summary) {
+    if (big == 4) return warp_cut<IAWarpCutLight>(k, planes, buf, cap, summary);
     if (big == 3) {
         if (k > kWarpMaxK) return -11;
         auto* c = new IAWarpCutDev();
