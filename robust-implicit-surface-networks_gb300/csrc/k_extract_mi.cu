@@ -178,21 +178,23 @@ __global__ void __launch_bounds__(kBs) k_mi_bnd_keys(MICtx C) {
     for (int f = 0; f < r.nf; ++f) {
         const int L = r.len(f);
         if (r.pos(f) <= 3) {
-            int64_t mn = 0, mx = 0;
-            int mpos = 0;
+            // smallest, second smallest (of the other vertices) and largest code in one walk
+            int64_t mn = 0, mx = 0, second = INT64_MAX;
             for (int t = 0; t < L; ++t) {
-                int64_t c = bnd_code(C, r, r.loopv(off + t), tv, fl, b0);
-                if (t == 0 || c < mn) {
-                    mn = c;
-                    mpos = t;
+                const int64_t c = bnd_code(C, r, r.loopv(off + t), tv, fl, b0);
+                if (t == 0) {
+                    mn = mx = c;
+                    continue;
                 }
-                if (t == 0 || c > mx) mx = c;
+                if (c < mn) {
+                    second = mn;
+                    mn = c;
+                } else if (c < second) {
+                    second = c;
+                }
+                if (c > mx) mx = c;
             }
-            int64_t second = mx + 1;
-            for (int t = 0; t < L; ++t) {
-                int64_t c = bnd_code(C, r, r.loopv(off + t), tv, fl, b0);
-                if (t != mpos && c < second) second = c;
-            }
+            if (L < 2) second = mx + 1;
             uint64_t k0, k1;
             pack3(mn, second, mx, k0, k1);
             int64_t s = ht_insert_min(C.hb, k0, k1, bpos);
