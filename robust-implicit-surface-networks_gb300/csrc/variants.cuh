@@ -21,7 +21,10 @@ using MICutMid = MICut<96, 96, 640, 128, 128, 1024, false>;
 using MICutBig = MICut<255, 255, 2048, 255, 512, 4096, true>;
 // warp variant: one warp per tet, state in shared memory, exact predicates (32 cells)
 using IAWarpCutDev = IAWarpCut<64, 128, 640>;
-// the same for the light bins' leftovers (three to five distinct planes): half the vertex and face
-// room, so about twice the resident warps per SM; a tet that does not fit goes to IAWarpCutDev
-using IAWarpCutLight = IAWarpCut<32, 64, 320>;
+// the same for the light bins' leftovers (three to five distinct planes): three quarters of the
+// vertex, face and loop room (7 KB against 9 KB, 7 resident blocks per SM against 6); a tet that
+// does not fit goes to IAWarpCutDev.  On the large degenerate workload this size measured fastest:
+// the half-size state (9 blocks) sent more tets to the second launch, whose few long cuts run after
+// the first launch ends
+using IAWarpCutLight = IAWarpCut<48, 96, 480>;
 }  // namespace ria

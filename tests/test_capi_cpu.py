@@ -325,9 +325,9 @@ def test_warp_variant_heavy_and_degenerate(hc, oracle):
 
 
 def test_warp_light_state_on_light_bins(hc, oracle, fns):
-    """The warp variant's light state (half the vertex and face room) on the tets it serves: the
-    light bins' leftovers of the large degenerate workload (three to five active functions) and random
-    three- to five-plane tets.  It reproduces the oracle's record, or reports its capacity (the full
+    """The warp variant's light state (three quarters of the vertex and face room) on the tets it
+    serves: the light bins' leftovers of the large degenerate workload (three to five active
+    functions) and random three- to five-plane tets.  It reproduces the oracle's record, or reports its capacity (the full
     warp state then takes the tet); most of these tets fit."""
     wl = fns.workload_ia_degenerate(res=12)
     pts, tets = fns.generate_tet_mesh(wl.res)
