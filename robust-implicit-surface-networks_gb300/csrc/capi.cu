@@ -694,7 +694,7 @@ ria_status run_pipeline(const ria_config* cfg, const Inputs& in, cudaStream_t s,
             // (a record with warp_route 0 sends every tet to the thread kernel)
             if (tune.warp_route > 0) {
                 cl.route_at = tune.warp_route;
-                // the smaller warp state first (about twice the resident warps); the tets it cannot
+                // the smaller warp state first (more resident warps per SM); the tets it cannot
                 // hold then go to the full warp variant
                 CutArgs cw = cl;
                 cw.next = (unsigned int*)(cnt + 14);

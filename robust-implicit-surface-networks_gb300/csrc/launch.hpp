@@ -188,7 +188,7 @@ void launch_seed_cache(const CutArgs& a, cudaStream_t s);
 void launch_cut_wait(const CutArgs& a, cudaStream_t s);
 // implicit arrangement, one warp per tet with its state in shared memory (exact predicates); a tet
 // beyond its capacity goes to the deferred list
-// light: the smaller state (IAWarpCutLight: about twice the resident warps), for the light bins
+// light: the smaller state (IAWarpCutLight: more resident warps per SM), for the light bins' leftovers
 void launch_cut_warp(const CutArgs& a, cudaStream_t s, bool light = false);
 // filtered variants, one thread per tet: `mid` for the heavy bins (four or more active functions,
 // up to 16), the small one otherwise; a tet that outgrows them, or whose record does not fit the
